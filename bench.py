@@ -1,0 +1,365 @@
+#!/usr/bin/env python
+"""Benchmark of the LBVH build + traversal hot path on GB300.
+
+Workload: the largest single-GPU case of the LBVH build + traversal
+microbenchmark -- 16 Mi random triangles (centroids uniform in [0,1]^3, edge
+length ~ Exp(mean 0.5 N^-1/3), fp32 SoA, unindexed), 30-bit Morton keys
+(10 bits per axis); 16 Mi closest-hit rays and 16 Mi shadow segments.  Seeded
+synthetic data (the reference ships no scenes for this path).
+
+One step = one LBVH build of the 16 Mi triangles.  The headline metric is the
+build time per million triangles (lower is better).  Inputs (576 MB of
+vertices) exceed the 129 MB L2, so no flush is needed between steps.
+
+Reported with it:
+  e2e        the same metric through the C ABI from pinned HOST vertex arrays:
+             each step copies the vertices host->device, builds, and reads the
+             root box (the scene bounds) back to the host;
+  roofline   the build's dominant kernel: algorithmic bytes / its CUDA-event
+             duration vs the measured HBM copy bandwidth;
+  traversal  closest-hit and shadow throughput (Mrays/s) on the built tree;
+  cpu_baseline  the oracle's restatement of the reference LBVH build
+             (single thread) on a 1 Mi-triangle sample of the same workload.
+
+--impl reference times the reference's algorithm on the host CPU instead (the
+reference's own code is OpenCL and cannot run here; its CPU restatement in
+oracle/ is timed), on the same metric.
+
+Multi-GPU: the build does not shard; --gpus N runs N independent replicas
+(one process per GPU under torchrun), value = total triangles / max time.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+N_TRIS = 1 << 24
+N_RAYS = 1 << 24
+BITS = 10
+CPU_SAMPLE_TRIS = 1 << 20
+METRIC = "LBVH build ms per 1M triangles"
+UNIT = "ms/Mtri"
+WORKLOAD = "lbvh-build+traversal, 16Mi random triangles (30-bit Morton), 16Mi closest + 16Mi shadow rays"
+
+# Algorithmic bytes per unit (triangle, or internal node ~ triangle) of each
+# build kernel; see DESIGN.md "Roofline".
+ALGO_BYTES = {
+    "scene_box": 36.0,          # read 9 floats per triangle
+    "morton": 40.0,             # read 9 floats, write one 4-byte key
+    "sort_pass_first": 12.0,    # read key, write key + index
+    "sort_pass": 16.0,          # read key + index, write key + index
+    "karras": 164.0,            # key 4 + node 64 + parent 4 + counter 4 | idx 4 + 36 gather + 48 record
+    "refit": 88.0,              # parent 4 + child boxes 48 + box 24 + counter 8 (+ leaf parent 4)
+}
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--tris", type=int, default=N_TRIS)
+    ap.add_argument("--rays", type=int, default=N_RAYS)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+def dist_env():
+    return int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)), int(os.environ.get("LOCAL_RANK", 0))
+
+
+class ClockSampler:
+    """nvidia-smi clock / throttle sampling while the timed loops run."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=self.f, stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def stop(self) -> dict:
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        self.f.close()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        with open(self.path) as fh:
+            for line in fh:
+                parts = [p.strip() for p in line.split(",")]
+                if len(parts) < 9:
+                    continue
+                try:
+                    sm.append(float(parts[1]))
+                    smax.append(float(parts[2]))
+                except ValueError:
+                    continue
+                for nm, v in zip(names, parts[5:9]):
+                    if v.lower().startswith("active"):
+                        reasons.add(nm)
+        os.unlink(self.path)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        top = max(sm)
+        loaded = [s for s in sm if s >= 0.5 * top] or sm
+        return {"sm_mhz": statistics.median(loaded), "sm_max_mhz": max(smax), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def measured_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as fh:
+            d = json.load(fh)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def ncu_traffic(kernel: str):
+    """DRAM bytes per launch of `kernel` from the committed ncu summary."""
+    p = os.path.join(ROOT, "profiles", "traffic.json")
+    if not os.path.exists(p):
+        return None
+    with open(p) as fh:
+        d = json.load(fh)
+    v = d.get(kernel)
+    return None if v is None else float(v["bytes_per_launch_scaled"])
+
+
+def cpu_baseline(n: int, budget_s: float = 20.0) -> dict:
+    import oracle
+    from clear_gb300 import workloads as W
+
+    vx, vy, vz = W.triangle_soup(n, seed=101)
+    oracle.lbvh_build(vx, vy, vz, None, n, BITS)  # warm
+    times = []
+    t_end = time.perf_counter() + budget_s
+    while time.perf_counter() < t_end and len(times) < 10:
+        t0 = time.perf_counter()
+        oracle.lbvh_build(vx, vy, vz, None, n, BITS)
+        times.append(time.perf_counter() - t0)
+    ms = 1e3 * statistics.median(times)
+    return {"value": ms / (n / 1e6), "unit": UNIT, "cores": 1, "kind": "port",
+            "sample": f"{n} triangles of the same distribution, oracle/lbvh_oracle.c restatement of "
+                      f"lbvh_construction.cl, median of {len(times)} builds"}
+
+
+def run_reference(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return
+    import oracle
+    from clear_gb300 import workloads as W
+
+    n = CPU_SAMPLE_TRIS
+    vx, vy, vz = W.triangle_soup(n, seed=101)
+    for _ in range(args.warmup):
+        oracle.lbvh_build(vx, vy, vz, None, n, BITS)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        oracle.lbvh_build(vx, vy, vz, None, n, BITS)
+    dt = (time.perf_counter() - t0) / args.steps
+    value = 1e3 * dt / (n / 1e6)
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * dt, "higher_is_better": False,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "sample_tris": n, "bits_per_dim": BITS,
+                   "note": "reference LBVH algorithm (lbvh_construction.cl) restated in C, one host thread; "
+                           "the reference's OpenCL kernels cannot run here"},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": 1, "kind": "port",
+                         "sample": f"{n}-triangle sample per step"},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args):
+    import torch
+    import torch.distributed as dist
+
+    from clear_gb300 import _lib, lbvh
+    from clear_gb300 import workloads as W
+    from clear_gb300.build import build
+
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    if world > 1:
+        dist.init_process_group("nccl", device_id=dev)
+    if rank == 0:
+        build()
+    if world > 1:
+        dist.barrier()
+    else:
+        build()
+
+    def barrier():
+        if world > 1:
+            dist.barrier()
+
+    n = args.tris
+    vx, vy, vz = W.triangle_soup(n, seed=1 + rank)
+    host = [torch.from_numpy(a).pin_memory() for a in (vx, vy, vz)]
+    verts = [h.to(dev) for h in host]
+    builder = lbvh.LBVHBuilder(n, dev)
+    bvh = lbvh.BVH(n, dev)
+    stream = torch.cuda.current_stream(dev)
+
+    clocks = ClockSampler(local)
+    clocks.start()
+    for _ in range(args.warmup):
+        builder.perform(verts, None, n, BITS, out=bvh)
+    torch.cuda.synchronize()
+
+    # ---- headline: K builds, device-resident inputs
+    barrier()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        builder.perform(verts, None, n, BITS, out=bvh)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    barrier()
+    ms_step = e0.elapsed_time(e1) / args.steps
+
+    # ---- per-kernel durations (CUDA events around each launch) over K builds
+    builder.set_profiling(True)
+    per = {}
+    for _ in range(args.steps):
+        builder.perform(verts, None, n, BITS, out=bvh)
+        for i, (name, ms) in enumerate(builder.pass_times()):
+            key = "sort_pass_first" if name == "sort_pass" and i == 2 else name
+            per.setdefault(key, []).append(ms)
+    builder.set_profiling(False)
+    kern_ms = {k: statistics.mean(v) for k, v in per.items()}
+    launches_per_build = sum(len(v) for v in per.values()) // args.steps
+
+    # ---- e2e through the C ABI from pinned host memory
+    root_host = torch.empty(8, dtype=torch.float32).pin_memory()
+    torch.cuda.synchronize()
+    barrier()
+    e2, e3 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e2.record(stream)
+    for _ in range(args.steps):
+        for d, h in zip(verts, host):
+            d.copy_(h, non_blocking=True)
+        builder.perform(verts, None, n, BITS, out=bvh)
+        root_host.copy_(bvh.root_box, non_blocking=True)
+    e3.record(stream)
+    torch.cuda.synchronize()
+    barrier()
+    e2e_ms = e2.elapsed_time(e3) / args.steps
+
+    # ---- traversal throughput on the built tree
+    m = args.rays
+    crays = torch.from_numpy(W.closest_rays(m, seed=11 + rank)).to(dev)
+    srays = torch.from_numpy(W.shadow_rays(m, seed=12 + rank)).to(dev)
+    hid = torch.empty(m, dtype=torch.int32, device=dev)
+    ht = torch.empty(m, dtype=torch.float32, device=dev)
+    occ = torch.empty(m, dtype=torch.uint8, device=dev)
+    trav_steps = max(3, args.steps // 4)
+    for _ in range(2):
+        lbvh.trace_closest(bvh, crays, hid, ht)
+        lbvh.trace_shadow(bvh, srays, occ)
+    torch.cuda.synchronize()
+    t0, t1, t2 = (torch.cuda.Event(enable_timing=True) for _ in range(3))
+    t0.record(stream)
+    for _ in range(trav_steps):
+        lbvh.trace_closest(bvh, crays, hid, ht)
+    t1.record(stream)
+    for _ in range(trav_steps):
+        lbvh.trace_shadow(bvh, srays, occ)
+    t2.record(stream)
+    torch.cuda.synchronize()
+    closest_ms = t0.elapsed_time(t1) / trav_steps
+    shadow_ms = t1.elapsed_time(t2) / trav_steps
+    hit_frac = float((hid >= 0).float().mean().item())
+    occ_frac = float(occ.float().mean().item())
+    clk = clocks.stop()
+    dev_err = _lib.device_status()
+
+    # ---- max over ranks
+    vals = torch.tensor([ms_step, e2e_ms, closest_ms, shadow_ms], dtype=torch.float64, device=dev)
+    if world > 1:
+        dist.all_reduce(vals, op=dist.ReduceOp.MAX)
+    ms_step, e2e_ms, closest_ms, shadow_ms = vals.tolist()
+    if rank != 0:
+        dist.destroy_process_group()
+        return
+
+    mtris_total = world * n / 1e6
+    value = ms_step / mtris_total
+    peak, peak_kind = measured_peaks()
+    dom = max(kern_ms, key=kern_ms.get)
+    dom_ms = kern_ms[dom]
+    achieved = ALGO_BYTES.get(dom, 0.0) * n / (dom_ms * 1e-3) / 1e9
+    traffic = ncu_traffic(dom)
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": False, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "tris_per_gpu": n, "rays_per_gpu": m, "bits_per_dim": BITS,
+                   "parallelism": f"replicas x{world}", "l2": "inputs (576 MB) larger than L2, no flush"},
+        "e2e": {"value": e2e_ms / mtris_total, "unit": UNIT, "h2d_bytes_per_step": 3 * 4 * 3 * n,
+                "d2h_bytes_per_step": 32},
+        "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak,
+                     "peak_source": f"{peak_kind} hbm_gbs", "unit": "GB/s", "frac": achieved / peak,
+                     "traffic": traffic, "algo_bytes_per_tri": ALGO_BYTES.get(dom),
+                     "kernel_ms": dom_ms},
+        "build_kernels_ms": kern_ms,
+        "traversal": {"closest_mrays_s": m / closest_ms / 1e3, "shadow_mrays_s": m / shadow_ms / 1e3,
+                      "closest_ms": closest_ms, "shadow_ms": shadow_ms, "closest_hit_frac": hit_frac,
+                      "shadow_occluded_frac": occ_frac},
+        "gpu_launches": launches_per_build * args.steps,
+        "clocks": clk,
+        "device_error_bits": dev_err,
+    }
+    if not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline(CPU_SAMPLE_TRIS)
+    print(json.dumps(line), flush=True)
+    if world > 1:
+        dist.destroy_process_group()
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,93 @@
+"""ctypes binding of ``libclear_gb300.so`` (the C ABI of include/clear_cuda.h).
+
+The library is the only compute path: if it is missing or cannot be loaded,
+``lib()`` raises -- there is no CPU fallback.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import re
+from pathlib import Path
+
+PKG = Path(__file__).resolve().parent
+LIB_PATH = PKG / "libclear_gb300.so"
+HEADER = PKG.parent / "include" / "clear_cuda.h"
+
+CLR_OK = 0
+DEVERR_SORT_TIMEOUT = 0x1
+DEVERR_STACK = 0x2
+DEVERR_REFIT = 0x4
+DEVERR_QUEUE = 0x8
+NODE_BYTES = 64
+TRI_BYTES = 48
+REF_NODE_BYTES = 48
+
+
+class ClrBvh(C.Structure):
+    _fields_ = [("num_tris", C.c_uint32), ("bits_per_dim", C.c_uint32), ("nodes", C.c_void_p),
+                ("tris", C.c_void_p), ("root_box", C.c_void_p)]
+
+
+_lib = None
+
+
+class ClrError(RuntimeError):
+    def __init__(self, fn: str, code: int, msg: str):
+        super().__init__(f"{fn} failed with status {code}: {msg}")
+        self.code = code
+
+
+def declared_symbols() -> list[str]:
+    """Entry points declared in include/clear_cuda.h."""
+    txt = HEADER.read_text()
+    return re.findall(r"CLR_API\s+(?:const\s+)?\w+\s*\*?\s*(clr_\w+)\s*\(", txt)
+
+
+def load(path: Path | None = None) -> C.CDLL:
+    """Load the library without touching the GPU (ctypes only)."""
+    p = Path(path or os.environ.get("CLEAR_GB300_LIB", LIB_PATH))
+    if not p.exists():
+        raise RuntimeError(f"{p} is not built; run clear_gb300/build.py (or __graft_entry__.build())")
+    return C.CDLL(str(p))
+
+
+def lib() -> C.CDLL:
+    global _lib
+    if _lib is None:
+        L = load()
+        vp, u32, i32 = C.c_void_p, C.c_uint32, C.c_int
+        L.clr_last_error_string.restype = C.c_char_p
+        sig = {
+            "clr_lbvh_create": [u32, C.POINTER(vp)],
+            "clr_lbvh_destroy": [vp],
+            "clr_lbvh_build": [vp, vp, vp, vp, vp, u32, u32, C.POINTER(ClrBvh), vp],
+            "clr_lbvh_export_reference": [vp, C.POINTER(ClrBvh), vp, vp, vp, vp, vp, vp],
+            "clr_trace_closest": [C.POINTER(ClrBvh), vp, u32, vp, vp, vp],
+            "clr_trace_shadow": [C.POINTER(ClrBvh), vp, u32, vp, vp],
+            "clr_device_status": [C.POINTER(u32), i32],
+            "clr_lbvh_set_profiling": [vp, i32],
+            "clr_lbvh_pass_times": [vp, C.POINTER(C.c_float), C.POINTER(C.c_char_p), i32, C.POINTER(i32)],
+        }
+        for name, args in sig.items():
+            fn = getattr(L, name)
+            fn.argtypes = args
+            fn.restype = i32
+        _lib = L
+    return _lib
+
+
+def check(fn: str, rc: int) -> None:
+    if rc != CLR_OK:
+        msg = lib().clr_last_error_string().decode(errors="replace")
+        raise ClrError(fn, rc, msg)
+
+
+def call(fn: str, *args) -> None:
+    check(fn, getattr(lib(), fn)(*args))
+
+
+def device_status(clear: bool = True) -> int:
+    v = C.c_uint32(0)
+    call("clr_device_status", C.byref(v), 1 if clear else 0)
+    return v.value

@@ -1,0 +1,33 @@
+// Error reporting shared by every C entry point.
+#include <stdarg.h>
+#include <stdio.h>
+
+#include "common.cuh"
+
+static thread_local char t_last_error[512] = "no error";
+
+int clr_set_error(int code, const char* fmt, ...) {
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(t_last_error, sizeof(t_last_error), fmt, ap);
+    va_end(ap);
+    return code;
+}
+
+extern "C" const char* clr_last_error_string(void) { return t_last_error; }
+
+cudaError_t clr_status_lbvh(unsigned int* v, int clear);
+cudaError_t clr_status_traverse(unsigned int* v, int clear);
+
+extern "C" int clr_device_status(uint32_t* bits, int clear) {
+    CLR_CUDA_TRY(cudaDeviceSynchronize());
+    unsigned int all = 0;
+    cudaError_t (*readers[])(unsigned int*, int) = {clr_status_lbvh, clr_status_traverse};
+    for (auto rd : readers) {
+        unsigned int v = 0;
+        CLR_CUDA_TRY(rd(&v, clear));
+        all |= v;
+    }
+    if (bits) *bits = all;
+    return CLR_OK;
+}

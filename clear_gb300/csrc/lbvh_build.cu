@@ -1,0 +1,794 @@
+// LBVH construction on sm_103a.
+//
+// Reference pipeline (OpenCL_PathTracer/LBVHBuilder.cpp:160-375) and what
+// replaces each step here:
+//   calcAABBs + unifyAABBs + host read-back (lbvh_construction.cl:81-162,
+//   LBVHBuilder.cpp:189-229)        -> k_scene_box: one pass over the vertices,
+//                                      block reduce + ordered-uint atomics; the
+//                                      scene box never leaves the device.
+//   calcMortonCodes (:169-181)      -> k_morton: per-triangle box/centre and
+//                                      quantisation, packed straight into an
+//                                      interleaved 3b-bit key whose order is the
+//                                      reference's LSD digit order, plus the
+//                                      digit histograms of every sort pass.
+//   b rounds of blockwiseSort / histograms / global scan / scatter
+//   (:231-316, CLGenericKernels.cpp:107-151)
+//                                   -> ceil(3b/8) passes of a one-sweep 8-bit LSD
+//                                      radix sort (warp match-any ranking,
+//                                      decoupled look-back).  Stable, so the
+//                                      sorted order is the reference's.
+//   constructBinaryRadixTree (:342-410)
+//                                   -> k_karras: same direction / range / split
+//                                      search on the sorted keys; leaf children
+//                                      get their box and triangle record here.
+//   calcNodeAABBs (:415-492)        -> k_refit: atomic-counter climb with device
+//                                      fences (the reference has none).
+#include <stdio.h>
+
+#include <new>
+
+#include "common.cuh"
+#include "lbvh_internal.cuh"
+
+CLR_DEFINE_STATUS_READER(lbvh)
+
+namespace clr {
+
+// -------------------------------------------------------------- key packing
+
+__device__ __forceinline__ uint32_t spread3_10(uint32_t x) {
+    x &= 0x3FFu;
+    x = (x | (x << 16)) & 0x030000FFu;
+    x = (x | (x << 8)) & 0x0300F00Fu;
+    x = (x | (x << 4)) & 0x030C30C3u;
+    x = (x | (x << 2)) & 0x09249249u;
+    return x;
+}
+
+__device__ __forceinline__ uint64_t spread3_21(uint64_t x) {
+    x &= 0x1FFFFFull;
+    x = (x | (x << 32)) & 0x001F00000000FFFFull;
+    x = (x | (x << 16)) & 0x001F0000FF0000FFull;
+    x = (x | (x << 8)) & 0x100F00F00F00F00Full;
+    x = (x | (x << 4)) & 0x10C30C30C30C30C3ull;
+    x = (x | (x << 2)) & 0x1249249249249249ull;
+    return x;
+}
+
+// Key whose ascending order is the reference's sort order: the per-bit digit
+// is x | y<<1 | z<<2 (lbvh_construction.cl:245-246), least significant bit
+// level sorted first (LBVHBuilder.cpp:263).
+template <typename KeyT>
+__device__ __forceinline__ KeyT make_key(uint32_t qx, uint32_t qy, uint32_t qz);
+template <>
+__device__ __forceinline__ uint32_t make_key<uint32_t>(uint32_t qx, uint32_t qy, uint32_t qz) {
+    return spread3_10(qx) | (spread3_10(qy) << 1) | (spread3_10(qz) << 2);
+}
+template <>
+__device__ __forceinline__ uint64_t make_key<uint64_t>(uint32_t qx, uint32_t qy, uint32_t qz) {
+    return spread3_21(qx) | (spread3_21(qy) << 1) | (spread3_21(qz) << 2);
+}
+
+__device__ __forceinline__ uint32_t tri_vertex(const uint32_t* tri, uint32_t t, uint32_t k) {
+    return tri ? __ldg(tri + 3u * t + k) : 3u * t + k;
+}
+
+// ----------------------------------------------------------- scene bounds
+
+__device__ __forceinline__ float warp_min(float v) {
+    for (int o = 16; o > 0; o >>= 1) v = fminf(v, __shfl_xor_sync(0xFFFFFFFFu, v, o));
+    return v;
+}
+__device__ __forceinline__ float warp_max(float v) {
+    for (int o = 16; o > 0; o >>= 1) v = fmaxf(v, __shfl_xor_sync(0xFFFFFFFFu, v, o));
+    return v;
+}
+
+// boxw[0..2] hold ~ordered(min) (atomicMax of the complement = atomicMin),
+// boxw[3..5] hold ordered(max); all start at 0.
+__global__ void __launch_bounds__(256) k_scene_box(const float* __restrict__ vx, const float* __restrict__ vy,
+                                                   const float* __restrict__ vz, const uint32_t* __restrict__ tri,
+                                                   uint32_t n, unsigned int* __restrict__ boxw) {
+    float mn[3] = {INFINITY, INFINITY, INFINITY}, mx[3] = {-INFINITY, -INFINITY, -INFINITY};
+    const uint32_t stride = gridDim.x * blockDim.x;
+    if (tri == nullptr) {
+        // unindexed soup: every vertex belongs to a triangle
+        const uint64_t nv = 3ull * n;
+        for (uint64_t i = blockIdx.x * blockDim.x + threadIdx.x; i < nv; i += stride) {
+            float x = __ldg(vx + i), y = __ldg(vy + i), z = __ldg(vz + i);
+            mn[0] = fminf(mn[0], x); mx[0] = fmaxf(mx[0], x);
+            mn[1] = fminf(mn[1], y); mx[1] = fmaxf(mx[1], y);
+            mn[2] = fminf(mn[2], z); mx[2] = fmaxf(mx[2], z);
+        }
+    } else {
+        for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += stride) {
+            for (int k = 0; k < 3; ++k) {
+                uint32_t v = __ldg(tri + 3u * t + k);
+                float x = __ldg(vx + v), y = __ldg(vy + v), z = __ldg(vz + v);
+                mn[0] = fminf(mn[0], x); mx[0] = fmaxf(mx[0], x);
+                mn[1] = fminf(mn[1], y); mx[1] = fmaxf(mx[1], y);
+                mn[2] = fminf(mn[2], z); mx[2] = fmaxf(mx[2], z);
+            }
+        }
+    }
+    __shared__ float s[6][8];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    for (int k = 0; k < 3; ++k) {
+        float a = warp_min(mn[k]), b = warp_max(mx[k]);
+        if (lane == 0) { s[k][warp] = a; s[3 + k][warp] = b; }
+    }
+    __syncthreads();
+    if (threadIdx.x < 6) {
+        const int k = threadIdx.x;
+        float v = s[k][0];
+        for (int w = 1; w < (int)(blockDim.x >> 5); ++w) v = k < 3 ? fminf(v, s[k][w]) : fmaxf(v, s[k][w]);
+        if (v == v) {  // skip NaN (fmin/fmax ignore NaN operands)
+            unsigned int e = float_to_ordered(v);
+            atomicMax(boxw + k, k < 3 ? ~e : e);
+        }
+    }
+}
+
+__device__ __forceinline__ void load_scene_box(const unsigned int* boxw, float smin[3], float ssize[3]) {
+    for (int k = 0; k < 3; ++k) {
+        float mn = ordered_to_float(~__ldcg(boxw + k));
+        float mx = ordered_to_float(__ldcg(boxw + 3 + k));
+        smin[k] = mn;
+        ssize[k] = fsub(mx, mn);  // host subtraction in the reference, LBVHBuilder.cpp:236-240
+    }
+}
+
+// ------------------------------------------------------------ Morton keys
+
+template <typename KeyT>
+__global__ void __launch_bounds__(256) k_morton(const float* __restrict__ vx, const float* __restrict__ vy,
+                                                const float* __restrict__ vz, const uint32_t* __restrict__ tri,
+                                                uint32_t n, uint32_t bits, const unsigned int* __restrict__ boxw,
+                                                KeyT* __restrict__ keys, unsigned int* __restrict__ hist,
+                                                int npasses) {
+    __shared__ unsigned int sh[kMaxPasses * kRadix];
+    for (int i = threadIdx.x; i < npasses * kRadix; i += blockDim.x) sh[i] = 0;
+    float smin[3], ssize[3];
+    load_scene_box(boxw, smin, ssize);
+    const uint32_t numDivs = 1u << bits;
+    const float fDivs = (float)numDivs;
+    __syncthreads();
+    for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
+        const uint32_t a = tri_vertex(tri, t, 0), b = tri_vertex(tri, t, 1), c = tri_vertex(tri, t, 2);
+        const float P[3][3] = {{__ldg(vx + a), __ldg(vy + a), __ldg(vz + a)},
+                               {__ldg(vx + b), __ldg(vy + b), __ldg(vz + b)},
+                               {__ldg(vx + c), __ldg(vy + c), __ldg(vz + c)}};
+        uint32_t q[3];
+        for (int k = 0; k < 3; ++k) {
+            // calcAABBs (lbvh_construction.cl:92-94) then calcMortonCodes (:178-179)
+            const float mn = fminf(P[0][k], fminf(P[1][k], P[2][k]));
+            const float mx = fmaxf(P[0][k], fmaxf(P[1][k], P[2][k]));
+            const float center = fmul(fadd(mn, mx), 0.5f);
+            const float normPos = fdiv(fsub(center, smin[k]), ssize[k]);
+            const uint32_t v = __float2uint_rz(fmul(normPos, fDivs));
+            q[k] = min(v, numDivs - 1u);
+        }
+        const KeyT key = make_key<KeyT>(q[0], q[1], q[2]);
+        keys[t] = key;
+        for (int p = 0; p < npasses; ++p) atomicAdd(&sh[p * kRadix + (uint32_t)((key >> (8 * p)) & 0xFFu)], 1u);
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < npasses * kRadix; i += blockDim.x)
+        if (sh[i]) atomicAdd(hist + i, sh[i]);
+}
+
+// ------------------------------------------------------ one-sweep radix pass
+
+__device__ __forceinline__ unsigned int lanemask_lt() {
+    unsigned int m;
+    asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
+    return m;
+}
+
+// Exclusive scan of one value per thread over a 256-thread block.
+__device__ __forceinline__ unsigned int block_excl_scan256(unsigned int v, unsigned int* s_warp) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    unsigned int x = v;
+    for (int o = 1; o < 32; o <<= 1) {
+        unsigned int y = __shfl_up_sync(0xFFFFFFFFu, x, o);
+        if (lane >= o) x += y;
+    }
+    if (lane == 31) s_warp[warp] = x;
+    __syncthreads();
+    unsigned int off = 0;
+    for (int w = 0; w < warp; ++w) off += s_warp[w];
+    __syncthreads();
+    return off + x - v;
+}
+
+template <typename KeyT>
+struct SortCfg;
+template <>
+struct SortCfg<uint32_t> { static constexpr int kItems = 16; };
+template <>
+struct SortCfg<uint64_t> { static constexpr int kItems = 8; };
+
+template <typename KeyT, bool kFirst>
+__global__ void __launch_bounds__(kSortThreads) k_onesweep(const KeyT* __restrict__ kin,
+                                                           const uint32_t* __restrict__ vin,
+                                                           KeyT* __restrict__ kout, uint32_t* __restrict__ vout,
+                                                           uint32_t n, uint32_t shift,
+                                                           const unsigned int* __restrict__ hist,
+                                                           unsigned int* __restrict__ status,
+                                                           unsigned int* __restrict__ tile_ctr) {
+    constexpr int kItems = SortCfg<KeyT>::kItems;
+    constexpr int kWarps = kSortThreads / 32;
+    constexpr int kWarpSpan = 32 * kItems;
+    constexpr int kTile = kSortThreads * kItems;
+    __shared__ unsigned int s_tile;
+    __shared__ unsigned int s_whist[kWarps][kRadix];
+    __shared__ unsigned int s_tile_off[kRadix];
+    __shared__ unsigned int s_gbase[kRadix];
+    __shared__ unsigned int s_scan[kWarps];
+    __shared__ KeyT s_keys[kTile];
+    __shared__ uint32_t s_vals[kTile];
+
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    if (tid == 0) s_tile = atomicAdd(tile_ctr, 1u);
+    for (int i = tid; i < kWarps * kRadix; i += kSortThreads) (&s_whist[0][0])[i] = 0;
+    __syncthreads();
+    const uint32_t tile = s_tile;
+    const uint32_t base = tile * (uint32_t)kTile;
+    const uint32_t tile_n = min((uint32_t)kTile, n - base);
+
+    // Load: warp w owns the contiguous span [base + w*kWarpSpan, +kWarpSpan),
+    // lane-striped so every load instruction is coalesced.
+    KeyT k[kItems];
+    uint32_t v[kItems];
+    uint32_t rank[kItems];
+    const uint32_t wbase = base + warp * kWarpSpan;
+#pragma unroll
+    for (int i = 0; i < kItems; ++i) {
+        const uint32_t idx = wbase + i * 32 + lane;
+        const bool ok = idx < n;
+        k[i] = ok ? kin[idx] : KeyT(0);
+        v[i] = kFirst ? idx : (ok ? vin[idx] : 0u);
+    }
+    // Rank in input order: step i handles 32 consecutive keys; lanes holding
+    // the same digit find each other with match.any and the lowest lane
+    // advances the warp's counter for that digit.
+    const unsigned int lt = lanemask_lt();
+#pragma unroll
+    for (int i = 0; i < kItems; ++i) {
+        const uint32_t idx = wbase + i * 32 + lane;
+        const bool ok = idx < n;
+        const unsigned int dig = ok ? (unsigned int)((k[i] >> shift) & 0xFFu) : 0xFFFFFFFFu;
+        const unsigned int peers = __match_any_sync(0xFFFFFFFFu, dig);
+        const int leader = __ffs(peers) - 1;
+        unsigned int old = 0;
+        if (ok && lane == leader) {
+            old = s_whist[warp][dig];
+            s_whist[warp][dig] = old + __popc(peers);
+        }
+        old = __shfl_sync(0xFFFFFFFFu, old, leader);
+        rank[i] = old + __popc(peers & lt);
+        __syncwarp();
+    }
+    __syncthreads();
+
+    // Per digit d (= tid): warp prefix, tile total, early publication of the
+    // tile's aggregate, then the look-back over earlier tiles.
+    const int d = tid;
+    unsigned int total = 0;
+#pragma unroll
+    for (int w = 0; w < kWarps; ++w) {
+        const unsigned int c = s_whist[w][d];
+        s_whist[w][d] = total;
+        total += c;
+    }
+    unsigned int* my_status = status + (size_t)tile * kRadix + d;
+    if (tile == 0) st_relaxed_gpu(my_status, kFlagInclusive | total);
+    else st_relaxed_gpu(my_status, kFlagAggregate | total);
+
+    const unsigned int tile_off = block_excl_scan256(total, s_scan);
+    const unsigned int gcount = __ldg(hist + d);
+    const unsigned int gexcl = block_excl_scan256(gcount, s_scan);
+
+    unsigned int excl = 0;
+    if (tile > 0) {
+        int j = (int)tile - 1;
+        unsigned int spins = 0;
+        while (j >= 0) {
+            const unsigned int s = ld_relaxed_gpu(status + (size_t)j * kRadix + d);
+            const unsigned int flag = s & kFlagMask;
+            if (flag == 0u) {
+                if (++spins > kSpinLimit) {
+                    clr_raise(CLR_DEVERR_SORT_TIMEOUT);
+                    break;
+                }
+                if (spins > 64) __nanosleep(32);
+                continue;
+            }
+            excl += s & kValueMask;
+            if (flag == kFlagInclusive) break;
+            --j;
+        }
+        st_relaxed_gpu(my_status, kFlagInclusive | (excl + total));
+    }
+    s_tile_off[d] = tile_off;
+    s_gbase[d] = gexcl + excl - tile_off;
+    __syncthreads();
+
+    // Scatter into shared memory in digit order.
+#pragma unroll
+    for (int i = 0; i < kItems; ++i) {
+        const uint32_t idx = wbase + i * 32 + lane;
+        if (idx < n) {
+            const unsigned int dig = (unsigned int)((k[i] >> shift) & 0xFFu);
+            const uint32_t pos = s_tile_off[dig] + s_whist[warp][dig] + rank[i];
+            s_keys[pos] = k[i];
+            s_vals[pos] = v[i];
+        }
+    }
+    __syncthreads();
+    // Write out: consecutive threads take consecutive sorted slots, so every
+    // digit's run is written contiguously.
+#pragma unroll
+    for (int i = 0; i < kItems; ++i) {
+        const uint32_t p = i * kSortThreads + tid;
+        if (p < tile_n) {
+            const KeyT key = s_keys[p];
+            const unsigned int dig = (unsigned int)((key >> shift) & 0xFFu);
+            const uint32_t g = s_gbase[dig] + p;
+            kout[g] = key;
+            vout[g] = s_vals[p];
+        }
+    }
+}
+
+// ------------------------------------------------------------ Karras tree
+
+template <typename KeyT>
+__device__ __forceinline__ int clz_key(KeyT x);
+template <>
+__device__ __forceinline__ int clz_key<uint32_t>(uint32_t x) { return __clz(x); }
+template <>
+__device__ __forceinline__ int clz_key<uint64_t>(uint64_t x) { return __clzll(x); }
+
+// _numCommonBits (lbvh_construction.cl:322-332) on packed keys: the leading
+// common bits of the 3b-bit keys, extended by the common bits of the sorted
+// positions when the keys are equal; -1 outside [0, n).
+template <typename KeyT>
+__device__ __forceinline__ int delta(const KeyT* __restrict__ keys, int64_t n, int kbits, KeyT ki, int64_t i,
+                                     int64_t j) {
+    if (j < 0 || j >= n) return -1;
+    const KeyT kj = keys[j];
+    const KeyT x = ki ^ kj;
+    if (x != 0) return clz_key<KeyT>(x) - ((int)(8 * sizeof(KeyT)) - kbits);
+    return kbits + __clz((uint32_t)i ^ (uint32_t)j);
+}
+
+struct TriVerts {
+    float p[3][3];
+};
+
+__device__ __forceinline__ TriVerts load_tri(const float* vx, const float* vy, const float* vz,
+                                             const uint32_t* tri, uint32_t t) {
+    TriVerts tv;
+    for (int k = 0; k < 3; ++k) {
+        const uint32_t v = tri_vertex(tri, t, k);
+        tv.p[k][0] = __ldg(vx + v);
+        tv.p[k][1] = __ldg(vy + v);
+        tv.p[k][2] = __ldg(vz + v);
+    }
+    return tv;
+}
+
+// Writes leaf `leaf`'s triangle record and returns its box (calcAABBs).
+__device__ __forceinline__ void emit_leaf(const float* vx, const float* vy, const float* vz, const uint32_t* tri,
+                                          uint32_t tid, uint32_t leaf, float4* __restrict__ tris, float box[6]) {
+    const TriVerts tv = load_tri(vx, vy, vz, tri, tid);
+    for (int k = 0; k < 3; ++k) {
+        box[k] = fminf(tv.p[0][k], fminf(tv.p[1][k], tv.p[2][k]));
+        box[3 + k] = fmaxf(tv.p[0][k], fmaxf(tv.p[1][k], tv.p[2][k]));
+    }
+    float4* r = tris + 3u * leaf;
+    r[0] = make_float4(tv.p[0][0], tv.p[0][1], tv.p[0][2], __uint_as_float(tid));
+    r[1] = make_float4(fsub(tv.p[1][0], tv.p[0][0]), fsub(tv.p[1][1], tv.p[0][1]), fsub(tv.p[1][2], tv.p[0][2]), 0.f);
+    r[2] = make_float4(fsub(tv.p[2][0], tv.p[0][0]), fsub(tv.p[2][1], tv.p[0][1]), fsub(tv.p[2][2], tv.p[0][2]), 0.f);
+}
+
+template <typename KeyT>
+__global__ void __launch_bounds__(256) k_karras(const KeyT* __restrict__ keys, const uint32_t* __restrict__ sidx,
+                                                uint32_t n, int kbits, const float* __restrict__ vx,
+                                                const float* __restrict__ vy, const float* __restrict__ vz,
+                                                const uint32_t* __restrict__ tri, float4* __restrict__ nodes,
+                                                float4* __restrict__ tris, uint32_t* __restrict__ parent_leaf,
+                                                uint32_t* __restrict__ parent_inner,
+                                                unsigned int* __restrict__ counters) {
+    const uint32_t g = blockIdx.x * blockDim.x + threadIdx.x;
+    if (g >= n - 1) return;
+    counters[g] = 0;
+    const int64_t gi = g, nn = n;
+    const KeyT ki = keys[g];
+    // direction, range and split searches of constructBinaryRadixTree
+    // (lbvh_construction.cl:363-392)
+    const int commonR = delta(keys, nn, kbits, ki, gi, gi + 1);
+    const int commonL = delta(keys, nn, kbits, ki, gi, gi - 1);
+    const int d = commonR > commonL ? 1 : (commonR < commonL ? -1 : 0);
+    const int minNum = d > 0 ? commonL : commonR;
+    int64_t lMax = 2;
+    while (delta(keys, nn, kbits, ki, gi, gi + lMax * d) > minNum) lMax <<= 1;
+    int64_t l = 0;
+    for (int64_t t = lMax >> 1; t >= 1; t >>= 1)
+        if (delta(keys, nn, kbits, ki, gi, gi + (l + t) * d) > minNum) l += t;
+    const int64_t otherEnd = gi + l * d;
+    const int numNode = delta(keys, nn, kbits, ki, gi, otherEnd);
+    int64_t split = 0;
+    float scale = 0.5f;
+    for (;;) {
+        const uint32_t t = (uint32_t)ceilf(fmul((float)(uint32_t)l, scale));
+        if (delta(keys, nn, kbits, ki, gi, gi + (split + (int64_t)t) * d) > numNode) split += t;
+        if (t <= 1) break;
+        scale = fmul(scale, 0.5f);
+    }
+    const int64_t splitPos = gi + split * d + (d < 0 ? d : 0);
+    const int64_t lo = min(gi, otherEnd), hi = max(gi, otherEnd);
+    const uint32_t c[2] = {(uint32_t)splitPos, (uint32_t)(splitPos + 1)};
+    const bool leaf[2] = {lo == splitPos, hi == splitPos + 1};
+
+    float box[2][6];
+    uint32_t ref[2];
+#pragma unroll
+    for (int s = 0; s < 2; ++s) {
+        if (leaf[s]) {
+            emit_leaf(vx, vy, vz, tri, __ldg(sidx + c[s]), c[s], tris, box[s]);
+            parent_leaf[c[s]] = g;
+            ref[s] = c[s] | kLeafBit;
+        } else {
+            // filled in by k_refit
+            for (int k = 0; k < 6; ++k) box[s][k] = 0.f;
+            parent_inner[c[s]] = g | ((uint32_t)s << 31);
+            ref[s] = c[s];
+        }
+    }
+    float4* nd = nodes + 4u * g;
+    nd[0] = make_float4(box[0][0], box[0][1], box[0][2], box[0][3]);
+    nd[1] = make_float4(box[0][4], box[0][5], box[1][0], box[1][1]);
+    nd[2] = make_float4(box[1][2], box[1][3], box[1][4], box[1][5]);
+    nd[3] = make_float4(__uint_as_float(ref[0]), __uint_as_float(ref[1]), 0.f, 0.f);
+}
+
+// Single-triangle scene: one leaf, no internal node (the reference requires
+// at least two triangles; here traversal treats the leaf as the root).
+__global__ void k_single(const float* vx, const float* vy, const float* vz, const uint32_t* tri, float4* tris,
+                         float* root_box) {
+    float box[6];
+    emit_leaf(vx, vy, vz, tri, 0u, 0u, tris, box);
+    for (int k = 0; k < 3; ++k) { root_box[k] = box[k]; root_box[4 + k] = box[3 + k]; }
+    root_box[3] = 0.f;
+    root_box[7] = 0.f;
+}
+
+// ----------------------------------------------------------------- refit
+
+__global__ void __launch_bounds__(256) k_refit(float* __restrict__ nodes, const uint32_t* __restrict__ parent_leaf,
+                                               const uint32_t* __restrict__ parent_inner,
+                                               unsigned int* __restrict__ counters, uint32_t n,
+                                               float* __restrict__ root_box) {
+    const uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= n) return;
+    uint32_t p = parent_leaf[j];
+    // The k-th internal node on a leaf-to-root path has a common prefix of at
+    // least k bits, so a climb never exceeds kMaxDepth steps.
+    for (int step = 0; step < kMaxDepth; ++step) {
+        __threadfence();  // publish the child box written by this thread
+        if (atomicAdd(counters + p, 1u) == 0u) return;  // sibling not done yet
+        __threadfence();  // observe the sibling's box
+        const float* nd = nodes + 16u * p;
+        float b[12];
+#pragma unroll
+        for (int k = 0; k < 12; ++k) b[k] = __ldcg(nd + k);
+        float u[6];
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            u[k] = fminf(b[k], b[6 + k]);
+            u[3 + k] = fmaxf(b[3 + k], b[9 + k]);
+        }
+        if (p == 0) {
+            root_box[0] = u[0]; root_box[1] = u[1]; root_box[2] = u[2]; root_box[3] = 0.f;
+            root_box[4] = u[3]; root_box[5] = u[4]; root_box[6] = u[5]; root_box[7] = 0.f;
+            return;
+        }
+        const uint32_t gp = parent_inner[p];
+        const uint32_t slot = gp >> 31, q = gp & 0x7FFFFFFFu;
+        float2* dst = reinterpret_cast<float2*>(nodes + 16u * q + 6u * slot);
+        __stcg(dst + 0, make_float2(u[0], u[1]));
+        __stcg(dst + 1, make_float2(u[2], u[3]));
+        __stcg(dst + 2, make_float2(u[4], u[5]));
+        p = q;
+    }
+    clr_raise(CLR_DEVERR_REFIT);
+}
+
+// --------------------------------------------------------- reference export
+
+__global__ void k_export(const float4* __restrict__ nodes, const float4* __restrict__ tris, uint32_t n,
+                         uint8_t* __restrict__ inodes, uint8_t* __restrict__ lnodes, uint32_t* __restrict__ parents) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n - 1) return;
+    const float4 a = nodes[4u * i], b = nodes[4u * i + 1], c = nodes[4u * i + 2], r = nodes[4u * i + 3];
+    const float bx[2][6] = {{a.x, a.y, a.z, a.w, b.x, b.y}, {b.z, b.w, c.x, c.y, c.z, c.w}};
+    const uint32_t ref[2] = {__float_as_uint(r.x), __float_as_uint(r.y)};
+    if (inodes) {
+        float* f = reinterpret_cast<float*>(inodes + 48u * i);
+        for (int k = 0; k < 3; ++k) {
+            f[k] = fminf(bx[0][k], bx[1][k]);
+            f[4 + k] = fmaxf(bx[0][3 + k], bx[1][3 + k]);
+        }
+        f[3] = 0.f;
+        f[7] = 0.f;
+        uint8_t* ch = inodes + 48u * i + 32u;
+        ch[0] = (uint8_t)(ref[0] >> 31);
+        ch[1] = (uint8_t)(ref[1] >> 31);
+        ch[2] = ch[3] = 0;
+        uint32_t* cc = reinterpret_cast<uint32_t*>(inodes + 48u * i + 36u);
+        cc[0] = ref[0] & 0x7FFFFFFFu;
+        cc[1] = ref[1] & 0x7FFFFFFFu;
+        cc[2] = 0;
+    }
+    for (int s = 0; s < 2; ++s) {
+        const uint32_t child = ref[s] & 0x7FFFFFFFu;
+        const bool is_leaf = ref[s] >> 31;
+        if (parents) parents[is_leaf ? child : n + child] = i;
+        if (is_leaf && lnodes) {
+            float* f = reinterpret_cast<float*>(lnodes + 48u * child);
+            for (int k = 0; k < 3; ++k) { f[k] = bx[s][k]; f[4 + k] = bx[s][3 + k]; }
+            f[3] = 0.f;
+            f[7] = 0.f;
+            uint32_t* u = reinterpret_cast<uint32_t*>(lnodes + 48u * child + 32u);
+            u[0] = __float_as_uint(tris[3u * child].w);
+            u[1] = u[2] = u[3] = 0;
+        }
+    }
+    if (i == 0 && parents) parents[n] = 0xFFFFFFFFu;
+}
+
+__global__ void k_export_single(const float* __restrict__ root_box, const float4* __restrict__ tris,
+                                uint8_t* __restrict__ lnodes, uint32_t* __restrict__ parents) {
+    if (lnodes) {
+        float* f = reinterpret_cast<float*>(lnodes);
+        for (int k = 0; k < 8; ++k) f[k] = root_box[k];
+        uint32_t* u = reinterpret_cast<uint32_t*>(lnodes + 32);
+        u[0] = __float_as_uint(tris[0].w);
+        u[1] = u[2] = u[3] = 0;
+    }
+    if (parents) parents[0] = 0xFFFFFFFFu;
+}
+
+template <typename KeyT>
+__global__ void k_keys_to_u64(const KeyT* __restrict__ in, uint64_t* __restrict__ out, uint32_t n) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) out[i] = (uint64_t)in[i];
+}
+
+}  // namespace clr
+
+// =============================================================== host side
+
+using namespace clr;
+
+static size_t align_up(size_t v, size_t a) { return (v + a - 1) / a * a; }
+
+// Lays the scratch pool out for `cap` triangles.  Returns its size; assigns
+// the handle's pointers when `base` is non-NULL.
+static size_t pool_layout(clr_lbvh* h, uint32_t cap, char* base) {
+    const size_t tiles = div_up(cap ? cap : 1, kMinSortTile) + 1;
+    size_t off = 0;
+    auto take = [&](size_t bytes) {
+        const size_t o = off;
+        off = align_up(off + bytes, 256);
+        return o;
+    };
+    const size_t o_keys0 = take(8ull * cap), o_keys1 = take(8ull * cap);
+    const size_t o_vals0 = take(4ull * cap), o_vals1 = take(4ull * cap);
+    const size_t o_pleaf = take(4ull * cap), o_pinner = take(4ull * cap), o_cnt = take(4ull * cap);
+    const size_t o_zero = off;
+    const size_t o_hist = take(4ull * kMaxPasses * kRadix);
+    const size_t o_status = take(4ull * kMaxPasses * tiles * kRadix);
+    const size_t o_tiles = take(4ull * kMaxPasses);
+    const size_t o_box = take(4ull * 8);
+    if (base) {
+        h->keys[0] = base + o_keys0;
+        h->keys[1] = base + o_keys1;
+        h->vals[0] = reinterpret_cast<uint32_t*>(base + o_vals0);
+        h->vals[1] = reinterpret_cast<uint32_t*>(base + o_vals1);
+        h->parent_leaf = reinterpret_cast<uint32_t*>(base + o_pleaf);
+        h->parent_inner = reinterpret_cast<uint32_t*>(base + o_pinner);
+        h->counters = reinterpret_cast<unsigned int*>(base + o_cnt);
+        h->zero_region = base + o_zero;
+        h->zero_bytes = off - o_zero;
+        h->hist = reinterpret_cast<unsigned int*>(base + o_hist);
+        h->status = reinterpret_cast<unsigned int*>(base + o_status);
+        h->status_stride = tiles * kRadix;
+        h->tile_ctr = reinterpret_cast<unsigned int*>(base + o_tiles);
+        h->boxw = reinterpret_cast<unsigned int*>(base + o_box);
+        h->pool_bytes = off;
+    }
+    return off;
+}
+
+static int pool_grow(clr_lbvh* h, uint32_t cap) {
+    if (h->pool && cap <= h->capacity) return CLR_OK;
+    if (h->pool) {
+        cudaFree(h->pool);
+        h->pool = nullptr;
+    }
+    const size_t bytes = pool_layout(h, cap, nullptr);
+    if (cudaMalloc(&h->pool, bytes) != cudaSuccess) {
+        cudaGetLastError();
+        h->pool = nullptr;
+        h->capacity = 0;
+        return clr_set_error(CLR_ENOMEM, "cudaMalloc(%zu) for the LBVH scratch pool failed", bytes);
+    }
+    h->capacity = cap;
+    pool_layout(h, cap, static_cast<char*>(h->pool));
+    return CLR_OK;
+}
+
+extern "C" int clr_lbvh_create(uint32_t capacity, clr_lbvh** out) {
+    if (!out) return clr_set_error(CLR_EINVAL, "clr_lbvh_create: out is NULL");
+    clr_lbvh* h = new (std::nothrow) clr_lbvh{};
+    if (!h) return clr_set_error(CLR_ENOMEM, "clr_lbvh_create: host allocation failed");
+    int rc = pool_grow(h, capacity > 0 ? capacity : 1);
+    if (rc != CLR_OK) {
+        delete h;
+        return rc;
+    }
+    *out = h;
+    return CLR_OK;
+}
+
+extern "C" int clr_lbvh_destroy(clr_lbvh* h) {
+    if (!h) return CLR_OK;
+    if (h->pool) cudaFree(h->pool);
+    for (auto& e : h->ev)
+        if (e) cudaEventDestroy(e);
+    delete h;
+    return CLR_OK;
+}
+
+// Event bookkeeping for clr_lbvh_set_profiling: mark(h, st, name) closes the
+// previous pass and opens the next.
+struct PassTimer {
+    clr_lbvh* h;
+    cudaStream_t st;
+    PassTimer(clr_lbvh* hh, cudaStream_t s) : h(hh), st(s) {
+        h->num_timed = 0;
+        if (h->profiling) cudaEventRecord(h->ev[0], st);
+    }
+    void done(const char* name) {
+        if (!h->profiling || h->num_timed >= clr_lbvh::kMaxTimed) return;
+        h->ev_name[h->num_timed] = name;
+        cudaEventRecord(h->ev[++h->num_timed], st);
+    }
+};
+
+template <typename KeyT>
+static int run_build(clr_lbvh* h, const float* vx, const float* vy, const float* vz, const uint32_t* tri,
+                     uint32_t n, uint32_t bits, clr_bvh* out, cudaStream_t st) {
+    const int kbits = 3 * (int)bits;
+    const int npasses = (kbits + 7) / 8;
+    const int grid_stream = kSmCount * 8;
+    PassTimer timer(h, st);
+    CLR_CUDA_TRY(cudaMemsetAsync(h->zero_region, 0, h->zero_bytes, st));
+    k_scene_box<<<grid_stream, 256, 0, st>>>(vx, vy, vz, tri, n, h->boxw);
+    CLR_LAUNCH_CHECK("k_scene_box");
+    timer.done("scene_box");
+    KeyT* keys[2] = {static_cast<KeyT*>(h->keys[0]), static_cast<KeyT*>(h->keys[1])};
+    k_morton<KeyT><<<grid_stream, 256, 0, st>>>(vx, vy, vz, tri, n, bits, h->boxw, keys[0], h->hist, npasses);
+    CLR_LAUNCH_CHECK("k_morton");
+    timer.done("morton");
+    constexpr int kTile = kSortThreads * SortCfg<KeyT>::kItems;
+    const unsigned int tiles = div_up(n, kTile);
+    for (int p = 0; p < npasses; ++p) {
+        const int src = p & 1, dst = src ^ 1;
+        if (p == 0)
+            k_onesweep<KeyT, true><<<tiles, kSortThreads, 0, st>>>(
+                keys[src], nullptr, keys[dst], h->vals[dst], n, 8 * p, h->hist + p * kRadix,
+                h->status + p * h->status_stride, h->tile_ctr + p);
+        else
+            k_onesweep<KeyT, false><<<tiles, kSortThreads, 0, st>>>(
+                keys[src], h->vals[src], keys[dst], h->vals[dst], n, 8 * p, h->hist + p * kRadix,
+                h->status + p * h->status_stride, h->tile_ctr + p);
+        CLR_LAUNCH_CHECK("k_onesweep");
+        timer.done("sort_pass");
+    }
+    const int fin = npasses & 1;
+    h->final_buf = fin;
+    float4* nodes = static_cast<float4*>(out->nodes);
+    float4* tris = static_cast<float4*>(out->tris);
+    if (n == 1) {
+        k_single<<<1, 1, 0, st>>>(vx, vy, vz, tri, tris, out->root_box);
+        CLR_LAUNCH_CHECK("k_single");
+        timer.done("single");
+    } else {
+        k_karras<KeyT><<<div_up(n - 1, 256), 256, 0, st>>>(keys[fin], h->vals[fin], n, kbits, vx, vy, vz, tri, nodes,
+                                                          tris, h->parent_leaf, h->parent_inner, h->counters);
+        CLR_LAUNCH_CHECK("k_karras");
+        timer.done("karras");
+        k_refit<<<div_up(n, 256), 256, 0, st>>>(reinterpret_cast<float*>(out->nodes), h->parent_leaf,
+                                                 h->parent_inner, h->counters, n, out->root_box);
+        CLR_LAUNCH_CHECK("k_refit");
+        timer.done("refit");
+    }
+    return CLR_OK;
+}
+
+extern "C" int clr_lbvh_build(clr_lbvh* h, const float* vx, const float* vy, const float* vz, const uint32_t* tri,
+                              uint32_t num_tris, uint32_t bits_per_dim, clr_bvh* out, void* stream) {
+    if (!h || !out) return clr_set_error(CLR_EINVAL, "clr_lbvh_build: NULL handle or output");
+    if (bits_per_dim < 1 || bits_per_dim > 21)
+        return clr_set_error(CLR_EINVAL, "clr_lbvh_build: bits_per_dim %u outside [1, 21]", bits_per_dim);
+    if (num_tris >= (1u << 30))
+        return clr_set_error(CLR_EINVAL, "clr_lbvh_build: %u triangles exceed the 2^30 limit", num_tris);
+    if (num_tris > 0 && (!vx || !vy || !vz || !out->tris || !out->root_box || (num_tris > 1 && !out->nodes)))
+        return clr_set_error(CLR_EINVAL, "clr_lbvh_build: NULL input or output buffer");
+    out->num_tris = num_tris;
+    out->bits_per_dim = bits_per_dim;
+    h->last_n = num_tris;
+    h->last_bits = bits_per_dim;
+    if (num_tris == 0) return CLR_OK;
+    int rc = pool_grow(h, num_tris);
+    if (rc != CLR_OK) return rc;
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    if (bits_per_dim <= 10) return run_build<uint32_t>(h, vx, vy, vz, tri, num_tris, bits_per_dim, out, st);
+    return run_build<uint64_t>(h, vx, vy, vz, tri, num_tris, bits_per_dim, out, st);
+}
+
+extern "C" int clr_lbvh_export_reference(clr_lbvh* h, const clr_bvh* bvh, void* inodes, void* lnodes,
+                                         uint32_t* parents, uint32_t* sorted_idx, uint64_t* keys, void* stream) {
+    if (!h || !bvh) return clr_set_error(CLR_EINVAL, "clr_lbvh_export_reference: NULL argument");
+    const uint32_t n = bvh->num_tris;
+    if (n != h->last_n) return clr_set_error(CLR_EINVAL, "clr_lbvh_export_reference: bvh is not the last build");
+    if (n == 0) return CLR_OK;
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    if (n == 1) {
+        k_export_single<<<1, 1, 0, st>>>(bvh->root_box, static_cast<const float4*>(bvh->tris),
+                                         static_cast<uint8_t*>(lnodes), parents);
+        CLR_LAUNCH_CHECK("k_export_single");
+    } else {
+        k_export<<<div_up(n - 1, 256), 256, 0, st>>>(static_cast<const float4*>(bvh->nodes),
+                                                     static_cast<const float4*>(bvh->tris), n,
+                                                     static_cast<uint8_t*>(inodes), static_cast<uint8_t*>(lnodes),
+                                                     parents);
+        CLR_LAUNCH_CHECK("k_export");
+    }
+    const int fin = h->final_buf;
+    if (sorted_idx) CLR_CUDA_TRY(cudaMemcpyAsync(sorted_idx, h->vals[fin], 4ull * n, cudaMemcpyDeviceToDevice, st));
+    if (keys) {
+        if (h->last_bits <= 10)
+            k_keys_to_u64<uint32_t><<<div_up(n, 256), 256, 0, st>>>(static_cast<const uint32_t*>(h->keys[fin]), keys, n);
+        else
+            k_keys_to_u64<uint64_t><<<div_up(n, 256), 256, 0, st>>>(static_cast<const uint64_t*>(h->keys[fin]), keys, n);
+        CLR_LAUNCH_CHECK("k_keys_to_u64");
+    }
+    return CLR_OK;
+}
+
+extern "C" int clr_lbvh_set_profiling(clr_lbvh* h, int enable) {
+    if (!h) return clr_set_error(CLR_EINVAL, "clr_lbvh_set_profiling: NULL handle");
+    if (enable && !h->ev[0])
+        for (auto& e : h->ev) CLR_CUDA_TRY(cudaEventCreate(&e));
+    h->profiling = enable != 0;
+    h->num_timed = 0;
+    return CLR_OK;
+}
+
+extern "C" int clr_lbvh_pass_times(clr_lbvh* h, float* ms, const char** names, int max_passes, int* num_passes) {
+    if (!h || !num_passes) return clr_set_error(CLR_EINVAL, "clr_lbvh_pass_times: NULL argument");
+    if (!h->profiling) return clr_set_error(CLR_EINVAL, "clr_lbvh_pass_times: profiling is off");
+    const int n = h->num_timed < max_passes ? h->num_timed : max_passes;
+    if (h->num_timed > 0) CLR_CUDA_TRY(cudaEventSynchronize(h->ev[h->num_timed]));
+    for (int i = 0; i < n; ++i) {
+        if (ms) CLR_CUDA_TRY(cudaEventElapsedTime(ms + i, h->ev[i], h->ev[i + 1]));
+        if (names) names[i] = h->ev_name[i];
+    }
+    *num_passes = n;
+    return CLR_OK;
+}

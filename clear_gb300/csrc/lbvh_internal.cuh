@@ -1,0 +1,52 @@
+// Internal constants and the builder handle of the LBVH build.
+#pragma once
+
+#include <stddef.h>
+#include <stdint.h>
+
+#include <cuda_runtime.h>
+
+namespace clr {
+
+constexpr int kSmCount = 152;        // GB300: 2 dies x 76 SMs
+constexpr int kRadix = 256;          // 8-bit digits
+constexpr int kMaxPasses = 8;        // 63-bit keys (21 bits per axis)
+constexpr int kSortThreads = 256;
+constexpr unsigned int kMinSortTile = 2048;  // smallest tile (64-bit keys)
+constexpr unsigned int kFlagAggregate = 1u << 30;
+constexpr unsigned int kFlagInclusive = 2u << 30;
+constexpr unsigned int kFlagMask = 3u << 30;
+constexpr unsigned int kValueMask = (1u << 30) - 1u;
+constexpr unsigned int kSpinLimit = 1u << 22;  // look-back polls before giving up
+// Depth bound of the Karras tree: every level down adds at least one common
+// bit of the (3b + 32)-bit extended key, so depth <= 63 + 32 for b = 21.
+constexpr int kMaxDepth = 96;
+
+}  // namespace clr
+
+// Builder handle: the scratch pool and what the last build left in it.
+struct clr_lbvh {
+    uint32_t capacity = 0;
+    void* pool = nullptr;
+    size_t pool_bytes = 0;
+    void* keys[2] = {nullptr, nullptr};     // sort ping-pong (up to 8 B per key)
+    uint32_t* vals[2] = {nullptr, nullptr};  // triangle ids riding with the keys
+    uint32_t* parent_leaf = nullptr;         // leaf -> internal parent
+    uint32_t* parent_inner = nullptr;        // internal -> parent | child slot << 31
+    unsigned int* counters = nullptr;        // refit arrival counters
+    void* zero_region = nullptr;             // cleared once per build:
+    size_t zero_bytes = 0;                   //   hist, status, tile_ctr, boxw
+    unsigned int* hist = nullptr;            // [pass][256] digit counts
+    unsigned int* status = nullptr;          // [pass][tile][256] look-back words
+    size_t status_stride = 0;
+    unsigned int* tile_ctr = nullptr;        // [pass] dynamic tile counter
+    unsigned int* boxw = nullptr;            // scene box, ordered-uint encoded
+    uint32_t last_n = 0, last_bits = 0;
+    int final_buf = 0;                       // ping-pong side holding sorted data
+    // profiling (clr_lbvh_set_profiling)
+    static constexpr int kMaxTimed = 16;
+    bool profiling = false;
+    int num_timed = 0;
+    cudaEvent_t ev[kMaxTimed + 1] = {};
+    const char* ev_name[kMaxTimed] = {};
+};

@@ -1,0 +1,107 @@
+// Device-side ray/box and ray/triangle tests and node access, shared by the
+// traversal kernels and the path tracer.  Every float operation is rounded
+// separately (common.cuh), matching the reference's expressions.
+#pragma once
+
+#include "common.cuh"
+
+namespace clr {
+
+// Depth bound of the radix tree plus one (3b + 32 levels for b <= 21).
+constexpr int kStackSize = 96;
+
+struct Ray {
+    float ox, oy, oz, tmax;
+    float dx, dy, dz;
+};
+
+__device__ __forceinline__ Ray load_ray(const float4* rays, uint32_t r) {
+    const float4 a = __ldg(rays + 2u * r), b = __ldg(rays + 2u * r + 1u);
+    return Ray{a.x, a.y, a.z, a.w, b.x, b.y, b.z};
+}
+
+// rayAABBIntersection (OpenCL/bvh_traversal.cl:160-179), Woo's outside-plane
+// test.  Returns the part of the test that does not depend on the bound;
+// `entry` receives the entry distance maxt (-inf when the origin is inside),
+// and the full test is  result && !(entry > tBound).
+__device__ __forceinline__ bool box_test(float mnx, float mny, float mnz, float mxx, float mxy, float mxz,
+                                         const Ray& r, float& entry) {
+    const bool lx = r.ox < mnx, ux = r.ox > mxx;
+    const bool ly = r.oy < mny, uy = r.oy > mxy;
+    const bool lz = r.oz < mnz, uz = r.oz > mxz;
+    if (!(lx | ux | ly | uy | lz | uz)) {
+        entry = -INFINITY;
+        return true;
+    }
+    const float cx = lx ? mnx : (ux ? mxx : 0.0f);
+    const float cy = ly ? mny : (uy ? mxy : 0.0f);
+    const float cz = lz ? mnz : (uz ? mxz : 0.0f);
+    const float tx = ((lx | ux) && r.dx != 0.0f) ? fdiv(fsub(cx, r.ox), r.dx) : -1.0f;
+    const float ty = ((ly | uy) && r.dy != 0.0f) ? fdiv(fsub(cy, r.oy), r.dy) : -1.0f;
+    const float tz = ((lz | uz) && r.dz != 0.0f) ? fdiv(fsub(cz, r.oz), r.dz) : -1.0f;
+    const float maxt = fmaxf(tx, fmaxf(ty, tz));
+    entry = maxt;
+    if (maxt < 0.0f) return false;
+    const float qx = fadd(r.ox, fmul(maxt, r.dx));
+    const float qy = fadd(r.oy, fmul(maxt, r.dy));
+    const float qz = fadd(r.oz, fmul(maxt, r.dz));
+    const bool hx = (qx >= mnx && qx <= mxx) || tx == maxt;
+    const bool hy = (qy >= mny && qy <= mxy) || ty == maxt;
+    const bool hz = (qz >= mnz && qz <= mxz) || tz == maxt;
+    return hx && hy && hz;
+}
+
+// rayTriangleIntersection (OpenCL/bvh_traversal.cl:54-108), Moller-Trumbore
+// with |det| < 1e-6 rejected and a hit at tt > t rejected (so an equal-t hit
+// tested later wins).  Record = {p0, id}, {p1-p0}, {p2-p0}.
+__device__ __forceinline__ bool tri_test(const float4 a, const float4 e1, const float4 e2, const Ray& r, float& t,
+                                         float* b1_out = nullptr, float* b2_out = nullptr) {
+    const float px = fsub(fmul(r.dy, e2.z), fmul(r.dz, e2.y));
+    const float py = fsub(fmul(r.dz, e2.x), fmul(r.dx, e2.z));
+    const float pz = fsub(fmul(r.dx, e2.y), fmul(r.dy, e2.x));
+    const float det = dot3(e1.x, e1.y, e1.z, px, py, pz);
+    if (det > -0.000001f && det < 0.000001f) return false;
+    const float invDet = fdiv(1.0f, det);
+    const float dx = fsub(r.ox, a.x), dy = fsub(r.oy, a.y), dz = fsub(r.oz, a.z);
+    const float b1 = fmul(dot3(dx, dy, dz, px, py, pz), invDet);
+    if (b1 < 0.0f || b1 > 1.0f) return false;
+    const float qx = fsub(fmul(dy, e1.z), fmul(dz, e1.y));
+    const float qy = fsub(fmul(dz, e1.x), fmul(dx, e1.z));
+    const float qz = fsub(fmul(dx, e1.y), fmul(dy, e1.x));
+    const float b2 = fmul(dot3(r.dx, r.dy, r.dz, qx, qy, qz), invDet);
+    if (b2 < 0.0f || fadd(b1, b2) > 1.0f) return false;
+    const float tt = fmul(dot3(e2.x, e2.y, e2.z, qx, qy, qz), invDet);
+    if (tt < 0.0f || tt > t) return false;
+    t = tt;
+    if (b1_out) *b1_out = b1;
+    if (b2_out) *b2_out = b2;
+    return true;
+}
+
+__device__ __forceinline__ bool tri_hit(const float4* __restrict__ tris, uint32_t leaf, const Ray& r, float& t,
+                                        uint32_t& id) {
+    const float4 a = __ldg(tris + 3u * leaf), b = __ldg(tris + 3u * leaf + 1u), c = __ldg(tris + 3u * leaf + 2u);
+    if (tri_test(a, b, c, r, t)) {
+        id = __float_as_uint(a.w);
+        return true;
+    }
+    return false;
+}
+
+struct NodeBoxes {
+    float b0[6], b1[6];
+    uint32_t ref0, ref1;
+};
+
+__device__ __forceinline__ NodeBoxes load_node(const float4* __restrict__ nodes, uint32_t i) {
+    const float4 a = __ldg(nodes + 4u * i), b = __ldg(nodes + 4u * i + 1u), c = __ldg(nodes + 4u * i + 2u),
+                 d = __ldg(nodes + 4u * i + 3u);
+    NodeBoxes nb;
+    nb.b0[0] = a.x; nb.b0[1] = a.y; nb.b0[2] = a.z; nb.b0[3] = a.w; nb.b0[4] = b.x; nb.b0[5] = b.y;
+    nb.b1[0] = b.z; nb.b1[1] = b.w; nb.b1[2] = c.x; nb.b1[3] = c.y; nb.b1[4] = c.z; nb.b1[5] = c.w;
+    nb.ref0 = __float_as_uint(d.x);
+    nb.ref1 = __float_as_uint(d.y);
+    return nb;
+}
+
+}  // namespace clr

@@ -1,0 +1,154 @@
+"""Host-side mirror of the reference's LBVH builder and ray queries.
+
+``LBVHBuilder(num_faces).perform(vertices, faces, num_faces, bits)`` follows
+``LBVHBuilder::LBVHBuilder`` / ``LBVHBuilder::perform``
+(OpenCL_PathTracer/LBVHBuilder.h:70-74): the builder owns a scratch pool that
+grows on demand, the caller owns inputs and outputs.  ``trace_closest`` and
+``trace_shadow`` replace ``rayIntersection`` (OpenCL/bvh_traversal.cl:182-215)
+for batches of rays.
+
+Device memory and streams come from PyTorch; all compute runs in
+``libclear_gb300.so`` through its C ABI.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import torch
+
+from . import _lib
+from ._lib import ClrBvh, call
+
+
+def _ptr(t: torch.Tensor | None):
+    return None if t is None else C.c_void_p(t.data_ptr())
+
+
+def _stream(device) -> C.c_void_p:
+    return C.c_void_p(torch.cuda.current_stream(device).cuda_stream)
+
+
+def _f32(t: torch.Tensor, device) -> torch.Tensor:
+    t = t.to(device=device, dtype=torch.float32)
+    return t.contiguous()
+
+
+class BVH:
+    """A built BVH: child-box nodes, leaf-ordered triangle records, root box."""
+
+    def __init__(self, num_tris: int, device):
+        self.device = torch.device(device)
+        n = int(num_tris)
+        self.nodes = torch.empty(max(n - 1, 1) * _lib.NODE_BYTES, dtype=torch.uint8, device=self.device)
+        self.tris = torch.empty(max(n, 1) * _lib.TRI_BYTES, dtype=torch.uint8, device=self.device)
+        self.root_box = torch.zeros(8, dtype=torch.float32, device=self.device)
+        self.c = ClrBvh(n, 0, self.nodes.data_ptr(), self.tris.data_ptr(), self.root_box.data_ptr())
+
+    @property
+    def num_tris(self) -> int:
+        return self.c.num_tris
+
+    @property
+    def bits_per_dim(self) -> int:
+        return self.c.bits_per_dim
+
+
+class LBVHBuilder:
+    def __init__(self, num_faces: int, device="cuda"):
+        self.device = torch.device(device)
+        if self.device.type != "cuda":
+            raise RuntimeError("LBVHBuilder needs a CUDA device; there is no CPU path")
+        with torch.cuda.device(self.device):
+            h = C.c_void_p()
+            call("clr_lbvh_create", C.c_uint32(max(int(num_faces), 1)), C.byref(h))
+        self._h = h
+
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            _lib.lib().clr_lbvh_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def perform(self, vertices, faces, num_faces: int, num_bits_per_dim: int = 10,
+                out: BVH | None = None) -> BVH:
+        """Build the LBVH.  vertices = (vx, vy, vz) float32 tensors; faces =
+        (num_faces, 3) integer tensor of vertex indices, or None for an
+        unindexed soup (vertex k of triangle t at 3t+k)."""
+        vx, vy, vz = (_f32(v, self.device) for v in vertices)
+        tri = None
+        if faces is not None:
+            tri = faces.to(device=self.device, dtype=torch.int32).contiguous()
+        n = int(num_faces)
+        bvh = out if out is not None and out.num_tris == n else BVH(n, self.device)
+        with torch.cuda.device(self.device):
+            call("clr_lbvh_build", self._h, _ptr(vx), _ptr(vy), _ptr(vz), _ptr(tri), C.c_uint32(n),
+                 C.c_uint32(int(num_bits_per_dim)), C.byref(bvh.c), _stream(self.device))
+        bvh._inputs = (vx, vy, vz, tri)  # keep alive until the stream has consumed them
+        return bvh
+
+    def set_profiling(self, enable: bool) -> None:
+        call("clr_lbvh_set_profiling", self._h, 1 if enable else 0)
+
+    def pass_times(self) -> list[tuple[str, float]]:
+        """(kernel, ms) of the last build; needs set_profiling(True)."""
+        ms = (C.c_float * 16)()
+        names = (C.c_char_p * 16)()
+        cnt = C.c_int(0)
+        call("clr_lbvh_pass_times", self._h, ms, names, 16, C.byref(cnt))
+        return [(names[i].decode(), float(ms[i])) for i in range(cnt.value)]
+
+    def export_reference(self, bvh: BVH) -> dict:
+        """The last build in the reference's 48-byte node layouts plus the
+        sorted triangle order and Morton keys (for parity checks)."""
+        n = bvh.num_tris
+        dev = self.device
+        out = {
+            "inodes": torch.zeros(max(n - 1, 0) * _lib.REF_NODE_BYTES, dtype=torch.uint8, device=dev),
+            "lnodes": torch.zeros(n * _lib.REF_NODE_BYTES, dtype=torch.uint8, device=dev),
+            "parents": torch.zeros(max(2 * n - 1, 0), dtype=torch.int32, device=dev),
+            "sorted_idx": torch.zeros(n, dtype=torch.int32, device=dev),
+            "keys": torch.zeros(n, dtype=torch.int64, device=dev),
+        }
+        with torch.cuda.device(dev):
+            call("clr_lbvh_export_reference", self._h, C.byref(bvh.c),
+                 _ptr(out["inodes"]) if n > 1 else None, _ptr(out["lnodes"]) if n else None,
+                 _ptr(out["parents"]) if n else None, _ptr(out["sorted_idx"]) if n else None,
+                 _ptr(out["keys"]) if n else None, _stream(dev))
+        return out
+
+
+def _rays(rays: torch.Tensor, device) -> torch.Tensor:
+    r = rays.to(device=device, dtype=torch.float32).contiguous().view(-1, 8)
+    return r
+
+
+def trace_closest(bvh: BVH, rays: torch.Tensor, hit_id: torch.Tensor | None = None,
+                  hit_t: torch.Tensor | None = None):
+    """Closest hit for rays packed {ox,oy,oz,tmax,dx,dy,dz,0}.  Returns
+    (hit_id int32 [-1 = miss], hit_t float32)."""
+    r = _rays(rays, bvh.device)
+    m = r.shape[0]
+    if hit_id is None:
+        hit_id = torch.empty(m, dtype=torch.int32, device=bvh.device)
+    if hit_t is None:
+        hit_t = torch.empty(m, dtype=torch.float32, device=bvh.device)
+    with torch.cuda.device(bvh.device):
+        call("clr_trace_closest", C.byref(bvh.c), _ptr(r), C.c_uint32(m), _ptr(hit_id), _ptr(hit_t),
+             _stream(bvh.device))
+    return hit_id, hit_t
+
+
+def trace_shadow(bvh: BVH, rays: torch.Tensor, occluded: torch.Tensor | None = None):
+    """Any-hit query: 1 where a triangle is hit at 0 <= t <= tmax."""
+    r = _rays(rays, bvh.device)
+    m = r.shape[0]
+    if occluded is None:
+        occluded = torch.empty(m, dtype=torch.uint8, device=bvh.device)
+    with torch.cuda.device(bvh.device):
+        call("clr_trace_shadow", C.byref(bvh.c), _ptr(r), C.c_uint32(m), _ptr(occluded), _stream(bvh.device))
+    return occluded

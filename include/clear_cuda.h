@@ -1,0 +1,145 @@
+/*
+ * clear_cuda.h -- C ABI of the GB300 (sm_103a) LBVH build, BVH traversal and
+ * path tracer.
+ *
+ * Conventions (all entry points):
+ *   - return an int status (CLR_OK = 0); no C++ exception crosses the ABI;
+ *     clr_last_error_string() describes the last failure of the calling thread;
+ *   - every data pointer is a DEVICE pointer owned by the caller, unless the
+ *     parameter says "host";
+ *   - `stream` is a cudaStream_t passed as void* (NULL = legacy default
+ *     stream); work is enqueued asynchronously on it;
+ *   - a handle is not thread-safe, distinct handles are independent.
+ *
+ * Each declaration cites the reference (shocker-0x15/CLeaR) interface it
+ * replaces, as file:line within that project.
+ */
+#ifndef CLEAR_CUDA_H
+#define CLEAR_CUDA_H
+
+#include <stdint.h>
+
+#if defined(__GNUC__)
+#define CLR_API __attribute__((visibility("default")))
+#else
+#define CLR_API
+#endif
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum {
+    CLR_OK = 0,
+    CLR_EINVAL = 1,     /* bad argument */
+    CLR_ECUDA = 2,      /* a CUDA runtime call failed */
+    CLR_ENOMEM = 3,     /* device allocation failed */
+    CLR_ETIMEOUT = 4,   /* a bounded device-side wait gave up */
+    CLR_ESTACK = 5,     /* a traversal stack would have overflowed */
+    CLR_ECAPACITY = 6   /* a fixed-size buffer is too small */
+};
+
+/* Device-side error bits, read back with clr_device_status(). */
+#define CLR_DEVERR_SORT_TIMEOUT 0x1u  /* radix-sort look-back spin hit its limit */
+#define CLR_DEVERR_STACK        0x2u  /* traversal stack full (ray reported as miss) */
+#define CLR_DEVERR_REFIT        0x4u  /* refit climb exceeded the tree depth bound */
+#define CLR_DEVERR_QUEUE        0x8u  /* a wavefront queue or bounded wait failed */
+
+/* Byte sizes of the records below. */
+#define CLR_NODE_BYTES 64u      /* internal node: both child boxes + child refs */
+#define CLR_TRI_BYTES 48u       /* triangle record: p0, p1-p0, p2-p0, triangle id */
+#define CLR_REF_NODE_BYTES 48u  /* reference LBVH::InternalNode / LeafNode */
+
+/*
+ * A built BVH.  The caller allocates the three device buffers, sized
+ *   nodes    : max(num_tris - 1, 1) * CLR_NODE_BYTES   (root = node 0)
+ *   tris     : num_tris * CLR_TRI_BYTES                (in leaf = sorted order)
+ *   root_box : 8 floats {min x,y,z, 0, max x,y,z, 0}
+ * Node i (16 floats): child-0 box {minx,miny,minz,maxx,maxy,maxz},
+ * child-1 box, then two uint32 child references (bit 31 set = leaf index,
+ * clear = internal-node index) and two zero words.  Leaf i's triangle record
+ * is tris[i] = {p0.xyz, id, (p1-p0).xyz, 0, (p2-p0).xyz, 0}.
+ * Topology is that of the reference's Karras radix tree
+ * (OpenCL/lbvh_construction.cl:342-410): node i's children are the reference's
+ * InternalNode[i].c[0..1] with isChild[k] mapped to bit 31.
+ */
+typedef struct clr_bvh {
+    uint32_t num_tris;
+    uint32_t bits_per_dim;
+    void* nodes;
+    void* tris;
+    float* root_box;
+} clr_bvh;
+
+/* ------------------------------------------------------------ LBVH build */
+
+typedef struct clr_lbvh clr_lbvh;
+
+/* Replaces LBVHBuilder::LBVHBuilder(context, device, numFaces)
+ * (OpenCL_PathTracer/LBVHBuilder.h:70, LBVHBuilder.cpp:19-48): allocates the
+ * builder's scratch pool for up to `capacity` triangles on the current
+ * device.  The pool grows on demand in clr_lbvh_build, as the reference's
+ * does (LBVHBuilder.cpp:167-170). */
+CLR_API int clr_lbvh_create(uint32_t capacity, clr_lbvh** out);
+CLR_API int clr_lbvh_destroy(clr_lbvh* h);
+
+/* Replaces LBVHBuilder::perform(queue, vertices, faces, numFaces,
+ * numBitsPerDim, internalNodes, leafNodes, events, profiling)
+ * (OpenCL_PathTracer/LBVHBuilder.h:72-74, LBVHBuilder.cpp:160-375).
+ * Vertex k of triangle t is (vx,vy,vz)[tri[3t+k]], or [3t+k] when tri is
+ * NULL (unindexed soup).  bits_per_dim in [1, 21] (the reference uses 20 in
+ * main.cpp:365; 10 gives 30-bit keys).  Fills out->nodes/tris/root_box and
+ * sets out->num_tris and out->bits_per_dim.  No host synchronisation:
+ * the scene box stays on the device (the reference reads it back,
+ * LBVHBuilder.cpp:229). */
+CLR_API int clr_lbvh_build(clr_lbvh* h, const float* vx, const float* vy, const float* vz, const uint32_t* tri,
+                   uint32_t num_tris, uint32_t bits_per_dim, clr_bvh* out, void* stream);
+
+/* Parity/debug export of the last build of `h` into the reference layouts:
+ * inodes: (n-1) x 48 B LBVH::InternalNode, lnodes: n x 48 B LBVH::LeafNode
+ * (LBVHBuilder.h:17-29), parents: 2n-1 uint32 (leaves at [0,n), internal at
+ * [n,2n-1), lbvh_construction.cl:399-409; root entry = 0xFFFFFFFF),
+ * sorted_idx: n uint32, keys: n uint64 sorted Morton keys.  Any output may be
+ * NULL. */
+CLR_API int clr_lbvh_export_reference(clr_lbvh* h, const clr_bvh* bvh, void* inodes, void* lnodes, uint32_t* parents,
+                              uint32_t* sorted_idx, uint64_t* keys, void* stream);
+
+/* Per-pass timing of the build, the counterpart of the reference's
+ * `profiling` flag (LBVHBuilder.cpp:173-348, one event per pass).  When
+ * enabled, clr_lbvh_build records a CUDA event around every kernel it
+ * launches; clr_lbvh_pass_times then waits for the last build and returns
+ * the per-kernel times in ms, in launch order: scene box, Morton, each sort
+ * pass, Karras, refit.  names (optional) receives a static label per pass. */
+CLR_API int clr_lbvh_set_profiling(clr_lbvh* h, int enable);
+CLR_API int clr_lbvh_pass_times(clr_lbvh* h, float* ms, const char** names, int max_passes, int* num_passes);
+
+/* ------------------------------------------------------------- traversal */
+
+/* rays: 8 floats per ray {ox,oy,oz,tmax, dx,dy,dz,0} (32 B, 16-B aligned).
+ *
+ * Closest hit.  Replaces rayIntersection (OpenCL/bvh_traversal.cl:182-215):
+ * the same depth-first visiting order and the same triangle/box arithmetic,
+ * so hit ids and t are those of the reference (with uint32 triangle ids; the
+ * reference truncates to ushort, bvh_traversal.cl:56).  t starts at tmax.
+ * Miss: hit_id = 0xFFFFFFFF, hit_t = tmax. */
+CLR_API int clr_trace_closest(const clr_bvh* bvh, const float* rays, uint32_t num_rays, uint32_t* hit_id, float* hit_t,
+                      void* stream);
+
+/* Shadow (any-hit) query; the reference shoots a closest-hit ray for this
+ * (OpenCL/pathtracer.cl:119-122).  occluded[r] = 1 when a triangle is hit at
+ * 0 <= t <= tmax. */
+CLR_API int clr_trace_shadow(const clr_bvh* bvh, const float* rays, uint32_t num_rays, uint8_t* occluded, void* stream);
+
+/* ----------------------------------------------------------------- misc */
+
+/* Reads (and optionally clears) the device error bits CLR_DEVERR_* of the
+ * current device.  Synchronises the device. */
+CLR_API int clr_device_status(uint32_t* bits, int clear);
+
+/* Thread-local description of the last failure. */
+CLR_API const char* clr_last_error_string(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* CLEAR_CUDA_H */

@@ -1,0 +1,226 @@
+"""ctypes front end of the CPU oracle (test infrastructure only).
+
+Only ``tests/``, ``__graft_entry__.smoke()`` and the CPU-baseline leg of
+``bench.py`` import this package; the shipped library never does.
+
+``lbvh_build`` / ``trace_closest`` / ``trace_shadow`` / ``midbvh_build`` wrap
+the C restatement in ``oracle/lbvh_oracle.c``; ``ref_*`` wrap the reference's
+own CPU code compiled in place (``oracle/_ref``), present only where the
+reference checkout was available at build time.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from pathlib import Path
+
+import numpy as np
+
+from .build_oracle import build_oracle, build_ref
+
+HERE = Path(__file__).resolve().parent
+
+INODE_DTYPE = np.dtype([("min", "<f4", 4), ("max", "<f4", 4), ("isChild", "u1", 2), ("pad0", "u1", 2),
+                        ("c", "<u4", 2), ("pad1", "u1", 4)])
+LNODE_DTYPE = np.dtype([("min", "<f4", 4), ("max", "<f4", 4), ("objIdx", "<u4"), ("pad", "u1", 12)])
+BVHNODE_DTYPE = np.dtype([("min", "<f4", 4), ("max", "<f4", 4), ("children", "<u4", 2), ("pad", "<u4", 2)])
+assert INODE_DTYPE.itemsize == 48 and LNODE_DTYPE.itemsize == 48 and BVHNODE_DTYPE.itemsize == 48
+
+_lib = None
+_ref_lbvh = None
+_ref_mid = None
+
+
+def _p(a):
+    return None if a is None else a.ctypes.data_as(C.c_void_p)
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        _lib = C.CDLL(str(build_oracle()))
+        _lib.orc_lbvh_build.restype = C.c_int
+        _lib.orc_trace_closest.restype = C.c_int
+        _lib.orc_trace_shadow.restype = C.c_int
+        _lib.orc_midbvh_build.restype = C.c_int64
+        _lib.orc_trace_closest_mid.restype = C.c_int
+        _lib.orc_morton_key.restype = C.c_uint64
+    return _lib
+
+
+def _f32(a):
+    return np.ascontiguousarray(a, dtype=np.float32)
+
+
+def _u32(a):
+    return None if a is None else np.ascontiguousarray(a, dtype=np.uint32)
+
+
+class OracleBVH:
+    """Reference-layout LBVH produced by the restatement."""
+
+    def __init__(self, inodes, lnodes, parents, sorted_idx, q, scene_box, bits):
+        self.inodes, self.lnodes, self.parents = inodes, lnodes, parents
+        self.sorted_idx, self.q, self.scene_box, self.bits = sorted_idx, q, scene_box, bits
+
+    def keys(self):
+        """3b-bit Morton keys of the triangles in sorted order (uint64)."""
+        return morton_keys(self.q[self.sorted_idx], self.bits)
+
+
+def morton_keys(q, bits):
+    q = np.asarray(q, dtype=np.uint64)
+    k = np.zeros(q.shape[0], dtype=np.uint64)
+    for b in range(bits):
+        d = ((q[:, 0] >> np.uint64(b)) & np.uint64(1)) | (((q[:, 1] >> np.uint64(b)) & np.uint64(1)) << np.uint64(1)) \
+            | (((q[:, 2] >> np.uint64(b)) & np.uint64(1)) << np.uint64(2))
+        k |= d << np.uint64(3 * b)
+    return k
+
+
+def lbvh_build(vx, vy, vz, tri, n, bits=10) -> OracleBVH:
+    vx, vy, vz, tri = _f32(vx), _f32(vy), _f32(vz), _u32(tri)
+    inodes = np.zeros(max(n - 1, 0), dtype=INODE_DTYPE)
+    lnodes = np.zeros(n, dtype=LNODE_DTYPE)
+    parents = np.zeros(max(2 * n - 1, 0), dtype=np.uint32)
+    sidx = np.zeros(n, dtype=np.uint32)
+    q = np.zeros((n, 3), dtype=np.uint32)
+    box = np.zeros(6, dtype=np.float32)
+    rc = lib().orc_lbvh_build(_p(vx), _p(vy), _p(vz), _p(tri), C.c_uint32(n), C.c_uint32(bits), _p(inodes),
+                              _p(lnodes), _p(parents), _p(sidx), _p(q), _p(box))
+    if rc != 0:
+        raise RuntimeError(f"orc_lbvh_build failed: {rc}")
+    return OracleBVH(inodes, lnodes, parents, sidx, q, box, bits)
+
+
+def trace_closest(vx, vy, vz, tri, bvh: OracleBVH, rays, stats=False):
+    vx, vy, vz, tri = _f32(vx), _f32(vy), _f32(vz), _u32(tri)
+    rays = _f32(rays).reshape(-1, 8)
+    nr = rays.shape[0]
+    ids = np.zeros(nr, dtype=np.uint32)
+    ts = np.zeros(nr, dtype=np.float32)
+    st = np.zeros((nr, 3), dtype=np.uint32) if stats else None
+    rc = lib().orc_trace_closest(_p(vx), _p(vy), _p(vz), _p(tri), _p(bvh.inodes), _p(bvh.lnodes),
+                                 C.c_uint32(len(bvh.lnodes)), _p(rays), C.c_uint32(nr), _p(ids), _p(ts), _p(st))
+    if rc != 0:
+        raise RuntimeError(f"orc_trace_closest failed: {rc}")
+    return (ids, ts, st) if stats else (ids, ts)
+
+
+def trace_shadow(vx, vy, vz, tri, bvh: OracleBVH, rays):
+    vx, vy, vz, tri = _f32(vx), _f32(vy), _f32(vz), _u32(tri)
+    rays = _f32(rays).reshape(-1, 8)
+    nr = rays.shape[0]
+    occ = np.zeros(nr, dtype=np.uint8)
+    rc = lib().orc_trace_shadow(_p(vx), _p(vy), _p(vz), _p(tri), _p(bvh.inodes), _p(bvh.lnodes),
+                                C.c_uint32(len(bvh.lnodes)), _p(rays), C.c_uint32(nr), _p(occ))
+    if rc != 0:
+        raise RuntimeError(f"orc_trace_shadow failed: {rc}")
+    return occ
+
+
+def midbvh_build(vx, vy, vz, tri, n):
+    vx, vy, vz, tri = _f32(vx), _f32(vy), _f32(vz), _u32(tri)
+    nodes = np.zeros(max(2 * n - 1, 1), dtype=BVHNODE_DTYPE)
+    cnt = lib().orc_midbvh_build(_p(vx), _p(vy), _p(vz), _p(tri), C.c_uint32(n), _p(nodes))
+    if cnt < 0:
+        raise RuntimeError("orc_midbvh_build failed")
+    return nodes[:cnt]
+
+
+def trace_closest_mid(vx, vy, vz, tri, nodes, n, rays):
+    vx, vy, vz, tri = _f32(vx), _f32(vy), _f32(vz), _u32(tri)
+    rays = _f32(rays).reshape(-1, 8)
+    nr = rays.shape[0]
+    ids = np.zeros(nr, dtype=np.uint32)
+    ts = np.zeros(nr, dtype=np.float32)
+    rc = lib().orc_trace_closest_mid(_p(vx), _p(vy), _p(vz), _p(tri), _p(nodes), C.c_uint32(n), _p(rays),
+                                     C.c_uint32(nr), _p(ids), _p(ts))
+    if rc != 0:
+        raise RuntimeError(f"orc_trace_closest_mid failed: {rc}")
+    return ids, ts
+
+
+# --------------------------------------------------------------- reference
+
+
+def ref_available() -> bool:
+    return bool(build_ref())
+
+
+def _ref(name):
+    global _ref_lbvh, _ref_mid
+    libs = {p.name: p for p in build_ref()}
+    if not libs:
+        raise RuntimeError("reference checkout not available; oracle/_ref not built")
+    if name == "lbvh":
+        if _ref_lbvh is None:
+            _ref_lbvh = C.CDLL(str(libs["libref_lbvh.so"]))
+        return _ref_lbvh
+    if _ref_mid is None:
+        _ref_mid = C.CDLL(str(libs["libref_mid.so"]))
+        _ref_mid.ref_midbvh_build.restype = C.c_int64
+    return _ref_mid
+
+
+def verts16(vx, vy, vz):
+    """float3 vertex array with the 16-byte stride of cl_float3."""
+    v = np.zeros((len(vx), 4), dtype=np.float32)
+    v[:, 0], v[:, 1], v[:, 2] = vx, vy, vz
+    return v
+
+
+FACE_DTYPE = np.dtype([("p", "<u4", 3), ("vn", "<u4", 3), ("vt", "<u4", 3), ("uv", "<u4", 3),
+                       ("alphaTexPtr", "<u4"), ("matPtr", "<u2"), ("lightPtr", "<u2")])
+assert FACE_DTYPE.itemsize == 56
+
+
+def faces_from_tri(tri, n):
+    f = np.zeros(n, dtype=FACE_DTYPE)
+    f["p"] = np.asarray(tri, dtype=np.uint32).reshape(n, 3) if tri is not None else np.arange(3 * n, dtype=np.uint32).reshape(n, 3)
+    f["vn"] = f["vt"] = f["uv"] = 0xFFFFFFFF
+    f["alphaTexPtr"] = 0xFFFFFFFF
+    f["matPtr"] = 0
+    f["lightPtr"] = 0xFFFF
+    return f
+
+
+def ref_trace_closest_lbvh(vx, vy, vz, tri, n, bvh: OracleBVH, rays):
+    v = verts16(vx, vy, vz)
+    faces = faces_from_tri(tri, n)
+    rays = _f32(rays).reshape(-1, 8)
+    nr = rays.shape[0]
+    ids = np.zeros(nr, dtype=np.uint32)
+    ts = np.zeros(nr, dtype=np.float32)
+    _ref("lbvh").ref_trace_closest_lbvh(_p(v), _p(faces), _p(bvh.inodes), _p(bvh.lnodes), _p(rays),
+                                        C.c_uint32(nr), _p(ids), _p(ts))
+    return ids, ts
+
+
+def ref_midbvh_build(vx, vy, vz, tri, n):
+    v = verts16(vx, vy, vz)
+    tri = _u32(tri) if tri is not None else np.arange(3 * n, dtype=np.uint32)
+    nodes = np.zeros(max(2 * n - 1, 1), dtype=BVHNODE_DTYPE)
+    cnt = _ref("mid").ref_midbvh_build(_p(v), _p(tri), C.c_uint32(n), _p(nodes))
+    return nodes[:cnt]
+
+
+def ref_trace_closest_mid(vx, vy, vz, tri, n, nodes, rays):
+    v = verts16(vx, vy, vz)
+    faces = faces_from_tri(tri, n)
+    rays = _f32(rays).reshape(-1, 8)
+    nr = rays.shape[0]
+    ids = np.zeros(nr, dtype=np.uint32)
+    ts = np.zeros(nr, dtype=np.float32)
+    _ref("mid").ref_trace_closest_mid(_p(v), _p(faces), _p(nodes), _p(rays), C.c_uint32(nr), _p(ids), _p(ts))
+    return ids, ts
+
+
+def ref_render(scene_blobs: dict, inodes, lnodes, rand_states, pixels, width, height, y0, y1, spp):
+    """sim::pathtracing over rows [y0, y1); rand_states (u32[4*W*H]) and
+    pixels (f32[W*H*4]) are updated in place."""
+    b = scene_blobs
+    _ref("lbvh").ref_render(_p(b["vertices"]), _p(b["normals"]), _p(b["tangents"]), _p(b["uvs"]),
+                            _p(b["faces"]), _p(b["lights"]), _p(b["materials"]), _p(b["textures"]),
+                            _p(b["others"]), _p(inodes), _p(lnodes), _p(rand_states), _p(pixels),
+                            C.c_uint32(width), C.c_uint32(height), C.c_uint32(y0), C.c_uint32(y1),
+                            C.c_uint32(spp))

@@ -1,0 +1,70 @@
+"""Build recipe for the CPU oracle (test infrastructure only).
+
+* ``oracle/liboracle.so`` -- the C restatement in ``oracle/lbvh_oracle.c``.
+  Built everywhere (here and on the GPU host) with ``-ffp-contract=off`` so the
+  reference's float expressions round exactly as written.
+* ``oracle/_ref/libref_lbvh.so`` and ``oracle/_ref/libref_mid.so`` -- the
+  reference's own CPU code (``OpenCL_PathTracer/Equivalent/sim_*.hpp`` and
+  ``OpenCL_PathTracer/BVH.hpp``) compiled in place from a reference checkout
+  with the stand-in headers of ``oracle/ref_stubs``.  Built only when the
+  checkout exists (``CLEAR_REFERENCE_DIR``, default ``/root/reference``);
+  nothing is copied out of it.
+"""
+from __future__ import annotations
+
+import os
+import subprocess
+import sys
+from pathlib import Path
+
+HERE = Path(__file__).resolve().parent
+REF_DIR = Path(os.environ.get("CLEAR_REFERENCE_DIR", "/root/reference"))
+CFLAGS = ["-O2", "-fPIC", "-shared", "-ffp-contract=off", "-fno-fast-math"]
+
+
+def _run(cmd: list[str]) -> None:
+    res = subprocess.run(cmd, capture_output=True, text=True)
+    if res.returncode != 0:
+        raise RuntimeError(f"oracle build failed: {' '.join(cmd)}\n{res.stderr}")
+
+
+def _stale(out: Path, srcs: list[Path]) -> bool:
+    if not out.exists():
+        return True
+    t = out.stat().st_mtime
+    return any(s.stat().st_mtime > t for s in srcs if s.exists())
+
+
+def build_oracle() -> Path:
+    out = HERE / "liboracle.so"
+    src = HERE / "lbvh_oracle.c"
+    if _stale(out, [src, Path(__file__)]):
+        _run(["gcc", "-std=c11", *CFLAGS, str(src), "-o", str(out), "-lm"])
+    return out
+
+
+def build_ref() -> list[Path]:
+    """Compile the reference's CPU code if its sources are present."""
+    eq = REF_DIR / "OpenCL_PathTracer" / "Equivalent"
+    if not eq.is_dir():
+        return []
+    outdir = HERE / "_ref"
+    outdir.mkdir(exist_ok=True)
+    src = HERE / "ref_harness.cpp"
+    stubs = HERE / "ref_stubs"
+    deps = [src, *stubs.iterdir(), Path(__file__)]
+    built = []
+    for name, defs in (("libref_lbvh.so", ["-D__USE_LBVH"]), ("libref_mid.so", [])):
+        out = outdir / name
+        if _stale(out, deps):
+            _run(["g++", "-std=c++17", "-w", *CFLAGS, *defs, f"-I{stubs}", f"-I{eq}",
+                  f"-I{REF_DIR / 'OpenCL_PathTracer'}", str(src), "-o", str(out)])
+        built.append(out)
+    return built
+
+
+if __name__ == "__main__":
+    print(build_oracle())
+    for p in build_ref():
+        print(p)
+    sys.exit(0)

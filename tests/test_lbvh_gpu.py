@@ -1,0 +1,153 @@
+"""GPU parity of the LBVH build and the traversal kernels against the oracle.
+
+Integer outputs (sorted order, keys, topology, parents, leaf objects, hit ids)
+must be bit-exact; boxes and hit distances are compared with float equality
+(the kernels use the reference's operations in the reference's order, so they
+are expected to be identical; +0 and -0 compare equal).
+"""
+import numpy as np
+import pytest
+import torch
+
+import oracle
+from clear_gb300 import _lib, lbvh
+from clear_gb300 import workloads as W
+
+MISS = 0xFFFFFFFF
+
+pytestmark = pytest.mark.gpu
+
+
+def gpu_build(cuda, vx, vy, vz, tri, n, bits):
+    b = lbvh.LBVHBuilder(max(n, 1), cuda)
+    v = tuple(torch.from_numpy(np.asarray(a)).to(cuda) for a in (vx, vy, vz))
+    t = None if tri is None else torch.from_numpy(np.asarray(tri, dtype=np.int32)).to(cuda)
+    bvh = b.perform(v, t, n, bits)
+    ref = {k: x.cpu().numpy() for k, x in b.export_reference(bvh).items()}
+    torch.cuda.synchronize()
+    return b, bvh, ref
+
+
+def assert_build_equal(ref, ob: oracle.OracleBVH, n):
+    np.testing.assert_array_equal(ref["sorted_idx"].view(np.uint32), ob.sorted_idx)
+    np.testing.assert_array_equal(ref["keys"].view(np.uint64), ob.keys())
+    ln = ref["lnodes"].view(oracle.LNODE_DTYPE)
+    np.testing.assert_array_equal(ln["objIdx"], ob.lnodes["objIdx"])
+    assert (ln["min"][:, :3] == ob.lnodes["min"][:, :3]).all()
+    assert (ln["max"][:, :3] == ob.lnodes["max"][:, :3]).all()
+    if n >= 2:
+        inn = ref["inodes"].view(oracle.INODE_DTYPE)
+        np.testing.assert_array_equal(inn["c"], ob.inodes["c"])
+        np.testing.assert_array_equal(inn["isChild"], ob.inodes["isChild"])
+        assert (inn["min"][:, :3] == ob.inodes["min"][:, :3]).all()
+        assert (inn["max"][:, :3] == ob.inodes["max"][:, :3]).all()
+        par = ref["parents"].view(np.uint32)
+        keep = np.ones(2 * n - 1, dtype=bool)
+        keep[n] = False  # the root has no parent (unwritten in the reference)
+        np.testing.assert_array_equal(par[keep], ob.parents[keep])
+
+
+def no_device_errors():
+    assert _lib.device_status(clear=True) == 0
+
+
+@pytest.mark.parametrize("bits", [10, 20])
+@pytest.mark.parametrize("n", [1, 2, 3, 5, 63, 64, 65, 1000, 2047, 2048, 2049, 4095, 4096, 4097, 65543, 300001])
+def test_build_parity(cuda, n, bits):
+    vx, vy, vz = W.triangle_soup(n, seed=1000 + n)
+    b, bvh, ref = gpu_build(cuda, vx, vy, vz, None, n, bits)
+    ob = oracle.lbvh_build(vx, vy, vz, None, n, bits)
+    assert_build_equal(ref, ob, n)
+    rb = bvh.root_box.cpu().numpy()
+    assert (rb[:3] == ob.scene_box[:3]).all() and (rb[4:7] == ob.scene_box[3:]).all()
+    no_device_errors()
+
+
+def test_build_parity_indexed_and_planar(cuda):
+    # indexed input with shared vertices, duplicate centroids and a flat z axis
+    rng = np.random.default_rng(5)
+    nv, n = 3000, 8000
+    vx = rng.random(nv).astype(np.float32)
+    vy = rng.random(nv).astype(np.float32)
+    vz = np.zeros(nv, dtype=np.float32)
+    tri = rng.integers(0, nv, size=(n, 3)).astype(np.uint32)
+    tri[:100] = tri[100:200]  # identical triangles -> equal keys
+    _, _, ref = gpu_build(cuda, vx, vy, vz, tri, n, 10)
+    ob = oracle.lbvh_build(vx, vy, vz, tri.reshape(-1), n, 10)
+    assert_build_equal(ref, ob, n)
+    no_device_errors()
+
+
+def test_build_is_deterministic_and_reusable(cuda):
+    n = 200000
+    vx, vy, vz = W.triangle_soup(n, seed=77)
+    b = lbvh.LBVHBuilder(1000, cuda)  # grows on demand
+    v = tuple(torch.from_numpy(a).to(cuda) for a in (vx, vy, vz))
+    bvh1 = b.perform(v, None, n, 10)
+    nodes1, tris1 = bvh1.nodes.clone(), bvh1.tris.clone()
+    bvh2 = b.perform(v, None, n, 10)
+    torch.cuda.synchronize()
+    assert torch.equal(nodes1, bvh2.nodes) and torch.equal(tris1, bvh2.tris)
+    no_device_errors()
+
+
+@pytest.mark.parametrize("n", [1, 2, 7, 5000, 300001])
+def test_trace_parity(cuda, n):
+    vx, vy, vz = W.triangle_soup(n, seed=2000 + n)
+    b, bvh, _ = gpu_build(cuda, vx, vy, vz, None, n, 10)
+    ob = oracle.lbvh_build(vx, vy, vz, None, n, 10)
+    rays = W.closest_rays(20000, seed=n)
+    rays[::7, 3] = 0.05  # some finite tmax
+    ids, ts = lbvh.trace_closest(bvh, torch.from_numpy(rays).to(cuda))
+    oids, ots = oracle.trace_closest(vx, vy, vz, None, ob, rays)
+    np.testing.assert_array_equal(ids.cpu().numpy().view(np.uint32), oids)
+    np.testing.assert_array_equal(ts.cpu().numpy(), ots)
+    srays = W.shadow_rays(20000, seed=n + 1)
+    occ = lbvh.trace_shadow(bvh, torch.from_numpy(srays).to(cuda)).cpu().numpy()
+    np.testing.assert_array_equal(occ, oracle.trace_shadow(vx, vy, vz, None, ob, srays))
+    no_device_errors()
+
+
+def test_trace_empty_scene_and_no_rays(cuda):
+    b = lbvh.LBVHBuilder(1, cuda)
+    e = torch.empty(0, dtype=torch.float32, device=cuda)
+    bvh = b.perform((e, e, e), None, 0, 10)
+    rays = torch.from_numpy(W.closest_rays(100, seed=1)).to(cuda)
+    ids, ts = lbvh.trace_closest(bvh, rays)
+    assert (ids.cpu().numpy().view(np.uint32) == MISS).all()
+    assert lbvh.trace_shadow(bvh, rays).sum().item() == 0
+    lbvh.trace_closest(bvh, rays[:0])
+    no_device_errors()
+
+
+def test_invalid_arguments_fail_loudly(cuda):
+    b = lbvh.LBVHBuilder(10, cuda)
+    vx, vy, vz = (torch.zeros(30, device=cuda) for _ in range(3))
+    with pytest.raises(_lib.ClrError):
+        b.perform((vx, vy, vz), None, 10, 0)
+    with pytest.raises(_lib.ClrError):
+        b.perform((vx, vy, vz), None, 10, 22)
+
+
+def test_full_size_properties(cuda):
+    """16 Mi triangles (the largest benchmark scene): properties that hold at
+    any size, plus bit-exact hits on a ray sample against the oracle tree."""
+    n = 1 << 24
+    vx, vy, vz = W.triangle_soup(n, seed=24)
+    b, bvh, ref = gpu_build(cuda, vx, vy, vz, None, n, 10)
+    keys = ref["keys"].view(np.uint64)
+    assert (keys[1:] >= keys[:-1]).all()
+    sidx = ref["sorted_idx"].view(np.uint32)
+    assert np.bincount(sidx, minlength=n).max() == 1
+    inn = ref["inodes"].view(oracle.INODE_DTYPE)
+    leaf_hits = np.bincount(inn["c"][inn["isChild"] == 1], minlength=n)
+    inner_hits = np.bincount(inn["c"][inn["isChild"] == 0], minlength=n - 1)
+    assert (leaf_hits == 1).all() and inner_hits[0] == 0 and (inner_hits[1:] == 1).all()
+    ob = oracle.lbvh_build(vx, vy, vz, None, n, 10)
+    assert_build_equal(ref, ob, n)
+    rays = W.closest_rays(50000, seed=3)
+    ids, ts = lbvh.trace_closest(bvh, torch.from_numpy(rays).to(cuda))
+    oids, ots = oracle.trace_closest(vx, vy, vz, None, ob, rays)
+    np.testing.assert_array_equal(ids.cpu().numpy().view(np.uint32), oids)
+    np.testing.assert_array_equal(ts.cpu().numpy(), ots)
+    no_device_errors()
