@@ -411,9 +411,13 @@ __global__ void __launch_bounds__(256) k_karras(const KeyT* __restrict__ keys, c
     const int commonR = delta(keys, nn, kbits, ki, gi, gi + 1);
     const int commonL = delta(keys, nn, kbits, ki, gi, gi - 1);
     const int d = commonR > commonL ? 1 : (commonR < commonL ? -1 : 0);
+    if (d == 0) {  // only possible if the keys were not sorted (a failed sort)
+        clr_raise(CLR_DEVERR_REFIT);
+        return;
+    }
     const int minNum = d > 0 ? commonL : commonR;
     int64_t lMax = 2;
-    while (delta(keys, nn, kbits, ki, gi, gi + lMax * d) > minNum) lMax <<= 1;
+    while (delta(keys, nn, kbits, ki, gi, gi + lMax * d) > minNum && lMax <= nn) lMax <<= 1;
     int64_t l = 0;
     for (int64_t t = lMax >> 1; t >= 1; t >>= 1)
         if (delta(keys, nn, kbits, ki, gi, gi + (l + t) * d) > minNum) l += t;
@@ -477,6 +481,7 @@ __global__ void __launch_bounds__(256) k_refit(float* __restrict__ nodes, const 
     // The k-th internal node on a leaf-to-root path has a common prefix of at
     // least k bits, so a climb never exceeds kMaxDepth steps.
     for (int step = 0; step < kMaxDepth; ++step) {
+        if (p >= n - 1) break;  // corrupt parent link: report, never index out of range
         __threadfence();  // publish the child box written by this thread
         if (atomicAdd(counters + p, 1u) == 0u) return;  // sibling not done yet
         __threadfence();  // observe the sibling's box
@@ -497,6 +502,7 @@ __global__ void __launch_bounds__(256) k_refit(float* __restrict__ nodes, const 
         }
         const uint32_t gp = parent_inner[p];
         const uint32_t slot = gp >> 31, q = gp & 0x7FFFFFFFu;
+        if (q >= n - 1) break;
         float2* dst = reinterpret_cast<float2*>(nodes + 16u * q + 6u * slot);
         __stcg(dst + 0, make_float2(u[0], u[1]));
         __stcg(dst + 1, make_float2(u[2], u[3]));

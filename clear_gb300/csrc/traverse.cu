@@ -39,7 +39,8 @@ __global__ void __launch_bounds__(kTraceThreads) k_trace_closest(const float4* _
         uint2 stack[kStackSize];
         int sp = 0;
         stack[sp++] = make_uint2(0u, __float_as_uint(entry));
-        while (sp > 0) {
+        // a valid tree visits each internal node at most once per ray
+        for (uint32_t guard = 0; sp > 0 && guard < n; ++guard) {
             --sp;
             const uint32_t node = stack[sp].x;
             if (__uint_as_float(stack[sp].y) > t) continue;  // the reference's bound test at pop
@@ -89,7 +90,7 @@ __global__ void __launch_bounds__(kTraceThreads) k_trace_shadow(const float4* __
         uint32_t stack[kStackSize];
         int sp = 0;
         stack[sp++] = 0u;
-        while (sp > 0 && !occ) {
+        for (uint32_t guard = 0; sp > 0 && !occ && guard < n; ++guard) {
             const uint32_t node = stack[--sp];
             const NodeBoxes nb = load_node(nodes, node);
             float e0, e1;
