@@ -1,0 +1,506 @@
+"""Scene description: the reference's byte-blob scene format, built on the host.
+
+Mirrors ``Scene`` (OpenCL_PathTracer/Scene.h:29-295, Scene.cpp:12-42) and
+``MaterialCreator`` (OpenCL_PathTracer/CreateFunctions.hpp:16-101,
+CreateFunctions.cpp:18-505).  The blobs (materials, textures, "other
+resources") have the reference's byte layout, read by the reference's render
+kernel (OpenCL/pathtracer.cl:25-46) and by this project's CUDA path tracer
+alike, so one encoder serves both.
+
+Deliberate differences from the reference's host code, each a defect there:
+  * The 2D environment distribution stores the marginal (row) distribution's
+    PDF/CDF offsets relative to its embedded ContinuousConsts1D, which is the
+    base the kernel adds them to (distribution.cl:296, 326); the reference
+    stores them relative to the enclosing 2D head (CreateFunctions.cpp:309-310),
+    8 bytes off.
+  * The light-power PMF has numItems entries; the reference's loop writes one
+    past the end (Scene.h:281-284).
+  * RGB8 images are stored with a 4-byte texel stride, which is what the
+    kernel's uchar3 reads use (texture.cl:72; OpenCL 3-vectors are 4 wide).
+  * createFloatCheckerBoardTexture tags its texture ColorProcedural as the
+    reference does (CreateFunctions.cpp:117), so evaluateFloatTexture reads 0
+    from it, as in the reference.
+"""
+from __future__ import annotations
+
+import math
+import struct
+
+import numpy as np
+
+FACE_DTYPE = np.dtype([("p", "<u4", 3), ("vn", "<u4", 3), ("vt", "<u4", 3), ("uv", "<u4", 3),
+                       ("alphaTexPtr", "<u4"), ("matPtr", "<u2"), ("lightPtr", "<u2")])
+NONE32 = 0xFFFFFFFF
+NONE16 = 0xFFFF
+
+# TextureType (TextureStructures.hpp)
+TEX_COLOR_CONSTANT, TEX_RGB8, TEX_RGBA8, TEX_RGBA16F, TEX_COLOR_PROCEDURAL, TEX_GRAY8, \
+    TEX_FLOAT_CONSTANT, TEX_FLOAT_IMAGE, TEX_FLOAT_PROCEDURAL = range(9)
+PROC_CHECKER, PROC_CHECKER_BUMP = 0, 1
+FRESNEL_NOOP, FRESNEL_CONDUCTOR, FRESNEL_DIELECTRIC = 0, 1, 2
+# MatElem (MaterialStructures.hpp)
+ME_DIFFUSE, ME_SPEC_R, ME_SPEC_T, ME_NEWWARD, ME_ASH_S, ME_ASH_D = range(6)
+LP_DIFFUSE = 0
+ENV_IMAGE = 0
+
+
+class Blob:
+    """Growable byte vector with the alignment rules of CLUtil::addDataAligned
+    / fillZerosAligned / align (CommonSources/clUtility.cpp:554-571)."""
+
+    def __init__(self, initial: bytes = b""):
+        self.b = bytearray(initial)
+
+    def __len__(self):
+        return len(self.b)
+
+    def align(self, a: int) -> int:
+        pad = (-len(self.b)) % a
+        self.b.extend(b"\0" * pad)
+        return len(self.b)
+
+    def add(self, data: bytes, a: int) -> int:
+        self.align(a)
+        off = len(self.b)
+        self.b.extend(data)
+        return off
+
+    def zeros(self, n: int, a: int) -> int:
+        return self.add(b"\0" * n, a)
+
+    def put(self, off: int, data: bytes):
+        self.b[off:off + len(data)] = data
+
+    def array(self) -> np.ndarray:
+        out = np.zeros(max(len(self.b), 16), dtype=np.uint8)
+        out[: len(self.b)] = np.frombuffer(bytes(self.b), dtype=np.uint8)
+        return out
+
+
+def _f3(x, y, z) -> bytes:
+    return struct.pack("<4f", x, y, z, 0.0)
+
+
+# ---------------------------------------------------------------- matrices
+# Column-major 4x4 like the reference's Matrix4f (matrix.cl reads s048c as
+# the first row).
+
+
+def translate(x, y, z):
+    m = np.eye(4)
+    m[:3, 3] = (x, y, z)
+    return m
+
+
+def scale(x, y, z):
+    return np.diag([x, y, z, 1.0])
+
+
+def rotate(angle, ax, ay, az):
+    a = np.array([ax, ay, az], dtype=np.float64)
+    a /= np.linalg.norm(a)
+    c, s = math.cos(angle), math.sin(angle)
+    x, y, z = a
+    r = np.array([[c + x * x * (1 - c), x * y * (1 - c) - z * s, x * z * (1 - c) + y * s],
+                  [y * x * (1 - c) + z * s, c + y * y * (1 - c), y * z * (1 - c) - x * s],
+                  [z * x * (1 - c) - y * s, z * y * (1 - c) + x * s, c + z * z * (1 - c)]])
+    m = np.eye(4)
+    m[:3, :3] = r
+    return m
+
+
+def look_at(eye, target, up):
+    """Camera-to-world transform of a camera at `eye` looking at `target`;
+    the camera looks down its local -z axis."""
+    eye, target, up = (np.asarray(v, dtype=np.float64) for v in (eye, target, up))
+    f = target - eye
+    f /= np.linalg.norm(f)
+    s = np.cross(f, up)
+    s /= np.linalg.norm(s)
+    u = np.cross(s, f)
+    m = np.eye(4)
+    m[:3, 0], m[:3, 1], m[:3, 2], m[:3, 3] = s, u, -f, eye
+    return m
+
+
+def _colmajor(m) -> bytes:
+    return np.asarray(m, dtype=np.float32).T.reshape(-1).tobytes()
+
+
+# ------------------------------------------------------------------- scene
+
+
+class Scene:
+    def __init__(self):
+        self.vertices: list = []
+        self.normals: list = []
+        self.tangents: list = []
+        self.uvs: list = []
+        self.faces: list = []
+        self.light_infos: list = []   # (atInfinity, reference)
+        self.light_powers: list = []
+        self.materials = Blob()
+        self.textures = Blob()
+        self.others = Blob(b"\0" * 12)  # offsets of camera, environment, light distribution
+        self.mat_ref, self.light_ref, self.tex_ref, self.other_ref = {}, {}, {}, {}
+        self.local_to_world = [np.eye(4)]
+        self._base = None
+        self.mc = MaterialCreator(self)
+
+    # Scene.h:62-81 -------------------------------------------------------
+    def push(self, m=None):
+        top = self.local_to_world[-1]
+        self.local_to_world.append(top @ m if m is not None else top.copy())
+
+    def pop(self):
+        self.local_to_world.pop()
+
+    def add_vertex(self, x, y, z):
+        p = self.local_to_world[-1] @ np.array([x, y, z, 1.0])
+        self.vertices.append(p[:3] / p[3])
+
+    def add_normal(self, x, y, z):
+        n = np.linalg.inv(self.local_to_world[-1]).T @ np.array([x, y, z, 0.0])
+        self.normals.append(n[:3])
+
+    def add_tangent(self, x, y, z):
+        self.tangents.append((self.local_to_world[-1] @ np.array([x, y, z, 0.0]))[:3])
+
+    def add_uv(self, u, v):
+        self.uvs.append((u, v))
+
+    def begin_object(self):
+        self._base = (len(self.vertices), len(self.normals), len(self.tangents), len(self.uvs))
+
+    def end_object(self):
+        self._base = None
+
+    def add_face(self, p, mat, light=NONE16, uv=None, vn=None, vt=None, alpha_tex=NONE32):
+        """Scene::addFace (Scene.h:82-116): indices are object-relative
+        between begin_object/end_object; an emissive face registers a light of
+        power 1."""
+        bv, bn, bt, bu = self._base or (0, 0, 0, 0)
+        f = np.zeros((), dtype=FACE_DTYPE)
+        f["p"] = [i + bv for i in p]
+        f["vn"] = [i + bn for i in vn] if vn is not None else [NONE32] * 3
+        f["vt"] = [i + bt for i in vt] if vt is not None else [NONE32] * 3
+        f["uv"] = [i + bu for i in uv] if uv is not None else [NONE32] * 3
+        f["alphaTexPtr"] = alpha_tex
+        f["matPtr"] = mat
+        f["lightPtr"] = light
+        self.faces.append(f)
+        if light != NONE16:
+            self.light_infos.append((0, len(self.faces) - 1))
+            self.light_powers.append(1.0)
+
+    # Scene.h:140-152 -----------------------------------------------------
+    def set_camera(self, width, height, cam_to_world, fov_y_deg=30.0, lens_radius=0.0, focus_dist=1.0):
+        """PerspectiveInfo blob (main.cpp:52-90, camera.cl:28-35); the camera
+        looks down its local -z axis."""
+        aspect = width / height
+        t = math.tan(math.radians(fov_y_deg) / 2)
+        near, far = 1.0, 100.0
+        clip_to_cam = np.linalg.inv(np.array([[1 / (aspect * t), 0, 0, 0], [0, 1 / t, 0, 0],
+                                              [0, 0, -(far + near) / (far - near), -2 * far * near / (far - near)],
+                                              [0, 0, -1, 0]]))
+        raster_to_screen = np.array([[2.0 / width, 0, 0, -1], [0, -2.0 / height, 0, 1], [0, 0, 2, -1],
+                                     [0, 0, 0, 1]])
+        raster_to_cam = clip_to_cam @ raster_to_screen
+        blob = bytearray(256)
+        struct.pack_into("<II", blob, 0, width, height)
+        blob[64:128] = _colmajor(cam_to_world)
+        struct.pack_into("<B3xfff", blob, 128, 0, aspect * t * t, lens_radius, focus_dist)
+        blob[192:256] = _colmajor(raster_to_cam)
+        self.other_ref["Camera"] = self.others.add(bytes(blob), 64)
+        self.width, self.height = width, height
+
+    def set_environment(self, light_prop_name):
+        self.other_ref["Environment"] = self.others.add(struct.pack("<I", self.light_ref[light_prop_name]), 4)
+        self.light_infos.append((1, NONE32))
+        self.light_powers.append(1.0)
+
+    def calc_light_power_distribution(self):
+        """Discrete1D over light powers (Scene.h:268-292)."""
+        head = self.others.zeros(16, 4)
+        p = np.asarray(self.light_powers, dtype=np.float32)
+        cdf = np.zeros(len(p) + 1, dtype=np.float32)
+        for i in range(1, len(cdf)):
+            cdf[i] = np.float32(cdf[i - 1] + p[i - 1])
+        total = cdf[-1]
+        cdf = (cdf / total).astype(np.float32)
+        pmf = (p / total).astype(np.float32)
+        o_cdf = self.others.add(cdf.tobytes(), 4)
+        o_pmf = self.others.add(pmf.tobytes(), 4)
+        self.others.put(head, struct.pack("<B3xIii", 0, len(p), o_pmf - head, o_cdf - head))
+        self.other_ref["LightPowerDistribution"] = head
+
+    def build(self):
+        """Scene::build (Scene.cpp:12-42) without the CPU BVH (the LBVH is
+        built on the device)."""
+        if "Environment" not in self.other_ref:
+            self.mc.begin_light_property("Dark")
+            self.mc.end_light_property()
+            self.other_ref["Environment"] = self.others.add(struct.pack("<I", self.light_ref["Dark"]), 4)
+        self.calc_light_power_distribution()
+        self.others.put(0, struct.pack("<III", self.other_ref["Camera"], self.other_ref["Environment"],
+                                       self.other_ref["LightPowerDistribution"]))
+
+    def blobs(self) -> dict:
+        def f4(v):
+            a = np.zeros((max(len(v), 1), 4), dtype=np.float32)
+            if v:
+                a[: len(v), :3] = np.asarray(v, dtype=np.float32)
+            return a
+
+        uv = np.zeros((max(len(self.uvs), 1), 2), dtype=np.float32)
+        if self.uvs:
+            uv[: len(self.uvs)] = np.asarray(self.uvs, dtype=np.float32)
+        lights = np.zeros((max(len(self.light_infos), 1), 2), dtype=np.uint32)
+        for i, (inf, ref) in enumerate(self.light_infos):
+            lights[i] = (inf, ref)
+        return {"vertices": f4(self.vertices), "normals": f4(self.normals), "tangents": f4(self.tangents),
+                "uvs": uv, "faces": np.array(self.faces, dtype=FACE_DTYPE), "lights": lights,
+                "materials": self.materials.array(), "textures": self.textures.array(),
+                "others": self.others.array(), "num_lights": len(self.light_infos)}
+
+    def soa(self):
+        """Vertex SoA + triangle index array for the LBVH build."""
+        v = np.asarray(self.vertices, dtype=np.float32)
+        f = np.array(self.faces, dtype=FACE_DTYPE)
+        return (np.ascontiguousarray(v[:, 0]), np.ascontiguousarray(v[:, 1]), np.ascontiguousarray(v[:, 2]),
+                np.ascontiguousarray(f["p"].reshape(-1)))
+
+
+class MaterialCreator:
+    """CreateFunctions.cpp:18-505 -- writes textures, materials, light
+    properties and the structures they point to into the scene blobs."""
+
+    def __init__(self, scene: Scene):
+        self.s = scene
+        self.num_bxdfs = 0
+        self.num_eedfs = 0
+
+    # textures ------------------------------------------------------------
+    def float3_constant_texture(self, name, r, g, b):
+        self.s.tex_ref[name] = self.s.textures.add(struct.pack("<B15x", TEX_COLOR_CONSTANT) + _f3(r, g, b), 16)
+
+    def float_constant_texture(self, name, v):
+        self.s.tex_ref[name] = self.s.textures.add(struct.pack("<B3xf", TEX_FLOAT_CONSTANT, v), 4)
+
+    def image_texture(self, name, data: np.ndarray, kind: str):
+        """kind: 'rgb8' (H,W,3 uint8), 'rgba8' (H,W,4 uint8), 'rgba16f'
+        (H,W,4 float16), 'gray8' (H,W uint8), 'float' (H,W float32)."""
+        t = self.s.textures
+        h, w = data.shape[:2]
+        head = t.zeros(16, 4)
+        img = t.align(128)
+        if kind == "rgb8":
+            px = np.zeros((h, w, 4), dtype=np.uint8)
+            px[..., :3] = data
+            t.b.extend(px.tobytes())
+            tt = TEX_RGB8
+        elif kind == "rgba8":
+            t.b.extend(np.ascontiguousarray(data, dtype=np.uint8).tobytes())
+            tt = TEX_RGBA8
+        elif kind == "rgba16f":
+            t.b.extend(np.ascontiguousarray(data, dtype=np.float16).tobytes())
+            tt = TEX_RGBA16F
+        elif kind == "gray8":
+            t.b.extend(np.ascontiguousarray(data, dtype=np.uint8).tobytes())
+            tt = TEX_GRAY8
+        elif kind == "float":
+            t.b.extend(np.ascontiguousarray(data, dtype=np.float32).tobytes())
+            tt = TEX_FLOAT_IMAGE
+        else:
+            raise ValueError(kind)
+        t.put(head, struct.pack("<B3xIIi", tt, w, h, img - head))
+        self.s.tex_ref[name] = head
+
+    def normal_map_texture(self, name, rgb8: np.ndarray):
+        self.image_texture(name, rgb8, "rgb8")
+
+    def float3_checkerboard_texture(self, name, c0, c1):
+        self.s.tex_ref[name] = self.s.textures.add(
+            struct.pack("<BB14x", TEX_COLOR_PROCEDURAL, PROC_CHECKER) + _f3(*c0) + _f3(*c1), 16)
+
+    def float3_checkerboard_bump_texture(self, name, width=0.01, reverse=False):
+        self.s.tex_ref[name] = self.s.textures.add(
+            struct.pack("<BB2xfB3x", TEX_COLOR_PROCEDURAL, PROC_CHECKER_BUMP, width, int(reverse)), 4)
+
+    def float_checkerboard_texture(self, name, v0, v1):
+        self.s.tex_ref[name] = self.s.textures.add(
+            struct.pack("<BB2xff", TEX_COLOR_PROCEDURAL, PROC_CHECKER, v0, v1), 4)
+
+    # fresnel (other resources) -------------------------------------------
+    def fresnel_noop(self, name):
+        self.s.other_ref[name] = self.s.others.add(struct.pack("<B", FRESNEL_NOOP), 1)
+
+    def fresnel_conductor(self, name, eta, k):
+        self.s.other_ref[name] = self.s.others.add(struct.pack("<B15x", FRESNEL_CONDUCTOR) + _f3(*eta) + _f3(*k), 16)
+
+    def fresnel_dielectric(self, name, eta_ext, eta_int):
+        self.s.other_ref[name] = self.s.others.add(struct.pack("<B3xff", FRESNEL_DIELECTRIC, eta_ext, eta_int), 4)
+
+    # environment distribution --------------------------------------------
+    def _average_luminance(self, rgb: np.ndarray, x0, x1, y0, y1):
+        """Area-weighted mean luminance of [x0,x1) x [y0,y1) texels,
+        CreateFunctions.cpp:159-244 (float accumulation)."""
+        lum = (np.float32(0.2126) * rgb[..., 0] + np.float32(0.7152) * rgb[..., 1] +
+               np.float32(0.0722) * rgb[..., 2]).astype(np.float32)
+        xl, xr, yt, yb = int(x0), int(math.ceil(x1)) - 1, int(y0), int(math.ceil(y1)) - 1
+        wx = np.ones(xr - xl + 1, dtype=np.float32)
+        wy = np.ones(yb - yt + 1, dtype=np.float32)
+        wx[0] = np.float32(xl + 1 - x0)
+        wx[-1] = np.float32(x1 - xr) if xr > xl else wx[-1]
+        wy[0] = np.float32(yt + 1 - y0)
+        wy[-1] = np.float32(y1 - yb) if yb > yt else wy[-1]
+        block = lum[yt:yb + 1, xl:xr + 1]
+        return float(np.float32((wy[:, None] * wx[None, :] * block).sum(dtype=np.float32) /
+                                np.float32((x1 - x0) * (y1 - y0))))
+
+    def continuous_consts_2d_h(self, name, rgb: np.ndarray, zenith_correction=True):
+        """ContinuousConsts2D_H over an equirectangular image, one stratum
+        per texel, rows weighted by sin(theta) (CreateFunctions.cpp:246-349)."""
+        o = self.s.others
+        h, w = rgb.shape[:2]
+        head = o.zeros(36, 4)
+        p_pdf = o.zeros(4 * h, 4)
+        p_cdf = o.zeros(4 * (h + 1), 4)
+        children = o.zeros(28 * h, 4)
+        c_pdfs = o.zeros(4 * w * h, 4)
+        c_cdfs = o.zeros(4 * (w + 1) * h, 4)
+        rgb = np.asarray(rgb, dtype=np.float32)
+        lum = (np.float32(0.2126) * rgb[..., 0] + np.float32(0.7152) * rgb[..., 1] +
+               np.float32(0.0722) * rgb[..., 2]).astype(np.float32)
+        width_c = np.float32(1.0) / np.float32(w)
+        row_mass = np.zeros(h, dtype=np.float32)
+        for i in range(h):
+            corr = np.float32(math.cos(math.pi * (0.5 - (i + 0.5) / h))) if zenith_correction else np.float32(1)
+            pdf = (lum[i] * corr).astype(np.float32)
+            cdf = np.zeros(w + 1, dtype=np.float32)
+            acc = np.float32(0)
+            for j in range(w):
+                acc = np.float32(acc + np.float32(pdf[j] * width_c))
+                cdf[j + 1] = acc
+            row_mass[i] = cdf[w]
+            norm = np.float32(1.0) / cdf[w] if cdf[w] > 0 else np.float32(0)
+            pdf = (pdf * norm).astype(np.float32)
+            cdf[1:] = (cdf[1:] * norm).astype(np.float32)
+            ch = children + 28 * i
+            o.put(ch, struct.pack("<B3xIfffii", 1, w, 0.0, 1.0, float(width_c),
+                                  c_pdfs + 4 * w * i - ch, c_cdfs + 4 * (w + 1) * i - ch))
+            o.put(c_pdfs + 4 * w * i, pdf.tobytes())
+            o.put(c_cdfs + 4 * (w + 1) * i, cdf.tobytes())
+        width_p = np.float32(1.0) / np.float32(h)
+        pcdf = np.zeros(h + 1, dtype=np.float32)
+        acc = np.float32(0)
+        for i in range(h):
+            acc = np.float32(acc + np.float32(row_mass[i] * width_p))
+            pcdf[i + 1] = acc
+        norm = np.float32(1.0) / pcdf[h]
+        ppdf = (row_mass * norm).astype(np.float32)
+        pcdf[1:] = (pcdf[1:] * norm).astype(np.float32)
+        o.put(p_pdf, ppdf.tobytes())
+        o.put(p_cdf, pcdf.tobytes())
+        parent = head + 8  # the embedded ContinuousConsts1D the kernel offsets from
+        o.put(head, struct.pack("<B3xi", 2, children - head) +
+              struct.pack("<B3xIfffii", 1, h, 0.0, 1.0, float(width_p), p_pdf - parent, p_cdf - parent))
+        self.s.other_ref[name] = head
+
+    # materials -----------------------------------------------------------
+    def begin_material(self, name, bump=None):
+        m = self.s.materials
+        self.num_bxdfs = 0
+        self.mat_head = m.add(b"\0", 1)
+        assert self.mat_head % 4 == 0, "MaterialInfo must start 4-byte aligned"
+        self.s.mat_ref[name] = self.mat_head
+        m.add(struct.pack("<B", bump is not None), 1)
+        m.add(struct.pack("<I", self.s.tex_ref[bump] if bump is not None else 0), 4)
+
+    def end_material(self):
+        assert self.num_bxdfs > 0
+        self.s.materials.b[self.mat_head] = self.num_bxdfs
+
+    def _elem(self, data: bytes):
+        self.num_bxdfs += 1
+        self.s.materials.align(4)
+        self.s.materials.b.extend(data)
+
+    def diffuse_elem(self, R, sigma):
+        self._elem(struct.pack("<B3xII", ME_DIFFUSE, self.s.tex_ref[R], self.s.tex_ref[sigma]))
+
+    def specular_r_elem(self, R, fresnel):
+        self._elem(struct.pack("<B3xII", ME_SPEC_R, self.s.tex_ref[R], self.s.other_ref[fresnel]))
+
+    def specular_t_elem(self, T, eta_ext, eta_int, mat_name):
+        fname = "internalFresnelDielectric_" + mat_name
+        self.fresnel_dielectric(fname, eta_ext, eta_int)
+        self._elem(struct.pack("<B3xIffI", ME_SPEC_T, self.s.tex_ref[T], eta_ext, eta_int, self.s.other_ref[fname]))
+
+    def newward_elem(self, R, ax, ay):
+        self._elem(struct.pack("<B3xIII", ME_NEWWARD, self.s.tex_ref[R], self.s.tex_ref[ax], self.s.tex_ref[ay]))
+
+    def ashikhmin_s_elem(self, Rs, nu, nv):
+        self._elem(struct.pack("<B3xIII", ME_ASH_S, self.s.tex_ref[Rs], self.s.tex_ref[nu], self.s.tex_ref[nv]))
+
+    def ashikhmin_d_elem(self, Rd, Rs):
+        self._elem(struct.pack("<B3xII", ME_ASH_D, self.s.tex_ref[Rs], self.s.tex_ref[Rd]))
+
+    def matte_material(self, name, bump, R, sigma):
+        self.begin_material(name, bump)
+        self.diffuse_elem(R, sigma)
+        self.end_material()
+
+    def glass_material(self, name, bump, R, T, eta_ext, eta_int):
+        self.begin_material(name, bump)
+        fname = "GlassInternalFresnelDielectric_" + name
+        self.fresnel_dielectric(fname, eta_ext, eta_int)
+        self.specular_r_elem(R, fname)
+        self.specular_t_elem(T, eta_ext, eta_int, name)
+        self.end_material()
+
+    def metal_material(self, name, bump, R, eta, k):
+        self.begin_material(name, bump)
+        fname = "MetalInternalFresnelConductor_" + name
+        self.fresnel_conductor(fname, eta, k)
+        self.specular_r_elem(R, fname)
+        self.end_material()
+
+    def newward_material(self, name, bump, R, ax, ay):
+        self.begin_material(name, bump)
+        self.newward_elem(R, ax, ay)
+        self.end_material()
+
+    def ashikhmin_material(self, name, bump, Rs, Rd, nu, nv):
+        self.begin_material(name, bump)
+        self.ashikhmin_s_elem(Rs, nu, nv)
+        self.ashikhmin_d_elem(Rd, Rs)
+        self.end_material()
+
+    # light properties ----------------------------------------------------
+    def begin_light_property(self, name):
+        self.num_eedfs = 0
+        self.lit_head = self.s.materials.add(b"\0", 1)
+        self.s.light_ref[name] = self.lit_head
+
+    def end_light_property(self):
+        self.s.materials.b[self.lit_head] = self.num_eedfs
+
+    def diffuse_light_property(self, name, M):
+        self.begin_light_property(name)
+        self.num_eedfs += 1
+        self.s.materials.align(4)
+        self.s.materials.b.extend(struct.pack("<B3xI", LP_DIFFUSE, self.s.tex_ref[M]))
+        self.end_light_property()
+
+    def image_based_env_light_property(self, name, radiance_tex, rgb: np.ndarray, multiplier=1.0):
+        """rgb: the texture's texels as float (H,W,3) for the importance
+        distribution (the reference reads the same texels as half floats)."""
+        dname = "InternalDistribution2D_" + radiance_tex
+        self.continuous_consts_2d_h(dname, rgb, True)
+        self.begin_light_property(name)
+        self.num_eedfs += 1
+        self.s.materials.align(4)
+        self.s.materials.b.extend(struct.pack("<B3xIfI", ENV_IMAGE, self.s.tex_ref[radiance_tex], multiplier,
+                                              self.s.other_ref[dname]))
+        self.end_light_property()
