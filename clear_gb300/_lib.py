@@ -62,6 +62,7 @@ def lib() -> C.CDLL:
             "clr_lbvh_create": [u32, C.POINTER(vp)],
             "clr_lbvh_destroy": [vp],
             "clr_lbvh_build": [vp, vp, vp, vp, vp, u32, u32, C.POINTER(ClrBvh), vp],
+            "clr_lbvh_build_noalloc": [vp, vp, vp, vp, u32, u32, C.POINTER(ClrBvh), vp],
             "clr_lbvh_export_reference": [vp, C.POINTER(ClrBvh), vp, vp, vp, vp, vp, vp],
             "clr_trace_closest": [C.POINTER(ClrBvh), vp, u32, vp, vp, vp],
             "clr_trace_shadow": [C.POINTER(ClrBvh), vp, u32, vp, vp],

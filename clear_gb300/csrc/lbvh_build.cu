@@ -25,6 +25,7 @@
 //                                      fences (the reference has none).
 #include <stdio.h>
 
+#include <mutex>
 #include <new>
 
 #include "common.cuh"
@@ -797,4 +798,71 @@ extern "C" int clr_lbvh_pass_times(clr_lbvh* h, float* ms, const char** names, i
     }
     *num_passes = n;
     return CLR_OK;
+}
+
+// ====================================================== allocation-free build
+//
+// clr_lbvh_build_noalloc serves callers that must not allocate device memory
+// themselves: hosts that hand this library a fixed device-memory budget
+// through their own allocator and forbid any other allocation, and per-frame
+// loops where the implicit device synchronisation of cudaMalloc/cudaFree
+// would stall the pipeline.  Its scratch lives in the file-scope array below,
+// sized for kNoAllocMaxTris triangles; every GPU that loads this library holds
+// that array until the process exits.  The build is the same pipeline as
+// clr_lbvh_build, run on a scratch layout carved out of the array.
+
+namespace {
+constexpr uint32_t kNoAllocMaxTris = 1u << 18;               // 262,144 triangles
+constexpr size_t kNoAllocScratchBytes = 12ull << 20;         // 12 MiB
+constexpr int kNoAllocMaxDevices = 64;
+}  // namespace
+
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
+
+// Device address of g_noalloc_scratch per device, resolved once per device by
+// the first call made while that device is current.
+static void* g_noalloc_addr[kNoAllocMaxDevices] = {};
+static std::mutex g_noalloc_mutex;
+
+static int noalloc_scratch(void** out) {
+    int dev = -1;
+    CLR_CUDA_TRY(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= kNoAllocMaxDevices)
+        return clr_set_error(CLR_EINVAL, "clr_lbvh_build_noalloc: device %d out of range", dev);
+    std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+    if (!g_noalloc_addr[dev]) {
+        void* p = nullptr;
+        CLR_CUDA_TRY(cudaGetSymbolAddress(&p, g_noalloc_scratch));
+        g_noalloc_addr[dev] = p;
+    }
+    *out = g_noalloc_addr[dev];
+    return CLR_OK;
+}
+
+extern "C" int clr_lbvh_build_noalloc(const float* vx, const float* vy, const float* vz, const uint32_t* tri,
+                                      uint32_t num_tris, uint32_t bits_per_dim, clr_bvh* out, void* stream) {
+    if (!out) return clr_set_error(CLR_EINVAL, "clr_lbvh_build_noalloc: NULL output");
+    if (bits_per_dim < 1 || bits_per_dim > 21)
+        return clr_set_error(CLR_EINVAL, "clr_lbvh_build_noalloc: bits_per_dim %u outside [1, 21]", bits_per_dim);
+    if (num_tris > kNoAllocMaxTris)
+        return clr_set_error(CLR_ECAPACITY,
+                             "clr_lbvh_build_noalloc: %u triangles exceed its fixed scratch limit of %u; "
+                             "use clr_lbvh_build",
+                             num_tris, kNoAllocMaxTris);
+    if (num_tris > 0 && (!vx || !vy || !vz || !out->tris || !out->root_box || (num_tris > 1 && !out->nodes)))
+        return clr_set_error(CLR_EINVAL, "clr_lbvh_build_noalloc: NULL input or output buffer");
+    out->num_tris = num_tris;
+    out->bits_per_dim = bits_per_dim;
+    if (num_tris == 0) return CLR_OK;
+    void* base = nullptr;
+    int rc = noalloc_scratch(&base);
+    if (rc != CLR_OK) return rc;
+    clr_lbvh h{};
+    if (pool_layout(&h, kNoAllocMaxTris, nullptr) > kNoAllocScratchBytes)
+        return clr_set_error(CLR_ECAPACITY, "clr_lbvh_build_noalloc: scratch layout exceeds the static array");
+    pool_layout(&h, kNoAllocMaxTris, static_cast<char*>(base));
+    h.capacity = kNoAllocMaxTris;
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    if (bits_per_dim <= 10) return run_build<uint32_t>(&h, vx, vy, vz, tri, num_tris, bits_per_dim, out, st);
+    return run_build<uint64_t>(&h, vx, vy, vz, tri, num_tris, bits_per_dim, out, st);
 }

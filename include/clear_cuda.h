@@ -95,6 +95,23 @@ CLR_API int clr_lbvh_destroy(clr_lbvh* h);
 CLR_API int clr_lbvh_build(clr_lbvh* h, const float* vx, const float* vy, const float* vz, const uint32_t* tri,
                    uint32_t num_tris, uint32_t bits_per_dim, clr_bvh* out, void* stream);
 
+/* Allocation-free build, for callers that may not allocate device memory:
+ * hosts that give this library a fixed device-memory budget through their own
+ * allocator and forbid any other allocation, and per-frame loops where the
+ * device synchronisation implied by cudaMalloc/cudaFree would stall the
+ * pipeline.  No counterpart in the reference (its builder allocates a scratch
+ * pool, LBVHBuilder.cpp:50-158).
+ * Same inputs, outputs and results as clr_lbvh_build, but the scratch is a
+ * fixed array inside this library: at most 262,144 triangles (larger inputs
+ * fail with CLR_ECAPACITY), and every GPU that loads the library keeps that
+ * 12 MiB array until the process exits.  The first call on a device resolves
+ * the array's device address (cudaGetSymbolAddress) with that device current;
+ * make that first call before any stream capture.  All calls share the one
+ * array, so calls that overlap on the GPU (different streams or threads)
+ * race: serialise them.  Nothing is allocated or freed. */
+CLR_API int clr_lbvh_build_noalloc(const float* vx, const float* vy, const float* vz, const uint32_t* tri,
+                                   uint32_t num_tris, uint32_t bits_per_dim, clr_bvh* out, void* stream);
+
 /* Parity/debug export of the last build of `h` into the reference layouts:
  * inodes: (n-1) x 48 B LBVH::InternalNode, lnodes: n x 48 B LBVH::LeafNode
  * (LBVHBuilder.h:17-29), parents: 2n-1 uint32 (leaves at [0,n), internal at
