@@ -294,7 +294,10 @@ def run_ours(args):
         lbvh.trace_closest(bvh, crays, hid, ht)
         lbvh.trace_shadow(bvh, srays, occ)
     torch.cuda.synchronize()
-    t0, t1, t2 = (torch.cuda.Event(enable_timing=True) for _ in range(3))
+    hid2 = torch.empty(m, dtype=torch.int32, device=dev)
+    ht2 = torch.empty(m, dtype=torch.float32, device=dev)
+    lbvh.trace_closest(bvh, crays, hid2, ht2, ordered=True)
+    t0, t1, t2, t3 = (torch.cuda.Event(enable_timing=True) for _ in range(4))
     t0.record(stream)
     for _ in range(trav_steps):
         lbvh.trace_closest(bvh, crays, hid, ht)
@@ -302,9 +305,15 @@ def run_ours(args):
     for _ in range(trav_steps):
         lbvh.trace_shadow(bvh, srays, occ)
     t2.record(stream)
+    for _ in range(trav_steps):
+        lbvh.trace_closest(bvh, crays, hid2, ht2, ordered=True)
+    t3.record(stream)
     torch.cuda.synchronize()
     closest_ms = t0.elapsed_time(t1) / trav_steps
     shadow_ms = t1.elapsed_time(t2) / trav_steps
+    ordered_ms = t2.elapsed_time(t3) / trav_steps
+    ordered_id_mismatch = int((hid != hid2).sum().item())
+    ordered_t_mismatch = int((ht != ht2).sum().item())
     hit_frac = float((hid >= 0).float().mean().item())
     occ_frac = float(occ.float().mean().item())
     clk = clocks.stop()
@@ -340,6 +349,9 @@ def run_ours(args):
                      "kernel_ms": dom_ms},
         "build_kernels_ms": kern_ms,
         "traversal": {"closest_mrays_s": m / closest_ms / 1e3, "shadow_mrays_s": m / shadow_ms / 1e3,
+                      "closest_ordered_mrays_s": m / ordered_ms / 1e3,
+                      "ordered_vs_exact_id_mismatches": ordered_id_mismatch,
+                      "ordered_vs_exact_t_mismatches": ordered_t_mismatch,
                       "closest_ms": closest_ms, "shadow_ms": shadow_ms, "closest_hit_frac": hit_frac,
                       "shadow_occluded_frac": occ_frac},
         "gpu_launches": launches_per_build * args.steps,

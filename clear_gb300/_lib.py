@@ -65,6 +65,7 @@ def lib() -> C.CDLL:
             "clr_lbvh_build_noalloc": [vp, vp, vp, vp, u32, u32, C.POINTER(ClrBvh), vp],
             "clr_lbvh_export_reference": [vp, C.POINTER(ClrBvh), vp, vp, vp, vp, vp, vp],
             "clr_trace_closest": [C.POINTER(ClrBvh), vp, u32, vp, vp, vp],
+            "clr_trace_closest_ordered": [C.POINTER(ClrBvh), vp, u32, vp, vp, vp],
             "clr_trace_shadow": [C.POINTER(ClrBvh), vp, u32, vp, vp],
             "clr_device_status": [C.POINTER(u32), i32],
             "clr_lbvh_set_profiling": [vp, i32],

@@ -16,54 +16,111 @@ CLR_DEFINE_STATUS_READER(traverse)
 
 namespace clr {
 
+constexpr int kSmCountFallback = 152;
 constexpr int kTraceThreads = 128;
 
+// Ray-per-lane loops.  Each thread walks the rays r, r + P, r + 2P, ... (P =
+// threads in the grid) one after the other, so a lane whose ray finishes
+// early starts its next ray instead of idling while the warp's longest ray
+// completes.  The grid is sized to fill the GPU once.  Rays are independent
+// and each is traversed exactly as alone, so results do not depend on P.
+
+struct ClosestState {
+    Ray ray;
+    float ix, iy, iz;
+    float t;
+    uint32_t best;
+    int sp;
+};
+
+__device__ __forceinline__ void closest_begin(ClosestState& s, const float4* __restrict__ rays, uint32_t r,
+                                              const float* __restrict__ root_box, uint32_t n,
+                                              const float4* __restrict__ tris, uint2* stack) {
+    s.ray = load_ray(rays, r);
+    s.ix = 1.0f / s.ray.dx;
+    s.iy = 1.0f / s.ray.dy;
+    s.iz = 1.0f / s.ray.dz;
+    s.t = s.ray.tmax;
+    s.best = 0xFFFFFFFFu;
+    s.sp = 0;
+    float entry;
+    const bool root_ok = box_test_fast(__ldg(root_box + 0), __ldg(root_box + 1), __ldg(root_box + 2),
+                                       __ldg(root_box + 4), __ldg(root_box + 5), __ldg(root_box + 6), s.ray, s.ix,
+                                       s.iy, s.iz, entry) &&
+                         !(entry > s.t);
+    if (!root_ok) return;
+    if (n == 1) tri_hit(tris, 0, s.ray, s.t, s.best);
+    else if (n >= 2) stack[s.sp++] = make_uint2(0u, __float_as_uint(entry));
+}
+
+// One pop of rayIntersection's loop (bvh_traversal.cl:191-208).  kOrdered
+// visits the nearer child first (by box entry distance) instead of the
+// reference's fixed child order: fewer nodes per ray, same closest t up to
+// ties and rounding-level near-ties (which the reference resolves by its
+// visiting order).
+template <bool kOrdered>
+__device__ __forceinline__ void closest_step(ClosestState& s, const float4* __restrict__ nodes,
+                                             const float4* __restrict__ tris, uint2* stack) {
+    --s.sp;
+    const uint32_t node = stack[s.sp].x;
+    if (__uint_as_float(stack[s.sp].y) > s.t) return;  // the reference's bound test at pop
+    const NodeBoxes nb = load_node(nodes, node);
+    float e0, e1;
+    const bool p0 = box_test_fast(nb.b0[0], nb.b0[1], nb.b0[2], nb.b0[3], nb.b0[4], nb.b0[5], s.ray, s.ix, s.iy, s.iz, e0);
+    const bool p1 = box_test_fast(nb.b1[0], nb.b1[1], nb.b1[2], nb.b1[3], nb.b1[4], nb.b1[5], s.ray, s.ix, s.iy, s.iz, e1);
+    // reference order: child 0 then child 1 (internal children pushed, so
+    // child 1's subtree pops first).  Ordered: far child handled first so the
+    // near internal child is popped first; near leaf tested first.
+    const bool swap = kOrdered && (e1 < e0);
+#pragma unroll
+    for (int k = 0; k < 2; ++k) {
+        int c = k;
+        if (kOrdered) {
+            const bool leaf0 = (nb.ref0 & kLeafBit) != 0, leaf1 = (nb.ref1 & kLeafBit) != 0;
+            // leaves: near first; internal: far pushed first
+            const bool both_internal = !leaf0 && !leaf1;
+            c = both_internal ? (swap ? k : 1 - k) : (swap ? 1 - k : k);
+        }
+        const uint32_t ref = c ? nb.ref1 : nb.ref0;
+        const bool pass = c ? p1 : p0;
+        const float e = c ? e1 : e0;
+        if (ref & kLeafBit) {
+            if (pass && !(e > s.t)) tri_hit(tris, ref & ~kLeafBit, s.ray, s.t, s.best);
+        } else if (pass) {
+            if (s.sp < kStackSize) stack[s.sp++] = make_uint2(ref, __float_as_uint(e));
+            else clr_raise(CLR_DEVERR_STACK);
+        }
+    }
+}
+
+template <bool kOrdered>
 __global__ void __launch_bounds__(kTraceThreads) k_trace_closest(const float4* __restrict__ nodes,
                                                                  const float4* __restrict__ tris,
                                                                  const float* __restrict__ root_box, uint32_t n,
                                                                  const float4* __restrict__ rays, uint32_t nr,
                                                                  uint32_t* __restrict__ hit_id,
                                                                  float* __restrict__ hit_t) {
-    const uint32_t r = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t P = gridDim.x * blockDim.x;
+    uint32_t r = blockIdx.x * blockDim.x + threadIdx.x;
     if (r >= nr) return;
-    const Ray ray = load_ray(rays, r);
-    float t = ray.tmax;
-    uint32_t best = 0xFFFFFFFFu;
-    float entry;
-    const bool root_ok = box_test(__ldg(root_box + 0), __ldg(root_box + 1), __ldg(root_box + 2), __ldg(root_box + 4),
-                                  __ldg(root_box + 5), __ldg(root_box + 6), ray, entry) &&
-                         !(entry > t);
-    if (n == 1) {
-        if (root_ok) tri_hit(tris, 0, ray, t, best);
-    } else if (n >= 2 && root_ok) {
-        uint2 stack[kStackSize];
-        int sp = 0;
-        stack[sp++] = make_uint2(0u, __float_as_uint(entry));
-        // a valid tree visits each internal node at most once per ray
-        for (uint32_t guard = 0; sp > 0 && guard < n; ++guard) {
-            --sp;
-            const uint32_t node = stack[sp].x;
-            if (__uint_as_float(stack[sp].y) > t) continue;  // the reference's bound test at pop
-            const NodeBoxes nb = load_node(nodes, node);
-            float e0, e1;
-            const bool p0 = box_test(nb.b0[0], nb.b0[1], nb.b0[2], nb.b0[3], nb.b0[4], nb.b0[5], ray, e0);
-            const bool p1 = box_test(nb.b1[0], nb.b1[1], nb.b1[2], nb.b1[3], nb.b1[4], nb.b1[5], ray, e1);
-#pragma unroll
-            for (int s = 0; s < 2; ++s) {
-                const uint32_t ref = s ? nb.ref1 : nb.ref0;
-                const bool pass = s ? p1 : p0;
-                const float e = s ? e1 : e0;
-                if (ref & kLeafBit) {
-                    if (pass && !(e > t)) tri_hit(tris, ref & ~kLeafBit, ray, t, best);
-                } else if (pass) {
-                    if (sp < kStackSize) stack[sp++] = make_uint2(ref, __float_as_uint(e));
-                    else clr_raise(CLR_DEVERR_STACK);
-                }
-            }
+    uint2 stack[kStackSize];
+    ClosestState s;
+    closest_begin(s, rays, r, root_box, n, tris, stack);
+    // a valid tree pops each internal node at most once per ray
+    uint32_t guard = 0;
+    for (;;) {
+        if (s.sp > 0 && guard < n) {
+            closest_step<kOrdered>(s, nodes, tris, stack);
+            ++guard;
+            continue;
         }
+        hit_id[r] = s.best;
+        hit_t[r] = s.t;
+        r += P;
+        if (r >= nr) break;
+        guard = 0;
+        closest_begin(s, rays, r, root_box, n, tris, stack);
     }
-    hit_id[r] = best;
-    hit_t[r] = t;
 }
 
 // Any-hit: the bound stays at tmax, so the accepted set of boxes does not
@@ -73,47 +130,70 @@ __global__ void __launch_bounds__(kTraceThreads) k_trace_shadow(const float4* __
                                                                 const float* __restrict__ root_box, uint32_t n,
                                                                 const float4* __restrict__ rays, uint32_t nr,
                                                                 uint8_t* __restrict__ occluded) {
-    const uint32_t r = blockIdx.x * blockDim.x + threadIdx.x;
-    if (r >= nr) return;
-    const Ray ray = load_ray(rays, r);
-    const float tmax = ray.tmax;
-    bool occ = false;
-    float entry;
-    const bool root_ok = box_test(__ldg(root_box + 0), __ldg(root_box + 1), __ldg(root_box + 2), __ldg(root_box + 4),
-                                  __ldg(root_box + 5), __ldg(root_box + 6), ray, entry) &&
-                         !(entry > tmax);
-    if (n == 1) {
-        float t = tmax;
-        uint32_t id;
-        if (root_ok) occ = tri_hit(tris, 0, ray, t, id);
-    } else if (n >= 2 && root_ok) {
-        uint32_t stack[kStackSize];
-        int sp = 0;
-        stack[sp++] = 0u;
-        for (uint32_t guard = 0; sp > 0 && !occ && guard < n; ++guard) {
-            const uint32_t node = stack[--sp];
-            const NodeBoxes nb = load_node(nodes, node);
-            float e0, e1;
-            const bool p0 = box_test(nb.b0[0], nb.b0[1], nb.b0[2], nb.b0[3], nb.b0[4], nb.b0[5], ray, e0) && !(e0 > tmax);
-            const bool p1 = box_test(nb.b1[0], nb.b1[1], nb.b1[2], nb.b1[3], nb.b1[4], nb.b1[5], ray, e1) && !(e1 > tmax);
+    const uint32_t P = gridDim.x * blockDim.x;
+    uint32_t stack[kStackSize];
+    for (uint32_t r = blockIdx.x * blockDim.x + threadIdx.x; r < nr; r += P) {
+        const Ray ray = load_ray(rays, r);
+        const float ix = 1.0f / ray.dx, iy = 1.0f / ray.dy, iz = 1.0f / ray.dz;
+        const float tmax = ray.tmax;
+        bool occ = false;
+        float entry;
+        const bool root_ok = box_test_fast(__ldg(root_box + 0), __ldg(root_box + 1), __ldg(root_box + 2),
+                                           __ldg(root_box + 4), __ldg(root_box + 5), __ldg(root_box + 6), ray, ix,
+                                           iy, iz, entry) &&
+                             !(entry > tmax);
+        if (n == 1) {
+            float t = tmax;
+            uint32_t id;
+            if (root_ok) occ = tri_hit(tris, 0, ray, t, id);
+        } else if (n >= 2 && root_ok) {
+            int sp = 0;
+            stack[sp++] = 0u;
+            for (uint32_t guard = 0; sp > 0 && !occ && guard < n; ++guard) {
+                const uint32_t node = stack[--sp];
+                const NodeBoxes nb = load_node(nodes, node);
+                float e0, e1;
+                const bool p0 = box_test_fast(nb.b0[0], nb.b0[1], nb.b0[2], nb.b0[3], nb.b0[4], nb.b0[5], ray, ix, iy,
+                                              iz, e0) && !(e0 > tmax);
+                const bool p1 = box_test_fast(nb.b1[0], nb.b1[1], nb.b1[2], nb.b1[3], nb.b1[4], nb.b1[5], ray, ix, iy,
+                                              iz, e1) && !(e1 > tmax);
 #pragma unroll
-            for (int s = 0; s < 2; ++s) {
-                const uint32_t ref = s ? nb.ref1 : nb.ref0;
-                const bool pass = s ? p1 : p0;
-                if (!pass || occ) continue;
-                if (ref & kLeafBit) {
-                    float t = tmax;
-                    uint32_t id;
-                    if (tri_hit(tris, ref & ~kLeafBit, ray, t, id)) occ = true;
-                } else if (sp < kStackSize) {
-                    stack[sp++] = ref;
-                } else {
-                    clr_raise(CLR_DEVERR_STACK);
+                for (int c = 0; c < 2; ++c) {
+                    const uint32_t ref = c ? nb.ref1 : nb.ref0;
+                    const bool pass = c ? p1 : p0;
+                    if (!pass || occ) continue;
+                    if (ref & kLeafBit) {
+                        float t = tmax;
+                        uint32_t id;
+                        if (tri_hit(tris, ref & ~kLeafBit, ray, t, id)) occ = true;
+                    } else if (sp < kStackSize) {
+                        stack[sp++] = ref;
+                    } else {
+                        clr_raise(CLR_DEVERR_STACK);
+                    }
                 }
             }
         }
+        occluded[r] = occ ? 1 : 0;
     }
-    occluded[r] = occ ? 1 : 0;
+}
+
+// Grid that fills every SM once for a ray-per-lane kernel.
+template <typename K>
+static unsigned int persistent_grid(K kernel, uint32_t nr) {
+    static int sms = 0;
+    if (!sms) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        if (sms <= 0) sms = kSmCountFallback;
+    }
+    int per_sm = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, kTraceThreads, 0) != cudaSuccess || per_sm <= 0)
+        per_sm = 1;
+    const unsigned int full = (unsigned int)(sms * per_sm);
+    const unsigned int need = div_up(nr, kTraceThreads);
+    return need < full ? need : full;
 }
 
 }  // namespace clr
@@ -130,17 +210,28 @@ static int check_trace_args(const clr_bvh* bvh, const float* rays, uint32_t num_
     return CLR_OK;
 }
 
-extern "C" int clr_trace_closest(const clr_bvh* bvh, const float* rays, uint32_t num_rays, uint32_t* hit_id,
-                                 float* hit_t, void* stream) {
+template <bool kOrdered>
+static int trace_closest(const clr_bvh* bvh, const float* rays, uint32_t num_rays, uint32_t* hit_id, float* hit_t,
+                         void* stream) {
     int rc = check_trace_args(bvh, rays, num_rays, hit_id);
     if (rc != CLR_OK || num_rays == 0) return rc;
     if (!hit_t) return clr_set_error(CLR_EINVAL, "clr_trace_closest: hit_t is NULL");
     cudaStream_t st = static_cast<cudaStream_t>(stream);
-    k_trace_closest<<<div_up(num_rays, kTraceThreads), kTraceThreads, 0, st>>>(
+    k_trace_closest<kOrdered><<<persistent_grid(k_trace_closest<kOrdered>, num_rays), kTraceThreads, 0, st>>>(
         static_cast<const float4*>(bvh->nodes), static_cast<const float4*>(bvh->tris), bvh->root_box, bvh->num_tris,
         reinterpret_cast<const float4*>(rays), num_rays, hit_id, hit_t);
     CLR_LAUNCH_CHECK("k_trace_closest");
     return CLR_OK;
+}
+
+extern "C" int clr_trace_closest(const clr_bvh* bvh, const float* rays, uint32_t num_rays, uint32_t* hit_id,
+                                 float* hit_t, void* stream) {
+    return trace_closest<false>(bvh, rays, num_rays, hit_id, hit_t, stream);
+}
+
+extern "C" int clr_trace_closest_ordered(const clr_bvh* bvh, const float* rays, uint32_t num_rays, uint32_t* hit_id,
+                                         float* hit_t, void* stream) {
+    return trace_closest<true>(bvh, rays, num_rays, hit_id, hit_t, stream);
 }
 
 extern "C" int clr_trace_shadow(const clr_bvh* bvh, const float* rays, uint32_t num_rays, uint8_t* occluded,
@@ -148,7 +239,7 @@ extern "C" int clr_trace_shadow(const clr_bvh* bvh, const float* rays, uint32_t 
     int rc = check_trace_args(bvh, rays, num_rays, occluded);
     if (rc != CLR_OK || num_rays == 0) return rc;
     cudaStream_t st = static_cast<cudaStream_t>(stream);
-    k_trace_shadow<<<div_up(num_rays, kTraceThreads), kTraceThreads, 0, st>>>(
+    k_trace_shadow<<<persistent_grid(k_trace_shadow, num_rays), kTraceThreads, 0, st>>>(
         static_cast<const float4*>(bvh->nodes), static_cast<const float4*>(bvh->tris), bvh->root_box, bvh->num_tris,
         reinterpret_cast<const float4*>(rays), num_rays, occluded);
     CLR_LAUNCH_CHECK("k_trace_shadow");

@@ -128,9 +128,10 @@ def _rays(rays: torch.Tensor, device) -> torch.Tensor:
 
 
 def trace_closest(bvh: BVH, rays: torch.Tensor, hit_id: torch.Tensor | None = None,
-                  hit_t: torch.Tensor | None = None):
+                  hit_t: torch.Tensor | None = None, ordered: bool = False):
     """Closest hit for rays packed {ox,oy,oz,tmax,dx,dy,dz,0}.  Returns
-    (hit_id int32 [-1 = miss], hit_t float32)."""
+    (hit_id int32 [-1 = miss], hit_t float32).  ordered=True visits the nearer
+    child first (faster; ids may differ from the reference on exact ties)."""
     r = _rays(rays, bvh.device)
     m = r.shape[0]
     if hit_id is None:
@@ -138,8 +139,8 @@ def trace_closest(bvh: BVH, rays: torch.Tensor, hit_id: torch.Tensor | None = No
     if hit_t is None:
         hit_t = torch.empty(m, dtype=torch.float32, device=bvh.device)
     with torch.cuda.device(bvh.device):
-        call("clr_trace_closest", C.byref(bvh.c), _ptr(r), C.c_uint32(m), _ptr(hit_id), _ptr(hit_t),
-             _stream(bvh.device))
+        call("clr_trace_closest_ordered" if ordered else "clr_trace_closest", C.byref(bvh.c), _ptr(r),
+             C.c_uint32(m), _ptr(hit_id), _ptr(hit_t), _stream(bvh.device))
     return hit_id, hit_t
 
 

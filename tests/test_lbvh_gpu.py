@@ -108,6 +108,22 @@ def test_trace_parity(cuda, n):
     no_device_errors()
 
 
+def test_trace_ordered_matches_closest_hit(cuda):
+    """The nearer-child-first query finds the same closest hit; only exact or
+    rounding-level ties may resolve differently (none expected here)."""
+    n = 300001
+    vx, vy, vz = W.triangle_soup(n, seed=99)
+    b, bvh, _ = gpu_build(cuda, vx, vy, vz, None, n, 10)
+    ob = oracle.lbvh_build(vx, vy, vz, None, n, 10)
+    rays = W.closest_rays(50000, seed=98)
+    ids, ts = lbvh.trace_closest(bvh, torch.from_numpy(rays).to(cuda), ordered=True)
+    oids, ots = oracle.trace_closest(vx, vy, vz, None, ob, rays)
+    id_mismatch = int((ids.cpu().numpy().view(np.uint32) != oids).sum())
+    t_mismatch = int((ts.cpu().numpy() != ots).sum())
+    assert id_mismatch <= 5 and t_mismatch <= 5, (id_mismatch, t_mismatch)
+    no_device_errors()
+
+
 def test_trace_empty_scene_and_no_rays(cuda):
     b = lbvh.LBVHBuilder(1, cuda)
     e = torch.empty(0, dtype=torch.float32, device=cuda)
