@@ -69,6 +69,7 @@ def lib() -> C.CDLL:
             "clr_trace_shadow": [C.POINTER(ClrBvh), vp, u32, vp, vp],
             "clr_device_status": [C.POINTER(u32), i32],
             "clr_lbvh_set_profiling": [vp, i32],
+            "clr_render": [vp, u32, u32, vp, vp, u32, u32, u32, vp],
             "clr_lbvh_pass_times": [vp, C.POINTER(C.c_float), C.POINTER(C.c_char_p), i32, C.POINTER(i32)],
         }
         for name, args in sig.items():

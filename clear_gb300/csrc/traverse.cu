@@ -239,7 +239,9 @@ extern "C" int clr_trace_shadow(const clr_bvh* bvh, const float* rays, uint32_t 
     int rc = check_trace_args(bvh, rays, num_rays, occluded);
     if (rc != CLR_OK || num_rays == 0) return rc;
     cudaStream_t st = static_cast<cudaStream_t>(stream);
-    k_trace_shadow<<<persistent_grid(k_trace_shadow, num_rays), kTraceThreads, 0, st>>>(
+    // shadow segments are short (most end at the first accepted triangle):
+    // one ray per thread with hardware block scheduling balances them best
+    k_trace_shadow<<<div_up(num_rays, kTraceThreads), kTraceThreads, 0, st>>>(
         static_cast<const float4*>(bvh->nodes), static_cast<const float4*>(bvh->tris), bvh->root_box, bvh->num_tris,
         reinterpret_cast<const float4*>(rays), num_rays, occluded);
     CLR_LAUNCH_CHECK("k_trace_shadow");

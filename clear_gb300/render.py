@@ -1,0 +1,62 @@
+"""Host side of the path tracer: uploads a scene's blobs, builds its LBVH and
+calls ``clr_render`` (the counterpart of enqueueing the reference's
+``pathtracing`` kernel per tile and sample, main.cpp:477-494)."""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+import torch
+
+from . import _lib, lbvh
+from .scene import Scene
+from .scenes import pixel_seeds
+
+RENDER_ORDERED = 0x1
+
+
+class ClrScene(C.Structure):
+    _fields_ = [("vertices", C.c_void_p), ("normals", C.c_void_p), ("tangents", C.c_void_p), ("uvs", C.c_void_p),
+                ("faces", C.c_void_p), ("lights", C.c_void_p), ("materials", C.c_void_p),
+                ("textures", C.c_void_p), ("others", C.c_void_p), ("bvh", C.POINTER(_lib.ClrBvh))]
+
+
+def _dev(a: np.ndarray, device) -> torch.Tensor:
+    return torch.from_numpy(np.ascontiguousarray(a).view(np.uint8).reshape(-1).copy()).to(device)
+
+
+class DeviceScene:
+    """A scene resident on the GPU with its LBVH."""
+
+    def __init__(self, scene: Scene, device="cuda", bits_per_dim: int = 10):
+        self.device = torch.device(device)
+        b = scene.blobs()
+        self.blobs = b
+        self.width, self.height = scene.width, scene.height
+        self.t = {k: _dev(b[k], self.device) for k in ("vertices", "normals", "tangents", "uvs", "faces", "lights",
+                                                        "materials", "textures", "others")}
+        vx, vy, vz, tri = scene.soa()
+        self.num_faces = len(scene.faces)
+        self.builder = lbvh.LBVHBuilder(self.num_faces, self.device)
+        self.soa = tuple(torch.from_numpy(a).to(self.device) for a in (vx, vy, vz))
+        self.tri = torch.from_numpy(tri.astype(np.int32)).to(self.device)
+        self.bvh = self.builder.perform(self.soa, self.tri, self.num_faces, bits_per_dim)
+        p = lambda k: self.t[k].data_ptr()  # noqa: E731
+        self.c = ClrScene(p("vertices"), p("normals"), p("tangents"), p("uvs"), p("faces"), p("lights"),
+                          p("materials"), p("textures"), p("others"), C.pointer(self.bvh.c))
+
+    def new_frame(self):
+        """Fresh per-pixel RNG states (seed = pixel index + 1) and a zeroed
+        accumulation buffer."""
+        w, h = self.width, self.height
+        rng = torch.from_numpy(pixel_seeds(w, h).view(np.int32)).to(self.device)
+        pix = torch.zeros((w * h, 4), dtype=torch.float32, device=self.device)
+        return rng, pix
+
+    def render(self, rng: torch.Tensor, pix: torch.Tensor, spp: int, max_depth: int = 100,
+               ordered: bool = True) -> None:
+        stream = C.c_void_p(torch.cuda.current_stream(self.device).cuda_stream)
+        with torch.cuda.device(self.device):
+            _lib.call("clr_render", C.byref(self.c), C.c_uint32(self.width), C.c_uint32(self.height),
+                      C.c_void_p(rng.data_ptr()), C.c_void_p(pix.data_ptr()), C.c_uint32(spp), C.c_uint32(max_depth),
+                      C.c_uint32(RENDER_ORDERED if ordered else 0), stream)

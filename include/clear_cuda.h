@@ -156,6 +156,46 @@ CLR_API int clr_trace_closest_ordered(const clr_bvh* bvh, const float* rays, uin
  * 0 <= t <= tmax. */
 CLR_API int clr_trace_shadow(const clr_bvh* bvh, const float* rays, uint32_t num_rays, uint8_t* occluded, void* stream);
 
+/* ----------------------------------------------------------- path tracer */
+
+/*
+ * Scene in the reference's byte-blob format (OpenCL/pathtracer.cl:25-46,
+ * OpenCL_PathTracer/Scene.h:165-225), all device pointers:
+ *   vertices, normals, tangents : float4 per entry (cl_float3 layout)
+ *   uvs       : float2 per entry
+ *   faces     : 56-byte Face records (Face.hpp:15-21)
+ *   lights    : 8-byte LightInfo {u8 atInfinity, u32 reference}
+ *   materials, textures, others : the three scene blobs; others[0..2] are the
+ *               u32 offsets of the camera, the environment head and the light
+ *               power distribution (Scene.cpp:39-41)
+ *   bvh       : an LBVH built over the faces' vertices (clr_lbvh_build)
+ */
+typedef struct clr_scene {
+    const float* vertices;
+    const float* normals;
+    const float* tangents;
+    const float* uvs;
+    const void* faces;
+    const void* lights;
+    const uint8_t* materials;
+    const uint8_t* textures;
+    const uint8_t* others;
+    const clr_bvh* bvh;
+} clr_scene;
+
+#define CLR_RENDER_ORDERED 0x1u  /* trace with nearer-child-first traversal */
+
+/* Replaces the `pathtracing` kernel (OpenCL/pathtracer.cl:25-271) launched
+ * once per tile per sample (main.cpp:477-494): adds `spp` path samples per
+ * pixel of a width x height image to `pixels` (float4 per pixel, xyz =
+ * accumulated radiance, w untouched), advancing the per-pixel XORShift128
+ * states `rand_states` (4 x uint32 per pixel, pixel (x,y) at 4*(y*width+x)).
+ * max_depth caps the number of bounces (0 = the reference's 100).  The
+ * caller divides by the sample count, as the reference's `scaling` pass does
+ * (post_processing.cl:20-26). */
+CLR_API int clr_render(const clr_scene* scene, uint32_t width, uint32_t height, uint32_t* rand_states, float* pixels,
+                       uint32_t spp, uint32_t max_depth, uint32_t flags, void* stream);
+
 /* ----------------------------------------------------------------- misc */
 
 /* Reads (and optionally clears) the device error bits CLR_DEVERR_* of the
