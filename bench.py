@@ -59,8 +59,9 @@ ALGO_BYTES = {
     "morton": 40.0,             # read 9 floats, write one 4-byte key
     "sort_pass_first": 12.0,    # read key, write key + index
     "sort_pass": 16.0,          # read key + index, write key + index
-    "karras": 164.0,            # key 4 + node 64 + parent 4 + counter 4 | idx 4 + 36 gather + 48 record
-    "refit": 88.0,              # parent 4 + child boxes 48 + box 24 + counter 8 (+ leaf parent 4)
+    # per triangle: leaf (index 4, vertex gather 36, record 48, box+ref+end into the parent slot 32)
+    # + internal node (2 adjacent keys 8, both slots 64, counter RMW 8, own slot 32, index 4)
+    "build_tree": 236.0,
 }
 
 

@@ -17,12 +17,12 @@
 //                                      radix sort (warp match-any ranking,
 //                                      decoupled look-back).  Stable, so the
 //                                      sorted order is the reference's.
-//   constructBinaryRadixTree (:342-410)
-//                                   -> k_karras: same direction / range / split
-//                                      search on the sorted keys; leaf children
-//                                      get their box and triangle record here.
-//   calcNodeAABBs (:415-492)        -> k_refit: atomic-counter climb with device
-//                                      fences (the reference has none).
+//   constructBinaryRadixTree (:342-410) + calcNodeAABBs (:415-492)
+//                                   -> k_build_tree: the same radix tree, emitted
+//                                      bottom-up in the atomic-counter climb that
+//                                      refits the boxes (with device fences, which
+//                                      the reference's refit lacks); each leaf
+//                                      thread writes its triangle record.
 #include <stdio.h>
 
 #include <mutex>
@@ -146,7 +146,7 @@ __global__ void __launch_bounds__(256) k_morton(const float* __restrict__ vx, co
                                                 const float* __restrict__ vz, const uint32_t* __restrict__ tri,
                                                 uint32_t n, uint32_t bits, const unsigned int* __restrict__ boxw,
                                                 KeyT* __restrict__ keys, unsigned int* __restrict__ hist,
-                                                int npasses) {
+                                                int npasses, unsigned int* __restrict__ counters) {
     __shared__ unsigned int sh[kMaxPasses * kRadix];
     for (int i = threadIdx.x; i < npasses * kRadix; i += blockDim.x) sh[i] = 0;
     float smin[3], ssize[3];
@@ -171,6 +171,7 @@ __global__ void __launch_bounds__(256) k_morton(const float* __restrict__ vx, co
         }
         const KeyT key = make_key<KeyT>(q[0], q[1], q[2]);
         keys[t] = key;
+        if (t + 1 < n) counters[t] = 0u;  // arrival counters of the tree pass
         for (int p = 0; p < npasses; ++p) atomicAdd(&sh[p * kRadix + (uint32_t)((key >> (8 * p)) & 0xFFu)], 1u);
     }
     __syncthreads();
@@ -353,16 +354,7 @@ __device__ __forceinline__ int clz_key<uint64_t>(uint64_t x) { return __clzll(x)
 
 // _numCommonBits (lbvh_construction.cl:322-332) on packed keys: the leading
 // common bits of the 3b-bit keys, extended by the common bits of the sorted
-// positions when the keys are equal; -1 outside [0, n).
-template <typename KeyT>
-__device__ __forceinline__ int delta(const KeyT* __restrict__ keys, int64_t n, int kbits, KeyT ki, int64_t i,
-                                     int64_t j) {
-    if (j < 0 || j >= n) return -1;
-    const KeyT kj = keys[j];
-    const KeyT x = ki ^ kj;
-    if (x != 0) return clz_key<KeyT>(x) - ((int)(8 * sizeof(KeyT)) - kbits);
-    return kbits + __clz((uint32_t)i ^ (uint32_t)j);
-}
+// positions when the keys are equal (delta_adj below, for adjacent pairs).
 
 struct TriVerts {
     float p[3][3];
@@ -394,69 +386,81 @@ __device__ __forceinline__ void emit_leaf(const float* vx, const float* vy, cons
     r[2] = make_float4(fsub(tv.p[2][0], tv.p[0][0]), fsub(tv.p[2][1], tv.p[0][1]), fsub(tv.p[2][2], tv.p[0][2]), 0.f);
 }
 
+// Adjacent common prefix delta(i, i+1), i in [0, n-2].
 template <typename KeyT>
-__global__ void __launch_bounds__(256) k_karras(const KeyT* __restrict__ keys, const uint32_t* __restrict__ sidx,
-                                                uint32_t n, int kbits, const float* __restrict__ vx,
-                                                const float* __restrict__ vy, const float* __restrict__ vz,
-                                                const uint32_t* __restrict__ tri, float4* __restrict__ nodes,
-                                                float4* __restrict__ tris, uint32_t* __restrict__ parent_leaf,
-                                                uint32_t* __restrict__ parent_inner,
-                                                unsigned int* __restrict__ counters) {
-    const uint32_t g = blockIdx.x * blockDim.x + threadIdx.x;
-    if (g >= n - 1) return;
-    counters[g] = 0;
-    const int64_t gi = g, nn = n;
-    const KeyT ki = keys[g];
-    // direction, range and split searches of constructBinaryRadixTree
-    // (lbvh_construction.cl:363-392)
-    const int commonR = delta(keys, nn, kbits, ki, gi, gi + 1);
-    const int commonL = delta(keys, nn, kbits, ki, gi, gi - 1);
-    const int d = commonR > commonL ? 1 : (commonR < commonL ? -1 : 0);
-    if (d == 0) {  // only possible if the keys were not sorted (a failed sort)
-        clr_raise(CLR_DEVERR_REFIT);
-        return;
-    }
-    const int minNum = d > 0 ? commonL : commonR;
-    int64_t lMax = 2;
-    while (delta(keys, nn, kbits, ki, gi, gi + lMax * d) > minNum && lMax <= nn) lMax <<= 1;
-    int64_t l = 0;
-    for (int64_t t = lMax >> 1; t >= 1; t >>= 1)
-        if (delta(keys, nn, kbits, ki, gi, gi + (l + t) * d) > minNum) l += t;
-    const int64_t otherEnd = gi + l * d;
-    const int numNode = delta(keys, nn, kbits, ki, gi, otherEnd);
-    int64_t split = 0;
-    float scale = 0.5f;
-    for (;;) {
-        const uint32_t t = (uint32_t)ceilf(fmul((float)(uint32_t)l, scale));
-        if (delta(keys, nn, kbits, ki, gi, gi + (split + (int64_t)t) * d) > numNode) split += t;
-        if (t <= 1) break;
-        scale = fmul(scale, 0.5f);
-    }
-    const int64_t splitPos = gi + split * d + (d < 0 ? d : 0);
-    const int64_t lo = min(gi, otherEnd), hi = max(gi, otherEnd);
-    const uint32_t c[2] = {(uint32_t)splitPos, (uint32_t)(splitPos + 1)};
-    const bool leaf[2] = {lo == splitPos, hi == splitPos + 1};
+__device__ __forceinline__ int delta_adj(const KeyT* __restrict__ keys, int kbits, uint32_t i) {
+    const KeyT x = __ldcg(keys + i) ^ __ldcg(keys + i + 1);
+    if (x != 0) return clz_key<KeyT>(x) - ((int)(8 * sizeof(KeyT)) - kbits);
+    return kbits + __clz(i ^ (i + 1));
+}
 
-    float box[2][6];
-    uint32_t ref[2];
-#pragma unroll
-    for (int s = 0; s < 2; ++s) {
-        if (leaf[s]) {
-            emit_leaf(vx, vy, vz, tri, __ldg(sidx + c[s]), c[s], tris, box[s]);
-            parent_leaf[c[s]] = g;
-            ref[s] = c[s] | kLeafBit;
-        } else {
-            // filled in by k_refit
-            for (int k = 0; k < 6; ++k) box[s][k] = 0.f;
-            parent_inner[c[s]] = g | ((uint32_t)s << 31);
-            ref[s] = c[s];
+// Tree emission and refit in one bottom-up pass (one thread per leaf).
+//
+// The binary radix tree of constructBinaryRadixTree (lbvh_construction.cl:
+// 342-410) is the unique tree in which a node covering sorted positions
+// [lo, hi] has as parent the node that extends it towards the neighbour with
+// the longer common prefix: to the right (split = hi, this node is child 0)
+// when delta(hi, hi+1) > delta(lo-1, lo), else to the left (split = lo-1,
+// child 1).  The two deltas never tie for distinct extended keys.  So each
+// leaf thread climbs: it writes its box, reference and far range end into the
+// parent's child slot, and the second of the two children to arrive (atomic
+// counter, device fences) merges both boxes and continues upwards, exactly as
+// calcNodeAABBs (:415-492) climbs.  Internal nodes are stored at index =
+// split position; the reference's index of a node (its hi if it is child 0,
+// its lo if child 1, 0 for the root) is recorded for the reference-layout
+// export, and children and visiting order are the reference's.
+template <typename KeyT>
+__global__ void __launch_bounds__(256) k_build_tree(const KeyT* __restrict__ keys, const uint32_t* __restrict__ sidx,
+                                                    uint32_t n, int kbits, const float* __restrict__ vx,
+                                                    const float* __restrict__ vy, const float* __restrict__ vz,
+                                                    const uint32_t* __restrict__ tri, float* __restrict__ nodes,
+                                                    float4* __restrict__ tris, unsigned int* __restrict__ counters,
+                                                    uint32_t* __restrict__ karras_idx, float* __restrict__ root_box) {
+    const uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= n) return;
+    float box[6];
+    emit_leaf(vx, vy, vz, tri, __ldg(sidx + j), j, tris, box);
+    uint32_t lo = j, hi = j, ref = j | kLeafBit;
+    // every level up adds at least one common bit of the (3b + 32)-bit key
+    for (int step = 0; step <= kMaxDepth; ++step) {
+        if (lo == 0 && hi == n - 1) {
+            if (!(ref & kLeafBit)) karras_idx[ref] = 0;
+            root_box[0] = box[0]; root_box[1] = box[1]; root_box[2] = box[2];
+            root_box[3] = __uint_as_float(ref);
+            root_box[4] = box[3]; root_box[5] = box[4]; root_box[6] = box[5];
+            root_box[7] = 0.f;
+            return;
         }
+        const bool left = (lo == 0) || (hi != n - 1 && delta_adj(keys, kbits, hi) > delta_adj(keys, kbits, lo - 1));
+        const uint32_t split = left ? hi : lo - 1;
+        if (!(ref & kLeafBit)) karras_idx[ref] = left ? hi : lo;
+        const int slot = left ? 0 : 1;
+        float* nd = nodes + 16u * split;
+        float2* b2 = reinterpret_cast<float2*>(nd + 6 * slot);
+        __stcg(b2 + 0, make_float2(box[0], box[1]));
+        __stcg(b2 + 1, make_float2(box[2], box[3]));
+        __stcg(b2 + 2, make_float2(box[4], box[5]));
+        unsigned int* w = reinterpret_cast<unsigned int*>(nd);
+        __stcg(w + 12 + slot, ref);
+        __stcg(w + 14 + slot, left ? lo : hi);
+        __threadfence();  // publish this child before arriving
+        if (atomicAdd(counters + split, 1u) == 0u) return;  // sibling still climbing
+        __threadfence();  // observe the sibling's slot
+        float b[12];
+#pragma unroll
+        for (int k = 0; k < 12; ++k) b[k] = __ldcg(nd + k);
+        const uint32_t far_end = __ldcg(w + 14 + (1 - slot));
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            box[k] = fminf(b[k], b[6 + k]);
+            box[3 + k] = fmaxf(b[3 + k], b[9 + k]);
+        }
+        if (left) hi = far_end;
+        else lo = far_end;
+        if (lo > hi || hi >= n) break;  // corrupt slot: report, never index out of range
+        ref = split;
     }
-    float4* nd = nodes + 4u * g;
-    nd[0] = make_float4(box[0][0], box[0][1], box[0][2], box[0][3]);
-    nd[1] = make_float4(box[0][4], box[0][5], box[1][0], box[1][1]);
-    nd[2] = make_float4(box[1][2], box[1][3], box[1][4], box[1][5]);
-    nd[3] = make_float4(__uint_as_float(ref[0]), __uint_as_float(ref[1]), 0.f, 0.f);
+    clr_raise(CLR_DEVERR_REFIT);
 }
 
 // Single-triangle scene: one leaf, no internal node (the reference requires
@@ -466,86 +470,47 @@ __global__ void k_single(const float* vx, const float* vy, const float* vz, cons
     float box[6];
     emit_leaf(vx, vy, vz, tri, 0u, 0u, tris, box);
     for (int k = 0; k < 3; ++k) { root_box[k] = box[k]; root_box[4 + k] = box[3 + k]; }
-    root_box[3] = 0.f;
+    root_box[3] = __uint_as_float(kLeafBit);
     root_box[7] = 0.f;
-}
-
-// ----------------------------------------------------------------- refit
-
-__global__ void __launch_bounds__(256) k_refit(float* __restrict__ nodes, const uint32_t* __restrict__ parent_leaf,
-                                               const uint32_t* __restrict__ parent_inner,
-                                               unsigned int* __restrict__ counters, uint32_t n,
-                                               float* __restrict__ root_box) {
-    const uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
-    if (j >= n) return;
-    uint32_t p = parent_leaf[j];
-    // The k-th internal node on a leaf-to-root path has a common prefix of at
-    // least k bits, so a climb never exceeds kMaxDepth steps.
-    for (int step = 0; step < kMaxDepth; ++step) {
-        if (p >= n - 1) break;  // corrupt parent link: report, never index out of range
-        __threadfence();  // publish the child box written by this thread
-        if (atomicAdd(counters + p, 1u) == 0u) return;  // sibling not done yet
-        __threadfence();  // observe the sibling's box
-        const float* nd = nodes + 16u * p;
-        float b[12];
-#pragma unroll
-        for (int k = 0; k < 12; ++k) b[k] = __ldcg(nd + k);
-        float u[6];
-#pragma unroll
-        for (int k = 0; k < 3; ++k) {
-            u[k] = fminf(b[k], b[6 + k]);
-            u[3 + k] = fmaxf(b[3 + k], b[9 + k]);
-        }
-        if (p == 0) {
-            root_box[0] = u[0]; root_box[1] = u[1]; root_box[2] = u[2]; root_box[3] = 0.f;
-            root_box[4] = u[3]; root_box[5] = u[4]; root_box[6] = u[5]; root_box[7] = 0.f;
-            return;
-        }
-        const uint32_t gp = parent_inner[p];
-        const uint32_t slot = gp >> 31, q = gp & 0x7FFFFFFFu;
-        if (q >= n - 1) break;
-        float2* dst = reinterpret_cast<float2*>(nodes + 16u * q + 6u * slot);
-        __stcg(dst + 0, make_float2(u[0], u[1]));
-        __stcg(dst + 1, make_float2(u[2], u[3]));
-        __stcg(dst + 2, make_float2(u[4], u[5]));
-        p = q;
-    }
-    clr_raise(CLR_DEVERR_REFIT);
 }
 
 // --------------------------------------------------------- reference export
 
-__global__ void k_export(const float4* __restrict__ nodes, const float4* __restrict__ tris, uint32_t n,
-                         uint8_t* __restrict__ inodes, uint8_t* __restrict__ lnodes, uint32_t* __restrict__ parents) {
-    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n - 1) return;
-    const float4 a = nodes[4u * i], b = nodes[4u * i + 1], c = nodes[4u * i + 2], r = nodes[4u * i + 3];
-    const float bx[2][6] = {{a.x, a.y, a.z, a.w, b.x, b.y}, {b.z, b.w, c.x, c.y, c.z, c.w}};
-    const uint32_t ref[2] = {__float_as_uint(r.x), __float_as_uint(r.y)};
+// Node a (stored at its split position) becomes InternalNode[karras_idx[a]]
+// with children c = {a, a+1}: in the reference's numbering a child-0 internal
+// node is indexed by its hi (= a) and a child-1 internal node by its lo (= a+1).
+__global__ void k_export(const float4* __restrict__ nodes, const float4* __restrict__ tris,
+                         const uint32_t* __restrict__ karras_idx, uint32_t n, uint8_t* __restrict__ inodes,
+                         uint8_t* __restrict__ lnodes, uint32_t* __restrict__ parents) {
+    const uint32_t a = blockIdx.x * blockDim.x + threadIdx.x;
+    if (a >= n - 1) return;
+    const uint32_t k = karras_idx[a];
+    const float4 q0 = nodes[4u * a], q1 = nodes[4u * a + 1], q2 = nodes[4u * a + 2], r = nodes[4u * a + 3];
+    const float bx[2][6] = {{q0.x, q0.y, q0.z, q0.w, q1.x, q1.y}, {q1.z, q1.w, q2.x, q2.y, q2.z, q2.w}};
+    const bool is_leaf[2] = {(__float_as_uint(r.x) & kLeafBit) != 0, (__float_as_uint(r.y) & kLeafBit) != 0};
     if (inodes) {
-        float* f = reinterpret_cast<float*>(inodes + 48u * i);
-        for (int k = 0; k < 3; ++k) {
-            f[k] = fminf(bx[0][k], bx[1][k]);
-            f[4 + k] = fmaxf(bx[0][3 + k], bx[1][3 + k]);
+        float* f = reinterpret_cast<float*>(inodes + 48u * k);
+        for (int c = 0; c < 3; ++c) {
+            f[c] = fminf(bx[0][c], bx[1][c]);
+            f[4 + c] = fmaxf(bx[0][3 + c], bx[1][3 + c]);
         }
         f[3] = 0.f;
         f[7] = 0.f;
-        uint8_t* ch = inodes + 48u * i + 32u;
-        ch[0] = (uint8_t)(ref[0] >> 31);
-        ch[1] = (uint8_t)(ref[1] >> 31);
+        uint8_t* ch = inodes + 48u * k + 32u;
+        ch[0] = is_leaf[0];
+        ch[1] = is_leaf[1];
         ch[2] = ch[3] = 0;
-        uint32_t* cc = reinterpret_cast<uint32_t*>(inodes + 48u * i + 36u);
-        cc[0] = ref[0] & 0x7FFFFFFFu;
-        cc[1] = ref[1] & 0x7FFFFFFFu;
+        uint32_t* cc = reinterpret_cast<uint32_t*>(inodes + 48u * k + 36u);
+        cc[0] = a;
+        cc[1] = a + 1;
         cc[2] = 0;
     }
     for (int s = 0; s < 2; ++s) {
-        const uint32_t child = ref[s] & 0x7FFFFFFFu;
-        const bool is_leaf = ref[s] >> 31;
-        if (parents) parents[is_leaf ? child : n + child] = i;
-        if (is_leaf && lnodes) {
+        const uint32_t child = a + s;
+        if (parents) parents[is_leaf[s] ? child : n + child] = k;
+        if (is_leaf[s] && lnodes) {
             float* f = reinterpret_cast<float*>(lnodes + 48u * child);
-            for (int k = 0; k < 3; ++k) { f[k] = bx[s][k]; f[4 + k] = bx[s][3 + k]; }
+            for (int c = 0; c < 3; ++c) { f[c] = bx[s][c]; f[4 + c] = bx[s][3 + c]; }
             f[3] = 0.f;
             f[7] = 0.f;
             uint32_t* u = reinterpret_cast<uint32_t*>(lnodes + 48u * child + 32u);
@@ -553,7 +518,7 @@ __global__ void k_export(const float4* __restrict__ nodes, const float4* __restr
             u[1] = u[2] = u[3] = 0;
         }
     }
-    if (i == 0 && parents) parents[n] = 0xFFFFFFFFu;
+    if (k == 0 && parents) parents[n] = 0xFFFFFFFFu;
 }
 
 __global__ void k_export_single(const float* __restrict__ root_box, const float4* __restrict__ tris,
@@ -561,6 +526,7 @@ __global__ void k_export_single(const float* __restrict__ root_box, const float4
     if (lnodes) {
         float* f = reinterpret_cast<float*>(lnodes);
         for (int k = 0; k < 8; ++k) f[k] = root_box[k];
+        f[3] = 0.f;
         uint32_t* u = reinterpret_cast<uint32_t*>(lnodes + 32);
         u[0] = __float_as_uint(tris[0].w);
         u[1] = u[2] = u[3] = 0;
@@ -594,7 +560,7 @@ static size_t pool_layout(clr_lbvh* h, uint32_t cap, char* base) {
     };
     const size_t o_keys0 = take(8ull * cap), o_keys1 = take(8ull * cap);
     const size_t o_vals0 = take(4ull * cap), o_vals1 = take(4ull * cap);
-    const size_t o_pleaf = take(4ull * cap), o_pinner = take(4ull * cap), o_cnt = take(4ull * cap);
+    const size_t o_kidx = take(4ull * cap), o_cnt = take(4ull * cap);
     const size_t o_zero = off;
     const size_t o_hist = take(4ull * kMaxPasses * kRadix);
     const size_t o_status = take(4ull * kMaxPasses * tiles * kRadix);
@@ -605,8 +571,7 @@ static size_t pool_layout(clr_lbvh* h, uint32_t cap, char* base) {
         h->keys[1] = base + o_keys1;
         h->vals[0] = reinterpret_cast<uint32_t*>(base + o_vals0);
         h->vals[1] = reinterpret_cast<uint32_t*>(base + o_vals1);
-        h->parent_leaf = reinterpret_cast<uint32_t*>(base + o_pleaf);
-        h->parent_inner = reinterpret_cast<uint32_t*>(base + o_pinner);
+        h->karras_idx = reinterpret_cast<uint32_t*>(base + o_kidx);
         h->counters = reinterpret_cast<unsigned int*>(base + o_cnt);
         h->zero_region = base + o_zero;
         h->zero_bytes = off - o_zero;
@@ -688,7 +653,8 @@ static int run_build(clr_lbvh* h, const float* vx, const float* vy, const float*
     CLR_LAUNCH_CHECK("k_scene_box");
     timer.done("scene_box");
     KeyT* keys[2] = {static_cast<KeyT*>(h->keys[0]), static_cast<KeyT*>(h->keys[1])};
-    k_morton<KeyT><<<grid_stream, 256, 0, st>>>(vx, vy, vz, tri, n, bits, h->boxw, keys[0], h->hist, npasses);
+    k_morton<KeyT><<<grid_stream, 256, 0, st>>>(vx, vy, vz, tri, n, bits, h->boxw, keys[0], h->hist, npasses,
+                                                          h->counters);
     CLR_LAUNCH_CHECK("k_morton");
     timer.done("morton");
     constexpr int kTile = kSortThreads * SortCfg<KeyT>::kItems;
@@ -715,14 +681,11 @@ static int run_build(clr_lbvh* h, const float* vx, const float* vy, const float*
         CLR_LAUNCH_CHECK("k_single");
         timer.done("single");
     } else {
-        k_karras<KeyT><<<div_up(n - 1, 256), 256, 0, st>>>(keys[fin], h->vals[fin], n, kbits, vx, vy, vz, tri, nodes,
-                                                          tris, h->parent_leaf, h->parent_inner, h->counters);
-        CLR_LAUNCH_CHECK("k_karras");
-        timer.done("karras");
-        k_refit<<<div_up(n, 256), 256, 0, st>>>(reinterpret_cast<float*>(out->nodes), h->parent_leaf,
-                                                 h->parent_inner, h->counters, n, out->root_box);
-        CLR_LAUNCH_CHECK("k_refit");
-        timer.done("refit");
+        k_build_tree<KeyT><<<div_up(n, 256), 256, 0, st>>>(keys[fin], h->vals[fin], n, kbits, vx, vy, vz, tri,
+                                                          reinterpret_cast<float*>(out->nodes), tris, h->counters,
+                                                          h->karras_idx, out->root_box);
+        CLR_LAUNCH_CHECK("k_build_tree");
+        timer.done("build_tree");
     }
     return CLR_OK;
 }
@@ -761,7 +724,7 @@ extern "C" int clr_lbvh_export_reference(clr_lbvh* h, const clr_bvh* bvh, void* 
         CLR_LAUNCH_CHECK("k_export_single");
     } else {
         k_export<<<div_up(n - 1, 256), 256, 0, st>>>(static_cast<const float4*>(bvh->nodes),
-                                                     static_cast<const float4*>(bvh->tris), n,
+                                                     static_cast<const float4*>(bvh->tris), h->karras_idx, n,
                                                      static_cast<uint8_t*>(inodes), static_cast<uint8_t*>(lnodes),
                                                      parents);
         CLR_LAUNCH_CHECK("k_export");

@@ -31,9 +31,8 @@ struct clr_lbvh {
     size_t pool_bytes = 0;
     void* keys[2] = {nullptr, nullptr};     // sort ping-pong (up to 8 B per key)
     uint32_t* vals[2] = {nullptr, nullptr};  // triangle ids riding with the keys
-    uint32_t* parent_leaf = nullptr;         // leaf -> internal parent
-    uint32_t* parent_inner = nullptr;        // internal -> parent | child slot << 31
-    unsigned int* counters = nullptr;        // refit arrival counters
+    uint32_t* karras_idx = nullptr;          // node (at its split) -> reference index
+    unsigned int* counters = nullptr;        // tree-pass arrival counters
     void* zero_region = nullptr;             // cleared once per build:
     size_t zero_bytes = 0;                   //   hist, status, tile_ctr, boxw
     unsigned int* hist = nullptr;            // [pass][256] digit counts

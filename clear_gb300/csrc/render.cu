@@ -108,7 +108,7 @@ __device__ bool intersect(const DScene& sc, f3 org, f3 dir, Hit& h, uint2* stack
         test_leaf(0);
     } else if (sc.num_tris >= 2) {
         int sp = 0;
-        stack[sp++] = make_uint2(0u, __float_as_uint(entry));
+        stack[sp++] = make_uint2(__float_as_uint(rb[3]), __float_as_uint(entry));
         for (uint32_t guard = 0; sp > 0 && guard < sc.num_tris; ++guard) {
             --sp;
             if (__uint_as_float(stack[sp].y) > t) continue;

@@ -1,6 +1,7 @@
 // BVH traversal on sm_103a: closest-hit and shadow (any-hit) queries.
 //
-// The closest-hit kernel visits nodes in the reference's order
+// The root node index is root_box[3] (bit pattern).  The closest-hit kernel
+// visits nodes in the reference's order
 // (OpenCL/bvh_traversal.cl:182-215): pop a node, handle child 0 then child 1,
 // a leaf child is box-tested and its triangle tested at once, an internal
 // child is pushed (so child 1's subtree is explored before child 0's).
@@ -50,7 +51,7 @@ __device__ __forceinline__ void closest_begin(ClosestState& s, const float4* __r
                          !(entry > s.t);
     if (!root_ok) return;
     if (n == 1) tri_hit(tris, 0, s.ray, s.t, s.best);
-    else if (n >= 2) stack[s.sp++] = make_uint2(0u, __float_as_uint(entry));
+    else if (n >= 2) stack[s.sp++] = make_uint2(__float_as_uint(__ldg(root_box + 3)), __float_as_uint(entry));
 }
 
 // One pop of rayIntersection's loop (bvh_traversal.cl:191-208).  kOrdered
@@ -148,7 +149,7 @@ __global__ void __launch_bounds__(kTraceThreads) k_trace_shadow(const float4* __
             if (root_ok) occ = tri_hit(tris, 0, ray, t, id);
         } else if (n >= 2 && root_ok) {
             int sp = 0;
-            stack[sp++] = 0u;
+            stack[sp++] = __float_as_uint(__ldg(root_box + 3));
             for (uint32_t guard = 0; sp > 0 && !occ && guard < n; ++guard) {
                 const uint32_t node = stack[--sp];
                 const NodeBoxes nb = load_node(nodes, node);

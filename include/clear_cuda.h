@@ -52,16 +52,19 @@ enum {
 
 /*
  * A built BVH.  The caller allocates the three device buffers, sized
- *   nodes    : max(num_tris - 1, 1) * CLR_NODE_BYTES   (root = node 0)
+ *   nodes    : max(num_tris - 1, 1) * CLR_NODE_BYTES
  *   tris     : num_tris * CLR_TRI_BYTES                (in leaf = sorted order)
- *   root_box : 8 floats {min x,y,z, 0, max x,y,z, 0}
- * Node i (16 floats): child-0 box {minx,miny,minz,maxx,maxy,maxz},
- * child-1 box, then two uint32 child references (bit 31 set = leaf index,
- * clear = internal-node index) and two zero words.  Leaf i's triangle record
- * is tris[i] = {p0.xyz, id, (p1-p0).xyz, 0, (p2-p0).xyz, 0}.
- * Topology is that of the reference's Karras radix tree
- * (OpenCL/lbvh_construction.cl:342-410): node i's children are the reference's
- * InternalNode[i].c[0..1] with isChild[k] mapped to bit 31.
+ *   root_box : 8 floats {min x,y,z, root, max x,y,z, 0}; `root` holds the
+ *              uint32 bit pattern of the root's child reference
+ * Internal node (16 floats), stored at the index of its split position (the
+ * last sorted leaf of its left subtree): child-0 box
+ * {minx,miny,minz,maxx,maxy,maxz}, child-1 box, two uint32 child references
+ * (bit 31 set = leaf index, clear = internal-node index), and the far ends of
+ * the two children's leaf ranges.  Leaf i's triangle record is
+ * tris[i] = {p0.xyz, id, (p1-p0).xyz, 0, (p2-p0).xyz, 0}.
+ * The tree is the reference's Karras radix tree
+ * (OpenCL/lbvh_construction.cl:342-410) with the same children in the same
+ * order; clr_lbvh_export_reference renumbers it into the reference layout.
  */
 typedef struct clr_bvh {
     uint32_t num_tris;
