@@ -74,6 +74,7 @@ def parse():
     ap.add_argument("--tris", type=int, default=N_TRIS)
     ap.add_argument("--rays", type=int, default=N_RAYS)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--render", type=int, default=1, help="also time the path tracer (0 = skip)")
     return ap.parse_args()
 
 
@@ -173,6 +174,38 @@ def cpu_baseline(n: int, budget_s: float = 20.0) -> dict:
     return {"value": ms / (n / 1e6), "unit": UNIT, "cores": 1, "kind": "port",
             "sample": f"{n} triangles of the same distribution, oracle/lbvh_oracle.c restatement of "
                       f"lbvh_construction.cl, median of {len(times)} builds"}
+
+
+def bench_render(dev, args) -> dict:
+    """Path tracing throughput on the procedural Cornell box (996 triangles,
+    coat-over-diffuse sphere, quad light): 256 x 256 pixels, 16 samples per
+    pixel, depth 5, pinhole camera -- Msamples/s for the exact-order and the
+    nearer-child-first traversal."""
+    import torch
+
+    from clear_gb300 import scenes
+    from clear_gb300.render import DeviceScene
+
+    w = h = 256
+    spp = 16
+    ds = DeviceScene(scenes.cornell_box(w, h), dev)
+    out = {"workload": "cornell box 996 tris, 256x256, 16 spp, depth 5", "samples": w * h * spp}
+    stream = torch.cuda.current_stream(dev)
+    for name, ordered in (("exact", False), ("ordered", True)):
+        rng, pix = ds.new_frame()
+        ds.render(rng, pix, 2, max_depth=5, ordered=ordered)  # warm-up
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        reps = 3
+        e0.record(stream)
+        for _ in range(reps):
+            ds.render(rng, pix, spp, max_depth=5, ordered=ordered)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1) / reps
+        out[f"{name}_ms"] = ms
+        out[f"{name}_msamples_s"] = w * h * spp / ms / 1e3
+    return out
 
 
 def run_reference(args):
@@ -315,6 +348,7 @@ def run_ours(args):
     ordered_ms = t2.elapsed_time(t3) / trav_steps
     ordered_id_mismatch = int((hid != hid2).sum().item())
     ordered_t_mismatch = int((ht != ht2).sum().item())
+    render = bench_render(dev, args) if args.render else None
     hit_frac = float((hid >= 0).float().mean().item())
     occ_frac = float(occ.float().mean().item())
     clk = clocks.stop()
@@ -355,6 +389,7 @@ def run_ours(args):
                       "ordered_vs_exact_t_mismatches": ordered_t_mismatch,
                       "closest_ms": closest_ms, "shadow_ms": shadow_ms, "closest_hit_frac": hit_frac,
                       "shadow_occluded_frac": occ_frac},
+        "render": render,
         "gpu_launches": launches_per_build * args.steps,
         "clocks": clk,
         "device_error_bits": dev_err,
