@@ -409,6 +409,21 @@ __device__ __forceinline__ int delta_adj(const KeyT* __restrict__ keys, int kbit
 // split position; the reference's index of a node (its hi if it is child 0,
 // its lo if child 1, 0 for the root) is recorded for the reference-layout
 // export, and children and visiting order are the reference's.
+__device__ __forceinline__ unsigned int atomic_add_acq_rel(unsigned int* p, unsigned int v) {
+    unsigned int old;
+    asm volatile("atom.add.acq_rel.gpu.global.u32 %0, [%1], %2;" : "=r"(old) : "l"(p), "r"(v) : "memory");
+    return old;
+}
+
+__device__ __forceinline__ void tri_box(const float* vx, const float* vy, const float* vz, const uint32_t* tri,
+                                        uint32_t t, float box[6]) {
+    const TriVerts tv = load_tri(vx, vy, vz, tri, t);
+    for (int k = 0; k < 3; ++k) {
+        box[k] = fminf(tv.p[0][k], fminf(tv.p[1][k], tv.p[2][k]));
+        box[3 + k] = fmaxf(tv.p[0][k], fmaxf(tv.p[1][k], tv.p[2][k]));
+    }
+}
+
 template <typename KeyT>
 __global__ void __launch_bounds__(256) k_build_tree(const KeyT* __restrict__ keys, const uint32_t* __restrict__ sidx,
                                                     uint32_t n, int kbits, const float* __restrict__ vx,
@@ -420,7 +435,40 @@ __global__ void __launch_bounds__(256) k_build_tree(const KeyT* __restrict__ key
     if (j >= n) return;
     float box[6];
     emit_leaf(vx, vy, vz, tri, __ldg(sidx + j), j, tris, box);
+    // adjacent deltas around leaf j (-1 outside the array)
+    const int dl = j > 0 ? delta_adj(keys, kbits, j - 1) : -1;
+    const int dj = j + 1 < n ? delta_adj(keys, kbits, j) : -1;
+    const bool j_left = (j == 0) || (j != n - 1 && dj > dl);
     uint32_t lo = j, hi = j, ref = j | kLeafBit;
+    // A node whose two children are the leaves j and j+1 is finished by leaf
+    // j's thread alone (no arrival counter); leaf j+1's thread stops here.
+    if (j > 0 && !j_left) {
+        const int dll = j > 1 ? delta_adj(keys, kbits, j - 2) : -1;
+        const bool prev_left = (j - 1 == 0) || (dl > dll);
+        if (prev_left) return;  // leaf j-1 builds our common parent
+    }
+    if (j_left && j + 1 < n) {
+        const int dr = j + 2 < n ? delta_adj(keys, kbits, j + 1) : -1;
+        const bool next_right = (j + 1 == n - 1) || (dr < dj);
+        if (next_right) {
+            float b1[6];
+            tri_box(vx, vy, vz, tri, __ldg(sidx + j + 1), b1);
+            float* nd = nodes + 16u * j;
+            float4* n4 = reinterpret_cast<float4*>(nd);
+            n4[0] = make_float4(box[0], box[1], box[2], box[3]);
+            n4[1] = make_float4(box[4], box[5], b1[0], b1[1]);
+            n4[2] = make_float4(b1[2], b1[3], b1[4], b1[5]);
+            n4[3] = make_float4(__uint_as_float(j | kLeafBit), __uint_as_float((j + 1) | kLeafBit),
+                                __uint_as_float(j), __uint_as_float(j + 1));
+#pragma unroll
+            for (int k = 0; k < 3; ++k) {
+                box[k] = fminf(box[k], b1[k]);
+                box[3 + k] = fmaxf(box[3 + k], b1[3 + k]);
+            }
+            hi = j + 1;
+            ref = j;
+        }
+    }
     // every level up adds at least one common bit of the (3b + 32)-bit key
     for (int step = 0; step <= kMaxDepth; ++step) {
         if (lo == 0 && hi == n - 1) {
@@ -443,9 +491,9 @@ __global__ void __launch_bounds__(256) k_build_tree(const KeyT* __restrict__ key
         unsigned int* w = reinterpret_cast<unsigned int*>(nd);
         __stcg(w + 12 + slot, ref);
         __stcg(w + 14 + slot, left ? lo : hi);
-        __threadfence();  // publish this child before arriving
-        if (atomicAdd(counters + split, 1u) == 0u) return;  // sibling still climbing
-        __threadfence();  // observe the sibling's slot
+        // release: this child's slot is visible before the arrival counts;
+        // acquire: the sibling's slot is visible to the second arrival
+        if (atomic_add_acq_rel(counters + split, 1u) == 0u) return;
         float b[12];
 #pragma unroll
         for (int k = 0; k < 12; ++k) b[k] = __ldcg(nd + k);

@@ -144,7 +144,7 @@ __device__ bool intersect(const DScene& sc, f3 org, f3 dir, Hit& h, uint2* stack
 
 // rayTriangleIntersection's hit record + calcHitpointParameters
 // (bvh_traversal.cl:87-100, 110-158).
-__device__ void surface_point(const DScene& sc, f3 org, f3 dir, const Hit& h, SurfPt& sp) {
+__device__ __forceinline__ void surface_point(const DScene& sc, f3 org, f3 dir, const Hit& h, SurfPt& sp) {
     const Face f = load_face(sc, h.id);
     const f3 p0 = vtx(sc.vertices, f.p[0]), p1 = vtx(sc.vertices, f.p[1]), p2 = vtx(sc.vertices, f.p[2]);
     const f3 e1 = p1 - p0, e2 = p2 - p0;
@@ -188,9 +188,8 @@ __device__ void surface_point(const DScene& sc, f3 org, f3 dir, const Hit& h, Su
 // ------------------------------------------------------------------ BSDF
 
 // BSDFAlloc, reflection.cl:185-342
-__device__ void bsdf_alloc(const DScene& sc, uint32_t offset, const SurfPt& sp, BSDF& f) {
+__device__ __forceinline__ void bsdf_alloc(const DScene& sc, uint32_t offset, const SurfPt& sp, BSDF& f) {
     const uint8_t* m = sc.materials + offset;
-    f.num = min((int)m[0], kMaxBxDFs);
     const bool hasBump = m[1] != 0;
     const uint32_t idx_bump = ldb<uint32_t>(m + 4);
     f.n = sp.sNormal;
@@ -216,88 +215,30 @@ __device__ void bsdf_alloc(const DScene& sc, uint32_t offset, const SurfPt& sp, 
     }
     f.t = cross(f.n, f.s);
     f.ng = sp.gNormal;
-    const uint8_t* p = m + 8;  // sizeof(MaterialInfo)
-    int k = 0;
-    for (int i = 0; i < (int)m[0] && k < kMaxBxDFs; ++i) {
-        p = align_ptr(p, 4);
-        BxDF& b = f.bx[k];
-        b.fresnel = nullptr;
-        b.a = b.b = 0.f;
-        b.c1 = mk(0, 0, 0);
-        switch (p[0]) {
-            case 0: {  // DiffuseRElem {id, idx_R, idx_sigma}
-                b.id = kBxDiffuse;
-                b.type = kTyReflection | kTyDiffuse;
-                b.c0 = eval_color_texture(sc.textures + ldb<uint32_t>(p + 4), sp.uv);
-                float sigma2 = eval_float_texture(sc.textures + ldb<uint32_t>(p + 8), sp.uv);
-                sigma2 *= sigma2;
-                b.a = 1.0f - (sigma2 / (2.0f * (sigma2 + 0.33f)));
-                b.b = 0.45f * sigma2 / (sigma2 + 0.09f);
-                p += 12;
-                ++k;
-                break;
-            }
-            case 1: {  // SpecularRElem {id, idx_R, idx_Fresnel}
-                b.id = kBxSpecR;
-                b.type = kTyReflection | kTySpecular;
-                b.c0 = eval_color_texture(sc.textures + ldb<uint32_t>(p + 4), sp.uv);
-                b.fresnel = sc.others + ldb<uint32_t>(p + 8);
-                p += 12;
-                ++k;
-                break;
-            }
-            case 2: {  // SpecularTElem {id, idx_T, etaExt, etaInt, idx_Fresnel}
-                b.id = kBxSpecT;
-                b.type = kTyTransmission | kTySpecular;
-                b.c0 = eval_color_texture(sc.textures + ldb<uint32_t>(p + 4), sp.uv);
-                b.a = ldb<float>(p + 8);
-                b.b = ldb<float>(p + 12);
-                b.fresnel = sc.others + ldb<uint32_t>(p + 16);
-                p += 20;
-                ++k;
-                break;
-            }
-            case 3: {  // NewWardElem {id, idx_R, idx_anisoX, idx_anisoY}
-                b.id = kBxNewWard;
-                b.type = kTyReflection | kTyGlossy;
-                b.c0 = eval_color_texture(sc.textures + ldb<uint32_t>(p + 4), sp.uv);
-                b.a = eval_float_texture(sc.textures + ldb<uint32_t>(p + 8), sp.uv);
-                b.b = eval_float_texture(sc.textures + ldb<uint32_t>(p + 12), sp.uv);
-                p += 16;
-                ++k;
-                break;
-            }
-            case 4: {  // AshikhminSElem {id, idx_Rs, idx_nu, idx_nv}
-                b.id = kBxAshS;
-                b.type = kTyReflection | kTyGlossy;
-                b.c0 = eval_color_texture(sc.textures + ldb<uint32_t>(p + 4), sp.uv);
-                b.a = eval_float_texture(sc.textures + ldb<uint32_t>(p + 8), sp.uv);
-                b.b = eval_float_texture(sc.textures + ldb<uint32_t>(p + 12), sp.uv);
-                p += 16;
-                ++k;
-                break;
-            }
-            case 5: {  // AshikhminDElem {id, idx_Rs, idx_Rd}
-                b.id = kBxAshD;
-                b.type = kTyReflection | kTyDiffuse;
-                b.c0 = eval_color_texture(sc.textures + ldb<uint32_t>(p + 8), sp.uv);  // Rd
-                b.c1 = eval_color_texture(sc.textures + ldb<uint32_t>(p + 4), sp.uv);  // Rs
-                p += 12;
-                ++k;
-                break;
-            }
-            default:
-                i = (int)m[0];  // unknown element: stop decoding (the reference leaves a zero offset)
-                break;
+    f.mat = m;
+    f.tex = sc.textures;
+    f.others = sc.others;
+    f.uv = sp.uv;
+    // component offsets (AlignPtrG(&matsData_p, 4) per element, reflection.cl:230-341)
+    const int num = min((int)m[0], kMaxBxDFs);
+    uint32_t off = 8;  // sizeof(MaterialInfo)
+#pragma unroll
+    for (int i = 0; i < kMaxBxDFs; ++i) {
+        if (i < num) {
+            off = (off + 3u) & ~3u;
+            f.off[i] = (uint16_t)off;
+            f.type[i] = elem_type(m[off]);
+            off += elem_size(m[off]);
+        } else {
+            f.off[i] = 0;
+            f.type[i] = 0;
         }
     }
-    f.num = k > 0 ? k : 1;
-    if (k == 0) {  // keep a defined BSDF for malformed blobs: black diffuse
-        f.bx[0].id = kBxDiffuse;
-        f.bx[0].type = kTyReflection | kTyDiffuse;
-        f.bx[0].c0 = mk(0, 0, 0);
-        f.bx[0].a = 1.0f;
-        f.bx[0].b = 0.0f;
+    f.num = num;
+    if (num == 0) {  // a material without components renders black
+        f.num = 1;
+        f.off[0] = 0xFFFF;
+        f.type[0] = kTyReflection | kTyDiffuse;
     }
 }
 
@@ -320,33 +261,32 @@ __device__ __forceinline__ const uint8_t* light_distribution(const DScene& sc) {
 }
 
 // EDFAlloc, light.cl:295-379
-__device__ void edf_alloc(const DScene& sc, uint32_t offset, const LightPt& lp, EDF& e) {
+__device__ __forceinline__ void edf_alloc(const DScene& sc, uint32_t offset, const LightPt& lp, EDF& e) {
     e.env = lp.atInfinity;
-    int k = 0;
-    if (lp.atInfinity) {
-        const uint8_t* l = env_light_property(sc);
-        const uint8_t* p = l + 1;
-        for (int i = 0; i < (int)l[0] && k < kMaxBxDFs; ++i) {
-            p = align_ptr(p, 4);
-            if (p[0] != 0) break;
-            // ImageBasedEnvLElem {id, idx_Le, multiplier, idx_Dist2D}
-            e.M[k++] = eval_color_texture(sc.textures + ldb<uint32_t>(p + 4), lp.uv) * ldb<float>(p + 8);
-            p += 16;
-        }
-    } else {
-        const uint8_t* l = sc.materials + offset;
+    e.tex = sc.textures;
+    e.uv = lp.uv;
+    e.prop = lp.atInfinity ? env_light_property(sc) : sc.materials + offset;
+    if (!lp.atInfinity) {
         e.n = lp.sNormal;
         if (lp.hasTangent) e.s = lp.sTangent;
         else make_tangent(lp.sNormal, e.s);
         e.t = cross(e.n, e.s);
         e.ng = lp.gNormal;
-        const uint8_t* p = l + 1;
-        for (int i = 0; i < (int)l[0] && k < kMaxBxDFs; ++i) {
-            p = align_ptr(p, 4);
-            if (p[0] != 0) break;
-            // DiffuseLElem {id, idx_M}
-            e.M[k++] = eval_color_texture(sc.textures + ldb<uint32_t>(p + 4), lp.uv);
-            p += 8;
+    }
+    // ImageBasedEnvLElem (16 B) / DiffuseLElem (8 B), 4-byte aligned after
+    // the 1-byte LightPropertyInfo
+    const int num = min((int)e.prop[0], kMaxBxDFs);
+    const uint32_t size = lp.atInfinity ? 16u : 8u;
+    uint32_t off = 1;
+    int k = 0;
+#pragma unroll
+    for (int i = 0; i < kMaxBxDFs; ++i) {
+        off = (off + 3u) & ~3u;
+        const bool ok = i < num && e.prop[off] == 0;
+        e.off[i] = (uint16_t)off;
+        if (ok && k == i) {
+            ++k;
+            off += size;
         }
     }
     e.num = k;
@@ -365,7 +305,7 @@ __device__ __forceinline__ void light_from_surface(const SurfPt& s, LightPt& l) 
 }
 
 // sampleLightPos, light.cl:138-245; returns the light property offset.
-__device__ void sample_light(const DScene& sc, float uL, float u0, float u1, LightPt& lp, EDF& e, float& areaPDF) {
+__device__ __forceinline__ void sample_light(const DScene& sc, float uL, float u0, float u1, LightPt& lp, EDF& e, float& areaPDF) {
     const uint8_t* dist = light_distribution(sc);
     const uint32_t li = sample_discrete_1d(dist, uL, &areaPDF);
     const uint8_t atInf = sc.lights[8u * li];
@@ -427,7 +367,7 @@ __device__ void sample_light(const DScene& sc, float uL, float u0, float u1, Lig
 }
 
 // getAreaPDF, light.cl:247-292
-__device__ float area_pdf(const DScene& sc, const LightPt& lp) {
+__device__ __forceinline__ float area_pdf(const DScene& sc, const LightPt& lp) {
     const uint8_t* dist = light_distribution(sc);
     const uint32_t numItems = ldb<uint32_t>(dist + 4);
     if (lp.atInfinity) {

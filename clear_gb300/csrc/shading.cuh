@@ -330,11 +330,104 @@ struct BxDF {
 
 constexpr int kMaxBxDFs = 4;
 
+// A BSDF as the reference's BSDFAlloc builds it (reflection.cl:185-342), but
+// holding only the shading frame and where each component's parameters live
+// in the material blob: a component's textures are evaluated when the
+// component is used (the blobs are small and cache resident), so no per-thread
+// array of decoded components is kept.
 struct BSDF {
+    const uint8_t* mat;
+    const uint8_t* tex;
+    const uint8_t* others;
+    float2 uv;
     int num;
+    uint16_t off[kMaxBxDFs];   // element offset from `mat`
+    uint8_t type[kMaxBxDFs];   // BxDFType of each component
     f3 n, s, t, ng;
-    BxDF bx[kMaxBxDFs];
 };
+
+__device__ __forceinline__ uint8_t elem_type(uint8_t id) {
+    switch (id) {
+        case kBxDiffuse: return kTyReflection | kTyDiffuse;
+        case kBxSpecR: return kTyReflection | kTySpecular;
+        case kBxSpecT: return kTyTransmission | kTySpecular;
+        case kBxNewWard: return kTyReflection | kTyGlossy;
+        case kBxAshS: return kTyReflection | kTyGlossy;
+        case kBxAshD: return kTyReflection | kTyDiffuse;
+        default: return kTyReflection | kTyDiffuse;
+    }
+}
+
+__device__ __forceinline__ int elem_size(uint8_t id) {
+    switch (id) {
+        case kBxSpecT: return 20;
+        case kBxNewWard: case kBxAshS: return 16;
+        default: return 12;
+    }
+}
+
+// Component i of the BSDF with its textures evaluated (the BxDF part of
+// BSDFAlloc, reflection.cl:230-341).  Unknown element ids decode as black
+// diffuse.
+__device__ BxDF load_bx(const BSDF& f, uint32_t off) {
+    BxDF b;
+    if (off == 0xFFFF) {  // empty material: black diffuse
+        b.id = kBxDiffuse;
+        b.type = kTyReflection | kTyDiffuse;
+        b.c0 = b.c1 = mk(0, 0, 0);
+        b.a = 1.0f;
+        b.b = 0.0f;
+        b.fresnel = nullptr;
+        return b;
+    }
+    const uint8_t* p = f.mat + off;
+    b.id = p[0];
+    b.type = elem_type(p[0]);
+    b.fresnel = nullptr;
+    b.a = b.b = 0.f;
+    b.c1 = mk(0, 0, 0);
+    switch (p[0]) {
+        case kBxDiffuse: {  // DiffuseRElem {id, idx_R, idx_sigma}
+            b.c0 = eval_color_texture(f.tex + ldb<uint32_t>(p + 4), f.uv);
+            float sigma2 = eval_float_texture(f.tex + ldb<uint32_t>(p + 8), f.uv);
+            sigma2 *= sigma2;
+            b.a = 1.0f - (sigma2 / (2.0f * (sigma2 + 0.33f)));
+            b.b = 0.45f * sigma2 / (sigma2 + 0.09f);
+            break;
+        }
+        case kBxSpecR:  // SpecularRElem {id, idx_R, idx_Fresnel}
+            b.c0 = eval_color_texture(f.tex + ldb<uint32_t>(p + 4), f.uv);
+            b.fresnel = f.others + ldb<uint32_t>(p + 8);
+            break;
+        case kBxSpecT:  // SpecularTElem {id, idx_T, etaExt, etaInt, idx_Fresnel}
+            b.c0 = eval_color_texture(f.tex + ldb<uint32_t>(p + 4), f.uv);
+            b.a = ldb<float>(p + 8);
+            b.b = ldb<float>(p + 12);
+            b.fresnel = f.others + ldb<uint32_t>(p + 16);
+            break;
+        case kBxNewWard:  // NewWardElem {id, idx_R, idx_anisoX, idx_anisoY}
+        case kBxAshS:     // AshikhminSElem {id, idx_Rs, idx_nu, idx_nv}
+            b.c0 = eval_color_texture(f.tex + ldb<uint32_t>(p + 4), f.uv);
+            b.a = eval_float_texture(f.tex + ldb<uint32_t>(p + 8), f.uv);
+            b.b = eval_float_texture(f.tex + ldb<uint32_t>(p + 12), f.uv);
+            break;
+        case kBxAshD:  // AshikhminDElem {id, idx_Rs, idx_Rd}
+            b.c0 = eval_color_texture(f.tex + ldb<uint32_t>(p + 8), f.uv);  // Rd
+            b.c1 = eval_color_texture(f.tex + ldb<uint32_t>(p + 4), f.uv);  // Rs
+            break;
+        default:
+            b.id = kBxDiffuse;
+            b.c0 = mk(0, 0, 0);
+            b.a = 1.0f;
+            break;
+    }
+    return b;
+}
+
+template <typename T>
+__device__ __forceinline__ T pick4(const T* a, uint32_t i) {
+    return i == 0 ? a[0] : (i == 1 ? a[1] : (i == 2 ? a[2] : a[3]));
+}
 
 __device__ f3 eval_fresnel(const uint8_t* fr, float cosi) {  // reflection.cl:345-390
     switch (fr[0]) {
@@ -535,22 +628,24 @@ __device__ f3 bx_sample(const BxDF& b, f3 vout, float u0, float u1, f3& vin, flo
 }
 
 __device__ __forceinline__ bool bsdf_has_non_specular(const BSDF& f) {
-    for (int i = 0; i < f.num; ++i)
-        if (f.bx[i].type & kTyNonSingular) return true;
-    return false;
+    bool r = false;
+#pragma unroll
+    for (int i = 0; i < kMaxBxDFs; ++i)
+        if (i < f.num && (f.type[i] & kTyNonSingular)) r = true;
+    return r;
 }
 
-__device__ __forceinline__ bool match_type(const BxDF& b, uint32_t mask) { return (b.type & mask) == b.type; }
+__device__ __forceinline__ bool match_type(uint8_t type, uint32_t mask) { return (type & mask) == type; }
 
 // sample_fs, reflection.cl:629-677
-__device__ f3 bsdf_sample(const BSDF& f, f3 vout, float uc, float u0, float u1, f3& vin, float& pdf,
+__device__ __forceinline__ f3 bsdf_sample(const BSDF& f, f3 vout, float uc, float u0, float u1, f3& vin, float& pdf,
                           uint32_t& sampledType) {
     const f3 zero = mk(0, 0, 0);
     uint32_t flags = kTyAll;
     const uint32_t numMatches = (uint32_t)f.num;
     const f3 vl = world_to_local(f.s, f.t, f.n, vout);
     const uint32_t which = rand_uint(uc, (uint32_t)f.num);
-    const BxDF& b = f.bx[which];
+    const BxDF b = load_bx(f, pick4(f.off, which));
     f3 vinl = zero;
     f3 ret = bx_sample(b, vl, u0, u1, vinl, pdf);
     if (pdf == 0.0f) {
@@ -560,58 +655,79 @@ __device__ f3 bsdf_sample(const BSDF& f, f3 vout, float uc, float u0, float u1, 
     sampledType = b.type;
     vin = local_to_world(f.s, f.t, f.n, vinl);
     if (!(b.type & kTySpecular) && numMatches > 1) {
-        for (int i = 0; i < f.num; ++i)
-            if ((uint32_t)i != which && match_type(f.bx[i], flags)) pdf += bx_pdf(f.bx[i], vl, vinl);
+#pragma unroll
+        for (int i = 0; i < kMaxBxDFs; ++i)
+            if (i < f.num && (uint32_t)i != which && match_type(f.type[i], flags))
+                pdf += bx_pdf(load_bx(f, f.off[i]), vl, vinl);
     }
     pdf /= (float)numMatches;
     if (!(b.type & kTySpecular)) {
         ret = zero;
         if (dot(vin, f.ng) * dot(vout, f.ng) > 0) flags &= ~kTyTransmission;
         else flags &= ~kTyReflection;
-        for (int i = 0; i < f.num; ++i)
-            if (match_type(f.bx[i], flags)) ret += bx_f(f.bx[i], vl, vinl);
+#pragma unroll
+        for (int i = 0; i < kMaxBxDFs; ++i)
+            if (i < f.num && match_type(f.type[i], flags)) ret += bx_f(load_bx(f, f.off[i]), vl, vinl);
     }
     return ret;
 }
 
 // fs, reflection.cl:679-702
-__device__ f3 bsdf_f(const BSDF& f, f3 vout, f3 vin) {
+__device__ __forceinline__ f3 bsdf_f(const BSDF& f, f3 vout, f3 vin) {
     uint32_t flags = kTyAll;
     const f3 vl = world_to_local(f.s, f.t, f.n, vout), il = world_to_local(f.s, f.t, f.n, vin);
     f3 ret = mk(0, 0, 0);
     if (dot(vin, f.ng) * dot(vout, f.ng) > 0) flags &= ~kTyTransmission;
     else flags &= ~kTyReflection;
-    for (int i = 0; i < f.num; ++i)
-        if (match_type(f.bx[i], flags)) ret += bx_f(f.bx[i], vl, il);
+#pragma unroll
+    for (int i = 0; i < kMaxBxDFs; ++i)
+        if (i < f.num && match_type(f.type[i], flags)) ret += bx_f(load_bx(f, f.off[i]), vl, il);
     return ret;
 }
 
 // fs_pdf, reflection.cl:704-723
-__device__ float bsdf_pdf(const BSDF& f, f3 vout, f3 vin) {
+__device__ __forceinline__ float bsdf_pdf(const BSDF& f, f3 vout, f3 vin) {
     const f3 vl = world_to_local(f.s, f.t, f.n, vout), il = world_to_local(f.s, f.t, f.n, vin);
     float pdf = 0.0f;
-    for (int i = 0; i < f.num; ++i)
-        if (match_type(f.bx[i], kTyAll)) pdf += bx_pdf(f.bx[i], vl, il);
+#pragma unroll
+    for (int i = 0; i < kMaxBxDFs; ++i)
+        if (i < f.num && match_type(f.type[i], kTyAll)) pdf += bx_pdf(load_bx(f, f.off[i]), vl, il);
     return pdf / (uint32_t)f.num;
 }
 
 // ------------------------------------------------------------------- EDF
-// light.cl:46-84, 295-440.
+// light.cl:46-84, 295-440.  As for the BSDF, only the frame and the blob
+// offsets of the emission components are kept; their textures are evaluated
+// in Le.
 
 struct EDF {
     bool env;
     int num;
+    const uint8_t* prop;   // light property (materials blob)
+    const uint8_t* tex;
+    float2 uv;
+    uint16_t off[kMaxBxDFs];
     f3 n, s, t, ng;
-    f3 M[kMaxBxDFs];  // DiffuseEmission M, or EntireSceneEmission Le
 };
+
+__device__ __forceinline__ f3 edf_component(const EDF& e, uint32_t off) {
+    const uint8_t* p = e.prop + off;
+    if (e.env)  // ImageBasedEnvLElem {id, idx_Le, multiplier, idx_Dist2D}
+        return eval_color_texture(e.tex + ldb<uint32_t>(p + 4), e.uv) * ldb<float>(p + 8);
+    return eval_color_texture(e.tex + ldb<uint32_t>(p + 4), e.uv);  // DiffuseLElem {id, idx_M}
+}
 
 __device__ __forceinline__ f3 edf_le(const EDF& e, f3 vout) {  // Le, light.cl:409-436
     f3 r = mk(0, 0, 0);
     if (!e.env) {
         const f3 vl = world_to_local(e.s, e.t, e.n, vout);
-        for (int i = 0; i < e.num; ++i) r += vl.z > 0.0f ? e.M[i] / kPi : mk(0, 0, 0);
+#pragma unroll
+        for (int i = 0; i < kMaxBxDFs; ++i)
+            if (i < e.num) r += vl.z > 0.0f ? edf_component(e, e.off[i]) / kPi : mk(0, 0, 0);
     } else {
-        for (int i = 0; i < e.num; ++i) r += e.M[i];
+#pragma unroll
+        for (int i = 0; i < kMaxBxDFs; ++i)
+            if (i < e.num) r += edf_component(e, e.off[i]);
     }
     return r;
 }
