@@ -75,6 +75,7 @@ def parse():
     ap.add_argument("--rays", type=int, default=N_RAYS)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--render", type=int, default=1, help="also time the path tracer (0 = skip)")
+    ap.add_argument("--render-only", action="store_true", help="time only the path tracer (for profiling)")
     return ap.parse_args()
 
 
@@ -403,6 +404,15 @@ def run_ours(args):
 
 def main():
     args = parse()
+    if args.render_only:
+        import torch
+
+        from clear_gb300.build import build
+
+        build()
+        dev = torch.device("cuda", 0)
+        print(json.dumps({"render": bench_render(dev, args)}), flush=True)
+        return
     if args.impl == "reference":
         run_reference(args)
     else:
