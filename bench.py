@@ -192,15 +192,16 @@ def bench_render(dev, args) -> dict:
     ds = DeviceScene(scenes.cornell_box(w, h), dev)
     out = {"workload": "cornell box 996 tris, 256x256, 16 spp, depth 5", "samples": w * h * spp}
     stream = torch.cuda.current_stream(dev)
-    for name, ordered in (("exact", False), ("ordered", True)):
+    for name, ordered, wf in (("exact", False, False), ("ordered", True, False), ("wavefront_exact", False, True),
+                              ("wavefront_ordered", True, True)):
         rng, pix = ds.new_frame()
-        ds.render(rng, pix, 2, max_depth=5, ordered=ordered)  # warm-up
+        ds.render(rng, pix, 2, max_depth=5, ordered=ordered, wavefront=wf)  # warm-up
         torch.cuda.synchronize()
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         reps = 3
         e0.record(stream)
         for _ in range(reps):
-            ds.render(rng, pix, spp, max_depth=5, ordered=ordered)
+            ds.render(rng, pix, spp, max_depth=5, ordered=ordered, wavefront=wf)
         e1.record(stream)
         torch.cuda.synchronize()
         ms = e0.elapsed_time(e1) / reps

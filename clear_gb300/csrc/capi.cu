@@ -19,11 +19,13 @@ extern "C" const char* clr_last_error_string(void) { return t_last_error; }
 cudaError_t clr_status_lbvh(unsigned int* v, int clear);
 cudaError_t clr_status_traverse(unsigned int* v, int clear);
 cudaError_t clr_status_render(unsigned int* v, int clear);
+cudaError_t clr_status_render_wf(unsigned int* v, int clear);
 
 extern "C" int clr_device_status(uint32_t* bits, int clear) {
     CLR_CUDA_TRY(cudaDeviceSynchronize());
     unsigned int all = 0;
-    cudaError_t (*readers[])(unsigned int*, int) = {clr_status_lbvh, clr_status_traverse, clr_status_render};
+    cudaError_t (*readers[])(unsigned int*, int) = {clr_status_lbvh, clr_status_traverse, clr_status_render,
+                                                   clr_status_render_wf};
     for (auto rd : readers) {
         unsigned int v = 0;
         CLR_CUDA_TRY(rd(&v, clear));

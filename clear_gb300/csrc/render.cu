@@ -20,449 +20,20 @@
 //     unset face id when nothing is hit (pathtracer.cl:120-122);
 //   * samples-per-pixel loop inside the kernel (the reference launches once
 //     per sample); each pixel's contributions are added in the same order.
-#include "common.cuh"
-#include "shading.cuh"
-#include "traverse.cuh"
+#include "render_common.cuh"
 
 CLR_DEFINE_STATUS_READER(render)
 
 namespace clr {
-
-constexpr float kEpsilon = 0.00001f;  // global.cl:28
-constexpr uint16_t kNone16 = 0xFFFF;
-constexpr uint32_t kNone32 = 0xFFFFFFFFu;
-
-struct DScene {
-    const float4* vertices;
-    const float4* normals;
-    const float4* tangents;
-    const float2* uvs;
-    const uint8_t* faces;
-    const uint8_t* lights;
-    const uint8_t* materials;
-    const uint8_t* textures;
-    const uint8_t* others;
-    const float4* nodes;
-    const float4* tris;
-    const float* root_box;
-    uint32_t num_tris;
-};
-
-struct Face {
-    uint32_t p[3], vn[3], vt[3], uv[3];
-    uint32_t alphaTex;
-    uint16_t mat, light;
-};
-
-__device__ __forceinline__ Face load_face(const DScene& sc, uint32_t id) {
-    const uint32_t* w = reinterpret_cast<const uint32_t*>(sc.faces + 56u * id);
-    Face f;
-#pragma unroll
-    for (int k = 0; k < 3; ++k) {
-        f.p[k] = w[k];
-        f.vn[k] = w[3 + k];
-        f.vt[k] = w[6 + k];
-        f.uv[k] = w[9 + k];
-    }
-    f.alphaTex = w[12];
-    f.mat = (uint16_t)(w[13] & 0xFFFFu);
-    f.light = (uint16_t)(w[13] >> 16);
-    return f;
-}
-
-__device__ __forceinline__ f3 vtx(const float4* a, uint32_t i) {
-    const float4 v = __ldg(a + i);
-    return mk(v.x, v.y, v.z);
-}
-
-// ------------------------------------------------------------- traversal
-
-struct Hit {
-    uint32_t id;
-    float t, b1, b2;
-};
-
-// rayIntersection for the renderer: returns the closest hit with its
-// barycentrics.  kOrdered visits the nearer child first.
-template <bool kOrdered>
-__device__ bool intersect(const DScene& sc, f3 org, f3 dir, Hit& h, uint2* stack) {
-    Ray ray{org.x, org.y, org.z, INFINITY, dir.x, dir.y, dir.z};
-    const float ix = 1.0f / dir.x, iy = 1.0f / dir.y, iz = 1.0f / dir.z;
-    float t = INFINITY;
-    uint32_t best = kNone32;
-    float bb1 = 0.f, bb2 = 0.f;
-    float entry;
-    const float* rb = sc.root_box;
-    if (!box_test_fast(rb[0], rb[1], rb[2], rb[4], rb[5], rb[6], ray, ix, iy, iz, entry)) return false;
-    auto test_leaf = [&](uint32_t leaf) {
-        const float4 a = __ldg(sc.tris + 3u * leaf), b = __ldg(sc.tris + 3u * leaf + 1u),
-                     c = __ldg(sc.tris + 3u * leaf + 2u);
-        float b1, b2;
-        if (tri_test(a, b, c, ray, t, &b1, &b2)) {
-            best = __float_as_uint(a.w);
-            bb1 = b1;
-            bb2 = b2;
-        }
-    };
-    if (sc.num_tris == 1) {
-        test_leaf(0);
-    } else if (sc.num_tris >= 2) {
-        int sp = 0;
-        stack[sp++] = make_uint2(__float_as_uint(rb[3]), __float_as_uint(entry));
-        for (uint32_t guard = 0; sp > 0 && guard < sc.num_tris; ++guard) {
-            --sp;
-            if (__uint_as_float(stack[sp].y) > t) continue;
-            const NodeBoxes nb = load_node(sc.nodes, stack[sp].x);
-            float e0, e1;
-            const bool p0 = box_test_fast(nb.b0[0], nb.b0[1], nb.b0[2], nb.b0[3], nb.b0[4], nb.b0[5], ray, ix, iy, iz, e0);
-            const bool p1 = box_test_fast(nb.b1[0], nb.b1[1], nb.b1[2], nb.b1[3], nb.b1[4], nb.b1[5], ray, ix, iy, iz, e1);
-            const bool leaf0 = (nb.ref0 & kLeafBit) != 0, leaf1 = (nb.ref1 & kLeafBit) != 0;
-            const bool swap = kOrdered && (e1 < e0);
-#pragma unroll
-            for (int k = 0; k < 2; ++k) {
-                int c = k;
-                if (kOrdered) c = (!leaf0 && !leaf1) ? (swap ? k : 1 - k) : (swap ? 1 - k : k);
-                const uint32_t ref = c ? nb.ref1 : nb.ref0;
-                const bool pass = c ? p1 : p0;
-                const float e = c ? e1 : e0;
-                if (ref & kLeafBit) {
-                    if (pass && !(e > t)) test_leaf(ref & ~kLeafBit);
-                } else if (pass) {
-                    if (sp < kStackSize) stack[sp++] = make_uint2(ref, __float_as_uint(e));
-                    else clr_raise(CLR_DEVERR_STACK);
-                }
-            }
-        }
-    }
-    if (best == kNone32) return false;
-    h.id = best;
-    h.t = t;
-    h.b1 = bb1;
-    h.b2 = bb2;
-    return true;
-}
-
-// rayTriangleIntersection's hit record + calcHitpointParameters
-// (bvh_traversal.cl:87-100, 110-158).
-__device__ __forceinline__ void surface_point(const DScene& sc, f3 org, f3 dir, const Hit& h, SurfPt& sp) {
-    const Face f = load_face(sc, h.id);
-    const f3 p0 = vtx(sc.vertices, f.p[0]), p1 = vtx(sc.vertices, f.p[1]), p2 = vtx(sc.vertices, f.p[2]);
-    const f3 e1 = p1 - p0, e2 = p2 - p0;
-    const float b1 = h.b1, b2 = h.b2;
-    const float b0 = 1.0f - b1 - b2;
-    sp.p = org + dir * h.t;
-    sp.gNormal = normalize(cross(e1, e2));
-    sp.faceID = h.id;
-    const bool hasUV = f.uv[0] != kNone32;
-    float2 uv0 = make_float2(0.f, 0.f), uv1 = uv0, uv2 = uv0;
-    sp.uv = make_float2(0.f, 0.f);
-    if (hasUV) {
-        uv0 = __ldg(sc.uvs + f.uv[0]);
-        uv1 = __ldg(sc.uvs + f.uv[1]);
-        uv2 = __ldg(sc.uvs + f.uv[2]);
-        sp.uv = make_float2(b0 * uv0.x + b1 * uv1.x + b2 * uv2.x, b0 * uv0.y + b1 * uv1.y + b2 * uv2.y);
-    }
-    // calcHitpointParameters recomputes b2 from (b0, b1)
-    const float c0 = b0, c1 = b1, c2 = 1.0f - c0 - c1;
-    const bool hasVN = f.vn[0] != kNone32;
-    if (hasVN)
-        sp.sNormal = normalize(c0 * vtx(sc.normals, f.vn[0]) + c1 * vtx(sc.normals, f.vn[1]) + c2 * vtx(sc.normals, f.vn[2]));
-    else
-        sp.sNormal = sp.gNormal;
-    sp.hasTangent = f.vt[0] != kNone32;
-    if (sp.hasTangent)
-        sp.sTangent = normalize(c0 * vtx(sc.tangents, f.vt[0]) + c1 * vtx(sc.tangents, f.vt[1]) +
-                                c2 * vtx(sc.tangents, f.vt[2]));
-    else
-        sp.sTangent = mk(0, 0, 0);
-    sp.uDir = mk(0, 0, 0);
-    if (hasUV) {
-        const float du0 = uv0.x - uv2.x, dv0 = uv0.y - uv2.y, du1 = uv1.x - uv2.x, dv1 = uv1.y - uv2.y;
-        const f3 dP0 = p0 - p2, dP1 = p1 - p2;
-        const float invDetUV = 1.0f / (du0 * dv1 - dv0 * du1);
-        const f3 uDir = invDetUV * mk(dv1 * dP0.x - dv0 * dP1.x, dv1 * dP0.y - dv0 * dP1.y, dv1 * dP0.z - dv0 * dP1.z);
-        sp.uDir = hasVN ? normalize(cross(cross(sp.sNormal, uDir), sp.sNormal)) : normalize(uDir);
-    }
-}
-
-// ------------------------------------------------------------------ BSDF
-
-// BSDFAlloc, reflection.cl:185-342
-__device__ __forceinline__ void bsdf_alloc(const DScene& sc, uint32_t offset, const SurfPt& sp, BSDF& f) {
-    const uint8_t* m = sc.materials + offset;
-    const bool hasBump = m[1] != 0;
-    const uint32_t idx_bump = ldb<uint32_t>(m + 4);
-    f.n = sp.sNormal;
-    if (sp.hasTangent) f.s = sp.sTangent;
-    else make_tangent(sp.sNormal, f.s);
-    if (hasBump) {
-        const f3 c = eval_color_texture(sc.textures + idx_bump, sp.uv);
-        const f3 nBump = normalize(mk(2.0f * c.x - 1.0f, 2.0f * c.y - 1.0f, 2.0f * c.z - 1.0f));
-        const f3 vDir = cross(sp.uDir, sp.sNormal);
-        f.n = mk(dot(mk(sp.uDir.x, vDir.x, sp.sNormal.x), nBump), dot(mk(sp.uDir.y, vDir.y, sp.sNormal.y), nBump),
-                 dot(mk(sp.uDir.z, vDir.z, sp.sNormal.z), nBump));
-        f3 ax = cross(sp.sNormal, f.n);
-        const float sinTH = fminf(length(ax), 1.0f);
-        if (sinTH > 0.0001f) {
-            ax = normalize(ax);
-            const float cosTH = cosf(asinf(sinTH));
-            const float om = 1 - cosTH;
-            const f3 s = f.s;
-            f.s = mk(dot(mk(ax.x * ax.x * om + cosTH, ax.x * ax.y * om - ax.z * sinTH, ax.z * ax.x * om + ax.y * sinTH), s),
-                     dot(mk(ax.x * ax.y * om + ax.z * sinTH, ax.y * ax.y * om + cosTH, ax.y * ax.z * om - ax.x * sinTH), s),
-                     dot(mk(ax.z * ax.x * om - ax.y * sinTH, ax.y * ax.z * om + ax.x * sinTH, ax.z * ax.z * om + cosTH), s));
-        }
-    }
-    f.t = cross(f.n, f.s);
-    f.ng = sp.gNormal;
-    f.mat = m;
-    f.tex = sc.textures;
-    f.others = sc.others;
-    f.uv = sp.uv;
-    // component offsets (AlignPtrG(&matsData_p, 4) per element, reflection.cl:230-341)
-    const int num = min((int)m[0], kMaxBxDFs);
-    uint32_t off = 8;  // sizeof(MaterialInfo)
-#pragma unroll
-    for (int i = 0; i < kMaxBxDFs; ++i) {
-        if (i < num) {
-            off = (off + 3u) & ~3u;
-            f.off[i] = (uint16_t)off;
-            f.type[i] = elem_type(m[off]);
-            off += elem_size(m[off]);
-        } else {
-            f.off[i] = 0;
-            f.type[i] = 0;
-        }
-    }
-    f.num = num;
-    if (num == 0) {  // a material without components renders black
-        f.num = 1;
-        f.off[0] = 0xFFFF;
-        f.type[0] = kTyReflection | kTyDiffuse;
-    }
-}
-
-// ---------------------------------------------------------------- lights
-
-struct LightPt {
-    f3 p, gNormal, sNormal, sTangent, uDir;
-    float2 uv;
-    uint32_t faceID;
-    bool hasTangent, atInfinity;
-};
-
-__device__ __forceinline__ const uint8_t* env_light_property(const DScene& sc) {
-    const uint32_t env_off = ldb<uint32_t>(sc.others + 4);
-    return sc.materials + ldb<uint32_t>(sc.others + env_off);
-}
-
-__device__ __forceinline__ const uint8_t* light_distribution(const DScene& sc) {
-    return sc.others + ldb<uint32_t>(sc.others + 8);
-}
-
-// EDFAlloc, light.cl:295-379
-__device__ __forceinline__ void edf_alloc(const DScene& sc, uint32_t offset, const LightPt& lp, EDF& e) {
-    e.env = lp.atInfinity;
-    e.tex = sc.textures;
-    e.uv = lp.uv;
-    e.prop = lp.atInfinity ? env_light_property(sc) : sc.materials + offset;
-    if (!lp.atInfinity) {
-        e.n = lp.sNormal;
-        if (lp.hasTangent) e.s = lp.sTangent;
-        else make_tangent(lp.sNormal, e.s);
-        e.t = cross(e.n, e.s);
-        e.ng = lp.gNormal;
-    }
-    // ImageBasedEnvLElem (16 B) / DiffuseLElem (8 B), 4-byte aligned after
-    // the 1-byte LightPropertyInfo
-    const int num = min((int)e.prop[0], kMaxBxDFs);
-    const uint32_t size = lp.atInfinity ? 16u : 8u;
-    uint32_t off = 1;
-    int k = 0;
-#pragma unroll
-    for (int i = 0; i < kMaxBxDFs; ++i) {
-        off = (off + 3u) & ~3u;
-        const bool ok = i < num && e.prop[off] == 0;
-        e.off[i] = (uint16_t)off;
-        if (ok && k == i) {
-            ++k;
-            off += size;
-        }
-    }
-    e.num = k;
-}
-
-__device__ __forceinline__ void light_from_surface(const SurfPt& s, LightPt& l) {
-    l.p = s.p;
-    l.gNormal = s.gNormal;
-    l.sNormal = s.sNormal;
-    l.sTangent = s.sTangent;
-    l.uDir = s.uDir;
-    l.uv = s.uv;
-    l.faceID = s.faceID;
-    l.hasTangent = s.hasTangent;
-    l.atInfinity = false;
-}
-
-// sampleLightPos, light.cl:138-245; returns the light property offset.
-__device__ __forceinline__ void sample_light(const DScene& sc, float uL, float u0, float u1, LightPt& lp, EDF& e, float& areaPDF) {
-    const uint8_t* dist = light_distribution(sc);
-    const uint32_t li = sample_discrete_1d(dist, uL, &areaPDF);
-    const uint8_t atInf = sc.lights[8u * li];
-    const uint32_t ref = ldb<uint32_t>(sc.lights + 8u * li + 4);
-    uint32_t lightProp = kNone16;
-    if (atInf) {
-        lp.atInfinity = true;
-        const uint8_t* l = env_light_property(sc);
-        areaPDF *= 1.0f;
-        const uint8_t* p = l + 1;
-        for (int i = 0; i < (int)l[0]; ++i) {
-            p = align_ptr(p, 4);
-            if (p[0] != 0) break;
-            if (i == 0) {  // whichIBL = 0
-                float uvPDF;
-                lp.uv = sample_cc_2d(sc.others + ldb<uint32_t>(p + 12), u0, u1, &uvPDF);
-                const float theta = lp.uv.y * kPi, phi = lp.uv.x * 2 * kPi;
-                const float sinTheta = sinf(theta);
-                lp.p = mk(-sinf(phi) * sinTheta, cosf(theta), cosf(phi) * sinTheta);
-                areaPDF *= uvPDF / (2 * kPi * kPi * sinTheta);
-                continue;
-            }
-            p += 16;
-        }
-    } else {
-        lp.atInfinity = false;
-        lp.faceID = ref;
-        const Face f = load_face(sc, ref);
-        const f3 p0 = vtx(sc.vertices, f.p[0]), p1 = vtx(sc.vertices, f.p[1]), p2 = vtx(sc.vertices, f.p[2]);
-        const float su1 = sqrtf(u0);
-        const float b0 = 1.0f - su1, b1 = u1 * su1;
-        const float b2 = 1.0f - b0 - b1;
-        const f3 ng = cross(p1 - p0, p2 - p0);
-        const float area = 0.5f * length(ng);
-        areaPDF *= 1.0f / area;
-        lp.p = b0 * p0 + b1 * p1 + b2 * p2;
-        lp.gNormal = normalize(ng);
-        const bool hasVN = f.vn[0] != kNone32 && f.vn[1] != kNone32 && f.vn[2] != kNone32;
-        lp.sNormal = hasVN ? normalize(b0 * vtx(sc.normals, f.vn[0]) + b1 * vtx(sc.normals, f.vn[1]) +
-                                       b2 * vtx(sc.normals, f.vn[2]))
-                           : lp.gNormal;
-        lp.hasTangent = f.vt[0] != kNone32 && f.vt[1] != kNone32 && f.vt[2] != kNone32;
-        if (lp.hasTangent)
-            lp.sTangent = normalize(b0 * vtx(sc.tangents, f.vt[0]) + b1 * vtx(sc.tangents, f.vt[1]) +
-                                    b2 * vtx(sc.tangents, f.vt[2]));
-        const bool hasUV = f.uv[0] != kNone32 && f.uv[1] != kNone32 && f.uv[2] != kNone32;
-        if (hasUV) {
-            const float2 uv0 = __ldg(sc.uvs + f.uv[0]), uv1 = __ldg(sc.uvs + f.uv[1]), uv2 = __ldg(sc.uvs + f.uv[2]);
-            lp.uv = make_float2(b0 * uv0.x + b1 * uv1.x + b2 * uv2.x, b0 * uv0.y + b1 * uv1.y + b2 * uv2.y);
-            const float du0 = uv0.x - uv2.x, dv0 = uv0.y - uv2.y, du1 = uv1.x - uv2.x, dv1 = uv1.y - uv2.y;
-            const f3 dP0 = p0 - p2, dP1 = p1 - p2;
-            const float invDetUV = 1.0f / (du0 * dv1 - dv0 * du1);
-            const f3 uDir = invDetUV * mk(dv1 * dP0.x - dv0 * dP1.x, dv1 * dP0.y - dv0 * dP1.y, dv1 * dP0.z - dv0 * dP1.z);
-            lp.uDir = hasVN ? normalize(cross(cross(lp.sNormal, uDir), lp.sNormal)) : normalize(uDir);
-        }
-        lightProp = f.light;
-    }
-    edf_alloc(sc, lightProp, lp, e);
-}
-
-// getAreaPDF, light.cl:247-292
-__device__ __forceinline__ float area_pdf(const DScene& sc, const LightPt& lp) {
-    const uint8_t* dist = light_distribution(sc);
-    const uint32_t numItems = ldb<uint32_t>(dist + 4);
-    if (lp.atInfinity) {
-        const uint8_t* l = env_light_property(sc);
-        float a = 0.0f;
-        const uint8_t* p = l + 1;
-        for (int i = 0; i < (int)l[0]; ++i) {
-            p = align_ptr(p, 4);
-            if (p[0] != 0) break;
-            const float uvPDF = pdf_cc_2d(sc.others + ldb<uint32_t>(p + 12), lp.uv);
-            a += uvPDF / (2 * kPi * kPi * sinf(lp.uv.y * kPi)) * 1.0f;
-            p += 16;
-        }
-        for (uint32_t i = 0; i < numItems; ++i)
-            if (sc.lights[8u * i]) return a * prob_discrete_1d(dist, i);
-    } else {
-        const Face f = load_face(sc, lp.faceID);
-        const f3 p0 = vtx(sc.vertices, f.p[0]), p1 = vtx(sc.vertices, f.p[1]), p2 = vtx(sc.vertices, f.p[2]);
-        const f3 ng = cross(p1 - p0, p2 - p0);
-        const float a = 1.0f / (0.5f * length(ng));
-        for (uint32_t i = 0; i < numItems; ++i)
-            if (!sc.lights[8u * i] && ldb<uint32_t>(sc.lights + 8u * i + 4) == lp.faceID)
-                return a * prob_discrete_1d(dist, i);
-    }
-    return 0.0f;
-}
-
-// ---------------------------------------------------------------- camera
-
-// mulMat4x4G_V3 / _P3 / _P4 (matrix.cl): column-major 4x4, row r = m[r], m[4+r], m[8+r], m[12+r]
-__device__ __forceinline__ f3 mat_v3(const float* m, f3 v) {
-    return mk(m[0] * v.x + m[4] * v.y + m[8] * v.z, m[1] * v.x + m[5] * v.y + m[9] * v.z,
-              m[2] * v.x + m[6] * v.y + m[10] * v.z);
-}
-__device__ __forceinline__ f3 mat_p3(const float* m, f3 p) {
-    f3 r = mk(m[0] * p.x + m[4] * p.y + m[8] * p.z + m[12] * 1.0f, m[1] * p.x + m[5] * p.y + m[9] * p.z + m[13] * 1.0f,
-              m[2] * p.x + m[6] * p.y + m[10] * p.z + m[14] * 1.0f);
-    const float w = m[3] * p.x + m[7] * p.y + m[11] * p.z + m[15] * 1.0f;
-    if (w != 1.0f) r = r / w;
-    return r;
-}
-
-struct Camera {
-    const uint8_t* blob;
-    const float* l2w;
-    float lensRadius, objPDistance, virtualPlaneArea;
-};
-
-__device__ __forceinline__ Camera load_camera(const DScene& sc) {
-    Camera c;
-    c.blob = sc.others + ldb<uint32_t>(sc.others + 0);
-    c.l2w = reinterpret_cast<const float*>(c.blob + 64);
-    c.virtualPlaneArea = ldb<float>(c.blob + 132);
-    c.lensRadius = ldb<float>(c.blob + 136);
-    c.objPDistance = ldb<float>(c.blob + 140);
-    return c;
-}
 
 // ----------------------------------------------------------- path tracer
 
 template <bool kOrdered>
 __device__ void trace_path(const DScene& sc, const Camera& cam, uint32_t gx, uint32_t gy, Rng& rng, f3& pix,
                            uint32_t max_depth, uint2* stack) {
-    // sampleLensPos + IDFAlloc (camera.cl:60-90)
-    const float cu0 = rng.uniform(), cu1 = rng.uniform();
-    float ux, uy;
-    concentric_disk(cu0, cu1, ux, uy);
-    const f3 idfDir = mat_v3(cam.l2w, mk(0.0f, 0.0f, 1.0f));
-    const f3 lensLocal = mk(ux * cam.lensRadius, uy * cam.lensRadius, 0.0f);
-    f3 org = mat_p3(cam.l2w, lensLocal);
-    // sample_We (camera.cl:93-115)
-    const float pxs = gx + rng.uniform();
-    const float pys = gy + rng.uniform();
-    const float* r2c = reinterpret_cast<const float*>(cam.blob + 192);
-    float4 pc = make_float4(r2c[0] * pxs + r2c[4] * pys + r2c[8] * 0.0f + r2c[12] * 1.0f,
-                            r2c[1] * pxs + r2c[5] * pys + r2c[9] * 0.0f + r2c[13] * 1.0f,
-                            r2c[2] * pxs + r2c[6] * pys + r2c[10] * 0.0f + r2c[14] * 1.0f,
-                            r2c[3] * pxs + r2c[7] * pys + r2c[11] * 0.0f + r2c[15] * 1.0f);
-    if (pc.w != 1.0f) {
-        const float rw = 1.0f / pc.w;
-        pc.x *= rw;
-        pc.y *= rw;
-        pc.z *= rw;
-        pc.w *= rw;
-    }
-    f3 d = normalize(mk(pc.x, pc.y, pc.z));
-    if (cam.lensRadius > 0.0f) {
-        const float ft = -cam.objPDistance / d.z;
-        const f3 pFocus = mk(0, 0, 0) + ft * d;
-        d = normalize(pFocus - mk(lensLocal.x, lensLocal.y, 0.0f));
-    }
-    f3 dir = mat_v3(cam.l2w, d);
-    float dirPDF = 1.0f / (powf(-d.z, 3) * cam.virtualPlaneArea);
-    f3 alpha = mk(1, 1, 1);
-    alpha *= fabsf(dot(idfDir, dir)) / dirPDF;
+    f3 org, dir, alpha;
+    float dirPDF;
+    camera_ray(cam, gx, gy, rng, org, dir, alpha, dirPDF);
     const float initY = luminance(alpha);
 
     uint32_t depth = 0;
@@ -555,9 +126,7 @@ __device__ void trace_path(const DScene& sc, const Camera& cam, uint32_t gx, uin
     if (traceContinue) {
         vout = -dir;
         lpos.atInfinity = true;
-        const float theta = acosf(clampf(dir.y, -1.0f, 1.0f));
-        const float phi = fmodf(atan2f(-dir.x, dir.z) + 2.0f * kPi, 2 * kPi);
-        lpos.uv = make_float2(phi / (2.0f * kPi), theta / kPi);
+        lpos.uv = env_uv(dir);
         edf_alloc(sc, kNone16, lpos, edf);
         MISWeight = 1.0f;
         if ((sampledType & kTyNonSingular) && depth > 0) {
@@ -596,29 +165,11 @@ using namespace clr;
 
 extern "C" int clr_render(const clr_scene* scene, uint32_t width, uint32_t height, uint32_t* rand_states,
                           float* pixels, uint32_t spp, uint32_t max_depth, uint32_t flags, void* stream) {
-    if (!scene || !scene->bvh) return clr_set_error(CLR_EINVAL, "clr_render: NULL scene or bvh");
+    int rc = check_render_args(scene, rand_states, pixels);
+    if (rc != CLR_OK) return rc;
     if (width == 0 || height == 0 || spp == 0) return CLR_OK;
-    if (!rand_states || !pixels || !scene->vertices || !scene->faces || !scene->lights || !scene->materials ||
-        !scene->textures || !scene->others)
-        return clr_set_error(CLR_EINVAL, "clr_render: NULL buffer");
-    if ((reinterpret_cast<uintptr_t>(pixels) | reinterpret_cast<uintptr_t>(rand_states) |
-         reinterpret_cast<uintptr_t>(scene->vertices) | reinterpret_cast<uintptr_t>(scene->others)) & 15u)
-        return clr_set_error(CLR_EINVAL, "clr_render: pixels, rand_states, vertices and others must be 16-byte aligned");
     if (max_depth == 0) max_depth = 100;
-    DScene sc;
-    sc.vertices = reinterpret_cast<const float4*>(scene->vertices);
-    sc.normals = reinterpret_cast<const float4*>(scene->normals);
-    sc.tangents = reinterpret_cast<const float4*>(scene->tangents);
-    sc.uvs = reinterpret_cast<const float2*>(scene->uvs);
-    sc.faces = static_cast<const uint8_t*>(scene->faces);
-    sc.lights = static_cast<const uint8_t*>(scene->lights);
-    sc.materials = scene->materials;
-    sc.textures = scene->textures;
-    sc.others = scene->others;
-    sc.nodes = static_cast<const float4*>(scene->bvh->nodes);
-    sc.tris = static_cast<const float4*>(scene->bvh->tris);
-    sc.root_box = scene->bvh->root_box;
-    sc.num_tris = scene->bvh->num_tris;
+    const DScene sc = make_dscene(scene);
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     const dim3 grid(div_up(width, 16), div_up(height, 8));
     if (flags & CLR_RENDER_ORDERED)

@@ -1,0 +1,353 @@
+// Wavefront path tracer: the megakernel (render.cu) split into small kernels
+// over path state kept in SoA device buffers (SURVEY: generate / extend /
+// shade / shadow-connect).
+//
+// One path slot per pixel: a pixel's samples are sequential in its own
+// XORShift128 stream (the reference's per-pixel stream), so a finished path
+// immediately starts the pixel's next sample in the same slot ("path
+// regeneration") and the pool stays full until pixels run out of samples.
+// Per iteration:
+//   extend : closest hit of every active path's ray;
+//   shade  : emission with MIS at the hit (or environment on a miss), the
+//            depth cap and Russian roulette, BSDF construction, next-event
+//            estimation (writes a shadow-ray entry with its contribution),
+//            BSDF sampling of the continuation ray; finished paths
+//            regenerate (camera ray of the pixel's next sample);
+//   shadow : closest hit of every shadow ray; adds the contribution when the
+//            sampled light point is visible.
+// Random numbers are drawn in the reference's order (camera 4, then per
+// bounce NEE 3, BSDF 3, roulette 1) and each pixel's contributions are added
+// in the reference's order (a bounce's NEE term lands in the shadow pass,
+// before the next bounce's emission term), so results match the megakernel
+// path for path.
+#include "render_common.cuh"
+
+CLR_DEFINE_STATUS_READER(render_wf)
+
+namespace clr {
+
+constexpr int kWfThreads = 128;
+
+struct WfState {
+    float4* org;     // xyz ray origin
+    float4* dir;     // xyz ray direction, w dirPDF
+    float4* alpha;   // xyz throughput, w initY
+    uint4* misc;     // x depth, y sampledType, z samples done, w pixel
+    float4* hit;     // x id bits, y t, z b1, w b2
+    uint32_t* q[2];  // active path queues
+    float4* sh;      // shadow entries: org (w light face | 0xFFFFFFFF env), dir (w path), contribution
+    unsigned int* count;  // [0],[1] active counts, [2] shadow count
+};
+
+__device__ __forceinline__ Rng load_rng(const uint32_t* rs, uint32_t p) {
+    const uint4 s = reinterpret_cast<const uint4*>(rs)[p];
+    Rng r;
+    r.s[0] = s.x;
+    r.s[1] = s.y;
+    r.s[2] = s.z;
+    r.s[3] = s.w;
+    return r;
+}
+__device__ __forceinline__ void store_rng(uint32_t* rs, uint32_t p, const Rng& r) {
+    reinterpret_cast<uint4*>(rs)[p] = make_uint4(r.s[0], r.s[1], r.s[2], r.s[3]);
+}
+
+// Warp-aggregated queue append.
+__device__ __forceinline__ uint32_t queue_slot(unsigned int* count, bool want) {
+    const unsigned int m = __ballot_sync(0xFFFFFFFFu, want);
+    if (!m) return 0;
+    const int lane = threadIdx.x & 31, leader = __ffs(m) - 1;
+    uint32_t base = 0;
+    if (lane == leader) base = atomicAdd(count, (unsigned int)__popc(m));
+    base = __shfl_sync(0xFFFFFFFFu, base, leader);
+    unsigned int lt;
+    asm("mov.u32 %0, %%lanemask_lt;" : "=r"(lt));
+    return base + __popc(m & lt);
+}
+
+__device__ __forceinline__ void start_sample(const Camera& cam, WfState& S, uint32_t p, uint32_t width, Rng& rng,
+                                             uint32_t done) {
+    f3 org, dir, alpha;
+    float dirPDF;
+    camera_ray(cam, p % width, p / width, rng, org, dir, alpha, dirPDF);
+    S.org[p] = make_float4(org.x, org.y, org.z, 0.f);
+    S.dir[p] = make_float4(dir.x, dir.y, dir.z, dirPDF);
+    S.alpha[p] = make_float4(alpha.x, alpha.y, alpha.z, luminance(alpha));
+    S.misc[p] = make_uint4(0u, 0u, done, p);
+}
+
+__global__ void __launch_bounds__(kWfThreads) k_wf_init(DScene sc, WfState S, uint32_t npix, uint32_t width,
+                                                        uint32_t* __restrict__ rand_states) {
+    const Camera cam = load_camera(sc);
+    for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < npix; p += gridDim.x * blockDim.x) {
+        Rng rng = load_rng(rand_states, p);
+        start_sample(cam, S, p, width, rng, 0u);
+        store_rng(rand_states, p, rng);
+        S.q[0][p] = p;
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        S.count[0] = npix;
+        S.count[1] = 0;
+        S.count[2] = 0;
+    }
+}
+
+template <bool kOrdered>
+__global__ void __launch_bounds__(kWfThreads) k_wf_extend(DScene sc, WfState S, int cur) {
+    const uint32_t n = S.count[cur];
+    uint2 stack[kStackSize];
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const uint32_t p = S.q[cur][i];
+        const float4 o = S.org[p], d = S.dir[p];
+        Hit h;
+        if (intersect<kOrdered>(sc, mk(o.x, o.y, o.z), mk(d.x, d.y, d.z), h, stack))
+            S.hit[p] = make_float4(__uint_as_float(h.id), h.t, h.b1, h.b2);
+        else
+            S.hit[p] = make_float4(__uint_as_float(kNone32), INFINITY, 0.f, 0.f);
+    }
+}
+
+__global__ void __launch_bounds__(kWfThreads) k_wf_shade(DScene sc, WfState S, int cur, uint32_t width,
+                                                         uint32_t* __restrict__ rand_states,
+                                                         float4* __restrict__ pixels, uint32_t spp,
+                                                         uint32_t max_depth) {
+    const uint32_t n = S.count[cur];
+    const Camera cam = load_camera(sc);
+    const uint32_t stride = gridDim.x * blockDim.x;
+    // whole warps iterate together so the queue appends can use warp votes
+    const uint32_t n_round = (n + 31u) & ~31u;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n_round; i += stride) {
+        bool cont = false;      // path goes on to the next extend
+        bool shadow = false;    // a shadow entry is written
+        uint32_t p = 0;
+        float4 sh0, sh1, sh2;
+        if (i < n) {
+            p = S.q[cur][i];
+            Rng rng = load_rng(rand_states, p);
+            const float4 o4 = S.org[p], d4 = S.dir[p], a4 = S.alpha[p];
+            uint4 m = S.misc[p];
+            const float4 h4 = S.hit[p];
+            f3 org = mk(o4.x, o4.y, o4.z), dir = mk(d4.x, d4.y, d4.z), alpha = mk(a4.x, a4.y, a4.z);
+            float dirPDF = d4.w;
+            const float initY = a4.w;
+            uint32_t depth = m.x, sampledType = m.y;
+            const float4 px = pixels[p];
+            f3 pix = mk(px.x, px.y, px.z);
+            bool ended = false;
+            const uint32_t hid = __float_as_uint(h4.x);
+            if (hid == kNone32) {
+                // escaped: environment emission (pathtracer.cl:183-196)
+                LightPt lpos;
+                lpos.atInfinity = true;
+                lpos.uv = env_uv(dir);
+                const f3 vout = -dir;
+                EDF edf;
+                edf_alloc(sc, kNone16, lpos, edf);
+                float MISWeight = 1.0f;
+                if ((sampledType & kTyNonSingular) && depth > 0) {
+                    const float lightPDF = area_pdf(sc, lpos) * 1.0f / edf_abs_cos(edf, vout);
+                    MISWeight = (dirPDF * dirPDF) / (lightPDF * lightPDF + dirPDF * dirPDF);
+                }
+                pix += MISWeight * alpha * edf_le(edf, vout);
+                ended = true;
+            } else {
+                Hit h{hid, h4.y, h4.z, h4.w};
+                SurfPt sp;
+                surface_point(sc, org, dir, h, sp);
+                const Face face = load_face(sc, sp.faceID);
+                const f3 vout = -dir;
+                LightPt lpos;
+                lpos.faceID = kNone32;
+                if (face.light != kNone16) {
+                    light_from_surface(sp, lpos);
+                    EDF edf;
+                    edf_alloc(sc, face.light, lpos, edf);
+                    float MISWeight = 1.0f;
+                    if (depth > 0 && (sampledType & kTyNonSingular)) {
+                        const float d2 = (org.x - sp.p.x) * (org.x - sp.p.x) + (org.y - sp.p.y) * (org.y - sp.p.y) +
+                                         (org.z - sp.p.z) * (org.z - sp.p.z);
+                        const float lightPDF = area_pdf(sc, lpos) * d2 / edf_abs_cos(edf, vout);
+                        MISWeight = (dirPDF * dirPDF) / (lightPDF * lightPDF + dirPDF * dirPDF);
+                    }
+                    pix += depth > 0 ? MISWeight * alpha * edf_le(edf, vout) : alpha * edf_le(edf, vout);
+                }
+                if (depth > 0) {
+                    if (depth >= max_depth) ended = true;
+                    else {
+                        const float continueProb = fminf(luminance(alpha) * (1.0f / initY), 1.0f);
+                        if (rng.uniform() < continueProb) {
+                            alpha *= 1.0f / continueProb;
+                            dirPDF *= continueProb;
+                        } else {
+                            ended = true;
+                        }
+                    }
+                }
+                if (!ended) {
+                    BSDF bsdf;
+                    bsdf_alloc(sc, face.mat, sp, bsdf);
+                    if (bsdf_has_non_specular(bsdf)) {
+                        const float uL = rng.uniform(), u0 = rng.uniform(), u1 = rng.uniform();
+                        EDF edf;
+                        float lightPDF;
+                        sample_light(sc, uL, u0, u1, lpos, edf, lightPDF);
+                        f3 vinL = lpos.p - sp.p;
+                        float dist2 = dot(vinL, vinL);
+                        vinL = vinL * (1.0f / sqrtf(dist2));
+                        if (lpos.atInfinity) {
+                            vinL = lpos.p;
+                            dist2 = 1.0f;
+                        }
+                        const f3 sorg = sp.p + vinL * kEpsilon;
+                        const f3 vinLrev = -vinL;
+                        const float fsPDF = bsdf_pdf(bsdf, vout, vinL) * edf_abs_cos(edf, vinL) / dist2;
+                        const float MISWeight = (lightPDF * lightPDF) / (lightPDF * lightPDF + fsPDF * fsPDF);
+                        const f3 c = (MISWeight * edf_abs_cos(edf, vinL) * fabsf(dot(bsdf.n, vinL)) / dist2 / lightPDF) *
+                                     (alpha * edf_le(edf, vinLrev) * bsdf_f(bsdf, vout, vinL));
+                        sh0 = make_float4(sorg.x, sorg.y, sorg.z, __uint_as_float(lpos.atInfinity ? kNone32 : lpos.faceID));
+                        sh1 = make_float4(vinL.x, vinL.y, vinL.z, __uint_as_float(p));
+                        sh2 = make_float4(c.x, c.y, c.z, 0.f);
+                        shadow = true;
+                    }
+                    const float uc = rng.uniform(), v0 = rng.uniform(), v1 = rng.uniform();
+                    const f3 fs = bsdf_sample(bsdf, vout, uc, v0, v1, dir, dirPDF, sampledType);
+                    if (zero_vec(fs) || dirPDF == 0.0f) {
+                        ended = true;
+                    } else {
+                        alpha *= fs * (fabsf(dot(bsdf.n, dir)) / dirPDF);
+                        org = sp.p + dir * kEpsilon;
+                        ++depth;
+                    }
+                }
+            }
+            pixels[p] = make_float4(pix.x, pix.y, pix.z, px.w);
+            if (ended) {
+                const uint32_t done = m.z + 1;
+                if (done < spp) {
+                    start_sample(cam, S, p, width, rng, done);
+                    cont = true;
+                } else {
+                    S.misc[p] = make_uint4(depth, sampledType, done, p);
+                }
+            } else {
+                S.org[p] = make_float4(org.x, org.y, org.z, 0.f);
+                S.dir[p] = make_float4(dir.x, dir.y, dir.z, dirPDF);
+                S.alpha[p] = make_float4(alpha.x, alpha.y, alpha.z, initY);
+                S.misc[p] = make_uint4(depth, sampledType, m.z, p);
+                cont = true;
+            }
+            store_rng(rand_states, p, rng);
+        }
+        const uint32_t qs = queue_slot(S.count + (cur ^ 1), cont);
+        if (cont) S.q[cur ^ 1][qs] = p;
+        const uint32_t ss = queue_slot(S.count + 2, shadow);
+        if (shadow) {
+            S.sh[3u * ss] = sh0;
+            S.sh[3u * ss + 1] = sh1;
+            S.sh[3u * ss + 2] = sh2;
+        }
+    }
+}
+
+template <bool kOrdered>
+__global__ void __launch_bounds__(kWfThreads) k_wf_shadow(DScene sc, WfState S, float4* __restrict__ pixels) {
+    const uint32_t n = S.count[2];
+    uint2 stack[kStackSize];
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const float4 a = S.sh[3u * i], b = S.sh[3u * i + 1], c = S.sh[3u * i + 2];
+        const uint32_t light_face = __float_as_uint(a.w), p = __float_as_uint(b.w);
+        Hit h;
+        const bool hit = intersect<kOrdered>(sc, mk(a.x, a.y, a.z), mk(b.x, b.y, b.z), h, stack);
+        const bool visible = light_face == kNone32 ? !hit : (hit && h.id == light_face);
+        if (visible) {
+            float4 px = pixels[p];
+            px.x += c.x;
+            px.y += c.y;
+            px.z += c.z;
+            pixels[p] = px;
+        }
+    }
+}
+
+__global__ void k_wf_reset(WfState S, int next) {
+    S.count[next] = 0;
+    S.count[2] = 0;
+}
+
+static size_t wf_layout(uint32_t npix, char* base, WfState* S) {
+    size_t off = 0;
+    auto take = [&](size_t bytes) {
+        const size_t o = off;
+        off = (off + bytes + 255) / 256 * 256;
+        return o;
+    };
+    const size_t o_org = take(16ull * npix), o_dir = take(16ull * npix), o_alpha = take(16ull * npix),
+                 o_misc = take(16ull * npix), o_hit = take(16ull * npix), o_q0 = take(4ull * npix),
+                 o_q1 = take(4ull * npix), o_sh = take(48ull * npix), o_cnt = take(16);
+    if (base && S) {
+        S->org = reinterpret_cast<float4*>(base + o_org);
+        S->dir = reinterpret_cast<float4*>(base + o_dir);
+        S->alpha = reinterpret_cast<float4*>(base + o_alpha);
+        S->misc = reinterpret_cast<uint4*>(base + o_misc);
+        S->hit = reinterpret_cast<float4*>(base + o_hit);
+        S->q[0] = reinterpret_cast<uint32_t*>(base + o_q0);
+        S->q[1] = reinterpret_cast<uint32_t*>(base + o_q1);
+        S->sh = reinterpret_cast<float4*>(base + o_sh);
+        S->count = reinterpret_cast<unsigned int*>(base + o_cnt);
+    }
+    return off;
+}
+
+}  // namespace clr
+
+using namespace clr;
+
+extern "C" int clr_render_workspace_bytes(uint32_t width, uint32_t height, uint64_t* bytes) {
+    if (!bytes) return clr_set_error(CLR_EINVAL, "clr_render_workspace_bytes: bytes is NULL");
+    *bytes = wf_layout(width * height, nullptr, nullptr);
+    return CLR_OK;
+}
+
+extern "C" int clr_render_wavefront(const clr_scene* scene, uint32_t width, uint32_t height, uint32_t* rand_states,
+                                    float* pixels, uint32_t spp, uint32_t max_depth, uint32_t flags, void* workspace,
+                                    uint64_t workspace_bytes, void* stream) {
+    int rc = check_render_args(scene, rand_states, pixels);
+    if (rc != CLR_OK) return rc;
+    if (width == 0 || height == 0 || spp == 0) return CLR_OK;
+    const uint32_t npix = width * height;
+    if (!workspace || workspace_bytes < wf_layout(npix, nullptr, nullptr))
+        return clr_set_error(CLR_ECAPACITY, "clr_render_wavefront: workspace of %llu bytes is smaller than %zu",
+                             (unsigned long long)workspace_bytes, wf_layout(npix, nullptr, nullptr));
+    if (reinterpret_cast<uintptr_t>(workspace) & 255u)
+        return clr_set_error(CLR_EINVAL, "clr_render_wavefront: workspace must be 256-byte aligned");
+    if (max_depth == 0) max_depth = 100;
+    const DScene sc = make_dscene(scene);
+    WfState S;
+    wf_layout(npix, static_cast<char*>(workspace), &S);
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    const bool ordered = (flags & CLR_RENDER_ORDERED) != 0;
+    const unsigned int grid = std::min(div_up(npix, kWfThreads), 152u * 16u);
+    float4* px = reinterpret_cast<float4*>(pixels);
+    k_wf_init<<<grid, kWfThreads, 0, st>>>(sc, S, npix, width, rand_states);
+    CLR_LAUNCH_CHECK("k_wf_init");
+    // every iteration advances each unfinished pixel by one path vertex
+    const uint64_t max_iters = (uint64_t)spp * (max_depth + 1) + 1;
+    for (uint64_t it = 0; it < max_iters; ++it) {
+        const int cur = (int)(it & 1);
+        if (ordered) k_wf_extend<true><<<grid, kWfThreads, 0, st>>>(sc, S, cur);
+        else k_wf_extend<false><<<grid, kWfThreads, 0, st>>>(sc, S, cur);
+        k_wf_reset<<<1, 1, 0, st>>>(S, cur ^ 1);
+        k_wf_shade<<<grid, kWfThreads, 0, st>>>(sc, S, cur, width, rand_states, px, spp, max_depth);
+        if (ordered) k_wf_shadow<true><<<grid, kWfThreads, 0, st>>>(sc, S, px);
+        else k_wf_shadow<false><<<grid, kWfThreads, 0, st>>>(sc, S, px);
+        CLR_LAUNCH_CHECK("wavefront iteration");
+        // stop once no path is left (checked every 8 iterations)
+        if ((it & 7) == 7) {
+            unsigned int left = 0;
+            CLR_CUDA_TRY(cudaMemcpyAsync(&left, S.count + (cur ^ 1), sizeof(left), cudaMemcpyDeviceToHost, st));
+            CLR_CUDA_TRY(cudaStreamSynchronize(st));
+            if (left == 0) break;
+        }
+    }
+    return CLR_OK;
+}

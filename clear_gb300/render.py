@@ -54,9 +54,25 @@ class DeviceScene:
         return rng, pix
 
     def render(self, rng: torch.Tensor, pix: torch.Tensor, spp: int, max_depth: int = 100,
-               ordered: bool = True) -> None:
+               ordered: bool = True, wavefront: bool = False) -> None:
+        """Adds `spp` samples per pixel to `pix`.  wavefront=True runs the
+        extend/shade/shadow kernel split (same results as the megakernel)."""
         stream = C.c_void_p(torch.cuda.current_stream(self.device).cuda_stream)
+        flags = C.c_uint32(RENDER_ORDERED if ordered else 0)
+        args = (C.byref(self.c), C.c_uint32(self.width), C.c_uint32(self.height), C.c_void_p(rng.data_ptr()),
+                C.c_void_p(pix.data_ptr()), C.c_uint32(spp), C.c_uint32(max_depth), flags)
         with torch.cuda.device(self.device):
-            _lib.call("clr_render", C.byref(self.c), C.c_uint32(self.width), C.c_uint32(self.height),
-                      C.c_void_p(rng.data_ptr()), C.c_void_p(pix.data_ptr()), C.c_uint32(spp), C.c_uint32(max_depth),
-                      C.c_uint32(RENDER_ORDERED if ordered else 0), stream)
+            if not wavefront:
+                _lib.call("clr_render", *args, stream)
+                return
+            ws = self.workspace()
+            _lib.call("clr_render_wavefront", *args, C.c_void_p(ws.data_ptr()), C.c_uint64(ws.numel()), stream)
+
+    def workspace(self) -> torch.Tensor:
+        if getattr(self, "_ws", None) is None:
+            n = C.c_uint64(0)
+            _lib.call("clr_render_workspace_bytes", C.c_uint32(self.width), C.c_uint32(self.height), C.byref(n))
+            self._ws = torch.empty(int(n.value) + 256, dtype=torch.uint8, device=self.device)
+            off = (-self._ws.data_ptr()) % 256
+            self._ws = self._ws[off:off + int(n.value)]
+        return self._ws

@@ -199,6 +199,17 @@ typedef struct clr_scene {
 CLR_API int clr_render(const clr_scene* scene, uint32_t width, uint32_t height, uint32_t* rand_states, float* pixels,
                        uint32_t spp, uint32_t max_depth, uint32_t flags, void* stream);
 
+/* Wavefront form of clr_render: the same paths, random numbers and
+ * contributions (identical results), split into extend / shade / shadow
+ * kernels over path state in `workspace`, with per-pixel path regeneration.
+ * The caller provides a 256-byte aligned device workspace of at least
+ * clr_render_workspace_bytes(width, height) bytes.  Waits on `stream` every
+ * few iterations to stop once every pixel has its spp samples. */
+CLR_API int clr_render_workspace_bytes(uint32_t width, uint32_t height, uint64_t* bytes);
+CLR_API int clr_render_wavefront(const clr_scene* scene, uint32_t width, uint32_t height, uint32_t* rand_states,
+                                 float* pixels, uint32_t spp, uint32_t max_depth, uint32_t flags, void* workspace,
+                                 uint64_t workspace_bytes, void* stream);
+
 /* ----------------------------------------------------------------- misc */
 
 /* Reads (and optionally clears) the device error bits CLR_DEVERR_* of the

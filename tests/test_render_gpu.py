@@ -58,6 +58,27 @@ def test_render_matches_reference_sim(cuda, variant):
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("variant", ["plain", "env"])
+def test_wavefront_equals_megakernel(cuda, variant):
+    """The wavefront split draws the same random numbers and adds the same
+    contributions in the same order: the image is identical to the
+    megakernel's, and within the reference bars."""
+    g = np.load(GOLDEN)
+    w, h, spp = int(g["width"]), int(g["height"]), int(g["spp"])
+    ds = DeviceScene(scenes.cornell_box(w, h, env=env_map() if variant == "env" else None), cuda)
+    rng_a, pix_a = ds.new_frame()
+    ds.render(rng_a, pix_a, spp, max_depth=100, ordered=False)
+    rng_b, pix_b = ds.new_frame()
+    ds.render(rng_b, pix_b, spp, max_depth=100, ordered=False, wavefront=True)
+    torch.cuda.synchronize()
+    assert torch.equal(rng_a, rng_b)
+    assert torch.equal(pix_a, pix_b)
+    rel_rmse, mean_err, frac_close = metrics(pix_b[:, :3].cpu().numpy(), g[variant])
+    assert rel_rmse <= 0.02 and mean_err <= 0.005 and frac_close >= 0.90
+    assert _lib.device_status() == 0
+
+
+@pytest.mark.gpu
 def test_render_ordered_traversal_agrees(cuda):
     """Nearer-child-first traversal in the renderer: same image statistics."""
     g = np.load(GOLDEN)
