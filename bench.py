@@ -210,6 +210,37 @@ def bench_render(dev, args) -> dict:
     return out
 
 
+def bench_render_terrain(dev, spp=4) -> dict:
+    """Wavefront vs megakernel on the large scene: 2.23 M triangles
+    (1024^2 heightfield + 256 spheres), 1024 x 512 sky, 8 bump-mapped
+    materials, thin lens 0.02 / 1.5, 1920 x 1080, depth 8; `spp` samples per
+    pixel per timed render."""
+    import torch
+
+    from clear_gb300 import scenes
+    from clear_gb300.render import DeviceScene
+
+    sc = scenes.terrain_scene()
+    ds = DeviceScene(sc, dev)
+    w, h = sc.width, sc.height
+    out = {"workload": "terrain 2.23M tris, 1920x1080, depth 8, thin lens", "spp": spp, "samples": w * h * spp}
+    stream = torch.cuda.current_stream(dev)
+    for name, ordered, wf in (("megakernel_ordered", True, False), ("wavefront_exact", False, True),
+                              ("wavefront_ordered", True, True)):
+        rng, pix = ds.new_frame()
+        ds.render(rng, pix, 1, max_depth=8, ordered=ordered, wavefront=wf)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        ds.render(rng, pix, spp, max_depth=8, ordered=ordered, wavefront=wf)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1)
+        out[f"{name}_ms"] = ms
+        out[f"{name}_msamples_s"] = w * h * spp / ms / 1e3
+    return out
+
+
 def run_reference(args):
     rank, world, _ = dist_env()
     if rank != 0:
@@ -351,6 +382,7 @@ def run_ours(args):
     ordered_id_mismatch = int((hid != hid2).sum().item())
     ordered_t_mismatch = int((ht != ht2).sum().item())
     render = bench_render(dev, args) if args.render else None
+    render_terrain = bench_render_terrain(dev) if args.render else None
     hit_frac = float((hid >= 0).float().mean().item())
     occ_frac = float(occ.float().mean().item())
     clk = clocks.stop()
@@ -392,6 +424,7 @@ def run_ours(args):
                       "closest_ms": closest_ms, "shadow_ms": shadow_ms, "closest_hit_frac": hit_frac,
                       "shadow_occluded_frac": occ_frac},
         "render": render,
+        "render_terrain": render_terrain,
         "gpu_launches": launches_per_build * args.steps,
         "clocks": clk,
         "device_error_bits": dev_err,
@@ -412,7 +445,7 @@ def main():
 
         build()
         dev = torch.device("cuda", 0)
-        print(json.dumps({"render": bench_render(dev, args)}), flush=True)
+        print(json.dumps({"render": bench_render(dev, args), "render_terrain": bench_render_terrain(dev)}), flush=True)
         return
     if args.impl == "reference":
         run_reference(args)

@@ -123,6 +123,50 @@ static __device__ bool intersect(const DScene& sc, f3 org, f3 dir, Hit& h, uint2
     return true;
 }
 
+// Whether the ray hits any triangle at all (environment shadow rays: the
+// reference's test "closest hit exists" has the same answer, since any
+// triangle the closest-hit search would accept is also reachable with the
+// bound held at infinity, and vice versa).
+template <bool kOrdered>
+__device__ bool occluded_any(const DScene& sc, f3 org, f3 dir, uint2* stack) {
+    Ray ray{org.x, org.y, org.z, INFINITY, dir.x, dir.y, dir.z};
+    const float ix = 1.0f / dir.x, iy = 1.0f / dir.y, iz = 1.0f / dir.z;
+    float entry;
+    const float* rb = sc.root_box;
+    if (!box_test_fast(rb[0], rb[1], rb[2], rb[4], rb[5], rb[6], ray, ix, iy, iz, entry)) return false;
+    auto hit_leaf = [&](uint32_t leaf) {
+        float t = INFINITY;
+        return tri_test(__ldg(sc.tris + 3u * leaf), __ldg(sc.tris + 3u * leaf + 1u), __ldg(sc.tris + 3u * leaf + 2u),
+                        ray, t);
+    };
+    if (sc.num_tris == 1) return hit_leaf(0);
+    if (sc.num_tris < 2) return false;
+    int sp = 0;
+    stack[sp++] = make_uint2(__float_as_uint(rb[3]), 0u);
+    for (uint32_t guard = 0; sp > 0 && guard < sc.num_tris; ++guard) {
+        const NodeBoxes nb = load_node(sc.nodes, stack[--sp].x);
+        float e0, e1;
+        const bool p0 = box_test_fast(nb.b0[0], nb.b0[1], nb.b0[2], nb.b0[3], nb.b0[4], nb.b0[5], ray, ix, iy, iz, e0);
+        const bool p1 = box_test_fast(nb.b1[0], nb.b1[1], nb.b1[2], nb.b1[3], nb.b1[4], nb.b1[5], ray, ix, iy, iz, e1);
+        // nearer child last on the stack so it is explored first
+        const bool near1 = kOrdered && (e1 < e0);
+#pragma unroll
+        for (int k = 0; k < 2; ++k) {
+            const int c = near1 ? k : 1 - k;
+            const uint32_t ref = c ? nb.ref1 : nb.ref0;
+            if (!(c ? p1 : p0)) continue;
+            if (ref & kLeafBit) {
+                if (hit_leaf(ref & ~kLeafBit)) return true;
+            } else if (sp < kStackSize) {
+                stack[sp++] = make_uint2(ref, 0u);
+            } else {
+                clr_raise(CLR_DEVERR_STACK);
+            }
+        }
+    }
+    return false;
+}
+
 // rayTriangleIntersection's hit record + calcHitpointParameters
 // (bvh_traversal.cl:87-100, 110-158).
 __device__ __forceinline__ void surface_point(const DScene& sc, f3 org, f3 dir, const Hit& h, SurfPt& sp) {

@@ -256,9 +256,13 @@ __global__ void __launch_bounds__(kWfThreads) k_wf_shadow(DScene sc, WfState S, 
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         const float4 a = S.sh[3u * i], b = S.sh[3u * i + 1], c = S.sh[3u * i + 2];
         const uint32_t light_face = __float_as_uint(a.w), p = __float_as_uint(b.w);
-        Hit h;
-        const bool hit = intersect<kOrdered>(sc, mk(a.x, a.y, a.z), mk(b.x, b.y, b.z), h, stack);
-        const bool visible = light_face == kNone32 ? !hit : (hit && h.id == light_face);
+        bool visible;
+        if (light_face == kNone32) {
+            visible = !occluded_any<kOrdered>(sc, mk(a.x, a.y, a.z), mk(b.x, b.y, b.z), stack);
+        } else {
+            Hit h;
+            visible = intersect<kOrdered>(sc, mk(a.x, a.y, a.z), mk(b.x, b.y, b.z), h, stack) && h.id == light_face;
+        }
         if (visible) {
             float4 px = pixels[p];
             px.x += c.x;

@@ -130,13 +130,49 @@ def _colmajor(m) -> bytes:
 # ------------------------------------------------------------------- scene
 
 
+class _Rows:
+    """Append-only table built from single rows or whole arrays."""
+
+    def __init__(self, dtype, width=None):
+        self.dtype, self.width = dtype, width
+        self.parts, self.pending, self.n = [], [], 0
+
+    def __len__(self):
+        return self.n
+
+    def _flush(self):
+        if self.pending:
+            a = np.array(self.pending, dtype=self.dtype)
+            self.parts.append(a.reshape(-1, self.width) if self.width else a)
+            self.pending = []
+
+    def append(self, row):
+        self.pending.append(row)
+        self.n += 1
+
+    def extend(self, arr):
+        self._flush()
+        arr = np.asarray(arr, dtype=self.dtype)
+        self.parts.append(arr.reshape(-1, self.width) if self.width else arr)
+        self.n += len(self.parts[-1])
+
+    def array(self):
+        self._flush()
+        if not self.parts:
+            shape = (0, self.width) if self.width else (0,)
+            return np.zeros(shape, dtype=self.dtype)
+        if len(self.parts) > 1:
+            self.parts = [np.concatenate(self.parts)]
+        return self.parts[0]
+
+
 class Scene:
     def __init__(self):
-        self.vertices: list = []
-        self.normals: list = []
-        self.tangents: list = []
-        self.uvs: list = []
-        self.faces: list = []
+        self.vertices = _Rows(np.float64, 3)
+        self.normals = _Rows(np.float64, 3)
+        self.tangents = _Rows(np.float64, 3)
+        self.uvs = _Rows(np.float64, 2)
+        self.faces = _Rows(FACE_DTYPE)
         self.light_infos: list = []   # (atInfinity, reference)
         self.light_powers: list = []
         self.materials = Blob()
@@ -174,6 +210,37 @@ class Scene:
 
     def end_object(self):
         self._base = None
+
+    def add_mesh(self, verts, tris, mat, uvs=None, normals=None, light=NONE16):
+        """Bulk form of add_vertex/add_uv/add_normal/add_face for a whole
+        mesh: verts (n,3) in object space (transformed by the current
+        matrix), tris (m,3) object-relative vertex indices; uvs and normals,
+        if given, are per vertex and indexed like the vertices."""
+        verts = np.asarray(verts, dtype=np.float64)
+        m4 = self.local_to_world[-1]
+        vh = np.concatenate([verts, np.ones((len(verts), 1))], axis=1) @ m4.T
+        bv, bn, bu = len(self.vertices), len(self.normals), len(self.uvs)
+        self.vertices.extend(vh[:, :3] / vh[:, 3:4])
+        tris = np.asarray(tris, dtype=np.int64)
+        f = np.zeros(len(tris), dtype=FACE_DTYPE)
+        f["p"] = tris + bv
+        f["vn"] = f["vt"] = f["uv"] = NONE32
+        if normals is not None:
+            nm = np.asarray(normals, dtype=np.float64) @ np.linalg.inv(m4)[:3, :3]
+            self.normals.extend(nm)
+            f["vn"] = tris + bn
+        if uvs is not None:
+            self.uvs.extend(np.asarray(uvs, dtype=np.float64))
+            f["uv"] = tris + bu
+        f["alphaTexPtr"] = NONE32
+        f["matPtr"] = mat
+        f["lightPtr"] = light
+        base_f = len(self.faces)
+        self.faces.extend(f)
+        if light != NONE16:
+            for i in range(len(tris)):
+                self.light_infos.append((0, base_f + i))
+                self.light_powers.append(1.0)
 
     def add_face(self, p, mat, light=NONE16, uv=None, vn=None, vt=None, alpha_tex=NONE32):
         """Scene::addFace (Scene.h:82-116): indices are object-relative
@@ -248,25 +315,25 @@ class Scene:
     def blobs(self) -> dict:
         def f4(v):
             a = np.zeros((max(len(v), 1), 4), dtype=np.float32)
-            if v:
-                a[: len(v), :3] = np.asarray(v, dtype=np.float32)
+            if len(v):
+                a[: len(v), :3] = v.array().astype(np.float32)
             return a
 
         uv = np.zeros((max(len(self.uvs), 1), 2), dtype=np.float32)
-        if self.uvs:
-            uv[: len(self.uvs)] = np.asarray(self.uvs, dtype=np.float32)
+        if len(self.uvs):
+            uv[: len(self.uvs)] = self.uvs.array().astype(np.float32)
         lights = np.zeros((max(len(self.light_infos), 1), 2), dtype=np.uint32)
         for i, (inf, ref) in enumerate(self.light_infos):
             lights[i] = (inf, ref)
         return {"vertices": f4(self.vertices), "normals": f4(self.normals), "tangents": f4(self.tangents),
-                "uvs": uv, "faces": np.array(self.faces, dtype=FACE_DTYPE), "lights": lights,
+                "uvs": uv, "faces": self.faces.array(), "lights": lights,
                 "materials": self.materials.array(), "textures": self.textures.array(),
                 "others": self.others.array(), "num_lights": len(self.light_infos)}
 
     def soa(self):
         """Vertex SoA + triangle index array for the LBVH build."""
-        v = np.asarray(self.vertices, dtype=np.float32)
-        f = np.array(self.faces, dtype=FACE_DTYPE)
+        v = self.vertices.array().astype(np.float32)
+        f = self.faces.array()
         return (np.ascontiguousarray(v[:, 0]), np.ascontiguousarray(v[:, 1]), np.ascontiguousarray(v[:, 2]),
                 np.ascontiguousarray(f["p"].reshape(-1)))
 
@@ -373,30 +440,26 @@ class MaterialCreator:
         lum = (np.float32(0.2126) * rgb[..., 0] + np.float32(0.7152) * rgb[..., 1] +
                np.float32(0.0722) * rgb[..., 2]).astype(np.float32)
         width_c = np.float32(1.0) / np.float32(w)
-        row_mass = np.zeros(h, dtype=np.float32)
+        corr = np.array([math.cos(math.pi * (0.5 - (i + 0.5) / h)) if zenith_correction else 1.0 for i in range(h)],
+                        dtype=np.float32)
+        pdf = (lum * corr[:, None]).astype(np.float32)
+        # running sums in float32, left to right, as the reference's loop
+        cdf = np.zeros((h, w + 1), dtype=np.float32)
+        cdf[:, 1:] = np.cumsum((pdf * width_c).astype(np.float32), axis=1, dtype=np.float32)
+        row_mass = cdf[:, w].copy()
+        with np.errstate(divide="ignore"):
+            norm = np.where(row_mass > 0, np.float32(1.0) / row_mass, np.float32(0)).astype(np.float32)
+        pdf = (pdf * norm[:, None]).astype(np.float32)
+        cdf[:, 1:] = (cdf[:, 1:] * norm[:, None]).astype(np.float32)
         for i in range(h):
-            corr = np.float32(math.cos(math.pi * (0.5 - (i + 0.5) / h))) if zenith_correction else np.float32(1)
-            pdf = (lum[i] * corr).astype(np.float32)
-            cdf = np.zeros(w + 1, dtype=np.float32)
-            acc = np.float32(0)
-            for j in range(w):
-                acc = np.float32(acc + np.float32(pdf[j] * width_c))
-                cdf[j + 1] = acc
-            row_mass[i] = cdf[w]
-            norm = np.float32(1.0) / cdf[w] if cdf[w] > 0 else np.float32(0)
-            pdf = (pdf * norm).astype(np.float32)
-            cdf[1:] = (cdf[1:] * norm).astype(np.float32)
             ch = children + 28 * i
             o.put(ch, struct.pack("<B3xIfffii", 1, w, 0.0, 1.0, float(width_c),
                                   c_pdfs + 4 * w * i - ch, c_cdfs + 4 * (w + 1) * i - ch))
-            o.put(c_pdfs + 4 * w * i, pdf.tobytes())
-            o.put(c_cdfs + 4 * (w + 1) * i, cdf.tobytes())
+        o.put(c_pdfs, pdf.tobytes())
+        o.put(c_cdfs, cdf.tobytes())
         width_p = np.float32(1.0) / np.float32(h)
         pcdf = np.zeros(h + 1, dtype=np.float32)
-        acc = np.float32(0)
-        for i in range(h):
-            acc = np.float32(acc + np.float32(row_mass[i] * width_p))
-            pcdf[i + 1] = acc
+        pcdf[1:] = np.cumsum((row_mass * width_p).astype(np.float32), dtype=np.float32)
         norm = np.float32(1.0) / pcdf[h]
         ppdf = (row_mass * norm).astype(np.float32)
         pcdf[1:] = (pcdf[1:] * norm).astype(np.float32)

@@ -127,3 +127,145 @@ def pixel_seeds(width: int, height: int) -> np.ndarray:
         s = (np.uint64(1812433253) * (s ^ (s >> np.uint64(30))) + np.uint64(k)) & m
         out[:, k] = s.astype(np.uint32)
     return out
+
+
+# ------------------------------------------------------------- large scene
+
+
+def value_noise(shape, octaves, seed, base_cells=4):
+    """Seeded fractal value noise on [0,1]^2 sampled on a (h, w) grid:
+    `octaves` lattices of random values, each twice as fine and half as
+    strong, smoothstep-interpolated; result in roughly [-1, 1]."""
+    rng = np.random.default_rng(seed)
+    h, w = shape
+    y = np.linspace(0.0, 1.0, h)[:, None]
+    x = np.linspace(0.0, 1.0, w)[None, :]
+    out = np.zeros((h, w))
+    amp, total = 1.0, 0.0
+    for o in range(octaves):
+        cells = base_cells * (2 ** o)
+        lat = rng.uniform(-1.0, 1.0, size=(cells + 1, cells + 1))
+        fx, fy = x * cells, y * cells
+        ix, iy = np.minimum(fx.astype(int), cells - 1), np.minimum(fy.astype(int), cells - 1)
+        tx, ty = fx - ix, fy - iy
+        sx, sy = tx * tx * (3 - 2 * tx), ty * ty * (3 - 2 * ty)
+        v00, v10 = lat[iy, ix], lat[iy, ix + 1]
+        v01, v11 = lat[iy + 1, ix], lat[iy + 1, ix + 1]
+        out += amp * ((v00 * (1 - sx) + v10 * sx) * (1 - sy) + (v01 * (1 - sx) + v11 * sx) * sy)
+        total += amp
+        amp *= 0.5
+    return out / total
+
+
+def normal_map(size, seed):
+    """RGB8 tangent-space normal map from seeded noise heights."""
+    hgt = value_noise((size, size), 5, seed, base_cells=8) * 2.0
+    gy, gx = np.gradient(hgt, 1.0 / size)
+    n = np.stack([-gx * 0.02, -gy * 0.02, np.ones_like(hgt)], axis=-1)
+    n /= np.linalg.norm(n, axis=-1, keepdims=True)
+    return np.clip((n * 0.5 + 0.5) * 255.0 + 0.5, 0, 255).astype(np.uint8)
+
+
+def sky_map(w, h, seed, sun_dir=(0.4, 0.6, -0.5), sun_peak=5e3, sun_sigma_deg=1.0):
+    """Equirectangular fp32 RGB sky: lognormal(0, 1) radiance plus a Gaussian
+    sun spot (peak `sun_peak`, sigma `sun_sigma_deg`)."""
+    rng = np.random.default_rng(seed)
+    img = np.exp(rng.normal(0.0, 1.0, size=(h, w, 3)))
+    v = (np.arange(h) + 0.5) / h
+    u = (np.arange(w) + 0.5) / w
+    theta = (v * np.pi)[:, None]
+    phi = (u * 2 * np.pi)[None, :]
+    # direction of texel (u, v) as the kernels map it (light.cl:165-168)
+    d = np.stack([-np.sin(phi) * np.sin(theta), np.cos(theta) * np.ones_like(phi), np.cos(phi) * np.sin(theta)], -1)
+    s = np.asarray(sun_dir, dtype=np.float64)
+    s /= np.linalg.norm(s)
+    ang = np.arccos(np.clip(d @ s, -1.0, 1.0))
+    sig = math.radians(sun_sigma_deg)
+    img += (sun_peak * np.exp(-0.5 * (ang / sig) ** 2))[..., None]
+    return img.astype(np.float32)
+
+
+def _sphere_mesh(seg, rings):
+    th = np.pi * np.arange(rings + 1) / rings
+    ph = 2 * np.pi * np.arange(seg + 1) / seg
+    n = np.stack([np.sin(th)[:, None] * np.cos(ph)[None, :], np.cos(th)[:, None] * np.ones_like(ph)[None, :],
+                  np.sin(th)[:, None] * np.sin(ph)[None, :]], -1).reshape(-1, 3)
+    uv = np.stack(np.meshgrid(np.arange(seg + 1) / seg, np.arange(rings + 1) / rings), -1).reshape(-1, 2)
+    row = seg + 1
+    tris = []
+    for j in range(rings):
+        for i in range(seg):
+            a, b, c, d = j * row + i, j * row + i + 1, (j + 1) * row + i, (j + 1) * row + i + 1
+            if j != 0:
+                tris.append((a, b, c))
+            if j != rings - 1:
+                tris.append((b, d, c))
+    return n, uv, np.array(tris, dtype=np.int64)
+
+
+def terrain_scene(width=1920, height=1080, grid=1024, n_spheres=256, env_w=1024, env_h=512, seed=7,
+                  aperture=0.02, focus=1.5) -> S.Scene:
+    """Large path-tracing scene: a grid x grid heightfield (2 triangles per
+    cell) displaced by 6-octave value noise (amplitude 0.15), 256 UV spheres
+    (24 x 12) with log-uniform radii 0.005-0.05 resting on it, 8 materials
+    drawn from {Lambertian, Lambertian + coat, rough conductor, dielectric}
+    with albedo U[0.05, 0.9] and roughness U[0.02, 0.6}, one 512 x 512 RGB8
+    normal map per material, lit only by an equirectangular sky (stored as
+    RGBA16F, the reference's environment texture format), thin-lens camera."""
+    rng = np.random.default_rng(seed)
+    sc = S.Scene()
+    mc = sc.mc
+    # materials
+    kinds = rng.integers(0, 4, size=8)
+    mats = []
+    for m in range(8):
+        alb = rng.uniform(0.05, 0.9, size=3)
+        rough = float(rng.uniform(0.02, 0.6))
+        mc.normal_map_texture(f"bump{m}", normal_map(512, seed * 100 + m))
+        mc.float3_constant_texture(f"alb{m}", *alb)
+        name = f"mat{m}"
+        if kinds[m] == 0:
+            mc.float_constant_texture(f"sig{m}", 0.0)
+            mc.matte_material(name, f"bump{m}", f"alb{m}", f"sig{m}")
+        elif kinds[m] == 1:
+            mc.float3_constant_texture(f"rs{m}", 0.04, 0.04, 0.04)
+            mc.float_constant_texture(f"n{m}", 2.0 / (rough * rough) - 2.0)
+            mc.ashikhmin_material(name, f"bump{m}", f"rs{m}", f"alb{m}", f"n{m}", f"n{m}")
+        elif kinds[m] == 2:
+            mc.float_constant_texture(f"r{m}", rough)
+            mc.newward_material(name, f"bump{m}", f"alb{m}", f"r{m}", f"r{m}")
+        else:
+            mc.float3_constant_texture(f"one{m}", 1.0, 1.0, 1.0)
+            mc.glass_material(name, f"bump{m}", f"one{m}", f"one{m}", 1.0, 1.5)
+        mats.append(sc.mat_ref[name])
+    # heightfield over [0,1]^2 in xz, uv tiled 4x
+    hgt = 0.15 * value_noise((grid + 1, grid + 1), 6, seed)
+    xs = np.linspace(0.0, 1.0, grid + 1)
+    X, Z = np.meshgrid(xs, xs)
+    verts = np.stack([X, hgt, Z], -1).reshape(-1, 3)
+    uvs = np.stack([X * 4.0, Z * 4.0], -1).reshape(-1, 2)
+    i = np.arange(grid)
+    a = (i[:, None] * (grid + 1) + i[None, :]).reshape(-1)
+    b, c, d = a + 1, a + (grid + 1), a + (grid + 1) + 1
+    tris = np.concatenate([np.stack([a, c, b], -1), np.stack([b, c, d], -1)])
+    sc.add_mesh(verts, tris, mats[0], uvs=uvs)
+    # spheres resting on the terrain
+    n_unit, uv_unit, t_unit = _sphere_mesh(24, 12)
+    for k in range(n_spheres):
+        r = float(np.exp(rng.uniform(np.log(0.005), np.log(0.05))))
+        px, pz = rng.uniform(0.05, 0.95, size=2)
+        gx, gz = int(round(px * grid)), int(round(pz * grid))
+        cy = float(hgt[gz, gx]) + r
+        sc.add_mesh(n_unit * r + np.array([px, cy, pz]), t_unit, mats[int(rng.integers(0, 8))], uvs=uv_unit,
+                    normals=n_unit)
+    # sky
+    sky = sky_map(env_w, env_h, seed + 1)
+    rgba = np.ones((env_h, env_w, 4), dtype=np.float16)
+    rgba[..., :3] = sky.astype(np.float16)
+    mc.image_texture("sky", rgba, "rgba16f")
+    mc.image_based_env_light_property("IBL", "sky", rgba[..., :3].astype(np.float32), 1.0)
+    sc.set_environment("IBL")
+    cam = S.look_at((0.5, 0.45, 1.45), (0.5, 0.05, 0.35), (0, 1, 0))
+    sc.set_camera(width, height, cam, fov_y_deg=40.0, lens_radius=aperture, focus_dist=focus)
+    sc.build()
+    return sc
