@@ -76,6 +76,7 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--render", type=int, default=1, help="also time the path tracer (0 = skip)")
     ap.add_argument("--render-only", action="store_true", help="time only the path tracer (for profiling)")
+    ap.add_argument("--adjoint-only", action="store_true", help="time only the adjoint renderer (for profiling)")
     return ap.parse_args()
 
 
@@ -241,6 +242,66 @@ def bench_render_terrain(dev, spp=4) -> dict:
     return out
 
 
+def bench_adjoint(dev, spp=32) -> dict:
+    """Differentiable render: the 8-material Cornell box with a 64 x 32
+    environment, 512 x 512, `spp` samples per pixel, depth 5.  Times the
+    forward wavefront render and the adjoint pass (path replay; gradients of
+    an L2 image loss against a target rendered with perturbed parameters for
+    8 RGB albedos, 8 roughness values and 2048 x 3 environment texels), both
+    with nearer-child-first traversal."""
+    import numpy as np
+    import torch
+
+    from clear_gb300 import scenes
+    from clear_gb300.render import DeviceScene
+
+    w = h = 512
+    sc, info = scenes.cornell_adjoint(w, h)
+    ds = DeviceScene(sc, dev)
+    r = np.random.default_rng(11)
+    alb = np.clip(info["albedo"] + r.normal(0, 0.1, info["albedo"].shape), 0.01, 0.99)
+    rough = info["roughness"].copy()
+    rough[:7] = np.maximum(rough[:7] + r.normal(0, 0.05, 7), 0.02)
+    env = info["env"] * np.exp(r.normal(0, 0.3, info["env"].shape))
+    tsc, _ = scenes.cornell_adjoint(w, h, albedo=alb, roughness=rough, env=env)
+    tds = DeviceScene(tsc, dev)
+    rng, target = tds.new_frame()
+    tds.render(rng, target, spp, max_depth=5, wavefront=True)
+    tex = torch.tensor(info["albedo_tex"] + info["rough_tex"], dtype=torch.int32, device=dev)
+    kind = torch.tensor([0] * 8 + [1] * 8, dtype=torch.uint8, device=dev)
+    grad = torch.zeros((16, 4), dtype=torch.float32, device=dev)
+    genv = torch.zeros((info["env"].shape[0] * info["env"].shape[1], 4), dtype=torch.float32, device=dev)
+    stream = torch.cuda.current_stream(dev)
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
+    seeds, pix = ds.new_frame()
+    ds.render(seeds.clone(), pix, 2, max_depth=5, wavefront=True)  # warm-up
+    ds.render_adjoint(seeds.clone(), torch.zeros_like(pix), 2, 5, tex, kind, grad, info["env_tex"], genv)
+    torch.cuda.synchronize()
+    pix.zero_()
+    reps = 2
+    ev[0].record(stream)
+    for _ in range(reps):
+        pix.zero_()
+        ds.render(seeds.clone(), pix, spp, max_depth=5, wavefront=True)
+    ev[1].record(stream)
+    dloss = torch.zeros_like(pix)
+    dloss[:, :3] = 2.0 * (pix[:, :3] - target[:, :3]) / (spp * spp)
+    grad.zero_()
+    genv.zero_()
+    ev[2].record(stream)
+    for _ in range(reps):
+        ds.render_adjoint(seeds.clone(), dloss, spp, 5, tex, kind, grad, info["env_tex"], genv)
+    ev[3].record(stream)
+    torch.cuda.synchronize()
+    fwd = ev[0].elapsed_time(ev[1]) / reps
+    adj = ev[2].elapsed_time(ev[3]) / reps
+    return {"workload": "adjoint cornell 8 materials + 64x32 env, 512x512, 32 spp, depth 5",
+            "params": 16 * 3 + genv.shape[0] * 3, "forward_ms": fwd, "adjoint_ms": adj,
+            "adjoint_over_forward": adj / fwd, "forward_msamples_s": w * h * spp / fwd / 1e3,
+            "adjoint_msamples_s": w * h * spp / adj / 1e3,
+            "grad_norm": float(torch.linalg.norm(grad).item()), "env_grad_norm": float(torch.linalg.norm(genv).item())}
+
+
 def run_reference(args):
     rank, world, _ = dist_env()
     if rank != 0:
@@ -383,6 +444,7 @@ def run_ours(args):
     ordered_t_mismatch = int((ht != ht2).sum().item())
     render = bench_render(dev, args) if args.render else None
     render_terrain = bench_render_terrain(dev) if args.render else None
+    adjoint = bench_adjoint(dev) if args.render else None
     hit_frac = float((hid >= 0).float().mean().item())
     occ_frac = float(occ.float().mean().item())
     clk = clocks.stop()
@@ -425,6 +487,7 @@ def run_ours(args):
                       "shadow_occluded_frac": occ_frac},
         "render": render,
         "render_terrain": render_terrain,
+        "adjoint": adjoint,
         "gpu_launches": launches_per_build * args.steps,
         "clocks": clk,
         "device_error_bits": dev_err,
@@ -446,6 +509,14 @@ def main():
         build()
         dev = torch.device("cuda", 0)
         print(json.dumps({"render": bench_render(dev, args), "render_terrain": bench_render_terrain(dev)}), flush=True)
+        return
+    if args.adjoint_only:
+        import torch
+
+        from clear_gb300.build import build
+
+        build()
+        print(json.dumps({"adjoint": bench_adjoint(torch.device("cuda", 0))}), flush=True)
         return
     if args.impl == "reference":
         run_reference(args)

@@ -29,6 +29,12 @@ class ClrBvh(C.Structure):
                 ("tris", C.c_void_p), ("root_box", C.c_void_p)]
 
 
+class ClrAdjointParams(C.Structure):
+    _fields_ = [("param_tex", C.c_void_p), ("param_kind", C.c_void_p), ("num_params", C.c_uint32),
+                ("grad_params", C.c_void_p), ("env_tex", C.c_uint32), ("grad_env", C.c_void_p),
+                ("tape", C.c_void_p), ("tape_capacity", C.c_uint32), ("tape_count", C.c_void_p)]
+
+
 _lib = None
 
 
@@ -72,6 +78,9 @@ def lib() -> C.CDLL:
             "clr_render": [vp, u32, u32, vp, vp, u32, u32, u32, vp],
             "clr_render_workspace_bytes": [u32, u32, C.POINTER(C.c_uint64)],
             "clr_render_wavefront": [vp, u32, u32, vp, vp, u32, u32, u32, vp, C.c_uint64, vp],
+            "clr_render_adjoint_workspace_bytes": [u32, u32, u32, C.POINTER(C.c_uint64)],
+            "clr_render_adjoint": [vp, u32, u32, vp, vp, u32, u32, u32, C.POINTER(ClrAdjointParams), vp,
+                                   C.c_uint64, vp],
             "clr_lbvh_pass_times": [vp, C.POINTER(C.c_float), C.POINTER(C.c_char_p), i32, C.POINTER(i32)],
         }
         for name, args in sig.items():

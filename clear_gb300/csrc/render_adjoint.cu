@@ -1,0 +1,754 @@
+// Adjoint path tracer: path-replay backpropagation in wavefront form.
+//
+// Gives G = sum_p dLoss/dAccum_p . dAccum_p/dtheta for a per-pixel weight
+// dLoss/dAccum (the gradient of an image loss) with respect to constant
+// textures of the materials (colour: albedo R / T / Rs / Rd; float: Oren-Nayar
+// sigma, Ward ax / ay, Ashikhmin nu / nv) and the texels of the environment's
+// image texture.  Sampling is detached: directions, pdfs, MIS weights, light
+// selection and Russian-roulette probabilities are constants, so G is the
+// derivative of the estimator over the sampled paths (no visibility or
+// geometry terms).
+//
+// Every sample of a pixel runs twice from the same RNG state in the pixel's
+// path slot:
+//   primal pass : the forward path tracer (render_wf.cu) with the radiance of
+//                 the sample summed into L instead of the pixel;
+//   replay pass : the same path, same random numbers; each term is subtracted
+//                 from L when it is met, so L is the radiance still ahead.
+//                 The BSDF value sampled at vertex k scales every later term:
+//                 it adds dlog(fs_k)/dtheta * L, taken at vertex k+1 after the
+//                 shadow pass has removed vertex k's next-event term.  Emission
+//                 and next-event terms add their own BSDF / environment-texel
+//                 derivatives.
+// Nothing of a path is stored between its passes but its RNG state.
+//
+// Gradients of the material parameters are summed per block in shared memory
+// and kept per block in the workspace; one reduction adds them to the caller's
+// buffer at the end.  Environment texels (many addresses, little contention)
+// take global atomics.
+//
+// An optional tape records every factor of every replayed path (camera
+// weight, emission, roulette, next-event and BSDF-sample records) so that the
+// estimator can be re-evaluated on the host with perturbed parameters.
+#include "adjoint.cuh"
+#include "render_common.cuh"
+
+CLR_DEFINE_STATUS_READER(render_adjoint)
+
+namespace clr {
+
+constexpr int kAdThreads = 128;
+constexpr uint32_t kSmemParams = 1024;  // parameters summed in shared memory (K * 16 B)
+constexpr int kShWords = 4 + kMaxGrad;  // float4s per shadow entry
+
+// Tape record kinds (word 3, bits 0-7); bit 8 marks a visible next-event record.
+enum : uint32_t { kTapeCam = 0, kTapeEmit = 1, kTapeRR = 2, kTapeNee = 3, kTapeSample = 4, kTapeVisible = 0x100 };
+constexpr uint32_t kTapeWords = 32;
+constexpr uint32_t kTapeSpecular = 0x80000000u;  // BSDF-sample record: specular component index follows
+
+struct AdState {
+    float4* org;     // xyz ray origin
+    float4* dir;     // xyz direction, w dirPDF
+    float4* alpha;   // xyz throughput, w initY
+    uint4* misc;     // x depth, y sampledType, z samples done, w pass (0 primal, 1 replay)
+    float4* hit;     // x id bits, y t, z b1, w b2
+    float4* L;       // xyz radiance of the sample (primal: summed so far; replay: still ahead)
+    uint4* rng0;     // RNG state at the start of the current sample
+    float4* pd;      // kMaxGrad per path: pending dlog(fs)/dtheta per channel, w = slot bits (-1 = none)
+    uint32_t* q[2];  // active path queues
+    float4* sh;      // kShWords float4s per shadow entry
+    unsigned int* count;  // [0],[1] active counts, [2] shadow count
+    float* partial;  // per-block parameter gradients (grid x K x 4), or null
+};
+
+struct Tape {
+    uint32_t* rec;
+    uint32_t cap;
+    uint32_t* count;
+};
+
+struct AdParams {
+    ParamTable pt;
+    float4* grad;         // K entries: xyz per channel (colour) or x (float)
+    uint32_t env_tex;     // textures-blob offset of the differentiated environment texture, kNoTex = none
+    float4* grad_env;     // one per texel of that texture
+    const float4* dloss;  // dLoss / dAccum per pixel
+    Tape tape;
+};
+
+__device__ __forceinline__ Rng rng_from(uint4 s) {
+    Rng r;
+    r.s[0] = s.x;
+    r.s[1] = s.y;
+    r.s[2] = s.z;
+    r.s[3] = s.w;
+    return r;
+}
+__device__ __forceinline__ uint4 rng_bits(const Rng& r) { return make_uint4(r.s[0], r.s[1], r.s[2], r.s[3]); }
+
+__device__ __forceinline__ uint32_t ad_queue_slot(unsigned int* count, bool want) {
+    const unsigned int m = __ballot_sync(0xFFFFFFFFu, want);
+    if (!m) return 0;
+    const int lane = threadIdx.x & 31, leader = __ffs(m) - 1;
+    uint32_t base = 0;
+    if (lane == leader) base = atomicAdd(count, (unsigned int)__popc(m));
+    base = __shfl_sync(0xFFFFFFFFu, base, leader);
+    unsigned int lt;
+    asm("mov.u32 %0, %%lanemask_lt;" : "=r"(lt));
+    return base + __popc(m & lt);
+}
+
+// Parameter-gradient sink of one block: shared memory when the table fits,
+// else the caller's buffer directly.
+struct GradSink {
+    float* s;  // 4 floats per parameter
+    const uint8_t* kind;
+    __device__ __forceinline__ void add(int slot, f3 w) const {
+        if (slot < 0) return;
+        float* g = s + 4 * slot;
+        if (__ldg(kind + slot) == 1) {
+            atomicAdd(g, w.x + w.y + w.z);
+        } else {
+            atomicAdd(g, w.x);
+            atomicAdd(g + 1, w.y);
+            atomicAdd(g + 2, w.z);
+        }
+    }
+};
+
+extern __shared__ float s_grad[];
+
+__device__ __forceinline__ GradSink sink_begin(const AdState& S, const AdParams& P) {
+    GradSink g;
+    g.kind = P.pt.kind;
+    if (S.partial) {
+        for (uint32_t i = threadIdx.x; i < 4u * P.pt.k; i += blockDim.x) s_grad[i] = 0.f;
+        __syncthreads();
+        g.s = s_grad;
+    } else {
+        g.s = reinterpret_cast<float*>(P.grad);
+    }
+    return g;
+}
+
+// Adds the block's sums to its row of the per-block buffer (the row's only
+// writer: kernels of one call run in stream order).
+__device__ __forceinline__ void sink_end(const AdState& S, const AdParams& P) {
+    if (!S.partial) return;
+    __syncthreads();
+    float* row = S.partial + (size_t)blockIdx.x * 4u * P.pt.k;
+    for (uint32_t i = threadIdx.x; i < 4u * P.pt.k; i += blockDim.x) {
+        const float v = s_grad[i];
+        if (v != 0.f) row[i] += v;
+    }
+}
+
+__device__ __forceinline__ void add_env_grad(const AdParams& P, int texel, f3 g) {
+    float4* ge = P.grad_env + texel;
+    atomicAdd(&ge->x, g.x);
+    atomicAdd(&ge->y, g.y);
+    atomicAdd(&ge->z, g.z);
+}
+
+// Texel of the differentiated environment texture seen in direction uv
+// (image lookup of texture.cl:76-80), with the light's multiplier, or -1
+// when the environment's first component does not read that texture.
+__device__ __forceinline__ int env_texel(const DScene& sc, const AdParams& P, float2 uv, float& mult) {
+    mult = 0.f;
+    if (P.env_tex == kNoTex) return -1;
+    const uint8_t* l = env_light_property(sc);
+    if (l[0] == 0) return -1;
+    const uint8_t* e = l + 4;  // ImageBasedEnvLElem {id, idx_Le, multiplier, idx_Dist2D}
+    if (e[0] != 0 || ldb<uint32_t>(e + 4) != P.env_tex) return -1;
+    mult = ldb<float>(e + 8);
+    const uint8_t* t = sc.textures + P.env_tex;
+    uint32_t x, y;
+    const uint8_t* d;
+    image_xy(t, uv, x, y, d);
+    return (int)(y * ldb<uint32_t>(t + 4) + x);
+}
+
+// ------------------------------------------------------------------ tape
+
+__device__ __forceinline__ uint32_t tape_alloc(const Tape& t) {
+    if (!t.rec) return kNone32;
+    const uint32_t i = atomicAdd(t.count, 1u);
+    return i < t.cap ? i : kNone32;
+}
+
+struct TapeRec {
+    uint32_t w[kTapeWords];
+    __device__ __forceinline__ void head(uint32_t p, uint32_t sample, uint32_t depth, uint32_t kind) {
+#pragma unroll
+        for (int k = 0; k < (int)kTapeWords; ++k) w[k] = 0;
+        w[0] = p;
+        w[1] = sample;
+        w[2] = depth;
+        w[3] = kind;
+    }
+    __device__ __forceinline__ void f(int k, float v) { w[k] = __float_as_uint(v); }
+    __device__ __forceinline__ void f3at(int k, f3 v) {
+        f(k, v.x);
+        f(k + 1, v.y);
+        f(k + 2, v.z);
+    }
+    __device__ __forceinline__ void store(const Tape& t, uint32_t i) const {
+        uint4* dst = reinterpret_cast<uint4*>(t.rec + (size_t)kTapeWords * i);
+#pragma unroll
+        for (int k = 0; k < (int)kTapeWords / 4; ++k)
+            dst[k] = make_uint4(w[4 * k], w[4 * k + 1], w[4 * k + 2], w[4 * k + 3]);
+    }
+};
+
+__device__ __forceinline__ void tape_put(const Tape& t, const TapeRec& r) {
+    const uint32_t i = tape_alloc(t);
+    if (i != kNone32) r.store(t, i);
+}
+
+// ---------------------------------------------------------------- kernels
+
+__device__ __forceinline__ void ad_start(const Camera& cam, const AdState& S, uint32_t p, uint32_t width, Rng& rng,
+                                         uint32_t done, uint32_t pass, const Tape& tape) {
+    f3 org, dir, alpha;
+    float dirPDF;
+    camera_ray(cam, p % width, p / width, rng, org, dir, alpha, dirPDF);
+    S.org[p] = make_float4(org.x, org.y, org.z, 0.f);
+    S.dir[p] = make_float4(dir.x, dir.y, dir.z, dirPDF);
+    S.alpha[p] = make_float4(alpha.x, alpha.y, alpha.z, luminance(alpha));
+    S.misc[p] = make_uint4(0u, 0u, done, pass);
+    S.pd[(size_t)kMaxGrad * p] = make_float4(0.f, 0.f, 0.f, __int_as_float(-1));
+    if (pass == 1u && tape.rec) {
+        TapeRec r;
+        r.head(p, done, 0, kTapeCam);
+        r.f3at(4, alpha);
+        tape_put(tape, r);
+    }
+}
+
+__global__ void __launch_bounds__(kAdThreads) k_ad_init(DScene sc, AdState S, uint32_t npix, uint32_t width,
+                                                        uint32_t* __restrict__ rand_states, uint32_t partial_floats) {
+    const Camera cam = load_camera(sc);
+    const Tape none{nullptr, 0, nullptr};
+    for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < npix; p += gridDim.x * blockDim.x) {
+        const uint4 s = reinterpret_cast<const uint4*>(rand_states)[p];
+        Rng rng = rng_from(s);
+        S.rng0[p] = s;
+        ad_start(cam, S, p, width, rng, 0u, 0u, none);
+        S.L[p] = make_float4(0.f, 0.f, 0.f, 0.f);
+        reinterpret_cast<uint4*>(rand_states)[p] = rng_bits(rng);
+        S.q[0][p] = p;
+    }
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < partial_floats; i += gridDim.x * blockDim.x)
+        S.partial[i] = 0.f;
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        S.count[0] = npix;
+        S.count[1] = 0;
+        S.count[2] = 0;
+    }
+}
+
+template <bool kOrdered>
+__global__ void __launch_bounds__(kAdThreads) k_ad_extend(DScene sc, AdState S, int cur) {
+    const uint32_t n = S.count[cur];
+    uint2 stack[kStackSize];
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const uint32_t p = S.q[cur][i];
+        const float4 o = S.org[p], d = S.dir[p];
+        Hit h;
+        if (intersect<kOrdered>(sc, mk(o.x, o.y, o.z), mk(d.x, d.y, d.z), h, stack))
+            S.hit[p] = make_float4(__uint_as_float(h.id), h.t, h.b1, h.b2);
+        else
+            S.hit[p] = make_float4(__uint_as_float(kNone32), INFINITY, 0.f, 0.f);
+    }
+}
+
+// Reflection / transmission mask of the components fs sums (reflection.cl:679-702).
+__device__ __forceinline__ uint32_t side_flags(const BSDF& f, f3 vout, f3 vin) {
+    return dot(vin, f.ng) * dot(vout, f.ng) > 0 ? (kTyAll & ~kTyTransmission) : (kTyAll & ~kTyReflection);
+}
+
+__device__ __forceinline__ void grad_of_sum(const BSDF& f, const ParamTable& pt, uint32_t flags, f3 vl, f3 il,
+                                            GradList& g) {
+#pragma unroll
+    for (int k = 0; k < kMaxBxDFs; ++k)
+        if (k < f.num && match_type(f.type[k], flags)) bx_grad(f, f.off[k], pt, vl, il, g);
+}
+
+// One path vertex (pathtracer.cl:128-262 per bounce) in either pass.
+// Shadow entry: [0] origin, w light face (0xFFFFFFFF = environment);
+// [1] direction, w path; [2] contribution c, w flags (bit 0 add to L, bit 1
+// replay, bits 2.. tape record + 1); replay only: [3] dc/d(env texel), w
+// texel (-1 = none); [4 + k] dc/dtheta of parameter k, w slot (-1 = end).
+__global__ void __launch_bounds__(kAdThreads) k_ad_shade(DScene sc, AdState S, AdParams P, int cur, uint32_t width,
+                                                         uint32_t* __restrict__ rand_states, uint32_t spp,
+                                                         uint32_t max_depth) {
+    const GradSink sink = sink_begin(S, P);
+    const uint32_t n = S.count[cur];
+    const Camera cam = load_camera(sc);
+    const uint32_t stride = gridDim.x * blockDim.x;
+    const uint32_t n_round = (n + 31u) & ~31u;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n_round; i += stride) {
+        bool cont = false, shadow = false;
+        uint32_t p = 0;
+        float4 e[kShWords];
+        if (i < n) {
+            p = S.q[cur][i];
+            Rng rng = rng_from(reinterpret_cast<const uint4*>(rand_states)[p]);
+            const float4 o4 = S.org[p], d4 = S.dir[p], a4 = S.alpha[p], h4 = S.hit[p];
+            const uint4 m = S.misc[p];
+            f3 org = mk(o4.x, o4.y, o4.z), dir = mk(d4.x, d4.y, d4.z), alpha = mk(a4.x, a4.y, a4.z);
+            float dirPDF = d4.w;
+            const float initY = a4.w;
+            uint32_t depth = m.x, sampledType = m.y;
+            const uint32_t done = m.z;
+            const bool replay = m.w == 1u;
+            const bool taping = replay && P.tape.rec != nullptr;
+            const float4 L4 = S.L[p];
+            f3 L = mk(L4.x, L4.y, L4.z);
+            f3 dL = mk(0.f, 0.f, 0.f);
+            if (replay) {
+                const float4 dl4 = __ldg(P.dloss + p);
+                dL = mk(dl4.x, dl4.y, dl4.z);
+                // the BSDF value sampled at the previous vertex scales all that is ahead
+                for (int k = 0; k < kMaxGrad; ++k) {
+                    const float4 dd = S.pd[(size_t)kMaxGrad * p + k];
+                    const int slot = __float_as_int(dd.w);
+                    if (slot < 0) break;
+                    sink.add(slot, dL * L * mk(dd.x, dd.y, dd.z));
+                }
+            }
+            int npend = 0;
+            bool ended = false;
+            const uint32_t hid = __float_as_uint(h4.x);
+            if (hid == kNone32) {
+                // escaped: environment emission (pathtracer.cl:183-196)
+                LightPt lpos;
+                lpos.atInfinity = true;
+                lpos.uv = env_uv(dir);
+                const f3 vout = -dir;
+                EDF edf;
+                edf_alloc(sc, kNone16, lpos, edf);
+                float MISWeight = 1.0f;
+                if ((sampledType & kTyNonSingular) && depth > 0) {
+                    const float lightPDF = area_pdf(sc, lpos) * 1.0f / edf_abs_cos(edf, vout);
+                    MISWeight = (dirPDF * dirPDF) / (lightPDF * lightPDF + dirPDF * dirPDF);
+                }
+                const f3 le = edf_le(edf, vout);
+                const f3 T = MISWeight * alpha * le;
+                if (replay) {
+                    L = mk(L.x - T.x, L.y - T.y, L.z - T.z);
+                    float mult;
+                    const int tx = env_texel(sc, P, lpos.uv, mult);
+                    if (tx >= 0) add_env_grad(P, tx, dL * (MISWeight * alpha) * mult);
+                    if (taping) {
+                        TapeRec r;
+                        r.head(p, done, depth, kTapeEmit);
+                        r.f(4, MISWeight);
+                        r.f3at(5, le);
+                        r.w[8] = (uint32_t)tx;
+                        r.f(9, mult);
+                        tape_put(P.tape, r);
+                    }
+                } else {
+                    L += T;
+                }
+                ended = true;
+            } else {
+                Hit h{hid, h4.y, h4.z, h4.w};
+                SurfPt sp;
+                surface_point(sc, org, dir, h, sp);
+                const Face face = load_face(sc, sp.faceID);
+                const f3 vout = -dir;
+                LightPt lpos;
+                lpos.faceID = kNone32;
+                if (face.light != kNone16) {
+                    light_from_surface(sp, lpos);
+                    EDF edf;
+                    edf_alloc(sc, face.light, lpos, edf);
+                    float MISWeight = 1.0f;
+                    if (depth > 0 && (sampledType & kTyNonSingular)) {
+                        const float d2 = (org.x - sp.p.x) * (org.x - sp.p.x) + (org.y - sp.p.y) * (org.y - sp.p.y) +
+                                         (org.z - sp.p.z) * (org.z - sp.p.z);
+                        const float lightPDF = area_pdf(sc, lpos) * d2 / edf_abs_cos(edf, vout);
+                        MISWeight = (dirPDF * dirPDF) / (lightPDF * lightPDF + dirPDF * dirPDF);
+                    }
+                    const f3 le = edf_le(edf, vout);
+                    const f3 T = depth > 0 ? MISWeight * alpha * le : alpha * le;
+                    if (replay) {
+                        L = mk(L.x - T.x, L.y - T.y, L.z - T.z);
+                        if (taping) {
+                            TapeRec r;
+                            r.head(p, done, depth, kTapeEmit);
+                            r.f(4, depth > 0 ? MISWeight : 1.0f);
+                            r.f3at(5, le);
+                            r.w[8] = kNone32;
+                            tape_put(P.tape, r);
+                        }
+                    } else {
+                        L += T;
+                    }
+                }
+                // Russian roulette (pathtracer.cl:206-214)
+                if (depth > 0) {
+                    if (depth >= max_depth) ended = true;
+                    else {
+                        const float continueProb = fminf(luminance(alpha) * (1.0f / initY), 1.0f);
+                        if (rng.uniform() < continueProb) {
+                            alpha *= 1.0f / continueProb;
+                            dirPDF *= continueProb;
+                            if (taping) {
+                                TapeRec r;
+                                r.head(p, done, depth, kTapeRR);
+                                r.f(4, 1.0f / continueProb);
+                                tape_put(P.tape, r);
+                            }
+                        } else {
+                            ended = true;
+                        }
+                    }
+                }
+                if (!ended) {
+                    BSDF bsdf;
+                    bsdf_alloc(sc, face.mat, sp, bsdf);
+                    if (bsdf_has_non_specular(bsdf)) {
+                        // next-event estimation (pathtracer.cl:216-240)
+                        const float uL = rng.uniform(), u0 = rng.uniform(), u1 = rng.uniform();
+                        EDF edf;
+                        float lightPDF;
+                        sample_light(sc, uL, u0, u1, lpos, edf, lightPDF);
+                        f3 vinL = lpos.p - sp.p;
+                        float dist2 = dot(vinL, vinL);
+                        vinL = vinL * (1.0f / sqrtf(dist2));
+                        if (lpos.atInfinity) {
+                            vinL = lpos.p;
+                            dist2 = 1.0f;
+                        }
+                        const f3 sorg = sp.p + vinL * kEpsilon;
+                        const f3 vinLrev = -vinL;
+                        const float fsPDF = bsdf_pdf(bsdf, vout, vinL) * edf_abs_cos(edf, vinL) / dist2;
+                        const float MISWeight = (lightPDF * lightPDF) / (lightPDF * lightPDF + fsPDF * fsPDF);
+                        const float s = MISWeight * edf_abs_cos(edf, vinL) * fabsf(dot(bsdf.n, vinL)) / dist2 / lightPDF;
+                        const f3 le = edf_le(edf, vinLrev);
+                        const f3 fsn = bsdf_f(bsdf, vout, vinL);
+                        const f3 c = s * (alpha * le * fsn);
+                        e[0] = make_float4(sorg.x, sorg.y, sorg.z, __uint_as_float(lpos.atInfinity ? kNone32 : lpos.faceID));
+                        e[1] = make_float4(vinL.x, vinL.y, vinL.z, __uint_as_float(p));
+                        e[2] = make_float4(c.x, c.y, c.z, 0.f);
+                        if (replay) {
+                            const uint32_t flags = side_flags(bsdf, vout, vinL);
+                            const f3 vl = world_to_local(bsdf.s, bsdf.t, bsdf.n, vout);
+                            const f3 il = world_to_local(bsdf.s, bsdf.t, bsdf.n, vinL);
+                            GradList g;
+                            g.clear();
+                            grad_of_sum(bsdf, P.pt, flags, vl, il, g);
+                            const f3 pre = s * (alpha * le);
+#pragma unroll
+                            for (int k = 0; k < kMaxGrad; ++k) {
+                                const f3 d = k < g.n ? pre * g.d[k] : mk(0.f, 0.f, 0.f);
+                                e[4 + k] = make_float4(d.x, d.y, d.z, __int_as_float(k < g.n ? g.slot[k] : -1));
+                            }
+                            float mult = 0.f;
+                            const int tx = lpos.atInfinity ? env_texel(sc, P, lpos.uv, mult) : -1;
+                            const f3 dt = s * (alpha * fsn) * mult;
+                            e[3] = make_float4(dt.x, dt.y, dt.z, __int_as_float(tx));
+                            if (taping) {
+                                const uint32_t ti = tape_alloc(P.tape);
+                                if (ti != kNone32) {
+                                    TapeRec r;
+                                    r.head(p, done, depth, kTapeNee);
+                                    r.f(4, s);
+                                    r.f3at(5, le);
+                                    r.w[8] = (uint32_t)tx;
+                                    r.f(9, mult);
+                                    r.w[10] = face.mat;
+                                    r.f(11, sp.uv.x);
+                                    r.f(12, sp.uv.y);
+                                    r.f3at(13, vl);
+                                    r.f3at(16, il);
+                                    r.w[19] = flags;
+                                    r.store(P.tape, ti);
+                                    e[2].w = __uint_as_float((ti + 1u) << 2);
+                                }
+                            }
+                        }
+                        shadow = true;
+                    }
+                    // BSDF sampling (pathtracer.cl:242-257)
+                    const float uc = rng.uniform(), v0 = rng.uniform(), v1 = rng.uniform();
+                    const f3 fs = bsdf_sample(bsdf, vout, uc, v0, v1, dir, dirPDF, sampledType);
+                    if (zero_vec(fs) || dirPDF == 0.0f) {
+                        ended = true;
+                    } else {
+                        if (replay) {
+                            // dlog of the sampled value: the summed components for a
+                            // non-specular sample, the chosen component for a specular one
+                            const f3 vl = world_to_local(bsdf.s, bsdf.t, bsdf.n, vout);
+                            const f3 il = world_to_local(bsdf.s, bsdf.t, bsdf.n, dir);
+                            GradList g;
+                            g.clear();
+                            uint32_t flags;
+                            if (sampledType & kTySpecular) {
+                                const uint32_t which = rand_uint(uc, (uint32_t)bsdf.num);
+                                const uint32_t off = pick4(bsdf.off, which);
+                                g.add(param_slot(P.pt, bx_tex(bsdf, off).c0), spec_dc0(load_bx(bsdf, off), vl, il));
+                                flags = kTapeSpecular | which;
+                            } else {
+                                flags = side_flags(bsdf, vout, dir);
+                                grad_of_sum(bsdf, P.pt, flags, vl, il, g);
+                            }
+                            const f3 inv = mk(fs.x != 0.f ? 1.0f / fs.x : 0.f, fs.y != 0.f ? 1.0f / fs.y : 0.f,
+                                              fs.z != 0.f ? 1.0f / fs.z : 0.f);
+                            for (int k = 0; k < g.n; ++k) {
+                                const f3 d = g.d[k] * inv;
+                                S.pd[(size_t)kMaxGrad * p + k] = make_float4(d.x, d.y, d.z, __int_as_float(g.slot[k]));
+                            }
+                            npend = g.n;
+                            if (taping) {
+                                TapeRec r;
+                                r.head(p, done, depth, kTapeSample);
+                                r.f(4, fabsf(dot(bsdf.n, dir)) / dirPDF);
+                                r.w[10] = face.mat;
+                                r.f(11, sp.uv.x);
+                                r.f(12, sp.uv.y);
+                                r.f3at(13, vl);
+                                r.f3at(16, il);
+                                r.w[19] = flags;
+                                tape_put(P.tape, r);
+                            }
+                        }
+                        alpha *= fs * (fabsf(dot(bsdf.n, dir)) / dirPDF);
+                        org = sp.p + dir * kEpsilon;
+                        ++depth;
+                    }
+                }
+            }
+            bool apply_L = true;
+            if (ended) {
+                if (!replay) {
+                    // primal pass over: replay the sample from its first random number
+                    rng = rng_from(S.rng0[p]);
+                    ad_start(cam, S, p, width, rng, done, 1u, P.tape);
+                    cont = true;
+                } else {
+                    apply_L = false;  // L of this sample is no longer needed
+                    if (done + 1 < spp) {
+                        S.rng0[p] = rng_bits(rng);
+                        ad_start(cam, S, p, width, rng, done + 1, 0u, P.tape);
+                        L = mk(0.f, 0.f, 0.f);
+                        cont = true;
+                    } else {
+                        S.misc[p] = make_uint4(depth, sampledType, done + 1, 0u);
+                    }
+                }
+            } else {
+                S.org[p] = make_float4(org.x, org.y, org.z, 0.f);
+                S.dir[p] = make_float4(dir.x, dir.y, dir.z, dirPDF);
+                S.alpha[p] = make_float4(alpha.x, alpha.y, alpha.z, initY);
+                S.misc[p] = make_uint4(depth, sampledType, done, m.w);
+                if (npend < kMaxGrad)
+                    S.pd[(size_t)kMaxGrad * p + npend] = make_float4(0.f, 0.f, 0.f, __int_as_float(-1));
+                cont = true;
+            }
+            S.L[p] = make_float4(L.x, L.y, L.z, 0.f);
+            reinterpret_cast<uint4*>(rand_states)[p] = rng_bits(rng);
+            if (shadow) e[2].w = __uint_as_float(__float_as_uint(e[2].w) | (apply_L ? 1u : 0u) | (replay ? 2u : 0u));
+        }
+        const uint32_t qs = ad_queue_slot(S.count + (cur ^ 1), cont);
+        if (cont) S.q[cur ^ 1][qs] = p;
+        const uint32_t ss = ad_queue_slot(S.count + 2, shadow);
+        if (shadow) {
+            float4* dst = S.sh + (size_t)kShWords * ss;
+            dst[0] = e[0];
+            dst[1] = e[1];
+            dst[2] = e[2];
+            if (__float_as_uint(e[2].w) & 2u)
+                for (int k = 3; k < kShWords; ++k) dst[k] = e[k];
+        }
+    }
+    sink_end(S, P);
+}
+
+template <bool kOrdered>
+__global__ void __launch_bounds__(kAdThreads) k_ad_shadow(DScene sc, AdState S, AdParams P) {
+    const GradSink sink = sink_begin(S, P);
+    const uint32_t n = S.count[2];
+    uint2 stack[kStackSize];
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const float4* e = S.sh + (size_t)kShWords * i;
+        const float4 a = e[0], b = e[1], c = e[2];
+        const uint32_t light_face = __float_as_uint(a.w), p = __float_as_uint(b.w), flags = __float_as_uint(c.w);
+        bool visible;
+        if (light_face == kNone32) {
+            visible = !occluded_any<kOrdered>(sc, mk(a.x, a.y, a.z), mk(b.x, b.y, b.z), stack);
+        } else {
+            Hit h;
+            visible = intersect<kOrdered>(sc, mk(a.x, a.y, a.z), mk(b.x, b.y, b.z), h, stack) && h.id == light_face;
+        }
+        if (!visible) continue;
+        const bool replay = (flags & 2u) != 0;
+        if (flags & 1u) {
+            float4 L = S.L[p];
+            if (replay) {
+                L.x -= c.x;
+                L.y -= c.y;
+                L.z -= c.z;
+            } else {
+                L.x += c.x;
+                L.y += c.y;
+                L.z += c.z;
+            }
+            S.L[p] = L;
+        }
+        if (!replay) continue;
+        if (flags >> 2) P.tape.rec[(size_t)kTapeWords * ((flags >> 2) - 1u) + 3] |= kTapeVisible;
+        const float4 dl4 = __ldg(P.dloss + p);
+        const f3 dL = mk(dl4.x, dl4.y, dl4.z);
+        for (int k = 0; k < kMaxGrad; ++k) {
+            const float4 g = e[4 + k];
+            const int slot = __float_as_int(g.w);
+            if (slot < 0) break;
+            sink.add(slot, dL * mk(g.x, g.y, g.z));
+        }
+        const float4 t = e[3];
+        const int tx = __float_as_int(t.w);
+        if (tx >= 0) add_env_grad(P, tx, dL * mk(t.x, t.y, t.z));
+    }
+    sink_end(S, P);
+}
+
+__global__ void k_ad_reset(AdState S, int next) {
+    S.count[next] = 0;
+    S.count[2] = 0;
+}
+
+// grad[i] += sum over blocks of partial[b][i]; one block per float of the table.
+__global__ void __launch_bounds__(256) k_ad_reduce(const float* __restrict__ partial, uint32_t nblocks,
+                                                   uint32_t nfloats, float* __restrict__ grad) {
+    const uint32_t i = blockIdx.x;
+    float acc = 0.f;
+    for (uint32_t b = threadIdx.x; b < nblocks; b += blockDim.x) acc += partial[(size_t)b * nfloats + i];
+    __shared__ float red[8];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xFFFFFFFFu, acc, o);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = acc;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        float s = 0.f;
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) s += red[w];
+        if ((i & 3u) != 3u) grad[i] += s;
+    }
+}
+
+static uint32_t ad_grid(uint32_t npix) { return std::min(div_up(npix, kAdThreads), 152u * 16u); }
+
+static size_t ad_layout(uint32_t npix, uint32_t num_params, char* base, AdState* S) {
+    size_t off = 0;
+    auto take = [&](size_t bytes) {
+        const size_t o = off;
+        off = (off + bytes + 255) / 256 * 256;
+        return o;
+    };
+    const size_t n = npix;
+    const size_t o_org = take(16 * n), o_dir = take(16 * n), o_alpha = take(16 * n), o_misc = take(16 * n),
+                 o_hit = take(16 * n), o_L = take(16 * n), o_rng0 = take(16 * n), o_pd = take(16 * kMaxGrad * n),
+                 o_q0 = take(4 * n), o_q1 = take(4 * n), o_sh = take(16 * kShWords * n), o_cnt = take(16);
+    const bool use_partial = num_params > 0 && num_params <= kSmemParams;
+    const size_t o_part = use_partial ? take((size_t)ad_grid(npix) * num_params * 16) : 0;
+    if (base && S) {
+        S->org = reinterpret_cast<float4*>(base + o_org);
+        S->dir = reinterpret_cast<float4*>(base + o_dir);
+        S->alpha = reinterpret_cast<float4*>(base + o_alpha);
+        S->misc = reinterpret_cast<uint4*>(base + o_misc);
+        S->hit = reinterpret_cast<float4*>(base + o_hit);
+        S->L = reinterpret_cast<float4*>(base + o_L);
+        S->rng0 = reinterpret_cast<uint4*>(base + o_rng0);
+        S->pd = reinterpret_cast<float4*>(base + o_pd);
+        S->q[0] = reinterpret_cast<uint32_t*>(base + o_q0);
+        S->q[1] = reinterpret_cast<uint32_t*>(base + o_q1);
+        S->sh = reinterpret_cast<float4*>(base + o_sh);
+        S->count = reinterpret_cast<unsigned int*>(base + o_cnt);
+        S->partial = use_partial ? reinterpret_cast<float*>(base + o_part) : nullptr;
+    }
+    return off;
+}
+
+}  // namespace clr
+
+using namespace clr;
+
+extern "C" int clr_render_adjoint_workspace_bytes(uint32_t width, uint32_t height, uint32_t num_params,
+                                                  uint64_t* bytes) {
+    if (!bytes) return clr_set_error(CLR_EINVAL, "clr_render_adjoint_workspace_bytes: bytes is NULL");
+    *bytes = ad_layout(width * height, num_params, nullptr, nullptr);
+    return CLR_OK;
+}
+
+extern "C" int clr_render_adjoint(const clr_scene* scene, uint32_t width, uint32_t height, uint32_t* rand_states,
+                                  const float* dloss_daccum, uint32_t spp, uint32_t max_depth, uint32_t flags,
+                                  const clr_adjoint_params* params, void* workspace, uint64_t workspace_bytes,
+                                  void* stream) {
+    int rc = check_render_args(scene, rand_states, const_cast<float*>(dloss_daccum));
+    if (rc != CLR_OK) return rc;
+    if (!params) return clr_set_error(CLR_EINVAL, "clr_render_adjoint: params is NULL");
+    const clr_adjoint_params& A = *params;
+    if (A.num_params > 0 && (!A.param_tex || !A.param_kind || !A.grad_params))
+        return clr_set_error(CLR_EINVAL, "clr_render_adjoint: NULL parameter table or gradient buffer");
+    if (A.env_tex != kNoTex && !A.grad_env) return clr_set_error(CLR_EINVAL, "clr_render_adjoint: grad_env is NULL");
+    if (A.tape && (!A.tape_count || A.tape_capacity == 0 || A.tape_capacity > (1u << 29)))
+        return clr_set_error(CLR_EINVAL, "clr_render_adjoint: a tape needs a counter and 1 .. 2^29 records");
+    if ((reinterpret_cast<uintptr_t>(A.grad_params) | reinterpret_cast<uintptr_t>(A.grad_env) |
+         reinterpret_cast<uintptr_t>(A.tape)) & 15u)
+        return clr_set_error(CLR_EINVAL, "clr_render_adjoint: gradient and tape buffers must be 16-byte aligned");
+    if (width == 0 || height == 0 || spp == 0) return CLR_OK;
+    const uint32_t npix = width * height;
+    const size_t need = ad_layout(npix, A.num_params, nullptr, nullptr);
+    if (!workspace || workspace_bytes < need)
+        return clr_set_error(CLR_ECAPACITY, "clr_render_adjoint: workspace of %llu bytes is smaller than %zu",
+                             (unsigned long long)workspace_bytes, need);
+    if (reinterpret_cast<uintptr_t>(workspace) & 255u)
+        return clr_set_error(CLR_EINVAL, "clr_render_adjoint: workspace must be 256-byte aligned");
+    if (max_depth == 0) max_depth = 100;
+    const DScene sc = make_dscene(scene);
+    AdState S;
+    ad_layout(npix, A.num_params, static_cast<char*>(workspace), &S);
+    AdParams P;
+    P.pt.tex = A.param_tex;
+    P.pt.kind = A.param_kind;
+    P.pt.k = A.num_params;
+    P.grad = reinterpret_cast<float4*>(A.grad_params);
+    P.env_tex = A.env_tex;
+    P.grad_env = reinterpret_cast<float4*>(A.grad_env);
+    P.dloss = reinterpret_cast<const float4*>(dloss_daccum);
+    P.tape = Tape{A.tape, A.tape_capacity, A.tape_count};
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    const bool ordered = (flags & CLR_RENDER_ORDERED) != 0;
+    const unsigned int grid = ad_grid(npix);
+    const uint32_t nfloats = 4u * A.num_params;
+    const size_t smem = S.partial ? (size_t)nfloats * sizeof(float) : 0;
+    k_ad_init<<<grid, kAdThreads, 0, st>>>(sc, S, npix, width, rand_states, S.partial ? grid * nfloats : 0u);
+    CLR_LAUNCH_CHECK("k_ad_init");
+    // every iteration advances each unfinished path by one vertex; a sample
+    // takes at most (max_depth + 1) vertices per pass
+    const uint64_t max_iters = 2ull * spp * (max_depth + 1) + 2;
+    for (uint64_t it = 0; it < max_iters; ++it) {
+        const int cur = (int)(it & 1);
+        if (ordered) k_ad_extend<true><<<grid, kAdThreads, 0, st>>>(sc, S, cur);
+        else k_ad_extend<false><<<grid, kAdThreads, 0, st>>>(sc, S, cur);
+        k_ad_reset<<<1, 1, 0, st>>>(S, cur ^ 1);
+        k_ad_shade<<<grid, kAdThreads, smem, st>>>(sc, S, P, cur, width, rand_states, spp, max_depth);
+        if (ordered) k_ad_shadow<true><<<grid, kAdThreads, smem, st>>>(sc, S, P);
+        else k_ad_shadow<false><<<grid, kAdThreads, smem, st>>>(sc, S, P);
+        CLR_LAUNCH_CHECK("adjoint iteration");
+        if ((it & 7) == 7) {
+            unsigned int left = 0;
+            CLR_CUDA_TRY(cudaMemcpyAsync(&left, S.count + (cur ^ 1), sizeof(left), cudaMemcpyDeviceToHost, st));
+            CLR_CUDA_TRY(cudaStreamSynchronize(st));
+            if (left == 0) break;
+        }
+    }
+    if (S.partial) {
+        k_ad_reduce<<<nfloats, 256, 0, st>>>(S.partial, grid, nfloats, A.grad_params);
+        CLR_LAUNCH_CHECK("k_ad_reduce");
+    }
+    return CLR_OK;
+}

@@ -13,6 +13,9 @@ from .scene import Scene
 from .scenes import pixel_seeds
 
 RENDER_ORDERED = 0x1
+NO_TEX = 0xFFFFFFFF
+TAPE_WORDS = 32
+TAPE_VISIBLE = 0x100
 
 
 class ClrScene(C.Structure):
@@ -67,6 +70,43 @@ class DeviceScene:
                 return
             ws = self.workspace()
             _lib.call("clr_render_wavefront", *args, C.c_void_p(ws.data_ptr()), C.c_uint64(ws.numel()), stream)
+
+    def render_adjoint(self, rng: torch.Tensor, dloss: torch.Tensor, spp: int, max_depth: int,
+                       param_tex: torch.Tensor, param_kind: torch.Tensor, grad: torch.Tensor,
+                       env_tex: int | None = None, grad_env: torch.Tensor | None = None,
+                       tape: torch.Tensor | None = None, tape_count: torch.Tensor | None = None,
+                       ordered: bool = True) -> None:
+        """Adds sum_p dloss[p] . dAccum[p]/dtheta to `grad` (K x 4 float32) and
+        `grad_env` (texels x 4) for the samples clr_render_wavefront would
+        take from the same `rng` (advanced in place).  param_tex (int32) /
+        param_kind (uint8) list the differentiated constant textures by their
+        textures-blob offsets.  `tape` (records x 32 int32) with `tape_count`
+        (1 int32, zeroed by the caller) records the replayed paths."""
+        K = int(param_tex.numel())
+        p = _lib.ClrAdjointParams(
+            param_tex.data_ptr() if K else None, param_kind.data_ptr() if K else None, K,
+            grad.data_ptr() if K else None, NO_TEX if env_tex is None else int(env_tex),
+            grad_env.data_ptr() if grad_env is not None else None,
+            tape.data_ptr() if tape is not None else None, int(tape.shape[0]) if tape is not None else 0,
+            tape_count.data_ptr() if tape_count is not None else None)
+        stream = C.c_void_p(torch.cuda.current_stream(self.device).cuda_stream)
+        ws = self.adjoint_workspace(K)
+        with torch.cuda.device(self.device):
+            _lib.call("clr_render_adjoint", C.byref(self.c), C.c_uint32(self.width), C.c_uint32(self.height),
+                      C.c_void_p(rng.data_ptr()), C.c_void_p(dloss.data_ptr()), C.c_uint32(spp),
+                      C.c_uint32(max_depth), C.c_uint32(RENDER_ORDERED if ordered else 0), C.byref(p),
+                      C.c_void_p(ws.data_ptr()), C.c_uint64(ws.numel()), stream)
+
+    def adjoint_workspace(self, num_params: int) -> torch.Tensor:
+        n = C.c_uint64(0)
+        _lib.call("clr_render_adjoint_workspace_bytes", C.c_uint32(self.width), C.c_uint32(self.height),
+                  C.c_uint32(num_params), C.byref(n))
+        cur = getattr(self, "_aws", None)
+        if cur is None or cur.numel() < int(n.value):
+            buf = torch.empty(int(n.value) + 256, dtype=torch.uint8, device=self.device)
+            off = (-buf.data_ptr()) % 256
+            self._aws = buf[off:off + int(n.value)]
+        return self._aws
 
     def workspace(self) -> torch.Tensor:
         if getattr(self, "_ws", None) is None:

@@ -117,6 +117,103 @@ def cornell_box(width=256, height=256, env: np.ndarray | None = None, env_multip
     return sc
 
 
+# Differentiable Cornell box: 8 materials, each with one colour (albedo) and
+# one float (roughness) constant texture.  Kinds: "matte" = Oren-Nayar
+# diffuse (roughness = sigma), "plastic" = diffuse + Ward coat (roughness =
+# ax = ay, coat colour 0.04), "ashikhmin" = Ashikhmin-Shirley coat over a
+# diffuse base (roughness = the exponent nu = nv, coat colour 0.04).
+ADJ_MATERIALS = [  # (surface, kind, albedo, roughness)
+    ("left", "matte", (0.63, 0.06, 0.06), 0.3),
+    ("right", "matte", (0.14, 0.45, 0.09), 0.3),
+    ("floor", "plastic", (0.73, 0.73, 0.73), 0.15),
+    ("ceiling", "matte", (0.75, 0.75, 0.75), 0.2),
+    ("back", "matte", (0.70, 0.70, 0.68), 0.25),
+    ("tall", "plastic", (0.60, 0.55, 0.50), 0.2),
+    ("short", "matte", (0.50, 0.60, 0.70), 0.3),
+    ("sphere", "ashikhmin", (0.80, 0.70, 0.30), 40.0),
+]
+
+
+def adjoint_env(w=64, h=32, seed=3) -> np.ndarray:
+    """A seeded equirectangular fill-light map (h, w, 3) float32: a sky
+    gradient times smooth noise."""
+    v = (np.arange(h, dtype=np.float32) + 0.5) / h
+    sky = np.stack([0.5 + 0.3 * (1 - v), 0.6 + 0.3 * (1 - v), 0.8 + 0.2 * (1 - v)], axis=-1)
+    n = value_noise((h, w), 3, seed)
+    return (sky[:, None, :] * (0.6 + 0.4 * n[..., None])).astype(np.float32)
+
+
+def cornell_adjoint(width=512, height=512, albedo=None, roughness=None, env=None, env_multiplier=1.0):
+    """The Cornell box with its 8 surfaces as separate parameterised
+    materials and an image-based environment seen through the open front.
+    Returns (scene, info): info["albedo_tex"] / info["rough_tex"] hold the
+    textures-blob offsets of the 8 albedo (colour) and roughness (float)
+    textures, info["env_tex"] that of the environment image (RGBA16F)."""
+    sc = S.Scene()
+    mc = sc.mc
+    albedo = np.asarray(albedo if albedo is not None else [m[2] for m in ADJ_MATERIALS], dtype=np.float32)
+    roughness = np.asarray(roughness if roughness is not None else [m[3] for m in ADJ_MATERIALS], dtype=np.float32)
+    env = adjoint_env() if env is None else np.asarray(env, dtype=np.float32)
+    mc.float3_constant_texture("coat_Rs", 0.04, 0.04, 0.04)
+    mc.float_constant_texture("sigma0", 0.0)
+    mat, alb_tex, rough_tex = {}, [], []
+    for i, (name, kind, _, _) in enumerate(ADJ_MATERIALS):
+        mc.float3_constant_texture("A_" + name, *map(float, albedo[i]))
+        mc.float_constant_texture("r_" + name, float(roughness[i]))
+        alb_tex.append(sc.tex_ref["A_" + name])
+        rough_tex.append(sc.tex_ref["r_" + name])
+        if kind == "matte":
+            mc.matte_material("m_" + name, None, "A_" + name, "r_" + name)
+        elif kind == "plastic":
+            mc.begin_material("m_" + name)
+            mc.diffuse_elem("A_" + name, "sigma0")
+            mc.newward_elem("coat_Rs", "r_" + name, "r_" + name)
+            mc.end_material()
+        else:
+            mc.ashikhmin_material("m_" + name, None, "coat_Rs", "A_" + name, "r_" + name, "r_" + name)
+        mat[name] = sc.mat_ref["m_" + name]
+    mc.float3_constant_texture("M_light", 15.0 * math.pi, 15.0 * math.pi, 15.0 * math.pi)
+    mc.diffuse_light_property("light", "M_light")
+    sc.begin_object()
+    for x in (0.0, 1.0):
+        for y in (0.0, 1.0):
+            for z in (0.0, 1.0):
+                sc.add_vertex(x, y, z)
+    V = lambda x, y, z: 4 * x + 2 * y + z  # noqa: E731
+    walls = [
+        ((V(0, 0, 0), V(1, 0, 0), V(1, 0, 1), V(0, 0, 1)), "floor"),
+        ((V(0, 1, 0), V(0, 1, 1), V(1, 1, 1), V(1, 1, 0)), "ceiling"),
+        ((V(0, 0, 0), V(0, 1, 0), V(1, 1, 0), V(1, 0, 0)), "back"),
+        ((V(0, 0, 0), V(0, 0, 1), V(0, 1, 1), V(0, 1, 0)), "left"),
+        ((V(1, 0, 0), V(1, 1, 0), V(1, 1, 1), V(1, 0, 1)), "right"),
+    ]
+    for (a, b, c, d), m in walls:
+        sc.add_face((a, b, c), mat[m])
+        sc.add_face((a, c, d), mat[m])
+    sc.end_object()
+    sc.begin_object()
+    for x, z in ((0.375, 0.375), (0.625, 0.375), (0.625, 0.625), (0.375, 0.625)):
+        sc.add_vertex(x, 0.999, z)
+    sc.add_face((0, 1, 2), mat["ceiling"], light=sc.light_ref["light"])
+    sc.add_face((0, 2, 3), mat["ceiling"], light=sc.light_ref["light"])
+    sc.end_object()
+    _box(sc, mat["tall"], (0.72, 0.3, 0.33), (0.27, 0.6, 0.27), -18.0)
+    _box(sc, mat["short"], (0.70, 0.14, 0.76), (0.25, 0.28, 0.25), 15.0)
+    _uv_sphere(sc, mat["sphere"], (0.3, 0.25, 0.6), 0.2)
+    h, w = env.shape[:2]
+    rgba = np.ones((h, w, 4), dtype=np.float16)
+    rgba[..., :3] = env.astype(np.float16)
+    mc.image_texture("env", rgba, "rgba16f")
+    mc.image_based_env_light_property("IBL", "env", rgba[..., :3].astype(np.float32), env_multiplier)
+    sc.set_environment("IBL")
+    cam = S.look_at((0.5, 0.5, 2.35), (0.5, 0.5, 0.0), (0, 1, 0))
+    sc.set_camera(width, height, cam, fov_y_deg=38.0)
+    sc.build()
+    info = {"albedo_tex": alb_tex, "rough_tex": rough_tex, "env_tex": sc.tex_ref["env"], "env_shape": (h, w),
+            "albedo": albedo, "roughness": roughness, "env": rgba[..., :3].astype(np.float32)}
+    return sc, info
+
+
 def pixel_seeds(width: int, height: int) -> np.ndarray:
     """Per-pixel XORShift128 states, seed = pixel index + 1, expanded as the
     reference does (main.cpp:101-104): s = 1812433253*(s ^ (s >> 30)) + k."""

@@ -210,6 +210,57 @@ CLR_API int clr_render_wavefront(const clr_scene* scene, uint32_t width, uint32_
                                  float* pixels, uint32_t spp, uint32_t max_depth, uint32_t flags, void* workspace,
                                  uint64_t workspace_bytes, void* stream);
 
+/* ------------------------------------------------------------- adjoint */
+
+/* Parameters of clr_render_adjoint (all pointers are device pointers).
+ * A differentiated parameter is a constant texture of the textures blob
+ * (TEX_COLOR_CONSTANT: 3 channels, kind 0; TEX_FLOAT_CONSTANT: 1 channel,
+ * kind 1), named by its byte offset; every material component that reads it
+ * contributes.  The environment parameter is the image texture the scene's
+ * image-based environment light reads (its texels, as decoded colours). */
+typedef struct clr_adjoint_params {
+    const uint32_t* param_tex;   /* K textures-blob offsets */
+    const uint8_t* param_kind;   /* K kinds: 0 colour, 1 float */
+    uint32_t num_params;         /* K */
+    float* grad_params;          /* K x 4 floats, accumulated: xyz (colour) or x (float) */
+    uint32_t env_tex;            /* textures-blob offset of the environment texture, 0xFFFFFFFF = none */
+    float* grad_env;             /* texels x 4 floats (row-major), accumulated: xyz */
+    uint32_t* tape;              /* optional: tape_capacity records of CLR_TAPE_WORDS words */
+    uint32_t tape_capacity;
+    uint32_t* tape_count;        /* records written (may exceed the capacity: the rest were dropped) */
+} clr_adjoint_params;
+
+/* Tape records (32 uint32 words) of every replayed path, for checking the
+ * gradient against a re-evaluation of the same paths.  Words 0-3: pixel,
+ * sample, depth, kind (bits 0-7) | CLR_TAPE_VISIBLE.  Floats follow:
+ *   CAM    (0): 4-6 camera weight alpha0;
+ *   EMIT   (1): 4 MIS weight, 5-7 emitted radiance, 8 environment texel (or
+ *               0xFFFFFFFF), 9 environment multiplier;
+ *   RR     (2): 4 1 / continuation probability;
+ *   NEE    (3): 4 scalar weight, 5-7 light radiance, 8 texel, 9 multiplier,
+ *               10 material offset, 11-12 uv, 13-15 vout and 16-18 vin in
+ *               the shading frame, 19 component mask; counts if VISIBLE;
+ *   SAMPLE (4): 4 |cos| / pdf, 10-19 as NEE; word 19 = 0x80000000 | index
+ *               for a sampled specular component. */
+#define CLR_TAPE_WORDS 32u
+#define CLR_TAPE_VISIBLE 0x100u
+
+/* Path-replay backpropagation through the wavefront path tracer (an addition
+ * beside the reference, which has no derivatives).  Given dLoss/dAccum
+ * (float4 per pixel, xyz used) for the image that clr_render_wavefront would
+ * accumulate from the same rand_states, spp and max_depth, adds
+ * sum_pixels dLoss/dAccum . dAccum/dtheta to grad_params and grad_env, with
+ * sampling decisions, pdfs, MIS weights and roulette probabilities held
+ * constant.  rand_states advance exactly as in the forward render.  The
+ * workspace (256-byte aligned) holds at least
+ * clr_render_adjoint_workspace_bytes(width, height, num_params) bytes. */
+CLR_API int clr_render_adjoint_workspace_bytes(uint32_t width, uint32_t height, uint32_t num_params,
+                                               uint64_t* bytes);
+CLR_API int clr_render_adjoint(const clr_scene* scene, uint32_t width, uint32_t height, uint32_t* rand_states,
+                               const float* dloss_daccum, uint32_t spp, uint32_t max_depth, uint32_t flags,
+                               const clr_adjoint_params* params, void* workspace, uint64_t workspace_bytes,
+                               void* stream);
+
 /* ----------------------------------------------------------------- misc */
 
 /* Reads (and optionally clears) the device error bits CLR_DEVERR_* of the
