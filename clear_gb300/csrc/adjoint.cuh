@@ -77,6 +77,7 @@ static __device__ BxDeriv bx_f_deriv(const BxDF& b, float sigma, f3 vout, f3 vin
             const float k = expf(-(hx * hx + hy * hy) / (dotHN * dotHN)) /
                             (4 * kPi * b.a * b.b * dotHI * dotHI * dotHN * dotHN * dotHN * dotHN);
             d.dc0 = mk(k, k, k);
+            if (!(k > 0.0f) || !isfinite(k)) return d;  // underflow: the roughness terms vanish too
             const f3 f = b.c0 * k;
             const float n2 = dotHN * dotHN;
             d.da = f * (2.0f * hx * hx / (b.a * n2) - 1.0f / b.a);
@@ -95,6 +96,7 @@ static __device__ BxDeriv bx_f_deriv(const BxDF& b, float sigma, f3 vout, f3 vin
             const f3 fr = b.c0 + (mk(1, 1, 1) - b.c0) * w5;
             const f3 f = g * fr;
             d.dc0 = mk(g * (1.0f - w5), g * (1.0f - w5), g * (1.0f - w5));
+            if (!(g > 0.0f) || !isfinite(g)) return d;
             const float lnz = logf(fabsf(h.z));
             d.da = f * (0.5f / (b.a + 1) + lnz * h.x * h.x / s2);
             d.db = f * (0.5f / (b.b + 1) + lnz * h.y * h.y / s2);

@@ -98,31 +98,69 @@ __device__ __forceinline__ uint32_t ad_queue_slot(unsigned int* count, bool want
     return base + __popc(m & lt);
 }
 
-// Parameter-gradient sink of one block: shared memory when the table fits,
-// else the caller's buffer directly.
+// d / fs of one channel (0 where fs is 0 or the ratio overflows).
+__device__ __forceinline__ float dlog(float d, float fs) {
+    const float r = fs != 0.f ? d / fs : 0.f;
+    return isfinite(r) ? r : 0.f;
+}
+
+// Where a block sums its parameter gradients (the table's size picks it):
+//   kSinkPrivate : one private float per thread, parameter and channel in
+//                  shared memory (no atomics), summed per block at the end;
+//   kSinkShared  : per-block shared-memory atomics;
+//   kSinkGlobal  : global atomics straight into the caller's buffer.
+// The first two keep per-channel sums in the block's row of the per-block
+// buffer; k_ad_reduce folds float parameters' channels together.
+enum : int { kSinkNone = 0, kSinkPrivate = 1, kSinkShared = 2, kSinkGlobal = 3 };
+constexpr uint32_t kPrivStride = kAdThreads + 1;  // padded: the end-of-block sums read conflict-free
+constexpr uint32_t kPrivMaxParams = 31;           // 3 x 31 x 129 floats < 48 KB
+
+__host__ __device__ __forceinline__ int sink_mode(uint32_t k) {
+    return k == 0 ? kSinkNone : (k <= kPrivMaxParams ? kSinkPrivate : (k <= kSmemParams ? kSinkShared : kSinkGlobal));
+}
+__host__ __device__ __forceinline__ uint32_t sink_smem_bytes(uint32_t k) {
+    const int m = sink_mode(k);
+    return m == kSinkPrivate ? 3u * k * kPrivStride * 4u : (m == kSinkShared ? 4u * k * 4u : 0u);
+}
+
 struct GradSink {
-    float* s;  // 4 floats per parameter
+    int mode;
+    float* s;
     const uint8_t* kind;
     __device__ __forceinline__ void add(int slot, f3 w) const {
         if (slot < 0) return;
-        float* g = s + 4 * slot;
-        if (__ldg(kind + slot) == 1) {
-            atomicAdd(g, w.x + w.y + w.z);
-        } else {
+        if (mode == kSinkPrivate) {
+            float* a = s + (3u * slot) * kPrivStride + threadIdx.x;
+            a[0] += w.x;
+            a[kPrivStride] += w.y;
+            a[2 * kPrivStride] += w.z;
+        } else if (mode == kSinkShared) {
+            float* g = s + 4 * slot;
             atomicAdd(g, w.x);
             atomicAdd(g + 1, w.y);
             atomicAdd(g + 2, w.z);
+        } else {
+            float* g = s + 4 * slot;
+            if (__ldg(kind + slot) == 1) {
+                atomicAdd(g, w.x + w.y + w.z);
+            } else {
+                atomicAdd(g, w.x);
+                atomicAdd(g + 1, w.y);
+                atomicAdd(g + 2, w.z);
+            }
         }
     }
 };
 
 extern __shared__ float s_grad[];
 
-__device__ __forceinline__ GradSink sink_begin(const AdState& S, const AdParams& P) {
+__device__ __forceinline__ GradSink sink_begin(const AdParams& P) {
     GradSink g;
     g.kind = P.pt.kind;
-    if (S.partial) {
-        for (uint32_t i = threadIdx.x; i < 4u * P.pt.k; i += blockDim.x) s_grad[i] = 0.f;
+    g.mode = sink_mode(P.pt.k);
+    if (g.mode == kSinkPrivate || g.mode == kSinkShared) {
+        const uint32_t n = sink_smem_bytes(P.pt.k) / 4u;
+        for (uint32_t i = threadIdx.x; i < n; i += blockDim.x) s_grad[i] = 0.f;
         __syncthreads();
         g.s = s_grad;
     } else {
@@ -133,13 +171,22 @@ __device__ __forceinline__ GradSink sink_begin(const AdState& S, const AdParams&
 
 // Adds the block's sums to its row of the per-block buffer (the row's only
 // writer: kernels of one call run in stream order).
-__device__ __forceinline__ void sink_end(const AdState& S, const AdParams& P) {
-    if (!S.partial) return;
+__device__ __forceinline__ void sink_end(const AdState& S, const AdParams& P, const GradSink& g) {
+    if (g.mode != kSinkPrivate && g.mode != kSinkShared) return;
     __syncthreads();
     float* row = S.partial + (size_t)blockIdx.x * 4u * P.pt.k;
-    for (uint32_t i = threadIdx.x; i < 4u * P.pt.k; i += blockDim.x) {
-        const float v = s_grad[i];
-        if (v != 0.f) row[i] += v;
+    if (g.mode == kSinkShared) {
+        for (uint32_t i = threadIdx.x; i < 4u * P.pt.k; i += blockDim.x) {
+            const float v = s_grad[i];
+            if (v != 0.f) row[i] += v;
+        }
+        return;
+    }
+    for (uint32_t i = threadIdx.x; i < 3u * P.pt.k; i += blockDim.x) {
+        const float* a = s_grad + i * kPrivStride;
+        float v = 0.f;
+        for (uint32_t t = 0; t < kAdThreads; ++t) v += a[t];
+        if (v != 0.f) row[4u * (i / 3u) + i % 3u] += v;
     }
 }
 
@@ -282,7 +329,7 @@ __device__ __forceinline__ void grad_of_sum(const BSDF& f, const ParamTable& pt,
 __global__ void __launch_bounds__(kAdThreads) k_ad_shade(DScene sc, AdState S, AdParams P, int cur, uint32_t width,
                                                          uint32_t* __restrict__ rand_states, uint32_t spp,
                                                          uint32_t max_depth) {
-    const GradSink sink = sink_begin(S, P);
+    const GradSink sink = sink_begin(P);
     const uint32_t n = S.count[cur];
     const Camera cam = load_camera(sc);
     const uint32_t stride = gridDim.x * blockDim.x;
@@ -496,10 +543,8 @@ __global__ void __launch_bounds__(kAdThreads) k_ad_shade(DScene sc, AdState S, A
                                 flags = side_flags(bsdf, vout, dir);
                                 grad_of_sum(bsdf, P.pt, flags, vl, il, g);
                             }
-                            const f3 inv = mk(fs.x != 0.f ? 1.0f / fs.x : 0.f, fs.y != 0.f ? 1.0f / fs.y : 0.f,
-                                              fs.z != 0.f ? 1.0f / fs.z : 0.f);
                             for (int k = 0; k < g.n; ++k) {
-                                const f3 d = g.d[k] * inv;
+                                const f3 d = mk(dlog(g.d[k].x, fs.x), dlog(g.d[k].y, fs.y), dlog(g.d[k].z, fs.z));
                                 S.pd[(size_t)kMaxGrad * p + k] = make_float4(d.x, d.y, d.z, __int_as_float(g.slot[k]));
                             }
                             npend = g.n;
@@ -565,12 +610,12 @@ __global__ void __launch_bounds__(kAdThreads) k_ad_shade(DScene sc, AdState S, A
                 for (int k = 3; k < kShWords; ++k) dst[k] = e[k];
         }
     }
-    sink_end(S, P);
+    sink_end(S, P, sink);
 }
 
 template <bool kOrdered>
 __global__ void __launch_bounds__(kAdThreads) k_ad_shadow(DScene sc, AdState S, AdParams P) {
-    const GradSink sink = sink_begin(S, P);
+    const GradSink sink = sink_begin(P);
     const uint32_t n = S.count[2];
     uint2 stack[kStackSize];
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
@@ -613,7 +658,7 @@ __global__ void __launch_bounds__(kAdThreads) k_ad_shadow(DScene sc, AdState S, 
         const int tx = __float_as_int(t.w);
         if (tx >= 0) add_env_grad(P, tx, dL * mk(t.x, t.y, t.z));
     }
-    sink_end(S, P);
+    sink_end(S, P, sink);
 }
 
 __global__ void k_ad_reset(AdState S, int next) {
@@ -621,21 +666,38 @@ __global__ void k_ad_reset(AdState S, int next) {
     S.count[2] = 0;
 }
 
-// grad[i] += sum over blocks of partial[b][i]; one block per float of the table.
-__global__ void __launch_bounds__(256) k_ad_reduce(const float* __restrict__ partial, uint32_t nblocks,
-                                                   uint32_t nfloats, float* __restrict__ grad) {
-    const uint32_t i = blockIdx.x;
-    float acc = 0.f;
-    for (uint32_t b = threadIdx.x; b < nblocks; b += blockDim.x) acc += partial[(size_t)b * nfloats + i];
-    __shared__ float red[8];
+// grad[k] += sum over blocks of partial[b][k] (channels summed for a float
+// parameter); one block per parameter.
+__global__ void __launch_bounds__(256) k_ad_reduce(const float* __restrict__ partial, uint32_t nblocks, uint32_t k,
+                                                   const uint8_t* __restrict__ kind, float* __restrict__ grad) {
+    const uint32_t slot = blockIdx.x;
+    float acc[3] = {0.f, 0.f, 0.f};
+    for (uint32_t b = threadIdx.x; b < nblocks; b += blockDim.x) {
+        const float* r = partial + (size_t)b * 4u * k + 4u * slot;
+        acc[0] += r[0];
+        acc[1] += r[1];
+        acc[2] += r[2];
+    }
+    __shared__ float red[3][8];
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xFFFFFFFFu, acc, o);
-    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = acc;
+    for (int c = 0; c < 3; ++c) {
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) acc[c] += __shfl_xor_sync(0xFFFFFFFFu, acc[c], o);
+        if ((threadIdx.x & 31) == 0) red[c][threadIdx.x >> 5] = acc[c];
+    }
     __syncthreads();
     if (threadIdx.x == 0) {
-        float s = 0.f;
-        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) s += red[w];
-        if ((i & 3u) != 3u) grad[i] += s;
+        float s[3] = {0.f, 0.f, 0.f};
+        for (int c = 0; c < 3; ++c)
+            for (int w = 0; w < (int)(blockDim.x >> 5); ++w) s[c] += red[c][w];
+        float* g = grad + 4u * slot;
+        if (kind[slot] == 1) {
+            g[0] += s[0] + s[1] + s[2];
+        } else {
+            g[0] += s[0];
+            g[1] += s[1];
+            g[2] += s[2];
+        }
     }
 }
 
@@ -652,7 +714,8 @@ static size_t ad_layout(uint32_t npix, uint32_t num_params, char* base, AdState*
     const size_t o_org = take(16 * n), o_dir = take(16 * n), o_alpha = take(16 * n), o_misc = take(16 * n),
                  o_hit = take(16 * n), o_L = take(16 * n), o_rng0 = take(16 * n), o_pd = take(16 * kMaxGrad * n),
                  o_q0 = take(4 * n), o_q1 = take(4 * n), o_sh = take(16 * kShWords * n), o_cnt = take(16);
-    const bool use_partial = num_params > 0 && num_params <= kSmemParams;
+    const int mode = sink_mode(num_params);
+    const bool use_partial = mode == kSinkPrivate || mode == kSinkShared;
     const size_t o_part = use_partial ? take((size_t)ad_grid(npix) * num_params * 16) : 0;
     if (base && S) {
         S->org = reinterpret_cast<float4*>(base + o_org);
@@ -724,7 +787,7 @@ extern "C" int clr_render_adjoint(const clr_scene* scene, uint32_t width, uint32
     const bool ordered = (flags & CLR_RENDER_ORDERED) != 0;
     const unsigned int grid = ad_grid(npix);
     const uint32_t nfloats = 4u * A.num_params;
-    const size_t smem = S.partial ? (size_t)nfloats * sizeof(float) : 0;
+    const size_t smem = sink_smem_bytes(A.num_params);
     k_ad_init<<<grid, kAdThreads, 0, st>>>(sc, S, npix, width, rand_states, S.partial ? grid * nfloats : 0u);
     CLR_LAUNCH_CHECK("k_ad_init");
     // every iteration advances each unfinished path by one vertex; a sample
@@ -747,7 +810,7 @@ extern "C" int clr_render_adjoint(const clr_scene* scene, uint32_t width, uint32
         }
     }
     if (S.partial) {
-        k_ad_reduce<<<nfloats, 256, 0, st>>>(S.partial, grid, nfloats, A.grad_params);
+        k_ad_reduce<<<A.num_params, 256, 0, st>>>(S.partial, grid, A.num_params, A.param_kind, A.grad_params);
         CLR_LAUNCH_CHECK("k_ad_reduce");
     }
     return CLR_OK;
