@@ -77,6 +77,8 @@ def parse():
     ap.add_argument("--render", type=int, default=1, help="also time the path tracer (0 = skip)")
     ap.add_argument("--render-only", action="store_true", help="time only the path tracer (for profiling)")
     ap.add_argument("--adjoint-only", action="store_true", help="time only the adjoint renderer (for profiling)")
+    ap.add_argument("--adjoint-res", type=int, default=512)
+    ap.add_argument("--adjoint-spp", type=int, default=32)
     return ap.parse_args()
 
 
@@ -242,7 +244,7 @@ def bench_render_terrain(dev, spp=4) -> dict:
     return out
 
 
-def bench_adjoint(dev, spp=32) -> dict:
+def bench_adjoint(dev, spp=32, res=512) -> dict:
     """Differentiable render: the 8-material Cornell box with a 64 x 32
     environment, 512 x 512, `spp` samples per pixel, depth 5.  Times the
     forward wavefront render and the adjoint pass (path replay; gradients of
@@ -255,7 +257,7 @@ def bench_adjoint(dev, spp=32) -> dict:
     from clear_gb300 import scenes
     from clear_gb300.render import DeviceScene
 
-    w = h = 512
+    w = h = res
     sc, info = scenes.cornell_adjoint(w, h)
     ds = DeviceScene(sc, dev)
     r = np.random.default_rng(11)
@@ -295,7 +297,7 @@ def bench_adjoint(dev, spp=32) -> dict:
     torch.cuda.synchronize()
     fwd = ev[0].elapsed_time(ev[1]) / reps
     adj = ev[2].elapsed_time(ev[3]) / reps
-    return {"workload": "adjoint cornell 8 materials + 64x32 env, 512x512, 32 spp, depth 5",
+    return {"workload": f"adjoint cornell 8 materials + 64x32 env, {w}x{h}, {spp} spp, depth 5",
             "params": 16 * 3 + genv.shape[0] * 3, "forward_ms": fwd, "adjoint_ms": adj,
             "adjoint_over_forward": adj / fwd, "forward_msamples_s": w * h * spp / fwd / 1e3,
             "adjoint_msamples_s": w * h * spp / adj / 1e3,
@@ -516,7 +518,8 @@ def main():
         from clear_gb300.build import build
 
         build()
-        print(json.dumps({"adjoint": bench_adjoint(torch.device("cuda", 0))}), flush=True)
+        print(json.dumps({"adjoint": bench_adjoint(torch.device("cuda", 0), args.adjoint_spp, args.adjoint_res)}),
+              flush=True)
         return
     if args.impl == "reference":
         run_reference(args)

@@ -39,7 +39,7 @@ struct BxDeriv {
     f3 dc0, dc1, da, db;
 };
 
-static __device__ BxDeriv bx_f_deriv(const BxDF& b, float sigma, f3 vout, f3 vin) {
+static __device__ __noinline__ BxDeriv bx_f_deriv(const BxDF& b, float sigma, f3 vout, f3 vin) {
     const f3 zero = mk(0, 0, 0);
     BxDeriv d{zero, zero, zero, zero};
     switch (b.id) {

@@ -55,9 +55,9 @@ struct AdState {
     float4* L;       // xyz radiance of the sample (primal: summed so far; replay: still ahead)
     uint4* rng0;     // RNG state at the start of the current sample
     float4* pd;      // kMaxGrad per path: pending dlog(fs)/dtheta per channel, w = slot bits (-1 = none)
-    uint32_t* q[2];  // active path queues
+    uint32_t* q[4];  // path queues, [2 * parity + pass]
     float4* sh;      // kShWords float4s per shadow entry
-    unsigned int* count;  // [0],[1] active counts, [2] shadow count
+    unsigned int* count;  // [2 * parity + pass] queued paths, [4] shadow entries
     float* partial;  // per-block parameter gradients (grid x K x 4), or null
 };
 
@@ -253,9 +253,16 @@ __device__ __forceinline__ void tape_put(const Tape& t, const TapeRec& r) {
 }
 
 // ---------------------------------------------------------------- kernels
+//
+// Queues: q[buf][pass] holds the paths of one pass (0 primal, 1 replay) to
+// shade in iteration parity `buf`; count[2 * buf + pass] their number and
+// count[4] the shadow entries.  The two passes are shaded by separate kernels
+// so that neither carries the other's code or diverges on it.
+
+__device__ __forceinline__ uint32_t* queue(const AdState& S, int buf, int pass) { return S.q[2 * buf + pass]; }
 
 __device__ __forceinline__ void ad_start(const Camera& cam, const AdState& S, uint32_t p, uint32_t width, Rng& rng,
-                                         uint32_t done, uint32_t pass, const Tape& tape) {
+                                         uint32_t done, uint32_t pass) {
     f3 org, dir, alpha;
     float dirPDF;
     camera_ray(cam, p % width, p / width, rng, org, dir, alpha, dirPDF);
@@ -264,42 +271,37 @@ __device__ __forceinline__ void ad_start(const Camera& cam, const AdState& S, ui
     S.alpha[p] = make_float4(alpha.x, alpha.y, alpha.z, luminance(alpha));
     S.misc[p] = make_uint4(0u, 0u, done, pass);
     S.pd[(size_t)kMaxGrad * p] = make_float4(0.f, 0.f, 0.f, __int_as_float(-1));
-    if (pass == 1u && tape.rec) {
-        TapeRec r;
-        r.head(p, done, 0, kTapeCam);
-        r.f3at(4, alpha);
-        tape_put(tape, r);
-    }
 }
 
 __global__ void __launch_bounds__(kAdThreads) k_ad_init(DScene sc, AdState S, uint32_t npix, uint32_t width,
                                                         uint32_t* __restrict__ rand_states, uint32_t partial_floats) {
     const Camera cam = load_camera(sc);
-    const Tape none{nullptr, 0, nullptr};
     for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < npix; p += gridDim.x * blockDim.x) {
         const uint4 s = reinterpret_cast<const uint4*>(rand_states)[p];
         Rng rng = rng_from(s);
         S.rng0[p] = s;
-        ad_start(cam, S, p, width, rng, 0u, 0u, none);
+        ad_start(cam, S, p, width, rng, 0u, 0u);
         S.L[p] = make_float4(0.f, 0.f, 0.f, 0.f);
         reinterpret_cast<uint4*>(rand_states)[p] = rng_bits(rng);
-        S.q[0][p] = p;
+        queue(S, 0, 0)[p] = p;
     }
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < partial_floats; i += gridDim.x * blockDim.x)
         S.partial[i] = 0.f;
     if (blockIdx.x == 0 && threadIdx.x == 0) {
         S.count[0] = npix;
-        S.count[1] = 0;
-        S.count[2] = 0;
+        for (int k = 1; k < 5; ++k) S.count[k] = 0;
     }
 }
 
+// Closest hit of every queued path of both passes.
 template <bool kOrdered>
 __global__ void __launch_bounds__(kAdThreads) k_ad_extend(DScene sc, AdState S, int cur) {
-    const uint32_t n = S.count[cur];
+    const uint32_t n0 = S.count[2 * cur], n = n0 + S.count[2 * cur + 1];
+    const uint32_t* q0 = queue(S, cur, 0);
+    const uint32_t* q1 = queue(S, cur, 1);
     uint2 stack[kStackSize];
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        const uint32_t p = S.q[cur][i];
+        const uint32_t p = i < n0 ? q0[i] : q1[i - n0];
         const float4 o = S.org[p], d = S.dir[p];
         Hit h;
         if (intersect<kOrdered>(sc, mk(o.x, o.y, o.z), mk(d.x, d.y, d.z), h, stack))
@@ -314,128 +316,157 @@ __device__ __forceinline__ uint32_t side_flags(const BSDF& f, f3 vout, f3 vin) {
     return dot(vin, f.ng) * dot(vout, f.ng) > 0 ? (kTyAll & ~kTyTransmission) : (kTyAll & ~kTyReflection);
 }
 
-__device__ __forceinline__ void grad_of_sum(const BSDF& f, const ParamTable& pt, uint32_t flags, f3 vl, f3 il,
-                                            GradList& g) {
-#pragma unroll
-    for (int k = 0; k < kMaxBxDFs; ++k)
-        if (k < f.num && match_type(f.type[k], flags)) bx_grad(f, f.off[k], pt, vl, il, g);
+// Derivative of fs (the sum over the matching components) or, for a sampled
+// specular component `spec` (>= 0), of that component's value.  Kept out of
+// line: the replay kernel calls it from two places.
+static __device__ __noinline__ void bsdf_grad(const BSDF& f, const ParamTable& pt, uint32_t flags, int spec, f3 vl,
+                                              f3 il, GradList& g) {
+    g.clear();
+    if (spec >= 0) {
+        const uint32_t off = pick4(f.off, (uint32_t)spec);
+        g.add(param_slot(pt, bx_tex(f, off).c0), spec_dc0(load_bx(f, off), vl, il));
+        return;
+    }
+#pragma unroll 1
+    for (int k = 0; k < f.num; ++k)
+        if (match_type(f.type[k], flags)) bx_grad(f, f.off[k], pt, vl, il, g);
 }
 
-// One path vertex (pathtracer.cl:128-262 per bounce) in either pass.
 // Shadow entry: [0] origin, w light face (0xFFFFFFFF = environment);
 // [1] direction, w path; [2] contribution c, w flags (bit 0 add to L, bit 1
 // replay, bits 2.. tape record + 1); replay only: [3] dc/d(env texel), w
 // texel (-1 = none); [4 + k] dc/dtheta of parameter k, w slot (-1 = end).
-__global__ void __launch_bounds__(kAdThreads) k_ad_shade(DScene sc, AdState S, AdParams P, int cur, uint32_t width,
-                                                         uint32_t* __restrict__ rand_states, uint32_t spp,
-                                                         uint32_t max_depth) {
-    const GradSink sink = sink_begin(P);
-    const uint32_t n = S.count[cur];
+struct ShEntry {
+    float4 e[kShWords];
+};
+
+__device__ __forceinline__ void put_shadow3(const AdState& S, bool want, float4 e0, float4 e1, float4 e2) {
+    const uint32_t ss = ad_queue_slot(S.count + 4, want);
+    if (!want) return;
+    float4* dst = S.sh + (size_t)kShWords * ss;
+    dst[0] = e0;
+    dst[1] = e1;
+    dst[2] = e2;
+}
+
+__device__ __forceinline__ void put_shadow(const AdState& S, bool want, const ShEntry& e, bool replay) {
+    const uint32_t ss = ad_queue_slot(S.count + 4, want);
+    if (!want) return;
+    float4* dst = S.sh + (size_t)kShWords * ss;
+    dst[0] = e.e[0];
+    dst[1] = e.e[1];
+    dst[2] = e.e[2];
+    if (replay)
+#pragma unroll
+        for (int k = 3; k < kShWords; ++k) dst[k] = e.e[k];
+}
+
+// Emission seen at a path vertex and the MIS weight of the BSDF sample that
+// found it (pathtracer.cl:165-204).  Returns the emitted radiance and sets
+// `w` to the weight (1 for camera rays).
+__device__ __forceinline__ f3 vertex_emission(const DScene& sc, bool escaped, const SurfPt& sp, const Face& face,
+                                              f3 org, f3 dir, float dirPDF, uint32_t depth, uint32_t sampledType,
+                                              LightPt& lenv, float& w) {
+    w = 1.0f;
+    const f3 vout = -dir;
+    if (escaped) {
+        lenv.atInfinity = true;
+        lenv.uv = env_uv(dir);
+        EDF edf;
+        edf_alloc(sc, kNone16, lenv, edf);
+        if ((sampledType & kTyNonSingular) && depth > 0) {
+            const float lightPDF = area_pdf(sc, lenv) * 1.0f / edf_abs_cos(edf, vout);
+            w = (dirPDF * dirPDF) / (lightPDF * lightPDF + dirPDF * dirPDF);
+        }
+        return edf_le(edf, vout);
+    }
+    if (face.light == kNone16) return mk(0.f, 0.f, 0.f);
+    LightPt lpos;
+    light_from_surface(sp, lpos);
+    EDF edf;
+    edf_alloc(sc, face.light, lpos, edf);
+    if (depth > 0 && (sampledType & kTyNonSingular)) {
+        const float d2 = (org.x - sp.p.x) * (org.x - sp.p.x) + (org.y - sp.p.y) * (org.y - sp.p.y) +
+                         (org.z - sp.p.z) * (org.z - sp.p.z);
+        const float lightPDF = area_pdf(sc, lpos) * d2 / edf_abs_cos(edf, vout);
+        w = (dirPDF * dirPDF) / (lightPDF * lightPDF + dirPDF * dirPDF);
+    }
+    return edf_le(edf, vout);
+}
+
+// Next-event estimation at a surface point (pathtracer.cl:216-240): samples a
+// light, returns false when the BSDF has no non-specular component.  Sets the
+// shadow ray, the scalar weight s (MIS * |cos_l| * |cos| / dist^2 / pdf),
+// the light's radiance and the BSDF value toward it.
+struct Nee {
+    f3 org, dir, le, fs;
+    float s;
+    LightPt lpos;
+};
+
+__device__ __forceinline__ void next_event(const DScene& sc, const BSDF& bsdf, const SurfPt& sp, f3 vout, Rng& rng,
+                                           Nee& n) {
+    const float uL = rng.uniform(), u0 = rng.uniform(), u1 = rng.uniform();
+    EDF edf;
+    float lightPDF;
+    n.lpos.faceID = kNone32;
+    sample_light(sc, uL, u0, u1, n.lpos, edf, lightPDF);
+    f3 vinL = n.lpos.p - sp.p;
+    float dist2 = dot(vinL, vinL);
+    vinL = vinL * (1.0f / sqrtf(dist2));
+    if (n.lpos.atInfinity) {
+        vinL = n.lpos.p;
+        dist2 = 1.0f;
+    }
+    n.org = sp.p + vinL * kEpsilon;
+    n.dir = vinL;
+    const float fsPDF = bsdf_pdf(bsdf, vout, vinL) * edf_abs_cos(edf, vinL) / dist2;
+    const float MISWeight = (lightPDF * lightPDF) / (lightPDF * lightPDF + fsPDF * fsPDF);
+    n.s = MISWeight * edf_abs_cos(edf, vinL) * fabsf(dot(bsdf.n, vinL)) / dist2 / lightPDF;
+    n.le = edf_le(edf, -vinL);
+    n.fs = bsdf_f(bsdf, vout, vinL);
+}
+
+// Primal pass: the forward path tracer (render_wf.cu k_wf_shade) summing the
+// sample's radiance into L.  A finished sample is queued for its replay.
+__global__ void __launch_bounds__(kAdThreads) k_ad_primal(DScene sc, AdState S, int cur, uint32_t width,
+                                                          uint32_t* __restrict__ rand_states, uint32_t max_depth) {
+    const uint32_t n = S.count[2 * cur];
+    const uint32_t* qin = queue(S, cur, 0);
     const Camera cam = load_camera(sc);
-    const uint32_t stride = gridDim.x * blockDim.x;
     const uint32_t n_round = (n + 31u) & ~31u;
-    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n_round; i += stride) {
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n_round; i += gridDim.x * blockDim.x) {
         bool cont = false, shadow = false;
+        int next_pass = 0;
         uint32_t p = 0;
-        float4 e[kShWords];
+        float4 sh0, sh1, sh2;
         if (i < n) {
-            p = S.q[cur][i];
+            p = qin[i];
             Rng rng = rng_from(reinterpret_cast<const uint4*>(rand_states)[p]);
-            const float4 o4 = S.org[p], d4 = S.dir[p], a4 = S.alpha[p], h4 = S.hit[p];
+            const float4 o4 = S.org[p], d4 = S.dir[p], a4 = S.alpha[p], h4 = S.hit[p], L4 = S.L[p];
             const uint4 m = S.misc[p];
             f3 org = mk(o4.x, o4.y, o4.z), dir = mk(d4.x, d4.y, d4.z), alpha = mk(a4.x, a4.y, a4.z);
+            f3 L = mk(L4.x, L4.y, L4.z);
             float dirPDF = d4.w;
             const float initY = a4.w;
             uint32_t depth = m.x, sampledType = m.y;
-            const uint32_t done = m.z;
-            const bool replay = m.w == 1u;
-            const bool taping = replay && P.tape.rec != nullptr;
-            const float4 L4 = S.L[p];
-            f3 L = mk(L4.x, L4.y, L4.z);
-            f3 dL = mk(0.f, 0.f, 0.f);
-            if (replay) {
-                const float4 dl4 = __ldg(P.dloss + p);
-                dL = mk(dl4.x, dl4.y, dl4.z);
-                // the BSDF value sampled at the previous vertex scales all that is ahead
-                for (int k = 0; k < kMaxGrad; ++k) {
-                    const float4 dd = S.pd[(size_t)kMaxGrad * p + k];
-                    const int slot = __float_as_int(dd.w);
-                    if (slot < 0) break;
-                    sink.add(slot, dL * L * mk(dd.x, dd.y, dd.z));
-                }
-            }
-            int npend = 0;
             bool ended = false;
             const uint32_t hid = __float_as_uint(h4.x);
+            SurfPt sp;
+            Face face;
+            if (hid != kNone32) {
+                Hit h{hid, h4.y, h4.z, h4.w};
+                surface_point(sc, org, dir, h, sp);
+                face = load_face(sc, sp.faceID);
+            }
+            LightPt lenv;
+            float w;
+            const f3 le = vertex_emission(sc, hid == kNone32, sp, face, org, dir, dirPDF, depth, sampledType, lenv, w);
+            L += w * alpha * le;
             if (hid == kNone32) {
-                // escaped: environment emission (pathtracer.cl:183-196)
-                LightPt lpos;
-                lpos.atInfinity = true;
-                lpos.uv = env_uv(dir);
-                const f3 vout = -dir;
-                EDF edf;
-                edf_alloc(sc, kNone16, lpos, edf);
-                float MISWeight = 1.0f;
-                if ((sampledType & kTyNonSingular) && depth > 0) {
-                    const float lightPDF = area_pdf(sc, lpos) * 1.0f / edf_abs_cos(edf, vout);
-                    MISWeight = (dirPDF * dirPDF) / (lightPDF * lightPDF + dirPDF * dirPDF);
-                }
-                const f3 le = edf_le(edf, vout);
-                const f3 T = MISWeight * alpha * le;
-                if (replay) {
-                    L = mk(L.x - T.x, L.y - T.y, L.z - T.z);
-                    float mult;
-                    const int tx = env_texel(sc, P, lpos.uv, mult);
-                    if (tx >= 0) add_env_grad(P, tx, dL * (MISWeight * alpha) * mult);
-                    if (taping) {
-                        TapeRec r;
-                        r.head(p, done, depth, kTapeEmit);
-                        r.f(4, MISWeight);
-                        r.f3at(5, le);
-                        r.w[8] = (uint32_t)tx;
-                        r.f(9, mult);
-                        tape_put(P.tape, r);
-                    }
-                } else {
-                    L += T;
-                }
                 ended = true;
             } else {
-                Hit h{hid, h4.y, h4.z, h4.w};
-                SurfPt sp;
-                surface_point(sc, org, dir, h, sp);
-                const Face face = load_face(sc, sp.faceID);
                 const f3 vout = -dir;
-                LightPt lpos;
-                lpos.faceID = kNone32;
-                if (face.light != kNone16) {
-                    light_from_surface(sp, lpos);
-                    EDF edf;
-                    edf_alloc(sc, face.light, lpos, edf);
-                    float MISWeight = 1.0f;
-                    if (depth > 0 && (sampledType & kTyNonSingular)) {
-                        const float d2 = (org.x - sp.p.x) * (org.x - sp.p.x) + (org.y - sp.p.y) * (org.y - sp.p.y) +
-                                         (org.z - sp.p.z) * (org.z - sp.p.z);
-                        const float lightPDF = area_pdf(sc, lpos) * d2 / edf_abs_cos(edf, vout);
-                        MISWeight = (dirPDF * dirPDF) / (lightPDF * lightPDF + dirPDF * dirPDF);
-                    }
-                    const f3 le = edf_le(edf, vout);
-                    const f3 T = depth > 0 ? MISWeight * alpha * le : alpha * le;
-                    if (replay) {
-                        L = mk(L.x - T.x, L.y - T.y, L.z - T.z);
-                        if (taping) {
-                            TapeRec r;
-                            r.head(p, done, depth, kTapeEmit);
-                            r.f(4, depth > 0 ? MISWeight : 1.0f);
-                            r.f3at(5, le);
-                            r.w[8] = kNone32;
-                            tape_put(P.tape, r);
-                        }
-                    } else {
-                        L += T;
-                    }
-                }
-                // Russian roulette (pathtracer.cl:206-214)
                 if (depth > 0) {
                     if (depth >= max_depth) ended = true;
                     else {
@@ -443,7 +474,147 @@ __global__ void __launch_bounds__(kAdThreads) k_ad_shade(DScene sc, AdState S, A
                         if (rng.uniform() < continueProb) {
                             alpha *= 1.0f / continueProb;
                             dirPDF *= continueProb;
-                            if (taping) {
+                        } else {
+                            ended = true;
+                        }
+                    }
+                }
+                if (!ended) {
+                    BSDF bsdf;
+                    bsdf_alloc(sc, face.mat, sp, bsdf);
+                    if (bsdf_has_non_specular(bsdf)) {
+                        Nee ne;
+                        next_event(sc, bsdf, sp, vout, rng, ne);
+                        const f3 c = ne.s * (alpha * ne.le * ne.fs);
+                        sh0 = make_float4(ne.org.x, ne.org.y, ne.org.z,
+                                              __uint_as_float(ne.lpos.atInfinity ? kNone32 : ne.lpos.faceID));
+                        sh1 = make_float4(ne.dir.x, ne.dir.y, ne.dir.z, __uint_as_float(p));
+                        sh2 = make_float4(c.x, c.y, c.z, __uint_as_float(1u));  // add to L
+                        shadow = true;
+                    }
+                    const float uc = rng.uniform(), v0 = rng.uniform(), v1 = rng.uniform();
+                    const f3 fs = bsdf_sample(bsdf, vout, uc, v0, v1, dir, dirPDF, sampledType);
+                    if (zero_vec(fs) || dirPDF == 0.0f) {
+                        ended = true;
+                    } else {
+                        alpha *= fs * (fabsf(dot(bsdf.n, dir)) / dirPDF);
+                        org = sp.p + dir * kEpsilon;
+                        ++depth;
+                    }
+                }
+            }
+            if (ended) {
+                // replay the sample from its first random number
+                rng = rng_from(S.rng0[p]);
+                ad_start(cam, S, p, width, rng, m.z, 1u);
+                next_pass = 1;
+            } else {
+                S.org[p] = make_float4(org.x, org.y, org.z, 0.f);
+                S.dir[p] = make_float4(dir.x, dir.y, dir.z, dirPDF);
+                S.alpha[p] = make_float4(alpha.x, alpha.y, alpha.z, initY);
+                S.misc[p] = make_uint4(depth, sampledType, m.z, 0u);
+            }
+            cont = true;
+            S.L[p] = make_float4(L.x, L.y, L.z, 0.f);
+            reinterpret_cast<uint4*>(rand_states)[p] = rng_bits(rng);
+        }
+        const uint32_t s0 = ad_queue_slot(S.count + 2 * (cur ^ 1), cont && next_pass == 0);
+        const uint32_t s1 = ad_queue_slot(S.count + 2 * (cur ^ 1) + 1, cont && next_pass == 1);
+        if (cont) queue(S, cur ^ 1, next_pass)[next_pass ? s1 : s0] = p;
+        put_shadow3(S, shadow, sh0, sh1, sh2);
+    }
+}
+
+// Replay pass: the same vertex, subtracting each term from L and adding the
+// derivatives.  A finished replay starts the pixel's next sample (primal).
+template <bool kTape>
+__global__ void __launch_bounds__(kAdThreads) k_ad_replay(DScene sc, AdState S, AdParams P, int cur, uint32_t width,
+                                                          uint32_t* __restrict__ rand_states, uint32_t spp,
+                                                          uint32_t max_depth) {
+    const uint32_t n = S.count[2 * cur + 1];
+    const uint32_t n_round = (n + 31u) & ~31u;
+    if (blockIdx.x * blockDim.x >= n_round) return;  // whole block idle: skip the gradient sink
+    const GradSink sink = sink_begin(P);
+    const uint32_t* qin = queue(S, cur, 1);
+    const Camera cam = load_camera(sc);
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n_round; i += gridDim.x * blockDim.x) {
+        bool cont = false, shadow = false;
+        int next_pass = 1;
+        uint32_t p = 0;
+        ShEntry se;
+        if (i < n) {
+            p = qin[i];
+            Rng rng = rng_from(reinterpret_cast<const uint4*>(rand_states)[p]);
+            const float4 o4 = S.org[p], d4 = S.dir[p], a4 = S.alpha[p], h4 = S.hit[p], L4 = S.L[p];
+            const float4 dl4 = __ldg(P.dloss + p);
+            const uint4 m = S.misc[p];
+            f3 org = mk(o4.x, o4.y, o4.z), dir = mk(d4.x, d4.y, d4.z), alpha = mk(a4.x, a4.y, a4.z);
+            f3 L = mk(L4.x, L4.y, L4.z);
+            const f3 dL = mk(dl4.x, dl4.y, dl4.z);
+            float dirPDF = d4.w;
+            const float initY = a4.w;
+            uint32_t depth = m.x, sampledType = m.y;
+            const uint32_t done = m.z;
+            if (kTape && depth == 0) {
+                TapeRec r;
+                r.head(p, done, 0, kTapeCam);
+                r.f3at(4, alpha);
+                tape_put(P.tape, r);
+            }
+            // the BSDF value sampled at the previous vertex scales all that is ahead
+            for (int k = 0; k < kMaxGrad; ++k) {
+                const float4 dd = S.pd[(size_t)kMaxGrad * p + k];
+                const int slot = __float_as_int(dd.w);
+                if (slot < 0) break;
+                sink.add(slot, dL * L * mk(dd.x, dd.y, dd.z));
+            }
+            int npend = 0;
+            bool ended = false;
+            const uint32_t hid = __float_as_uint(h4.x);
+            SurfPt sp;
+            Face face;
+            if (hid != kNone32) {
+                Hit h{hid, h4.y, h4.z, h4.w};
+                surface_point(sc, org, dir, h, sp);
+                face = load_face(sc, sp.faceID);
+            }
+            LightPt lenv;
+            float w;
+            const f3 le = vertex_emission(sc, hid == kNone32, sp, face, org, dir, dirPDF, depth, sampledType, lenv, w);
+            const f3 T = w * alpha * le;
+            L = mk(L.x - T.x, L.y - T.y, L.z - T.z);
+            if (hid == kNone32) {
+                float mult;
+                const int tx = env_texel(sc, P, lenv.uv, mult);
+                if (tx >= 0) add_env_grad(P, tx, dL * (w * alpha) * mult);
+                if (kTape) {
+                    TapeRec r;
+                    r.head(p, done, depth, kTapeEmit);
+                    r.f(4, w);
+                    r.f3at(5, le);
+                    r.w[8] = (uint32_t)tx;
+                    r.f(9, mult);
+                    tape_put(P.tape, r);
+                }
+                ended = true;
+            } else {
+                if (kTape && face.light != kNone16) {
+                    TapeRec r;
+                    r.head(p, done, depth, kTapeEmit);
+                    r.f(4, w);
+                    r.f3at(5, le);
+                    r.w[8] = kNone32;
+                    tape_put(P.tape, r);
+                }
+                const f3 vout = -dir;
+                if (depth > 0) {
+                    if (depth >= max_depth) ended = true;
+                    else {
+                        const float continueProb = fminf(luminance(alpha) * (1.0f / initY), 1.0f);
+                        if (rng.uniform() < continueProb) {
+                            alpha *= 1.0f / continueProb;
+                            dirPDF *= continueProb;
+                            if (kTape) {
                                 TapeRec r;
                                 r.head(p, done, depth, kTapeRR);
                                 r.f(4, 1.0f / continueProb);
@@ -458,108 +629,85 @@ __global__ void __launch_bounds__(kAdThreads) k_ad_shade(DScene sc, AdState S, A
                     BSDF bsdf;
                     bsdf_alloc(sc, face.mat, sp, bsdf);
                     if (bsdf_has_non_specular(bsdf)) {
-                        // next-event estimation (pathtracer.cl:216-240)
-                        const float uL = rng.uniform(), u0 = rng.uniform(), u1 = rng.uniform();
-                        EDF edf;
-                        float lightPDF;
-                        sample_light(sc, uL, u0, u1, lpos, edf, lightPDF);
-                        f3 vinL = lpos.p - sp.p;
-                        float dist2 = dot(vinL, vinL);
-                        vinL = vinL * (1.0f / sqrtf(dist2));
-                        if (lpos.atInfinity) {
-                            vinL = lpos.p;
-                            dist2 = 1.0f;
-                        }
-                        const f3 sorg = sp.p + vinL * kEpsilon;
-                        const f3 vinLrev = -vinL;
-                        const float fsPDF = bsdf_pdf(bsdf, vout, vinL) * edf_abs_cos(edf, vinL) / dist2;
-                        const float MISWeight = (lightPDF * lightPDF) / (lightPDF * lightPDF + fsPDF * fsPDF);
-                        const float s = MISWeight * edf_abs_cos(edf, vinL) * fabsf(dot(bsdf.n, vinL)) / dist2 / lightPDF;
-                        const f3 le = edf_le(edf, vinLrev);
-                        const f3 fsn = bsdf_f(bsdf, vout, vinL);
-                        const f3 c = s * (alpha * le * fsn);
-                        e[0] = make_float4(sorg.x, sorg.y, sorg.z, __uint_as_float(lpos.atInfinity ? kNone32 : lpos.faceID));
-                        e[1] = make_float4(vinL.x, vinL.y, vinL.z, __uint_as_float(p));
-                        e[2] = make_float4(c.x, c.y, c.z, 0.f);
-                        if (replay) {
-                            const uint32_t flags = side_flags(bsdf, vout, vinL);
-                            const f3 vl = world_to_local(bsdf.s, bsdf.t, bsdf.n, vout);
-                            const f3 il = world_to_local(bsdf.s, bsdf.t, bsdf.n, vinL);
-                            GradList g;
-                            g.clear();
-                            grad_of_sum(bsdf, P.pt, flags, vl, il, g);
-                            const f3 pre = s * (alpha * le);
+                        Nee ne;
+                        next_event(sc, bsdf, sp, vout, rng, ne);
+                        const f3 c = ne.s * (alpha * ne.le * ne.fs);
+                        const uint32_t flags = side_flags(bsdf, vout, ne.dir);
+                        const f3 vl = world_to_local(bsdf.s, bsdf.t, bsdf.n, vout);
+                        const f3 il = world_to_local(bsdf.s, bsdf.t, bsdf.n, ne.dir);
+                        GradList g;
+                        bsdf_grad(bsdf, P.pt, flags, -1, vl, il, g);
+                        const f3 pre = ne.s * (alpha * ne.le);
 #pragma unroll
-                            for (int k = 0; k < kMaxGrad; ++k) {
-                                const f3 d = k < g.n ? pre * g.d[k] : mk(0.f, 0.f, 0.f);
-                                e[4 + k] = make_float4(d.x, d.y, d.z, __int_as_float(k < g.n ? g.slot[k] : -1));
-                            }
-                            float mult = 0.f;
-                            const int tx = lpos.atInfinity ? env_texel(sc, P, lpos.uv, mult) : -1;
-                            const f3 dt = s * (alpha * fsn) * mult;
-                            e[3] = make_float4(dt.x, dt.y, dt.z, __int_as_float(tx));
-                            if (taping) {
-                                const uint32_t ti = tape_alloc(P.tape);
-                                if (ti != kNone32) {
-                                    TapeRec r;
-                                    r.head(p, done, depth, kTapeNee);
-                                    r.f(4, s);
-                                    r.f3at(5, le);
-                                    r.w[8] = (uint32_t)tx;
-                                    r.f(9, mult);
-                                    r.w[10] = face.mat;
-                                    r.f(11, sp.uv.x);
-                                    r.f(12, sp.uv.y);
-                                    r.f3at(13, vl);
-                                    r.f3at(16, il);
-                                    r.w[19] = flags;
-                                    r.store(P.tape, ti);
-                                    e[2].w = __uint_as_float((ti + 1u) << 2);
-                                }
-                            }
+                        for (int k = 0; k < kMaxGrad; ++k) {
+                            const f3 d = k < g.n ? pre * g.d[k] : mk(0.f, 0.f, 0.f);
+                            se.e[4 + k] = make_float4(d.x, d.y, d.z, __int_as_float(k < g.n ? g.slot[k] : -1));
                         }
-                        shadow = true;
-                    }
-                    // BSDF sampling (pathtracer.cl:242-257)
-                    const float uc = rng.uniform(), v0 = rng.uniform(), v1 = rng.uniform();
-                    const f3 fs = bsdf_sample(bsdf, vout, uc, v0, v1, dir, dirPDF, sampledType);
-                    if (zero_vec(fs) || dirPDF == 0.0f) {
-                        ended = true;
-                    } else {
-                        if (replay) {
-                            // dlog of the sampled value: the summed components for a
-                            // non-specular sample, the chosen component for a specular one
-                            const f3 vl = world_to_local(bsdf.s, bsdf.t, bsdf.n, vout);
-                            const f3 il = world_to_local(bsdf.s, bsdf.t, bsdf.n, dir);
-                            GradList g;
-                            g.clear();
-                            uint32_t flags;
-                            if (sampledType & kTySpecular) {
-                                const uint32_t which = rand_uint(uc, (uint32_t)bsdf.num);
-                                const uint32_t off = pick4(bsdf.off, which);
-                                g.add(param_slot(P.pt, bx_tex(bsdf, off).c0), spec_dc0(load_bx(bsdf, off), vl, il));
-                                flags = kTapeSpecular | which;
-                            } else {
-                                flags = side_flags(bsdf, vout, dir);
-                                grad_of_sum(bsdf, P.pt, flags, vl, il, g);
-                            }
-                            for (int k = 0; k < g.n; ++k) {
-                                const f3 d = mk(dlog(g.d[k].x, fs.x), dlog(g.d[k].y, fs.y), dlog(g.d[k].z, fs.z));
-                                S.pd[(size_t)kMaxGrad * p + k] = make_float4(d.x, d.y, d.z, __int_as_float(g.slot[k]));
-                            }
-                            npend = g.n;
-                            if (taping) {
+                        float mult = 0.f;
+                        const int tx = ne.lpos.atInfinity ? env_texel(sc, P, ne.lpos.uv, mult) : -1;
+                        const f3 dt = ne.s * (alpha * ne.fs) * mult;
+                        se.e[3] = make_float4(dt.x, dt.y, dt.z, __int_as_float(tx));
+                        uint32_t tflag = 0;
+                        if (kTape) {
+                            const uint32_t ti = tape_alloc(P.tape);
+                            if (ti != kNone32) {
                                 TapeRec r;
-                                r.head(p, done, depth, kTapeSample);
-                                r.f(4, fabsf(dot(bsdf.n, dir)) / dirPDF);
+                                r.head(p, done, depth, kTapeNee);
+                                r.f(4, ne.s);
+                                r.f3at(5, ne.le);
+                                r.w[8] = (uint32_t)tx;
+                                r.f(9, mult);
                                 r.w[10] = face.mat;
                                 r.f(11, sp.uv.x);
                                 r.f(12, sp.uv.y);
                                 r.f3at(13, vl);
                                 r.f3at(16, il);
                                 r.w[19] = flags;
-                                tape_put(P.tape, r);
+                                r.store(P.tape, ti);
+                                tflag = (ti + 1u) << 2;
                             }
+                        }
+                        se.e[0] = make_float4(ne.org.x, ne.org.y, ne.org.z,
+                                              __uint_as_float(ne.lpos.atInfinity ? kNone32 : ne.lpos.faceID));
+                        se.e[1] = make_float4(ne.dir.x, ne.dir.y, ne.dir.z, __uint_as_float(p));
+                        se.e[2] = make_float4(c.x, c.y, c.z, __uint_as_float(tflag | 2u));  // bit 0 set below
+                        shadow = true;
+                    }
+                    const float uc = rng.uniform(), v0 = rng.uniform(), v1 = rng.uniform();
+                    const f3 fs = bsdf_sample(bsdf, vout, uc, v0, v1, dir, dirPDF, sampledType);
+                    if (zero_vec(fs) || dirPDF == 0.0f) {
+                        ended = true;
+                    } else {
+                        // dlog of the sampled value: the summed components for a
+                        // non-specular sample, the chosen component for a specular one
+                        const f3 vl = world_to_local(bsdf.s, bsdf.t, bsdf.n, vout);
+                        const f3 il = world_to_local(bsdf.s, bsdf.t, bsdf.n, dir);
+                        GradList g;
+                        uint32_t flags;
+                        int spec = -1;
+                        if (sampledType & kTySpecular) {
+                            spec = (int)rand_uint(uc, (uint32_t)bsdf.num);
+                            flags = kTapeSpecular | (uint32_t)spec;
+                        } else {
+                            flags = side_flags(bsdf, vout, dir);
+                        }
+                        bsdf_grad(bsdf, P.pt, flags, spec, vl, il, g);
+                        for (int k = 0; k < g.n; ++k) {
+                            const f3 d = mk(dlog(g.d[k].x, fs.x), dlog(g.d[k].y, fs.y), dlog(g.d[k].z, fs.z));
+                            S.pd[(size_t)kMaxGrad * p + k] = make_float4(d.x, d.y, d.z, __int_as_float(g.slot[k]));
+                        }
+                        npend = g.n;
+                        if (kTape) {
+                            TapeRec r;
+                            r.head(p, done, depth, kTapeSample);
+                            r.f(4, fabsf(dot(bsdf.n, dir)) / dirPDF);
+                            r.w[10] = face.mat;
+                            r.f(11, sp.uv.x);
+                            r.f(12, sp.uv.y);
+                            r.f3at(13, vl);
+                            r.f3at(16, il);
+                            r.w[19] = flags;
+                            tape_put(P.tape, r);
                         }
                         alpha *= fs * (fabsf(dot(bsdf.n, dir)) / dirPDF);
                         org = sp.p + dir * kEpsilon;
@@ -567,56 +715,43 @@ __global__ void __launch_bounds__(kAdThreads) k_ad_shade(DScene sc, AdState S, A
                     }
                 }
             }
-            bool apply_L = true;
             if (ended) {
-                if (!replay) {
-                    // primal pass over: replay the sample from its first random number
-                    rng = rng_from(S.rng0[p]);
-                    ad_start(cam, S, p, width, rng, done, 1u, P.tape);
+                // L of this sample is no longer needed: its last next-event term stays out of L
+                if (done + 1 < spp) {
+                    S.rng0[p] = rng_bits(rng);
+                    ad_start(cam, S, p, width, rng, done + 1, 0u);
+                    L = mk(0.f, 0.f, 0.f);
+                    next_pass = 0;
                     cont = true;
                 } else {
-                    apply_L = false;  // L of this sample is no longer needed
-                    if (done + 1 < spp) {
-                        S.rng0[p] = rng_bits(rng);
-                        ad_start(cam, S, p, width, rng, done + 1, 0u, P.tape);
-                        L = mk(0.f, 0.f, 0.f);
-                        cont = true;
-                    } else {
-                        S.misc[p] = make_uint4(depth, sampledType, done + 1, 0u);
-                    }
+                    S.misc[p] = make_uint4(depth, sampledType, done + 1, 1u);
                 }
             } else {
+                se.e[2].w = __uint_as_float(__float_as_uint(se.e[2].w) | 1u);
                 S.org[p] = make_float4(org.x, org.y, org.z, 0.f);
                 S.dir[p] = make_float4(dir.x, dir.y, dir.z, dirPDF);
                 S.alpha[p] = make_float4(alpha.x, alpha.y, alpha.z, initY);
-                S.misc[p] = make_uint4(depth, sampledType, done, m.w);
+                S.misc[p] = make_uint4(depth, sampledType, done, 1u);
                 if (npend < kMaxGrad)
                     S.pd[(size_t)kMaxGrad * p + npend] = make_float4(0.f, 0.f, 0.f, __int_as_float(-1));
                 cont = true;
             }
             S.L[p] = make_float4(L.x, L.y, L.z, 0.f);
             reinterpret_cast<uint4*>(rand_states)[p] = rng_bits(rng);
-            if (shadow) e[2].w = __uint_as_float(__float_as_uint(e[2].w) | (apply_L ? 1u : 0u) | (replay ? 2u : 0u));
         }
-        const uint32_t qs = ad_queue_slot(S.count + (cur ^ 1), cont);
-        if (cont) S.q[cur ^ 1][qs] = p;
-        const uint32_t ss = ad_queue_slot(S.count + 2, shadow);
-        if (shadow) {
-            float4* dst = S.sh + (size_t)kShWords * ss;
-            dst[0] = e[0];
-            dst[1] = e[1];
-            dst[2] = e[2];
-            if (__float_as_uint(e[2].w) & 2u)
-                for (int k = 3; k < kShWords; ++k) dst[k] = e[k];
-        }
+        const uint32_t s0 = ad_queue_slot(S.count + 2 * (cur ^ 1), cont && next_pass == 0);
+        const uint32_t s1 = ad_queue_slot(S.count + 2 * (cur ^ 1) + 1, cont && next_pass == 1);
+        if (cont) queue(S, cur ^ 1, next_pass)[next_pass ? s1 : s0] = p;
+        put_shadow(S, shadow, se, true);
     }
     sink_end(S, P, sink);
 }
 
 template <bool kOrdered>
 __global__ void __launch_bounds__(kAdThreads) k_ad_shadow(DScene sc, AdState S, AdParams P) {
+    const uint32_t n = S.count[4];
+    if (blockIdx.x * blockDim.x >= n) return;
     const GradSink sink = sink_begin(P);
-    const uint32_t n = S.count[2];
     uint2 stack[kStackSize];
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         const float4* e = S.sh + (size_t)kShWords * i;
@@ -662,8 +797,9 @@ __global__ void __launch_bounds__(kAdThreads) k_ad_shadow(DScene sc, AdState S, 
 }
 
 __global__ void k_ad_reset(AdState S, int next) {
-    S.count[next] = 0;
-    S.count[2] = 0;
+    S.count[2 * next] = 0;
+    S.count[2 * next + 1] = 0;
+    S.count[4] = 0;
 }
 
 // grad[k] += sum over blocks of partial[b][k] (channels summed for a float
@@ -713,7 +849,7 @@ static size_t ad_layout(uint32_t npix, uint32_t num_params, char* base, AdState*
     const size_t n = npix;
     const size_t o_org = take(16 * n), o_dir = take(16 * n), o_alpha = take(16 * n), o_misc = take(16 * n),
                  o_hit = take(16 * n), o_L = take(16 * n), o_rng0 = take(16 * n), o_pd = take(16 * kMaxGrad * n),
-                 o_q0 = take(4 * n), o_q1 = take(4 * n), o_sh = take(16 * kShWords * n), o_cnt = take(16);
+                 o_q = take(16 * n), o_sh = take(16 * kShWords * n), o_cnt = take(32);
     const int mode = sink_mode(num_params);
     const bool use_partial = mode == kSinkPrivate || mode == kSinkShared;
     const size_t o_part = use_partial ? take((size_t)ad_grid(npix) * num_params * 16) : 0;
@@ -726,8 +862,7 @@ static size_t ad_layout(uint32_t npix, uint32_t num_params, char* base, AdState*
         S->L = reinterpret_cast<float4*>(base + o_L);
         S->rng0 = reinterpret_cast<uint4*>(base + o_rng0);
         S->pd = reinterpret_cast<float4*>(base + o_pd);
-        S->q[0] = reinterpret_cast<uint32_t*>(base + o_q0);
-        S->q[1] = reinterpret_cast<uint32_t*>(base + o_q1);
+        for (int k = 0; k < 4; ++k) S->q[k] = reinterpret_cast<uint32_t*>(base + o_q) + (size_t)k * n;
         S->sh = reinterpret_cast<float4*>(base + o_sh);
         S->count = reinterpret_cast<unsigned int*>(base + o_cnt);
         S->partial = use_partial ? reinterpret_cast<float*>(base + o_part) : nullptr;
@@ -793,20 +928,23 @@ extern "C" int clr_render_adjoint(const clr_scene* scene, uint32_t width, uint32
     // every iteration advances each unfinished path by one vertex; a sample
     // takes at most (max_depth + 1) vertices per pass
     const uint64_t max_iters = 2ull * spp * (max_depth + 1) + 2;
+    const bool tape = A.tape != nullptr;
     for (uint64_t it = 0; it < max_iters; ++it) {
         const int cur = (int)(it & 1);
         if (ordered) k_ad_extend<true><<<grid, kAdThreads, 0, st>>>(sc, S, cur);
         else k_ad_extend<false><<<grid, kAdThreads, 0, st>>>(sc, S, cur);
         k_ad_reset<<<1, 1, 0, st>>>(S, cur ^ 1);
-        k_ad_shade<<<grid, kAdThreads, smem, st>>>(sc, S, P, cur, width, rand_states, spp, max_depth);
+        k_ad_primal<<<grid, kAdThreads, 0, st>>>(sc, S, cur, width, rand_states, max_depth);
+        if (tape) k_ad_replay<true><<<grid, kAdThreads, smem, st>>>(sc, S, P, cur, width, rand_states, spp, max_depth);
+        else k_ad_replay<false><<<grid, kAdThreads, smem, st>>>(sc, S, P, cur, width, rand_states, spp, max_depth);
         if (ordered) k_ad_shadow<true><<<grid, kAdThreads, smem, st>>>(sc, S, P);
         else k_ad_shadow<false><<<grid, kAdThreads, smem, st>>>(sc, S, P);
         CLR_LAUNCH_CHECK("adjoint iteration");
         if ((it & 7) == 7) {
-            unsigned int left = 0;
-            CLR_CUDA_TRY(cudaMemcpyAsync(&left, S.count + (cur ^ 1), sizeof(left), cudaMemcpyDeviceToHost, st));
+            unsigned int left[2] = {0, 0};
+            CLR_CUDA_TRY(cudaMemcpyAsync(left, S.count + 2 * (cur ^ 1), sizeof(left), cudaMemcpyDeviceToHost, st));
             CLR_CUDA_TRY(cudaStreamSynchronize(st));
-            if (left == 0) break;
+            if (left[0] + left[1] == 0) break;
         }
     }
     if (S.partial) {

@@ -205,7 +205,7 @@ __device__ __forceinline__ void image_xy(const uint8_t* t, float2 uv, uint32_t& 
     data = t + ldb<int32_t>(t + 12);
 }
 
-static __device__ f3 eval_color_texture(const uint8_t* t, float2 uv) {
+static __device__ __noinline__ f3 eval_color_texture(const uint8_t* t, float2 uv) {
     switch (t[0]) {
         case kTexColorConst:
             return ldf3(t + 16);
@@ -265,7 +265,7 @@ static __device__ f3 eval_color_texture(const uint8_t* t, float2 uv) {
     }
 }
 
-static __device__ float eval_float_texture(const uint8_t* t, float2 uv) {
+static __device__ __noinline__ float eval_float_texture(const uint8_t* t, float2 uv) {
     switch (t[0]) {
         case kTexFloatConst:
             return ldb<float>(t + 4);
@@ -369,7 +369,7 @@ __device__ __forceinline__ int elem_size(uint8_t id) {
 // Component i of the BSDF with its textures evaluated (the BxDF part of
 // BSDFAlloc, reflection.cl:230-341).  Unknown element ids decode as black
 // diffuse.
-static __device__ BxDF load_bx(const BSDF& f, uint32_t off) {
+static __device__ __noinline__ BxDF load_bx(const BSDF& f, uint32_t off) {
     BxDF b;
     if (off == 0xFFFF) {  // empty material: black diffuse
         b.id = kBxDiffuse;
@@ -429,7 +429,7 @@ __device__ __forceinline__ T pick4(const T* a, uint32_t i) {
     return i == 0 ? a[0] : (i == 1 ? a[1] : (i == 2 ? a[2] : a[3]));
 }
 
-static __device__ f3 eval_fresnel(const uint8_t* fr, float cosi) {  // reflection.cl:345-390
+static __device__ __noinline__ f3 eval_fresnel(const uint8_t* fr, float cosi) {  // reflection.cl:345-390
     switch (fr[0]) {
         case 0:
             return mk(1, 1, 1);
@@ -480,7 +480,7 @@ __device__ __forceinline__ float sin_phi(f3 v) {
     return clampf(v.y / s, -1.0f, 1.0f);
 }
 
-static __device__ f3 bx_f(const BxDF& b, f3 vout, f3 vin) {  // fx, reflection.cl:500-583
+static __device__ __noinline__ f3 bx_f(const BxDF& b, f3 vout, f3 vin) {  // fx, reflection.cl:500-583
     const f3 zero = mk(0, 0, 0);
     switch (b.id) {
         case kBxDiffuse: {
@@ -531,7 +531,7 @@ static __device__ f3 bx_f(const BxDF& b, f3 vout, f3 vin) {  // fx, reflection.c
     }
 }
 
-static __device__ float bx_pdf(const BxDF& b, f3 vout, f3 vin) {  // fx_pdf, reflection.cl:585-626
+static __device__ __noinline__ float bx_pdf(const BxDF& b, f3 vout, f3 vin) {  // fx_pdf, reflection.cl:585-626
     switch (b.id) {
         case kBxDiffuse:
         case kBxAshD:
@@ -556,7 +556,7 @@ static __device__ float bx_pdf(const BxDF& b, f3 vout, f3 vin) {  // fx_pdf, ref
 
 // sample_fx, reflection.cl:393-498.  AshikhminS reads vin->z before it is
 // written (reflection.cl:474); vout.z is used instead, as NewWard does at :447.
-static __device__ f3 bx_sample(const BxDF& b, f3 vout, float u0, float u1, f3& vin, float& pdf) {
+static __device__ __noinline__ f3 bx_sample(const BxDF& b, f3 vout, float u0, float u1, f3& vin, float& pdf) {
     const f3 zero = mk(0, 0, 0);
     switch (b.id) {
         case kBxDiffuse:
@@ -655,9 +655,9 @@ __device__ __forceinline__ f3 bsdf_sample(const BSDF& f, f3 vout, float uc, floa
     sampledType = b.type;
     vin = local_to_world(f.s, f.t, f.n, vinl);
     if (!(b.type & kTySpecular) && numMatches > 1) {
-#pragma unroll
-        for (int i = 0; i < kMaxBxDFs; ++i)
-            if (i < f.num && (uint32_t)i != which && match_type(f.type[i], flags))
+#pragma unroll 1
+        for (int i = 0; i < f.num; ++i)
+            if ((uint32_t)i != which && match_type(f.type[i], flags))
                 pdf += bx_pdf(load_bx(f, f.off[i]), vl, vinl);
     }
     pdf /= (float)numMatches;
@@ -665,9 +665,9 @@ __device__ __forceinline__ f3 bsdf_sample(const BSDF& f, f3 vout, float uc, floa
         ret = zero;
         if (dot(vin, f.ng) * dot(vout, f.ng) > 0) flags &= ~kTyTransmission;
         else flags &= ~kTyReflection;
-#pragma unroll
-        for (int i = 0; i < kMaxBxDFs; ++i)
-            if (i < f.num && match_type(f.type[i], flags)) ret += bx_f(load_bx(f, f.off[i]), vl, vinl);
+#pragma unroll 1
+        for (int i = 0; i < f.num; ++i)
+            if (match_type(f.type[i], flags)) ret += bx_f(load_bx(f, f.off[i]), vl, vinl);
     }
     return ret;
 }
@@ -679,9 +679,9 @@ __device__ __forceinline__ f3 bsdf_f(const BSDF& f, f3 vout, f3 vin) {
     f3 ret = mk(0, 0, 0);
     if (dot(vin, f.ng) * dot(vout, f.ng) > 0) flags &= ~kTyTransmission;
     else flags &= ~kTyReflection;
-#pragma unroll
-    for (int i = 0; i < kMaxBxDFs; ++i)
-        if (i < f.num && match_type(f.type[i], flags)) ret += bx_f(load_bx(f, f.off[i]), vl, il);
+#pragma unroll 1
+    for (int i = 0; i < f.num; ++i)
+        if (match_type(f.type[i], flags)) ret += bx_f(load_bx(f, f.off[i]), vl, il);
     return ret;
 }
 
@@ -689,9 +689,9 @@ __device__ __forceinline__ f3 bsdf_f(const BSDF& f, f3 vout, f3 vin) {
 __device__ __forceinline__ float bsdf_pdf(const BSDF& f, f3 vout, f3 vin) {
     const f3 vl = world_to_local(f.s, f.t, f.n, vout), il = world_to_local(f.s, f.t, f.n, vin);
     float pdf = 0.0f;
-#pragma unroll
-    for (int i = 0; i < kMaxBxDFs; ++i)
-        if (i < f.num && match_type(f.type[i], kTyAll)) pdf += bx_pdf(load_bx(f, f.off[i]), vl, il);
+#pragma unroll 1
+    for (int i = 0; i < f.num; ++i)
+        if (match_type(f.type[i], kTyAll)) pdf += bx_pdf(load_bx(f, f.off[i]), vl, il);
     return pdf / (uint32_t)f.num;
 }
 
