@@ -69,6 +69,7 @@ def lib() -> C.CDLL:
             "clr_lbvh_destroy": [vp],
             "clr_lbvh_build": [vp, vp, vp, vp, vp, u32, u32, C.POINTER(ClrBvh), vp],
             "clr_lbvh_build_noalloc": [vp, vp, vp, vp, u32, u32, C.POINTER(ClrBvh), vp],
+            "clr_lbvh_build_batched": [vp, vp, vp, vp, vp, C.POINTER(u32), u32, u32, u32, vp, vp, vp, vp],
             "clr_lbvh_export_reference": [vp, C.POINTER(ClrBvh), vp, vp, vp, vp, vp, vp],
             "clr_trace_closest": [C.POINTER(ClrBvh), vp, u32, vp, vp, vp],
             "clr_trace_closest_ordered": [C.POINTER(ClrBvh), vp, u32, vp, vp, vp],
@@ -81,6 +82,12 @@ def lib() -> C.CDLL:
             "clr_render_adjoint_workspace_bytes": [u32, u32, u32, C.POINTER(C.c_uint64)],
             "clr_render_adjoint": [vp, u32, u32, vp, vp, u32, u32, u32, C.POINTER(ClrAdjointParams), vp,
                                    C.c_uint64, vp],
+            "clr_batch_create": [vp, C.POINTER(u32), C.POINTER(u32), u32, vp, C.POINTER(vp)],
+            "clr_batch_destroy": [vp],
+            "clr_batch_set_config": [vp, vp],
+            "clr_batch_get_config": [vp, vp],
+            "clr_batch_pixels": [vp, C.POINTER(u32)],
+            "clr_batch_render": [vp, vp, vp, u32, u32, u32, vp],
             "clr_lbvh_pass_times": [vp, C.POINTER(C.c_float), C.POINTER(C.c_char_p), i32, C.POINTER(i32)],
         }
         for name, args in sig.items():

@@ -210,7 +210,8 @@ struct SortCfg<uint32_t> { static constexpr int kItems = 16; };
 template <>
 struct SortCfg<uint64_t> { static constexpr int kItems = 8; };
 
-template <typename KeyT, bool kFirst>
+// kBits-bit digits (6, 7 or 8); the per-digit arrays keep a 256 stride.
+template <typename KeyT, bool kFirst, int kBits = 8>
 __global__ void __launch_bounds__(kSortThreads) k_onesweep(const KeyT* __restrict__ kin,
                                                            const uint32_t* __restrict__ vin,
                                                            KeyT* __restrict__ kout, uint32_t* __restrict__ vout,
@@ -219,6 +220,8 @@ __global__ void __launch_bounds__(kSortThreads) k_onesweep(const KeyT* __restric
                                                            unsigned int* __restrict__ status,
                                                            unsigned int* __restrict__ tile_ctr) {
     constexpr int kItems = SortCfg<KeyT>::kItems;
+    constexpr unsigned int kR = 1u << kBits, kDigitMask = kR - 1u;
+    static_assert(kBits >= 1 && kBits <= 8, "digits of 1..8 bits");
     constexpr int kWarps = kSortThreads / 32;
     constexpr int kWarpSpan = 32 * kItems;
     constexpr int kTile = kSortThreads * kItems;
@@ -259,7 +262,7 @@ __global__ void __launch_bounds__(kSortThreads) k_onesweep(const KeyT* __restric
     for (int i = 0; i < kItems; ++i) {
         const uint32_t idx = wbase + i * 32 + lane;
         const bool ok = idx < n;
-        const unsigned int dig = ok ? (unsigned int)((k[i] >> shift) & 0xFFu) : 0xFFFFFFFFu;
+        const unsigned int dig = ok ? (unsigned int)((k[i] >> shift) & kDigitMask) : 0xFFFFFFFFu;
         const unsigned int peers = __match_any_sync(0xFFFFFFFFu, dig);
         const int leader = __ffs(peers) - 1;
         unsigned int old = 0;
@@ -273,9 +276,10 @@ __global__ void __launch_bounds__(kSortThreads) k_onesweep(const KeyT* __restric
     }
     __syncthreads();
 
-    // Per digit d (= tid): warp prefix, tile total, early publication of the
-    // tile's aggregate, then the look-back over earlier tiles.
+    // Per digit d (= tid < kR): warp prefix, tile total, early publication of
+    // the tile's aggregate, then the look-back over earlier tiles.
     const int d = tid;
+    const bool dv = (unsigned int)d < kR;
     unsigned int total = 0;
 #pragma unroll
     for (int w = 0; w < kWarps; ++w) {
@@ -284,15 +288,17 @@ __global__ void __launch_bounds__(kSortThreads) k_onesweep(const KeyT* __restric
         total += c;
     }
     unsigned int* my_status = status + (size_t)tile * kRadix + d;
-    if (tile == 0) st_relaxed_gpu(my_status, kFlagInclusive | total);
-    else st_relaxed_gpu(my_status, kFlagAggregate | total);
+    if (dv) {
+        if (tile == 0) st_relaxed_gpu(my_status, kFlagInclusive | total);
+        else st_relaxed_gpu(my_status, kFlagAggregate | total);
+    }
 
     const unsigned int tile_off = block_excl_scan256(total, s_scan);
-    const unsigned int gcount = __ldg(hist + d);
+    const unsigned int gcount = dv ? __ldg(hist + d) : 0u;
     const unsigned int gexcl = block_excl_scan256(gcount, s_scan);
 
     unsigned int excl = 0;
-    if (tile > 0) {
+    if (tile > 0 && dv) {
         int j = (int)tile - 1;
         unsigned int spins = 0;
         while (j >= 0) {
@@ -321,7 +327,7 @@ __global__ void __launch_bounds__(kSortThreads) k_onesweep(const KeyT* __restric
     for (int i = 0; i < kItems; ++i) {
         const uint32_t idx = wbase + i * 32 + lane;
         if (idx < n) {
-            const unsigned int dig = (unsigned int)((k[i] >> shift) & 0xFFu);
+            const unsigned int dig = (unsigned int)((k[i] >> shift) & kDigitMask);
             const uint32_t pos = s_tile_off[dig] + s_whist[warp][dig] + rank[i];
             s_keys[pos] = k[i];
             s_vals[pos] = v[i];
@@ -335,7 +341,7 @@ __global__ void __launch_bounds__(kSortThreads) k_onesweep(const KeyT* __restric
         const uint32_t p = i * kSortThreads + tid;
         if (p < tile_n) {
             const KeyT key = s_keys[p];
-            const unsigned int dig = (unsigned int)((key >> shift) & 0xFFu);
+            const unsigned int dig = (unsigned int)((key >> shift) & kDigitMask);
             const uint32_t g = s_gbase[dig] + p;
             kout[g] = key;
             vout[g] = s_vals[p];
@@ -373,15 +379,17 @@ __device__ __forceinline__ TriVerts load_tri(const float* vx, const float* vy, c
 }
 
 // Writes leaf `leaf`'s triangle record and returns its box (calcAABBs).
+// `tid` indexes the (global) vertex arrays, `rec_id` is the id recorded.
 __device__ __forceinline__ void emit_leaf(const float* vx, const float* vy, const float* vz, const uint32_t* tri,
-                                          uint32_t tid, uint32_t leaf, float4* __restrict__ tris, float box[6]) {
+                                          uint32_t tid, uint32_t rec_id, uint32_t leaf, float4* __restrict__ tris,
+                                          float box[6]) {
     const TriVerts tv = load_tri(vx, vy, vz, tri, tid);
     for (int k = 0; k < 3; ++k) {
         box[k] = fminf(tv.p[0][k], fminf(tv.p[1][k], tv.p[2][k]));
         box[3 + k] = fmaxf(tv.p[0][k], fmaxf(tv.p[1][k], tv.p[2][k]));
     }
     float4* r = tris + 3u * leaf;
-    r[0] = make_float4(tv.p[0][0], tv.p[0][1], tv.p[0][2], __uint_as_float(tid));
+    r[0] = make_float4(tv.p[0][0], tv.p[0][1], tv.p[0][2], __uint_as_float(rec_id));
     r[1] = make_float4(fsub(tv.p[1][0], tv.p[0][0]), fsub(tv.p[1][1], tv.p[0][1]), fsub(tv.p[1][2], tv.p[0][2]), 0.f);
     r[2] = make_float4(fsub(tv.p[2][0], tv.p[0][0]), fsub(tv.p[2][1], tv.p[0][1]), fsub(tv.p[2][2], tv.p[0][2]), 0.f);
 }
@@ -424,17 +432,20 @@ __device__ __forceinline__ void tri_box(const float* vx, const float* vy, const 
     }
 }
 
+// Leaf j's climb over one tree of n leaves.  All arrays are the tree's own
+// (offset to its first leaf); sidx holds vertex-array triangle ids, recorded
+// minus id_base.
 template <typename KeyT>
-__global__ void __launch_bounds__(256) k_build_tree(const KeyT* __restrict__ keys, const uint32_t* __restrict__ sidx,
-                                                    uint32_t n, int kbits, const float* __restrict__ vx,
-                                                    const float* __restrict__ vy, const float* __restrict__ vz,
-                                                    const uint32_t* __restrict__ tri, float* __restrict__ nodes,
-                                                    float4* __restrict__ tris, unsigned int* __restrict__ counters,
-                                                    uint32_t* __restrict__ karras_idx, float* __restrict__ root_box) {
-    const uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
-    if (j >= n) return;
+__device__ __forceinline__ void tree_climb(const KeyT* __restrict__ keys, const uint32_t* __restrict__ sidx,
+                                           uint32_t n, int kbits, const float* __restrict__ vx,
+                                           const float* __restrict__ vy, const float* __restrict__ vz,
+                                           const uint32_t* __restrict__ tri, float* __restrict__ nodes,
+                                           float4* __restrict__ tris, unsigned int* __restrict__ counters,
+                                           uint32_t* __restrict__ karras_idx, float* __restrict__ root_box,
+                                           uint32_t j, uint32_t id_base) {
     float box[6];
-    emit_leaf(vx, vy, vz, tri, __ldg(sidx + j), j, tris, box);
+    const uint32_t tj = __ldg(sidx + j);
+    emit_leaf(vx, vy, vz, tri, tj, tj - id_base, j, tris, box);
     // adjacent deltas around leaf j (-1 outside the array)
     const int dl = j > 0 ? delta_adj(keys, kbits, j - 1) : -1;
     const int dj = j + 1 < n ? delta_adj(keys, kbits, j) : -1;
@@ -511,12 +522,24 @@ __global__ void __launch_bounds__(256) k_build_tree(const KeyT* __restrict__ key
     clr_raise(CLR_DEVERR_REFIT);
 }
 
+template <typename KeyT>
+__global__ void __launch_bounds__(256) k_build_tree(const KeyT* __restrict__ keys, const uint32_t* __restrict__ sidx,
+                                                    uint32_t n, int kbits, const float* __restrict__ vx,
+                                                    const float* __restrict__ vy, const float* __restrict__ vz,
+                                                    const uint32_t* __restrict__ tri, float* __restrict__ nodes,
+                                                    float4* __restrict__ tris, unsigned int* __restrict__ counters,
+                                                    uint32_t* __restrict__ karras_idx, float* __restrict__ root_box) {
+    const uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= n) return;
+    tree_climb<KeyT>(keys, sidx, n, kbits, vx, vy, vz, tri, nodes, tris, counters, karras_idx, root_box, j, 0u);
+}
+
 // Single-triangle scene: one leaf, no internal node (the reference requires
 // at least two triangles; here traversal treats the leaf as the root).
 __global__ void k_single(const float* vx, const float* vy, const float* vz, const uint32_t* tri, float4* tris,
                          float* root_box) {
     float box[6];
-    emit_leaf(vx, vy, vz, tri, 0u, 0u, tris, box);
+    emit_leaf(vx, vy, vz, tri, 0u, 0u, 0u, tris, box);
     for (int k = 0; k < 3; ++k) { root_box[k] = box[k]; root_box[4 + k] = box[3 + k]; }
     root_box[3] = __uint_as_float(kLeafBit);
     root_box[7] = 0.f;
@@ -586,6 +609,135 @@ template <typename KeyT>
 __global__ void k_keys_to_u64(const KeyT* __restrict__ in, uint64_t* __restrict__ out, uint32_t n) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < n) out[i] = (uint64_t)in[i];
+}
+
+// ------------------------------------------------- segmented (batched) build
+//
+// Many scenes in one build: scene s owns triangles [off[s], off[s+1]) of the
+// concatenated arrays.  Each scene is quantised in its own box, its keys carry
+// the scene id above the 3b Morton bits (so one stable sort keeps scenes
+// apart and each scene's order is its standalone order), and each scene's
+// tree is climbed with scene-local positions and ids.  The deltas of two keys
+// of one scene are the standalone deltas (the id bits are equal), so every
+// scene's nodes, triangle records and root are bit-identical to a build of
+// that scene alone.
+
+constexpr uint32_t kSegBoxChunk = 4096;  // triangles per block of k_seg_box
+
+// The scene owning position i: the largest s < nseg with off[s] <= i.
+__device__ __forceinline__ uint32_t seg_of(const uint32_t* __restrict__ off, uint32_t nseg, uint32_t i) {
+    uint32_t lo = 0, hi = nseg;
+    while (hi - lo > 1) {
+        const uint32_t mid = (lo + hi) >> 1;
+        if (__ldg(off + mid) <= i) lo = mid;
+        else hi = mid;
+    }
+    return lo;
+}
+
+__device__ __forceinline__ void seg_box_flush(unsigned int* __restrict__ boxw, uint32_t s, const float mn[3],
+                                              const float mx[3]) {
+    for (int k = 0; k < 3; ++k) {
+        if (mn[k] == mn[k]) atomicMax(boxw + 6u * s + k, ~float_to_ordered(mn[k]));
+        if (mx[k] == mx[k]) atomicMax(boxw + 6u * s + 3 + k, float_to_ordered(mx[k]));
+    }
+}
+
+// Per-scene bounds of the triangles' vertices (k_scene_box per scene).
+__global__ void __launch_bounds__(256) k_seg_box(const float* __restrict__ vx, const float* __restrict__ vy,
+                                                 const float* __restrict__ vz, const uint32_t* __restrict__ tri,
+                                                 const uint32_t* __restrict__ off, uint32_t nseg, uint32_t n,
+                                                 unsigned int* __restrict__ boxw) {
+    const uint32_t t0 = blockIdx.x * kSegBoxChunk, t1 = min(t0 + kSegBoxChunk, n);
+    float mn[3] = {INFINITY, INFINITY, INFINITY}, mx[3] = {-INFINITY, -INFINITY, -INFINITY};
+    uint32_t cur = 0xFFFFFFFFu;
+    for (uint32_t t = t0 + threadIdx.x; t < t1; t += blockDim.x) {
+        const uint32_t s = seg_of(off, nseg, t);
+        if (s != cur) {
+            if (cur != 0xFFFFFFFFu) seg_box_flush(boxw, cur, mn, mx);
+            cur = s;
+            for (int k = 0; k < 3; ++k) {
+                mn[k] = INFINITY;
+                mx[k] = -INFINITY;
+            }
+        }
+        const TriVerts tv = load_tri(vx, vy, vz, tri, t);
+        for (int v = 0; v < 3; ++v)
+            for (int k = 0; k < 3; ++k) {
+                mn[k] = fminf(mn[k], tv.p[v][k]);
+                mx[k] = fmaxf(mx[k], tv.p[v][k]);
+            }
+    }
+    // a warp whose lanes all end in one scene combines before the atomics
+    const unsigned int act = __activemask();
+    const uint32_t s0 = __shfl_sync(act, cur, __ffs(act) - 1);
+    if (__all_sync(act, cur == s0) && act == 0xFFFFFFFFu) {
+        for (int k = 0; k < 3; ++k) {
+            mn[k] = warp_min(mn[k]);
+            mx[k] = warp_max(mx[k]);
+        }
+        if ((threadIdx.x & 31) == 0 && cur != 0xFFFFFFFFu) seg_box_flush(boxw, cur, mn, mx);
+    } else if (cur != 0xFFFFFFFFu) {
+        seg_box_flush(boxw, cur, mn, mx);
+    }
+}
+
+// Keys (scene id << 3b | Morton code of the centroid in the scene's box) and
+// the digit histograms of every sort pass.
+template <int kBits>
+__global__ void __launch_bounds__(256) k_morton_seg(const float* __restrict__ vx, const float* __restrict__ vy,
+                                                    const float* __restrict__ vz, const uint32_t* __restrict__ tri,
+                                                    const uint32_t* __restrict__ off, uint32_t nseg, uint32_t n,
+                                                    uint32_t bits, const unsigned int* __restrict__ boxw,
+                                                    uint64_t* __restrict__ keys, unsigned int* __restrict__ hist,
+                                                    int npasses, unsigned int* __restrict__ counters) {
+    constexpr uint32_t kMask = (1u << kBits) - 1u;
+    __shared__ unsigned int sh[kMaxPasses * kRadix];
+    for (int i = threadIdx.x; i < npasses * kRadix; i += blockDim.x) sh[i] = 0;
+    const uint32_t numDivs = 1u << bits;
+    const float fDivs = (float)numDivs;
+    __syncthreads();
+    for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
+        const uint32_t s = seg_of(off, nseg, t);
+        float smin[3], ssize[3];
+        load_scene_box(boxw + 6u * s, smin, ssize);
+        const TriVerts tv = load_tri(vx, vy, vz, tri, t);
+        uint32_t q[3];
+        for (int k = 0; k < 3; ++k) {
+            const float mn = fminf(tv.p[0][k], fminf(tv.p[1][k], tv.p[2][k]));
+            const float mx = fmaxf(tv.p[0][k], fmaxf(tv.p[1][k], tv.p[2][k]));
+            const float center = fmul(fadd(mn, mx), 0.5f);
+            const float normPos = fdiv(fsub(center, smin[k]), ssize[k]);
+            const uint32_t v = __float2uint_rz(fmul(normPos, fDivs));
+            q[k] = min(v, numDivs - 1u);
+        }
+        const uint64_t key = ((uint64_t)s << (3 * bits)) | make_key<uint64_t>(q[0], q[1], q[2]);
+        keys[t] = key;
+        counters[t] = 0u;
+        for (int p = 0; p < npasses; ++p) atomicAdd(&sh[p * kRadix + (uint32_t)((key >> (kBits * p)) & kMask)], 1u);
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < npasses * kRadix; i += blockDim.x)
+        if (sh[i]) atomicAdd(hist + i, sh[i]);
+}
+
+// One thread per leaf; each climbs its own scene's tree.
+template <typename KeyT>
+__global__ void __launch_bounds__(256) k_build_tree_seg(const KeyT* __restrict__ keys,
+                                                        const uint32_t* __restrict__ sidx,
+                                                        const uint32_t* __restrict__ off, uint32_t nseg, uint32_t n,
+                                                        int kbits, const float* __restrict__ vx,
+                                                        const float* __restrict__ vy, const float* __restrict__ vz,
+                                                        const uint32_t* __restrict__ tri, float* __restrict__ nodes,
+                                                        float4* __restrict__ tris, unsigned int* __restrict__ counters,
+                                                        uint32_t* __restrict__ karras_idx,
+                                                        float* __restrict__ root_boxes) {
+    const uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= n) return;
+    const uint32_t s = seg_of(off, nseg, j);
+    const uint32_t s0 = __ldg(off + s), ns = __ldg(off + s + 1) - s0;
+    tree_climb<KeyT>(keys + s0, sidx + s0, ns, kbits, vx, vy, vz, tri, nodes + 16ull * s0, tris + 3ull * s0,
+                     counters + s0, karras_idx + s0, root_boxes + 8ull * s, j - s0, s0);
 }
 
 }  // namespace clr
@@ -667,6 +819,7 @@ extern "C" int clr_lbvh_create(uint32_t capacity, clr_lbvh** out) {
 extern "C" int clr_lbvh_destroy(clr_lbvh* h) {
     if (!h) return CLR_OK;
     if (h->pool) cudaFree(h->pool);
+    if (h->seg_pool) cudaFree(h->seg_pool);
     for (auto& e : h->ev)
         if (e) cudaEventDestroy(e);
     delete h;
@@ -722,7 +875,6 @@ static int run_build(clr_lbvh* h, const float* vx, const float* vy, const float*
     }
     const int fin = npasses & 1;
     h->final_buf = fin;
-    float4* nodes = static_cast<float4*>(out->nodes);
     float4* tris = static_cast<float4*>(out->tris);
     if (n == 1) {
         k_single<<<1, 1, 0, st>>>(vx, vy, vz, tri, tris, out->root_box);
@@ -757,6 +909,109 @@ extern "C" int clr_lbvh_build(clr_lbvh* h, const float* vx, const float* vy, con
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     if (bits_per_dim <= 10) return run_build<uint32_t>(h, vx, vy, vz, tri, num_tris, bits_per_dim, out, st);
     return run_build<uint64_t>(h, vx, vy, vz, tri, num_tris, bits_per_dim, out, st);
+}
+
+static int seg_grow(clr_lbvh* h, uint32_t nseg) {
+    if (h->seg_pool && nseg <= h->seg_cap) return CLR_OK;
+    if (h->seg_pool) cudaFree(h->seg_pool);
+    h->seg_pool = nullptr;
+    h->seg_cap = 0;
+    const size_t off_bytes = align_up(4ull * (nseg + 1), 256);
+    if (cudaMalloc(&h->seg_pool, off_bytes + 24ull * nseg) != cudaSuccess) {
+        cudaGetLastError();
+        h->seg_pool = nullptr;
+        return clr_set_error(CLR_ENOMEM, "cudaMalloc for %u scene descriptors failed", nseg);
+    }
+    h->seg_off = static_cast<uint32_t*>(h->seg_pool);
+    h->seg_box = reinterpret_cast<unsigned int*>(static_cast<char*>(h->seg_pool) + off_bytes);
+    h->seg_cap = nseg;
+    return CLR_OK;
+}
+
+template <int kBits>
+static void launch_sort_pass(uint64_t* kin, uint32_t* vin, uint64_t* kout, uint32_t* vout, uint32_t n, int p,
+                             clr_lbvh* h, unsigned int tiles, cudaStream_t st) {
+    if (p == 0)
+        k_onesweep<uint64_t, true, kBits><<<tiles, kSortThreads, 0, st>>>(
+            kin, nullptr, kout, vout, n, kBits * p, h->hist + p * kRadix, h->status + p * h->status_stride,
+            h->tile_ctr + p);
+    else
+        k_onesweep<uint64_t, false, kBits><<<tiles, kSortThreads, 0, st>>>(
+            kin, vin, kout, vout, n, kBits * p, h->hist + p * kRadix, h->status + p * h->status_stride,
+            h->tile_ctr + p);
+}
+
+extern "C" int clr_lbvh_build_batched(clr_lbvh* h, const float* vx, const float* vy, const float* vz,
+                                      const uint32_t* tri, const uint32_t* scene_offsets, uint32_t num_scenes,
+                                      uint32_t bits_per_dim, uint32_t radix_bits, void* nodes, void* tris,
+                                      float* root_boxes, void* stream) {
+    if (!h || !scene_offsets || num_scenes == 0)
+        return clr_set_error(CLR_EINVAL, "clr_lbvh_build_batched: NULL handle / offsets or no scene");
+    if (radix_bits == 0) radix_bits = 8;
+    if (radix_bits < 6 || radix_bits > 8)
+        return clr_set_error(CLR_EINVAL, "clr_lbvh_build_batched: radix_bits %u outside [6, 8]", radix_bits);
+    if (scene_offsets[0] != 0) return clr_set_error(CLR_EINVAL, "clr_lbvh_build_batched: offsets[0] must be 0");
+    for (uint32_t s = 0; s < num_scenes; ++s)
+        if (scene_offsets[s + 1] <= scene_offsets[s])
+            return clr_set_error(CLR_EINVAL, "clr_lbvh_build_batched: scene %u has no triangle", s);
+    const uint32_t n = scene_offsets[num_scenes];
+    if (n >= (1u << 30))
+        return clr_set_error(CLR_EINVAL, "clr_lbvh_build_batched: %u triangles exceed the 2^30 limit", n);
+    uint32_t sbits = 0;
+    while ((1ull << sbits) < num_scenes) ++sbits;
+    const int kbits = 3 * (int)bits_per_dim;
+    const int total_bits = kbits + (int)sbits;
+    const int npasses = (total_bits + (int)radix_bits - 1) / (int)radix_bits;
+    if (bits_per_dim < 1 || total_bits > 64 || npasses > kMaxPasses)
+        return clr_set_error(CLR_EINVAL,
+                             "clr_lbvh_build_batched: %u bits per axis and %u scenes need %d key bits / %d passes",
+                             bits_per_dim, num_scenes, total_bits, npasses);
+    if (!vx || !vy || !vz || !nodes || !tris || !root_boxes)
+        return clr_set_error(CLR_EINVAL, "clr_lbvh_build_batched: NULL input or output buffer");
+    int rc = pool_grow(h, n);
+    if (rc != CLR_OK) return rc;
+    rc = seg_grow(h, num_scenes);
+    if (rc != CLR_OK) return rc;
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    h->last_n = 0;  // the reference-layout export covers single-scene builds only
+    PassTimer timer(h, st);
+    CLR_CUDA_TRY(cudaMemcpyAsync(h->seg_off, scene_offsets, 4ull * (num_scenes + 1), cudaMemcpyHostToDevice, st));
+    CLR_CUDA_TRY(cudaMemsetAsync(h->zero_region, 0, h->zero_bytes, st));
+    CLR_CUDA_TRY(cudaMemsetAsync(h->seg_box, 0, 24ull * num_scenes, st));
+    k_seg_box<<<div_up(n, kSegBoxChunk), 256, 0, st>>>(vx, vy, vz, tri, h->seg_off, num_scenes, n, h->seg_box);
+    CLR_LAUNCH_CHECK("k_seg_box");
+    timer.done("scene_box");
+    uint64_t* keys[2] = {static_cast<uint64_t*>(h->keys[0]), static_cast<uint64_t*>(h->keys[1])};
+    const int grid_stream = kSmCount * 8;
+    if (radix_bits == 8)
+        k_morton_seg<8><<<grid_stream, 256, 0, st>>>(vx, vy, vz, tri, h->seg_off, num_scenes, n, bits_per_dim,
+                                                     h->seg_box, keys[0], h->hist, npasses, h->counters);
+    else if (radix_bits == 7)
+        k_morton_seg<7><<<grid_stream, 256, 0, st>>>(vx, vy, vz, tri, h->seg_off, num_scenes, n, bits_per_dim,
+                                                     h->seg_box, keys[0], h->hist, npasses, h->counters);
+    else
+        k_morton_seg<6><<<grid_stream, 256, 0, st>>>(vx, vy, vz, tri, h->seg_off, num_scenes, n, bits_per_dim,
+                                                     h->seg_box, keys[0], h->hist, npasses, h->counters);
+    CLR_LAUNCH_CHECK("k_morton_seg");
+    timer.done("morton");
+    constexpr int kTile = kSortThreads * SortCfg<uint64_t>::kItems;
+    const unsigned int tiles = div_up(n, kTile);
+    for (int p = 0; p < npasses; ++p) {
+        const int src = p & 1, dst = src ^ 1;
+        if (radix_bits == 8) launch_sort_pass<8>(keys[src], h->vals[src], keys[dst], h->vals[dst], n, p, h, tiles, st);
+        else if (radix_bits == 7) launch_sort_pass<7>(keys[src], h->vals[src], keys[dst], h->vals[dst], n, p, h, tiles, st);
+        else launch_sort_pass<6>(keys[src], h->vals[src], keys[dst], h->vals[dst], n, p, h, tiles, st);
+        CLR_LAUNCH_CHECK("k_onesweep");
+        timer.done("sort_pass");
+    }
+    const int fin = npasses & 1;
+    h->final_buf = fin;
+    k_build_tree_seg<uint64_t><<<div_up(n, 256), 256, 0, st>>>(
+        keys[fin], h->vals[fin], h->seg_off, num_scenes, n, kbits, vx, vy, vz, tri, static_cast<float*>(nodes),
+        static_cast<float4*>(tris), h->counters, h->karras_idx, root_boxes);
+    CLR_LAUNCH_CHECK("k_build_tree_seg");
+    timer.done("build_tree");
+    return CLR_OK;
 }
 
 extern "C" int clr_lbvh_export_reference(clr_lbvh* h, const clr_bvh* bvh, void* inodes, void* lnodes,

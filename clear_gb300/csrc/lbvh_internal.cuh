@@ -40,6 +40,11 @@ struct clr_lbvh {
     size_t status_stride = 0;
     unsigned int* tile_ctr = nullptr;        // [pass] dynamic tile counter
     unsigned int* boxw = nullptr;            // scene box, ordered-uint encoded
+    // batched builds: scene offsets and per-scene boxes (own allocation)
+    uint32_t seg_cap = 0;
+    void* seg_pool = nullptr;
+    uint32_t* seg_off = nullptr;
+    unsigned int* seg_box = nullptr;
     uint32_t last_n = 0, last_bits = 0;
     int final_buf = 0;                       // ping-pong side holding sorted data
     // profiling (clr_lbvh_set_profiling)

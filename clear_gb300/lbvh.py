@@ -53,6 +53,34 @@ class BVH:
         return self.c.bits_per_dim
 
 
+class BatchBVH:
+    """The BVHs of a segmented build: shared node / record buffers, one
+    root box per scene; ``scene(s)`` is scene s's BVH (a view)."""
+
+    def __init__(self, offsets: list[int], bits: int, device):
+        self.device = torch.device(device)
+        self.offsets = offsets
+        total = offsets[-1]
+        self.nodes = torch.empty(max(total, 1) * _lib.NODE_BYTES, dtype=torch.uint8, device=self.device)
+        self.tris = torch.empty(max(total, 1) * _lib.TRI_BYTES, dtype=torch.uint8, device=self.device)
+        self.root_boxes = torch.zeros((len(offsets) - 1, 8), dtype=torch.float32, device=self.device)
+        self.bits = bits
+
+    def __len__(self) -> int:
+        return len(self.offsets) - 1
+
+    def scene(self, s: int) -> BVH:
+        o, n = self.offsets[s], self.offsets[s + 1] - self.offsets[s]
+        b = BVH.__new__(BVH)
+        b.device = self.device
+        b.nodes = self.nodes[o * _lib.NODE_BYTES:(o + max(n - 1, 1)) * _lib.NODE_BYTES]
+        b.tris = self.tris[o * _lib.TRI_BYTES:(o + n) * _lib.TRI_BYTES]
+        b.root_box = self.root_boxes[s]
+        b.c = ClrBvh(n, self.bits, b.nodes.data_ptr(), b.tris.data_ptr(), b.root_box.data_ptr())
+        b._owner = self
+        return b
+
+
 class LBVHBuilder:
     def __init__(self, num_faces: int, device="cuda"):
         self.device = torch.device(device)
@@ -90,6 +118,25 @@ class LBVHBuilder:
                  C.c_uint32(int(num_bits_per_dim)), C.byref(bvh.c), _stream(self.device))
         bvh._inputs = (vx, vy, vz, tri)  # keep alive until the stream has consumed them
         return bvh
+
+    def perform_batched(self, vertices, faces, scene_offsets, num_bits_per_dim: int = 10,
+                        radix_bits: int = 8) -> "BatchBVH":
+        """Build one LBVH per scene in one segmented pass.  vertices and faces
+        are concatenated over the scenes (faces index the concatenated
+        vertices, or None for a soup); scene_offsets (host sequence of
+        num_scenes + 1 ints, from 0) delimits each scene's triangles."""
+        vx, vy, vz = (_f32(v, self.device) for v in vertices)
+        tri = None
+        if faces is not None:
+            tri = faces.to(device=self.device, dtype=torch.int32).contiguous()
+        offs = (C.c_uint32 * len(scene_offsets))(*[int(o) for o in scene_offsets])
+        b = BatchBVH([int(o) for o in scene_offsets], int(num_bits_per_dim), self.device)
+        with torch.cuda.device(self.device):
+            call("clr_lbvh_build_batched", self._h, _ptr(vx), _ptr(vy), _ptr(vz), _ptr(tri), offs,
+                 C.c_uint32(len(scene_offsets) - 1), C.c_uint32(int(num_bits_per_dim)), C.c_uint32(int(radix_bits)),
+                 _ptr(b.nodes), _ptr(b.tris), _ptr(b.root_boxes), _stream(self.device))
+        b._inputs = (vx, vy, vz, tri)
+        return b
 
     def set_profiling(self, enable: bool) -> None:
         call("clr_lbvh_set_profiling", self._h, 1 if enable else 0)

@@ -115,6 +115,24 @@ CLR_API int clr_lbvh_build(clr_lbvh* h, const float* vx, const float* vy, const 
 CLR_API int clr_lbvh_build_noalloc(const float* vx, const float* vy, const float* vz, const uint32_t* tri,
                                    uint32_t num_tris, uint32_t bits_per_dim, clr_bvh* out, void* stream);
 
+/* Segmented build of many scenes at once (an addition beside
+ * LBVHBuilder::perform, which builds one scene per call): scene s owns
+ * triangles [scene_offsets[s], scene_offsets[s+1]) of the concatenated inputs
+ * (`tri` holds indices into the concatenated vertex arrays, or is NULL for a
+ * soup); scene_offsets is a HOST array of num_scenes + 1 entries starting at
+ * 0, every scene non-empty.  One scene-box pass, one Morton pass (keys carry
+ * the scene id above the 3 x bits_per_dim Morton bits), one radix sort of
+ * radix_bits-bit digits (6, 7 or 8; 0 = 8) and one tree pass build every
+ * scene.  Scene s's BVH is
+ *   {n_s, bits_per_dim, nodes + CLR_NODE_BYTES * off_s,
+ *    tris + CLR_TRI_BYTES * off_s, root_boxes + 8 * s}
+ * (triangle ids scene-local) and is bit-identical to clr_lbvh_build of that
+ * scene alone.  `nodes` holds total_tris nodes, `tris` total_tris records. */
+CLR_API int clr_lbvh_build_batched(clr_lbvh* builder, const float* vx, const float* vy, const float* vz,
+                                   const uint32_t* tri, const uint32_t* scene_offsets, uint32_t num_scenes,
+                                   uint32_t bits_per_dim, uint32_t radix_bits, void* nodes, void* tris,
+                                   float* root_boxes, void* stream);
+
 /* Parity/debug export of the last build of `h` into the reference layouts:
  * inodes: (n-1) x 48 B LBVH::InternalNode, lnodes: n x 48 B LBVH::LeafNode
  * (LBVHBuilder.h:17-29), parents: 2n-1 uint32 (leaves at [0,n), internal at
@@ -209,6 +227,41 @@ CLR_API int clr_render_workspace_bytes(uint32_t width, uint32_t height, uint64_t
 CLR_API int clr_render_wavefront(const clr_scene* scene, uint32_t width, uint32_t height, uint32_t* rand_states,
                                  float* pixels, uint32_t spp, uint32_t max_depth, uint32_t flags, void* workspace,
                                  uint64_t workspace_bytes, void* stream);
+
+/* ------------------------------------------------------------- batched */
+
+/* Many scenes rendered by one wavefront (an addition; the reference renders
+ * one scene per process).  Scene s has its own blobs, BVH (e.g. one scene of
+ * clr_lbvh_build_batched), camera and widths[s] x heights[s] image; the
+ * batch's pixels are numbered scene after scene, and rand_states / pixels
+ * passed to clr_batch_render are the concatenation of the per-scene arrays.
+ * Each scene's result is bit-identical to clr_render_wavefront of that scene
+ * with the same states.  A fixed pool of pool_slots path slots renders every
+ * sample of one pixel, then takes the next unrendered pixel. */
+typedef struct clr_batch clr_batch;
+typedef struct clr_batch_config {
+    uint32_t trace_block;  /* threads per block of the extend and shadow kernels (32 .. 256, multiple of 32; 0 = 128) */
+    uint32_t shade_block;  /* threads per block of the shading kernel (32 .. 128, multiple of 32; 0 = 128) */
+    uint32_t pool_slots;   /* path slots = queue capacity (0 or more than the pixels = one per pixel) */
+    uint32_t reserved;
+} clr_batch_config;
+
+#define CLR_BATCH_GRAPH 0x2u /* clr_batch_render: run the whole frame loop as one CUDA graph launch */
+
+/* `scenes`, `widths`, `heights` are host arrays of num_scenes entries; the
+ * scene structs' device pointers must stay valid for the batch's life. */
+CLR_API int clr_batch_create(const clr_scene* scenes, const uint32_t* widths, const uint32_t* heights,
+                             uint32_t num_scenes, const clr_batch_config* cfg, clr_batch** out);
+CLR_API int clr_batch_destroy(clr_batch* batch);
+CLR_API int clr_batch_set_config(clr_batch* batch, const clr_batch_config* cfg);
+CLR_API int clr_batch_get_config(const clr_batch* batch, clr_batch_config* cfg);
+CLR_API int clr_batch_pixels(const clr_batch* batch, uint32_t* total_pixels);
+/* Adds spp samples to every pixel of every scene.  flags: CLR_RENDER_ORDERED,
+ * CLR_BATCH_GRAPH (the graph is captured on first use and reused while the
+ * buffers, spp, max_depth, flags and configuration stay the same; without it
+ * the host checks every 8 iterations whether paths remain). */
+CLR_API int clr_batch_render(clr_batch* batch, uint32_t* rand_states, float* pixels, uint32_t spp, uint32_t max_depth,
+                             uint32_t flags, void* stream);
 
 /* ------------------------------------------------------------- adjoint */
 
