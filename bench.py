@@ -77,6 +77,8 @@ def parse():
     ap.add_argument("--render", type=int, default=1, help="also time the path tracer (0 = skip)")
     ap.add_argument("--render-only", action="store_true", help="time only the path tracer (for profiling)")
     ap.add_argument("--adjoint-only", action="store_true", help="time only the adjoint renderer (for profiling)")
+    ap.add_argument("--batched-only", action="store_true", help="time only the batched form (for profiling)")
+    ap.add_argument("--batched-scenes", type=int, default=512)
     ap.add_argument("--adjoint-res", type=int, default=512)
     ap.add_argument("--adjoint-spp", type=int, default=32)
     return ap.parse_args()
@@ -304,6 +306,83 @@ def bench_adjoint(dev, spp=32, res=512) -> dict:
             "grad_norm": float(torch.linalg.norm(grad).item()), "env_grad_norm": float(torch.linalg.norm(genv).item())}
 
 
+def bench_batched(dev, num_scenes=512, spp=8, depth=5) -> dict:
+    """Many scenes per launch: `num_scenes` scenes with log-uniform 1k-200k
+    random triangles plus a quad light, square resolutions from {128, 256,
+    384, 512}, `spp` samples, depth `depth`.  Batched form: one segmented LBVH
+    build and one CUDA-graph wavefront over all scenes, configured by the
+    autotuner.  Plain form: a standalone build and a wavefront render per
+    scene.  Both produce bit-identical images (compared here)."""
+    import time as _t
+
+    import torch
+
+    from clear_gb300 import autotune
+    from clear_gb300.batch import BatchRenderer, PerSceneLoop, batch_workload, random_scene
+
+    t0 = _t.perf_counter()
+    wl = batch_workload(num_scenes)
+    scenes = [random_scene(n, w, h, seed) for n, w, h, seed in wl]
+    gen_s = _t.perf_counter() - t0
+    total_tris = sum(w[0] + 2 for w in wl)
+    stream = torch.cuda.current_stream(dev)
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(8)]
+
+    br = BatchRenderer(scenes, dev)
+    tuned = autotune.tune(br, depth, use_cache=False)
+    seeds, pix = br.new_frame()
+    # warm-up (also captures the graph for this spp)
+    rng = seeds.clone()
+    br.render(rng, pix, spp, depth, graph=True)
+    torch.cuda.synchronize()
+    pix.zero_()
+    rng.copy_(seeds)
+    ev[0].record(stream)
+    br.rebuild_into_current()
+    ev[1].record(stream)
+    br.render(rng, pix, spp, depth, graph=True)
+    ev[2].record(stream)
+    torch.cuda.synchronize()
+    b_build, b_render = ev[0].elapsed_time(ev[1]), ev[1].elapsed_time(ev[2])
+    batched_img = pix[:, :3].clone()
+    del pix, rng
+    br.close()
+    del br
+    torch.cuda.empty_cache()
+
+    loop = PerSceneLoop(scenes, dev)
+    rngs0, pixs = loop.new_frame()
+    rngs = [r.clone() for r in rngs0]
+    loop.render(rngs, pixs, 1, depth)  # warm-up (allocates the workspaces)
+    torch.cuda.synchronize()
+    for p_ in pixs:
+        p_.zero_()
+    for r, r0 in zip(rngs, rngs0):
+        r.copy_(r0)
+    torch.cuda.synchronize()
+    ev[3].record(stream)
+    loop.build_all()
+    ev[4].record(stream)
+    loop.render(rngs, pixs, spp, depth)
+    ev[5].record(stream)
+    torch.cuda.synchronize()
+    l_build, l_render = ev[3].elapsed_time(ev[4]), ev[4].elapsed_time(ev[5])
+    loop_img = torch.cat([p_[:, :3] for p_ in pixs])
+    diff = float((loop_img - batched_img).abs().max().item())
+    samples = int(loop_img.shape[0]) * spp
+    return {"workload": f"{num_scenes} scenes, {total_tris} triangles, {loop_img.shape[0]} pixels, {spp} spp, "
+                        f"depth {depth}", "host_scene_generation_s": gen_s,
+            "batched": {"build_ms": b_build, "render_ms": b_render,
+                        "msamples_s": samples / b_render / 1e3,
+                        "build_plus_render_msamples_s": samples / (b_build + b_render) / 1e3,
+                        "config": tuned["config"], "radix_bits": tuned["radix_bits"]},
+            "per_scene_loop": {"build_ms": l_build, "render_ms": l_render, "msamples_s": samples / l_render / 1e3,
+                               "build_plus_render_msamples_s": samples / (l_build + l_render) / 1e3},
+            "speedup_render": l_render / b_render, "speedup_build_plus_render": (l_build + l_render) /
+            (b_build + b_render), "max_abs_image_diff": diff,
+            "autotune_trials": len(tuned["render_trials"]), "autotune_build_ms": tuned["build_ms"]}
+
+
 def run_reference(args):
     rank, world, _ = dist_env()
     if rank != 0:
@@ -447,6 +526,7 @@ def run_ours(args):
     render = bench_render(dev, args) if args.render else None
     render_terrain = bench_render_terrain(dev) if args.render else None
     adjoint = bench_adjoint(dev) if args.render else None
+    batched = bench_batched(dev, args.batched_scenes) if args.render else None
     hit_frac = float((hid >= 0).float().mean().item())
     occ_frac = float(occ.float().mean().item())
     clk = clocks.stop()
@@ -490,6 +570,7 @@ def run_ours(args):
         "render": render,
         "render_terrain": render_terrain,
         "adjoint": adjoint,
+        "batched": batched,
         "gpu_launches": launches_per_build * args.steps,
         "clocks": clk,
         "device_error_bits": dev_err,
@@ -511,6 +592,14 @@ def main():
         build()
         dev = torch.device("cuda", 0)
         print(json.dumps({"render": bench_render(dev, args), "render_terrain": bench_render_terrain(dev)}), flush=True)
+        return
+    if args.batched_only:
+        import torch
+
+        from clear_gb300.build import build
+
+        build()
+        print(json.dumps({"batched": bench_batched(torch.device("cuda", 0), args.batched_scenes)}), flush=True)
         return
     if args.adjoint_only:
         import torch
