@@ -432,6 +432,56 @@ __device__ __forceinline__ void tri_box(const float* vx, const float* vy, const 
     }
 }
 
+// The device-scope climb from a finished node [lo, hi] (reference `ref`, box
+// `box`): write into the parent's child slot, count the arrival (acq_rel),
+// and continue with the merged parent if this was the second arrival.
+template <typename KeyT>
+__device__ __forceinline__ void climb_global(const KeyT* __restrict__ keys, uint32_t n, int kbits,
+                                             float* __restrict__ nodes, unsigned int* __restrict__ counters,
+                                             uint32_t* __restrict__ karras_idx, float* __restrict__ root_box,
+                                             uint32_t lo, uint32_t hi, uint32_t ref, float box[6]) {
+    // every level up adds at least one common bit of the (3b + 32)-bit key
+    for (int step = 0; step <= kMaxDepth; ++step) {
+        if (lo == 0 && hi == n - 1) {
+            if (!(ref & kLeafBit)) karras_idx[ref] = 0;
+            root_box[0] = box[0]; root_box[1] = box[1]; root_box[2] = box[2];
+            root_box[3] = __uint_as_float(ref);
+            root_box[4] = box[3]; root_box[5] = box[4]; root_box[6] = box[5];
+            root_box[7] = 0.f;
+            return;
+        }
+        const bool left = (lo == 0) || (hi != n - 1 && delta_adj(keys, kbits, hi) > delta_adj(keys, kbits, lo - 1));
+        const uint32_t split = left ? hi : lo - 1;
+        if (!(ref & kLeafBit)) karras_idx[ref] = left ? hi : lo;
+        const int slot = left ? 0 : 1;
+        float* nd = nodes + 16u * split;
+        float2* b2 = reinterpret_cast<float2*>(nd + 6 * slot);
+        __stcg(b2 + 0, make_float2(box[0], box[1]));
+        __stcg(b2 + 1, make_float2(box[2], box[3]));
+        __stcg(b2 + 2, make_float2(box[4], box[5]));
+        unsigned int* w = reinterpret_cast<unsigned int*>(nd);
+        __stcg(w + 12 + slot, ref);
+        __stcg(w + 14 + slot, left ? lo : hi);
+        // release: this child's slot is visible before the arrival counts;
+        // acquire: the sibling's slot is visible to the second arrival
+        if (atomic_add_acq_rel(counters + split, 1u) == 0u) return;
+        float b[12];
+#pragma unroll
+        for (int k = 0; k < 12; ++k) b[k] = __ldcg(nd + k);
+        const uint32_t far_end = __ldcg(w + 14 + (1 - slot));
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            box[k] = fminf(b[k], b[6 + k]);
+            box[3 + k] = fmaxf(b[3 + k], b[9 + k]);
+        }
+        if (left) hi = far_end;
+        else lo = far_end;
+        if (lo > hi || hi >= n) break;  // corrupt slot: report, never index out of range
+        ref = split;
+    }
+    clr_raise(CLR_DEVERR_REFIT);
+}
+
 // Leaf j's climb over one tree of n leaves.  All arrays are the tree's own
 // (offset to its first leaf); sidx holds vertex-array triangle ids, recorded
 // minus id_base.
@@ -480,7 +530,126 @@ __device__ __forceinline__ void tree_climb(const KeyT* __restrict__ keys, const 
             ref = j;
         }
     }
-    // every level up adds at least one common bit of the (3b + 32)-bit key
+    climb_global<KeyT>(keys, n, kbits, nodes, counters, karras_idx, root_box, lo, hi, ref, box);
+}
+
+// The same climb with block-local merging.  Block b owns leaves [B, E]
+// (kTreeBlock consecutive positions).  The node split at s covers the maximal
+// range around s whose other adjacent deltas all exceed delta(s, s+1), so it
+// lies inside [B, E] exactly when some delta(k, k+1) < delta(s, s+1) exists
+// for k in [B-1, s-1] and for k in [s+1, E] (out-of-array deltas count as
+// -1).  The block finds these nodes with prefix / suffix minima of its deltas;
+// both children of such a node are finished by threads of the block, which
+// meet in shared memory (CTA-scope acq_rel counter, no device fence), and the
+// second writes the whole 64-byte node.  A node that crosses a block edge is
+// reached by threads of two blocks and uses the device-scope protocol of
+// tree_climb; so are all its ancestors.
+constexpr int kTreeBlock = 256;
+
+__device__ __forceinline__ unsigned int atomic_add_acq_rel_cta(unsigned int* p, unsigned int v) {
+    unsigned int old;
+    asm volatile("atom.add.acq_rel.cta.shared::cta.u32 %0, [%1], %2;"
+                 : "=r"(old)
+                 : "r"((unsigned int)__cvta_generic_to_shared(p)), "r"(v)
+                 : "memory");
+    return old;
+}
+
+template <typename KeyT>
+__global__ void __launch_bounds__(kTreeBlock) k_build_tree(const KeyT* __restrict__ keys,
+                                                           const uint32_t* __restrict__ sidx, uint32_t n, int kbits,
+                                                           const float* __restrict__ vx, const float* __restrict__ vy,
+                                                           const float* __restrict__ vz, const uint32_t* __restrict__ tri,
+                                                           float* __restrict__ nodes, float4* __restrict__ tris,
+                                                           unsigned int* __restrict__ counters,
+                                                           uint32_t* __restrict__ karras_idx,
+                                                           float* __restrict__ root_box,
+                                                           uint32_t* __restrict__ worklist,
+                                                           unsigned int* __restrict__ wl_count) {
+    __shared__ int s_d[kTreeBlock + 1];      // delta(k, k+1), k = B-1 .. E
+    __shared__ int s_pmin[kTreeBlock + 1];   // prefix minima of s_d
+    __shared__ int s_smin[kTreeBlock + 1];   // suffix minima of s_d
+    __shared__ float s_box[kTreeBlock][2][6];
+    __shared__ uint32_t s_ref[kTreeBlock][2], s_end[kTreeBlock][2];
+    __shared__ unsigned int s_cnt[kTreeBlock];
+    const uint32_t B = blockIdx.x * kTreeBlock;
+    const uint32_t E = min(B + kTreeBlock - 1, n - 1);
+    const int nd = (int)(E - B) + 2;  // entries of s_d
+    const int t = threadIdx.x;
+    for (int i = t; i < nd; i += kTreeBlock) {
+        const int64_t k = (int64_t)B - 1 + i;
+        s_d[i] = (k < 0 || k + 1 >= (int64_t)n) ? -1 : delta_adj(keys, kbits, (uint32_t)k);
+    }
+    s_cnt[t] = 0u;
+    __syncthreads();
+    for (int i = t; i < nd; i += kTreeBlock) {
+        s_pmin[i] = s_d[i];
+        s_smin[i] = s_d[i];
+    }
+    __syncthreads();
+    // Hillis-Steele scans (nd <= 257: the thread of index 0 also takes entry 256)
+    for (int off = 1; off < nd; off <<= 1) {
+        int pv[2], sv[2];
+        for (int r = 0; r < 2; ++r) {
+            const int i = t + r * kTreeBlock;
+            if (i < nd) {
+                pv[r] = i >= off ? min(s_pmin[i], s_pmin[i - off]) : s_pmin[i];
+                sv[r] = i + off < nd ? min(s_smin[i], s_smin[i + off]) : s_smin[i];
+            }
+        }
+        __syncthreads();
+        for (int r = 0; r < 2; ++r) {
+            const int i = t + r * kTreeBlock;
+            if (i < nd) {
+                s_pmin[i] = pv[r];
+                s_smin[i] = sv[r];
+            }
+        }
+        __syncthreads();
+    }
+    const uint32_t j = B + t;
+    if (j >= n) return;
+    // split s in [B, E-1] sits at s_d index s - B + 1
+    auto block_local = [&](uint32_t split) -> bool {
+        if (split < B || split >= E) return false;
+        const int i = (int)(split - B) + 1;
+        return s_pmin[i - 1] < s_d[i] && s_smin[i + 1] < s_d[i];
+    };
+
+    float box[6];
+    const uint32_t tj = __ldg(sidx + j);
+    emit_leaf(vx, vy, vz, tri, tj, tj, j, tris, box);
+    const int dl = s_d[t];      // delta(j-1, j)
+    const int dj = s_d[t + 1];  // delta(j, j+1)
+    const bool j_left = (j == 0) || (j != n - 1 && dj > dl);
+    uint32_t lo = j, hi = j, ref = j | kLeafBit;
+    if (j > 0 && !j_left) {
+        const int dll = j > 1 ? delta_adj(keys, kbits, j - 2) : -1;
+        const bool prev_left = (j - 1 == 0) || (dl > dll);
+        if (prev_left) return;  // leaf j-1 builds our common parent
+    }
+    if (j_left && j + 1 < n) {
+        const int dr = j + 2 < n ? delta_adj(keys, kbits, j + 1) : -1;
+        const bool next_right = (j + 1 == n - 1) || (dr < dj);
+        if (next_right) {
+            float b1[6];
+            tri_box(vx, vy, vz, tri, __ldg(sidx + j + 1), b1);
+            float4* n4 = reinterpret_cast<float4*>(nodes + 16u * j);
+            n4[0] = make_float4(box[0], box[1], box[2], box[3]);
+            n4[1] = make_float4(box[4], box[5], b1[0], b1[1]);
+            n4[2] = make_float4(b1[2], b1[3], b1[4], b1[5]);
+            n4[3] = make_float4(__uint_as_float(j | kLeafBit), __uint_as_float((j + 1) | kLeafBit),
+                                __uint_as_float(j), __uint_as_float(j + 1));
+#pragma unroll
+            for (int k = 0; k < 3; ++k) {
+                box[k] = fminf(box[k], b1[k]);
+                box[3 + k] = fmaxf(box[3 + k], b1[3 + k]);
+            }
+            hi = j + 1;
+            ref = j;
+        }
+    }
+    bool local = true;  // false once the climb has left the block
     for (int step = 0; step <= kMaxDepth; ++step) {
         if (lo == 0 && hi == n - 1) {
             if (!(ref & kLeafBit)) karras_idx[ref] = 0;
@@ -490,29 +659,57 @@ __device__ __forceinline__ void tree_climb(const KeyT* __restrict__ keys, const 
             root_box[7] = 0.f;
             return;
         }
-        const bool left = (lo == 0) || (hi != n - 1 && delta_adj(keys, kbits, hi) > delta_adj(keys, kbits, lo - 1));
+        // delta(hi, hi+1) and delta(lo-1, lo): from shared memory inside the
+        // block's window, -1 past the array's ends
+        const int d_hi = hi + 1 >= n ? -1 : (hi >= B && hi <= E) ? s_d[hi - B + 1] : delta_adj(keys, kbits, hi);
+        const int d_lo = lo == 0 ? -1 : (lo >= B && lo <= E + 1) ? s_d[lo - B] : delta_adj(keys, kbits, lo - 1);
+        const bool left = (lo == 0) || (hi != n - 1 && d_hi > d_lo);
         const uint32_t split = left ? hi : lo - 1;
         if (!(ref & kLeafBit)) karras_idx[ref] = left ? hi : lo;
         const int slot = left ? 0 : 1;
-        float* nd = nodes + 16u * split;
-        float2* b2 = reinterpret_cast<float2*>(nd + 6 * slot);
-        __stcg(b2 + 0, make_float2(box[0], box[1]));
-        __stcg(b2 + 1, make_float2(box[2], box[3]));
-        __stcg(b2 + 2, make_float2(box[4], box[5]));
-        unsigned int* w = reinterpret_cast<unsigned int*>(nd);
-        __stcg(w + 12 + slot, ref);
-        __stcg(w + 14 + slot, left ? lo : hi);
-        // release: this child's slot is visible before the arrival counts;
-        // acquire: the sibling's slot is visible to the second arrival
-        if (atomic_add_acq_rel(counters + split, 1u) == 0u) return;
-        float b[12];
+        const uint32_t far_in = left ? lo : hi;
+        local = local && block_local(split);
+        uint32_t far_end;
+        if (local) {
+            const int ls = (int)(split - B);
 #pragma unroll
-        for (int k = 0; k < 12; ++k) b[k] = __ldcg(nd + k);
-        const uint32_t far_end = __ldcg(w + 14 + (1 - slot));
+            for (int k = 0; k < 6; ++k) s_box[ls][slot][k] = box[k];
+            s_ref[ls][slot] = ref;
+            s_end[ls][slot] = far_in;
+            if (atomic_add_acq_rel_cta(&s_cnt[ls], 1u) == 0u) return;
+            float b[12];
 #pragma unroll
-        for (int k = 0; k < 3; ++k) {
-            box[k] = fminf(b[k], b[6 + k]);
-            box[3 + k] = fmaxf(b[3 + k], b[9 + k]);
+            for (int k = 0; k < 6; ++k) {
+                b[k] = s_box[ls][0][k];
+                b[6 + k] = s_box[ls][1][k];
+            }
+            far_end = s_end[ls][1 - slot];
+            float4* n4 = reinterpret_cast<float4*>(nodes + 16u * split);
+            n4[0] = make_float4(b[0], b[1], b[2], b[3]);
+            n4[1] = make_float4(b[4], b[5], b[6], b[7]);
+            n4[2] = make_float4(b[8], b[9], b[10], b[11]);
+            n4[3] = make_float4(__uint_as_float(s_ref[ls][0]), __uint_as_float(s_ref[ls][1]),
+                                __uint_as_float(s_end[ls][0]), __uint_as_float(s_end[ls][1]));
+#pragma unroll
+            for (int k = 0; k < 3; ++k) {
+                box[k] = fminf(b[k], b[6 + k]);
+                box[3 + k] = fmaxf(b[3 + k], b[9 + k]);
+            }
+        } else {
+            // first node across a block edge: deliver this child; the second
+            // arrival hands the finished node to k_build_tree_top, so that this
+            // block retires instead of waiting on device-scope climbs
+            float* nd_ = nodes + 16u * split;
+            float2* b2 = reinterpret_cast<float2*>(nd_ + 6 * slot);
+            __stcg(b2 + 0, make_float2(box[0], box[1]));
+            __stcg(b2 + 1, make_float2(box[2], box[3]));
+            __stcg(b2 + 2, make_float2(box[4], box[5]));
+            unsigned int* w = reinterpret_cast<unsigned int*>(nd_);
+            __stcg(w + 12 + slot, ref);
+            __stcg(w + 14 + slot, far_in);
+            if (atomic_add_acq_rel(counters + split, 1u) == 0u) return;
+            worklist[atomicAdd(wl_count, 1u)] = split;
+            return;
         }
         if (left) hi = far_end;
         else lo = far_end;
@@ -522,16 +719,39 @@ __device__ __forceinline__ void tree_climb(const KeyT* __restrict__ keys, const 
     clr_raise(CLR_DEVERR_REFIT);
 }
 
+// The nodes across block edges finished by k_build_tree: each continues the
+// device-scope climb from its merged box and range.
 template <typename KeyT>
-__global__ void __launch_bounds__(256) k_build_tree(const KeyT* __restrict__ keys, const uint32_t* __restrict__ sidx,
-                                                    uint32_t n, int kbits, const float* __restrict__ vx,
-                                                    const float* __restrict__ vy, const float* __restrict__ vz,
-                                                    const uint32_t* __restrict__ tri, float* __restrict__ nodes,
-                                                    float4* __restrict__ tris, unsigned int* __restrict__ counters,
-                                                    uint32_t* __restrict__ karras_idx, float* __restrict__ root_box) {
-    const uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
-    if (j >= n) return;
-    tree_climb<KeyT>(keys, sidx, n, kbits, vx, vy, vz, tri, nodes, tris, counters, karras_idx, root_box, j, 0u);
+__global__ void __launch_bounds__(256) k_build_tree_top(const KeyT* __restrict__ keys, uint32_t n, int kbits,
+                                                        float* __restrict__ nodes, unsigned int* __restrict__ counters,
+                                                        uint32_t* __restrict__ karras_idx, float* __restrict__ root_box,
+                                                        const uint32_t* __restrict__ worklist,
+                                                        const unsigned int* __restrict__ wl_count) {
+    const uint32_t cnt = *wl_count;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < cnt; i += gridDim.x * blockDim.x) {
+        const uint32_t split = worklist[i];
+        if (split + 1 >= n) {  // corrupt entry: report, never index out of range
+            clr_raise(CLR_DEVERR_REFIT);
+            continue;
+        }
+        const float* nd = nodes + 16u * split;
+        const unsigned int* w = reinterpret_cast<const unsigned int*>(nd);
+        float b[12];
+#pragma unroll
+        for (int k = 0; k < 12; ++k) b[k] = __ldcg(nd + k);
+        float box[6];
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            box[k] = fminf(b[k], b[6 + k]);
+            box[3 + k] = fmaxf(b[3 + k], b[9 + k]);
+        }
+        const uint32_t lo = __ldcg(w + 14), hi = __ldcg(w + 15);
+        if (lo > hi || hi >= n) {
+            clr_raise(CLR_DEVERR_REFIT);
+            continue;
+        }
+        climb_global<KeyT>(keys, n, kbits, nodes, counters, karras_idx, root_box, lo, hi, split, box);
+    }
 }
 
 // Single-triangle scene: one leaf, no internal node (the reference requires
@@ -764,7 +984,7 @@ static size_t pool_layout(clr_lbvh* h, uint32_t cap, char* base) {
     const size_t o_zero = off;
     const size_t o_hist = take(4ull * kMaxPasses * kRadix);
     const size_t o_status = take(4ull * kMaxPasses * tiles * kRadix);
-    const size_t o_tiles = take(4ull * kMaxPasses);
+    const size_t o_tiles = take(4ull * (kMaxPasses + 1));  // + the tree pass's worklist count
     const size_t o_box = take(4ull * 8);
     if (base) {
         h->keys[0] = base + o_keys0;
@@ -881,10 +1101,17 @@ static int run_build(clr_lbvh* h, const float* vx, const float* vy, const float*
         CLR_LAUNCH_CHECK("k_single");
         timer.done("single");
     } else {
-        k_build_tree<KeyT><<<div_up(n, 256), 256, 0, st>>>(keys[fin], h->vals[fin], n, kbits, vx, vy, vz, tri,
-                                                          reinterpret_cast<float*>(out->nodes), tris, h->counters,
-                                                          h->karras_idx, out->root_box);
+        // worklist of the block-crossing nodes: the sort's free ping-pong side
+        uint32_t* worklist = h->vals[fin ^ 1];
+        unsigned int* wl_count = h->tile_ctr + kMaxPasses;
+        k_build_tree<KeyT><<<div_up(n, kTreeBlock), kTreeBlock, 0, st>>>(
+            keys[fin], h->vals[fin], n, kbits, vx, vy, vz, tri, reinterpret_cast<float*>(out->nodes), tris,
+            h->counters, h->karras_idx, out->root_box, worklist, wl_count);
         CLR_LAUNCH_CHECK("k_build_tree");
+        k_build_tree_top<KeyT><<<kSmCount * 4, 256, 0, st>>>(keys[fin], n, kbits, reinterpret_cast<float*>(out->nodes),
+                                                             h->counters, h->karras_idx, out->root_box, worklist,
+                                                             wl_count);
+        CLR_LAUNCH_CHECK("k_build_tree_top");
         timer.done("build_tree");
     }
     return CLR_OK;
