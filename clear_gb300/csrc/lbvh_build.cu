@@ -443,7 +443,6 @@ __device__ __forceinline__ void climb_global(const KeyT* __restrict__ keys, uint
     // every level up adds at least one common bit of the (3b + 32)-bit key
     for (int step = 0; step <= kMaxDepth; ++step) {
         if (lo == 0 && hi == n - 1) {
-            if (!(ref & kLeafBit)) karras_idx[ref] = 0;
             root_box[0] = box[0]; root_box[1] = box[1]; root_box[2] = box[2];
             root_box[3] = __uint_as_float(ref);
             root_box[4] = box[3]; root_box[5] = box[4]; root_box[6] = box[5];
@@ -452,7 +451,6 @@ __device__ __forceinline__ void climb_global(const KeyT* __restrict__ keys, uint
         }
         const bool left = (lo == 0) || (hi != n - 1 && delta_adj(keys, kbits, hi) > delta_adj(keys, kbits, lo - 1));
         const uint32_t split = left ? hi : lo - 1;
-        if (!(ref & kLeafBit)) karras_idx[ref] = left ? hi : lo;
         const int slot = left ? 0 : 1;
         float* nd = nodes + 16u * split;
         float2* b2 = reinterpret_cast<float2*>(nd + 6 * slot);
@@ -566,74 +564,90 @@ __global__ void __launch_bounds__(kTreeBlock) k_build_tree(const KeyT* __restric
                                                            float* __restrict__ root_box,
                                                            uint32_t* __restrict__ worklist,
                                                            unsigned int* __restrict__ wl_count) {
-    __shared__ int s_d[kTreeBlock + 1];      // delta(k, k+1), k = B-1 .. E
-    __shared__ int s_pmin[kTreeBlock + 1];   // prefix minima of s_d
-    __shared__ int s_smin[kTreeBlock + 1];   // suffix minima of s_d
+    __shared__ int s_d[kTreeBlock + 1];        // delta(k, k+1), k = B-1 .. E
+    __shared__ int s_wmin[2][kTreeBlock / 32];  // per-warp minima of s_d[0..255]
+    __shared__ unsigned char s_local[kTreeBlock];  // node split at B + i lies inside the block
     __shared__ float s_box[kTreeBlock][2][6];
     __shared__ uint32_t s_ref[kTreeBlock][2], s_end[kTreeBlock][2];
     __shared__ unsigned int s_cnt[kTreeBlock];
     const uint32_t B = blockIdx.x * kTreeBlock;
     const uint32_t E = min(B + kTreeBlock - 1, n - 1);
-    const int nd = (int)(E - B) + 2;  // entries of s_d
-    const int t = threadIdx.x;
+    const int nd = (int)(E - B) + 2;  // entries of s_d (<= kTreeBlock + 1)
+    const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
+    constexpr int kBig = 0x7FFFFFFF;
     for (int i = t; i < nd; i += kTreeBlock) {
         const int64_t k = (int64_t)B - 1 + i;
         s_d[i] = (k < 0 || k + 1 >= (int64_t)n) ? -1 : delta_adj(keys, kbits, (uint32_t)k);
     }
     s_cnt[t] = 0u;
     __syncthreads();
-    for (int i = t; i < nd; i += kTreeBlock) {
-        s_pmin[i] = s_d[i];
-        s_smin[i] = s_d[i];
+    // inclusive prefix minimum (pm) and suffix minimum (sm) of s_d[0..255]
+    // by warp shuffles, then across the 8 warps; s_d[256] is the last entry
+    const int v = t < nd ? s_d[t] : kBig;
+    int pm = v, sm = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const int a = __shfl_up_sync(0xFFFFFFFFu, pm, o), b = __shfl_down_sync(0xFFFFFFFFu, sm, o);
+        if (lane >= o) pm = min(pm, a);
+        if (lane + o < 32) sm = min(sm, b);
+    }
+    if (lane == 31) s_wmin[0][warp] = pm;
+    if (lane == 0) s_wmin[1][warp] = sm;
+    __syncthreads();
+    for (int w = 0; w < warp; ++w) pm = min(pm, s_wmin[0][w]);
+    for (int w = warp + 1; w < kTreeBlock / 32; ++w) sm = min(sm, s_wmin[1][w]);
+    if (nd == kTreeBlock + 1) sm = min(sm, s_d[kTreeBlock]);
+    // The node split at s = B + t (s_d index i = t + 1) is inside the block when
+    // min(s_d[0..t]) < s_d[t+1] and min(s_d[t+2..]) < s_d[t+1].  The suffix
+    // minimum from t+2 is thread t+2's value: exchange through shared memory.
+    __shared__ int s_sm[kTreeBlock + 2];
+    s_sm[t] = sm;
+    if (t == 0) {
+        s_sm[kTreeBlock] = nd == kTreeBlock + 1 ? s_d[kTreeBlock] : kBig;
+        s_sm[kTreeBlock + 1] = kBig;
     }
     __syncthreads();
-    // Hillis-Steele scans (nd <= 257: the thread of index 0 also takes entry 256)
-    for (int off = 1; off < nd; off <<= 1) {
-        int pv[2], sv[2];
-        for (int r = 0; r < 2; ++r) {
-            const int i = t + r * kTreeBlock;
-            if (i < nd) {
-                pv[r] = i >= off ? min(s_pmin[i], s_pmin[i - off]) : s_pmin[i];
-                sv[r] = i + off < nd ? min(s_smin[i], s_smin[i + off]) : s_smin[i];
-            }
-        }
-        __syncthreads();
-        for (int r = 0; r < 2; ++r) {
-            const int i = t + r * kTreeBlock;
-            if (i < nd) {
-                s_pmin[i] = pv[r];
-                s_smin[i] = sv[r];
-            }
-        }
-        __syncthreads();
+    if (t + 1 < nd - 1) {  // split B + t < E
+        const int ds = s_d[t + 1];
+        s_local[t] = (pm < ds && s_sm[t + 2] < ds) ? 1 : 0;
     }
+    __syncthreads();
     const uint32_t j = B + t;
-    if (j >= n) return;
-    // split s in [B, E-1] sits at s_d index s - B + 1
     auto block_local = [&](uint32_t split) -> bool {
-        if (split < B || split >= E) return false;
-        const int i = (int)(split - B) + 1;
-        return s_pmin[i - 1] < s_d[i] && s_smin[i + 1] < s_d[i];
+        return split >= B && split < E && s_local[split - B] != 0;
     };
-
-    float box[6];
-    const uint32_t tj = __ldg(sidx + j);
-    emit_leaf(vx, vy, vz, tri, tj, tj, j, tris, box);
+    // leaves: record and box; the box goes to the left neighbour lane, which
+    // merges two adjacent leaves whose parent is their own node (no block
+    // barrier here: a warp climbs while the block's other warps still gather)
+    float box[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+    if (j < n) {
+        const uint32_t tj = __ldg(sidx + j);
+        emit_leaf(vx, vy, vz, tri, tj, tj, j, tris, box);
+    }
+    float nbox[6];
+#pragma unroll
+    for (int k = 0; k < 6; ++k) nbox[k] = __shfl_down_sync(0xFFFFFFFFu, box[k], 1);
+    if (j >= n) return;
     const int dl = s_d[t];      // delta(j-1, j)
     const int dj = s_d[t + 1];  // delta(j, j+1)
     const bool j_left = (j == 0) || (j != n - 1 && dj > dl);
     uint32_t lo = j, hi = j, ref = j | kLeafBit;
     if (j > 0 && !j_left) {
-        const int dll = j > 1 ? delta_adj(keys, kbits, j - 2) : -1;
+        const int dll = j < 2 ? -1 : (t >= 1 ? s_d[t - 1] : delta_adj(keys, kbits, j - 2));
         const bool prev_left = (j - 1 == 0) || (dl > dll);
         if (prev_left) return;  // leaf j-1 builds our common parent
     }
     if (j_left && j + 1 < n) {
-        const int dr = j + 2 < n ? delta_adj(keys, kbits, j + 1) : -1;
+        const int dr = j + 2 >= n ? -1 : (t + 2 < nd ? s_d[t + 2] : delta_adj(keys, kbits, j + 1));
         const bool next_right = (j + 1 == n - 1) || (dr < dj);
         if (next_right) {
             float b1[6];
-            tri_box(vx, vy, vz, tri, __ldg(sidx + j + 1), b1);
+            if (lane < 31) {
+#pragma unroll
+                for (int k = 0; k < 6; ++k) b1[k] = nbox[k];
+            } else {
+                tri_box(vx, vy, vz, tri, __ldg(sidx + j + 1), b1);
+            }
             float4* n4 = reinterpret_cast<float4*>(nodes + 16u * j);
             n4[0] = make_float4(box[0], box[1], box[2], box[3]);
             n4[1] = make_float4(box[4], box[5], b1[0], b1[1]);
@@ -652,7 +666,6 @@ __global__ void __launch_bounds__(kTreeBlock) k_build_tree(const KeyT* __restric
     bool local = true;  // false once the climb has left the block
     for (int step = 0; step <= kMaxDepth; ++step) {
         if (lo == 0 && hi == n - 1) {
-            if (!(ref & kLeafBit)) karras_idx[ref] = 0;
             root_box[0] = box[0]; root_box[1] = box[1]; root_box[2] = box[2];
             root_box[3] = __uint_as_float(ref);
             root_box[4] = box[3]; root_box[5] = box[4]; root_box[6] = box[5];
@@ -665,7 +678,6 @@ __global__ void __launch_bounds__(kTreeBlock) k_build_tree(const KeyT* __restric
         const int d_lo = lo == 0 ? -1 : (lo >= B && lo <= E + 1) ? s_d[lo - B] : delta_adj(keys, kbits, lo - 1);
         const bool left = (lo == 0) || (hi != n - 1 && d_hi > d_lo);
         const uint32_t split = left ? hi : lo - 1;
-        if (!(ref & kLeafBit)) karras_idx[ref] = left ? hi : lo;
         const int slot = left ? 0 : 1;
         const uint32_t far_in = left ? lo : hi;
         local = local && block_local(split);
@@ -766,6 +778,23 @@ __global__ void k_single(const float* vx, const float* vy, const float* vz, cons
 }
 
 // --------------------------------------------------------- reference export
+
+// The reference's index of every internal node, from its parent's slots: a
+// child 0 covers [lo, p] and is indexed by its hi (= the parent's split p), a
+// child 1 covers [p+1, hi] and is indexed by its lo (= p + 1); the root is 0.
+__global__ void k_karras_index(const float4* __restrict__ nodes, const float* __restrict__ root_box, uint32_t n,
+                               uint32_t* __restrict__ karras_idx) {
+    const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p == 0) {
+        const uint32_t root = __float_as_uint(root_box[3]);
+        if (!(root & kLeafBit) && root + 1 < n) karras_idx[root] = 0;
+    }
+    if (p >= n - 1) return;
+    const float4 r = nodes[4u * p + 3];
+    const uint32_t c0 = __float_as_uint(r.x), c1 = __float_as_uint(r.y);
+    if (!(c0 & kLeafBit) && c0 + 1 < n) karras_idx[c0] = p;
+    if (!(c1 & kLeafBit) && c1 + 1 < n) karras_idx[c1] = p + 1;
+}
 
 // Node a (stored at its split position) becomes InternalNode[karras_idx[a]]
 // with children c = {a, a+1}: in the reference's numbering a child-0 internal
@@ -1253,6 +1282,9 @@ extern "C" int clr_lbvh_export_reference(clr_lbvh* h, const clr_bvh* bvh, void* 
                                          static_cast<uint8_t*>(lnodes), parents);
         CLR_LAUNCH_CHECK("k_export_single");
     } else {
+        k_karras_index<<<div_up(n - 1, 256), 256, 0, st>>>(static_cast<const float4*>(bvh->nodes), bvh->root_box, n,
+                                                           h->karras_idx);
+        CLR_LAUNCH_CHECK("k_karras_index");
         k_export<<<div_up(n - 1, 256), 256, 0, st>>>(static_cast<const float4*>(bvh->nodes),
                                                      static_cast<const float4*>(bvh->tris), h->karras_idx, n,
                                                      static_cast<uint8_t*>(inodes), static_cast<uint8_t*>(lnodes),
