@@ -56,12 +56,13 @@ WORKLOAD = "lbvh-build+traversal, 16Mi random triangles (30-bit Morton), 16Mi cl
 # build kernel; see DESIGN.md "Roofline".
 ALGO_BYTES = {
     "scene_box": 36.0,          # read 9 floats per triangle
-    "morton": 40.0,             # read 9 floats, write one 4-byte key
+    "morton": 108.0,            # read 9 floats; write a 4-byte key, the 64-byte staging record, the 4-byte counter
     "sort_pass_first": 12.0,    # read key, write key + index
     "sort_pass": 16.0,          # read key + index, write key + index
-    # per triangle: leaf (index 4, vertex gather 36, record 48, box+ref+end into the parent slot 32)
-    # + internal node (2 adjacent keys 8, both slots 64, counter RMW 8, own slot 32, index 4)
-    "build_tree": 236.0,
+    # per triangle: sorted index 4, its key 4, its 3 vertices 36, its 48-byte record,
+    # and one 64-byte internal node (n - 1 of them); child slots of nodes inside
+    # a block live in shared memory
+    "build_tree": 156.0,
 }
 
 

@@ -70,6 +70,17 @@ __device__ __forceinline__ uint64_t make_key<uint64_t>(uint32_t qx, uint32_t qy,
     return spread3_21(qx) | (spread3_21(qy) << 1) | (spread3_21(qz) << 2);
 }
 
+// 64-byte staging record of triangle t in input order: p0, p1, p2 as float4
+// and a zero pad, so that the tree pass gathers one DRAM atom per leaf
+// instead of three scattered 12-byte runs of the SoA arrays.
+__device__ __forceinline__ void stage_tri(float4* stage, uint32_t t, const float P[3][3]) {
+    float4* r = stage + 4ull * t;
+    r[0] = make_float4(P[0][0], P[0][1], P[0][2], 0.f);
+    r[1] = make_float4(P[1][0], P[1][1], P[1][2], 0.f);
+    r[2] = make_float4(P[2][0], P[2][1], P[2][2], 0.f);
+    r[3] = make_float4(0.f, 0.f, 0.f, 0.f);
+}
+
 __device__ __forceinline__ uint32_t tri_vertex(const uint32_t* tri, uint32_t t, uint32_t k) {
     return tri ? __ldg(tri + 3u * t + k) : 3u * t + k;
 }
@@ -146,7 +157,8 @@ __global__ void __launch_bounds__(256) k_morton(const float* __restrict__ vx, co
                                                 const float* __restrict__ vz, const uint32_t* __restrict__ tri,
                                                 uint32_t n, uint32_t bits, const unsigned int* __restrict__ boxw,
                                                 KeyT* __restrict__ keys, unsigned int* __restrict__ hist,
-                                                int npasses, unsigned int* __restrict__ counters) {
+                                                int npasses, unsigned int* __restrict__ counters,
+                                                float4* __restrict__ stage) {
     __shared__ unsigned int sh[kMaxPasses * kRadix];
     for (int i = threadIdx.x; i < npasses * kRadix; i += blockDim.x) sh[i] = 0;
     float smin[3], ssize[3];
@@ -171,6 +183,7 @@ __global__ void __launch_bounds__(256) k_morton(const float* __restrict__ vx, co
         }
         const KeyT key = make_key<KeyT>(q[0], q[1], q[2]);
         keys[t] = key;
+        if (stage) stage_tri(stage, t, P);
         if (t + 1 < n) counters[t] = 0u;  // arrival counters of the tree pass
         for (int p = 0; p < npasses; ++p) atomicAdd(&sh[p * kRadix + (uint32_t)((key >> (8 * p)) & 0xFFu)], 1u);
     }
@@ -366,6 +379,11 @@ struct TriVerts {
     float p[3][3];
 };
 
+// Triangle t's vertices: from its 64-byte staging record (p0, p1, p2 as three
+// float4, one DRAM atom) when the build staged them, else from the SoA arrays.
+__device__ __forceinline__ TriVerts load_tri_staged(const float* vx, const float* vy, const float* vz,
+                                                    const uint32_t* tri, const float4* stage, uint32_t t);
+
 __device__ __forceinline__ TriVerts load_tri(const float* vx, const float* vy, const float* vz,
                                              const uint32_t* tri, uint32_t t) {
     TriVerts tv;
@@ -378,12 +396,24 @@ __device__ __forceinline__ TriVerts load_tri(const float* vx, const float* vy, c
     return tv;
 }
 
+__device__ __forceinline__ TriVerts load_tri_staged(const float* vx, const float* vy, const float* vz,
+                                                    const uint32_t* tri, const float4* stage, uint32_t t) {
+    if (stage == nullptr) return load_tri(vx, vy, vz, tri, t);
+    const float4 a = __ldg(stage + 4ull * t), b = __ldg(stage + 4ull * t + 1), c = __ldg(stage + 4ull * t + 2);
+    TriVerts tv;
+    tv.p[0][0] = a.x; tv.p[0][1] = a.y; tv.p[0][2] = a.z;
+    tv.p[1][0] = b.x; tv.p[1][1] = b.y; tv.p[1][2] = b.z;
+    tv.p[2][0] = c.x; tv.p[2][1] = c.y; tv.p[2][2] = c.z;
+    return tv;
+}
+
+
 // Writes leaf `leaf`'s triangle record and returns its box (calcAABBs).
 // `tid` indexes the (global) vertex arrays, `rec_id` is the id recorded.
 __device__ __forceinline__ void emit_leaf(const float* vx, const float* vy, const float* vz, const uint32_t* tri,
-                                          uint32_t tid, uint32_t rec_id, uint32_t leaf, float4* __restrict__ tris,
-                                          float box[6]) {
-    const TriVerts tv = load_tri(vx, vy, vz, tri, tid);
+                                          const float4* stage, uint32_t tid, uint32_t rec_id, uint32_t leaf,
+                                          float4* __restrict__ tris, float box[6]) {
+    const TriVerts tv = load_tri_staged(vx, vy, vz, tri, stage, tid);
     for (int k = 0; k < 3; ++k) {
         box[k] = fminf(tv.p[0][k], fminf(tv.p[1][k], tv.p[2][k]));
         box[3 + k] = fmaxf(tv.p[0][k], fmaxf(tv.p[1][k], tv.p[2][k]));
@@ -424,8 +454,8 @@ __device__ __forceinline__ unsigned int atomic_add_acq_rel(unsigned int* p, unsi
 }
 
 __device__ __forceinline__ void tri_box(const float* vx, const float* vy, const float* vz, const uint32_t* tri,
-                                        uint32_t t, float box[6]) {
-    const TriVerts tv = load_tri(vx, vy, vz, tri, t);
+                                        const float4* stage, uint32_t t, float box[6]) {
+    const TriVerts tv = load_tri_staged(vx, vy, vz, tri, stage, t);
     for (int k = 0; k < 3; ++k) {
         box[k] = fminf(tv.p[0][k], fminf(tv.p[1][k], tv.p[2][k]));
         box[3 + k] = fmaxf(tv.p[0][k], fmaxf(tv.p[1][k], tv.p[2][k]));
@@ -487,13 +517,14 @@ template <typename KeyT>
 __device__ __forceinline__ void tree_climb(const KeyT* __restrict__ keys, const uint32_t* __restrict__ sidx,
                                            uint32_t n, int kbits, const float* __restrict__ vx,
                                            const float* __restrict__ vy, const float* __restrict__ vz,
-                                           const uint32_t* __restrict__ tri, float* __restrict__ nodes,
+                                           const uint32_t* __restrict__ tri, const float4* __restrict__ stage,
+                                           float* __restrict__ nodes,
                                            float4* __restrict__ tris, unsigned int* __restrict__ counters,
                                            uint32_t* __restrict__ karras_idx, float* __restrict__ root_box,
                                            uint32_t j, uint32_t id_base) {
     float box[6];
     const uint32_t tj = __ldg(sidx + j);
-    emit_leaf(vx, vy, vz, tri, tj, tj - id_base, j, tris, box);
+    emit_leaf(vx, vy, vz, tri, stage, tj, tj - id_base, j, tris, box);
     // adjacent deltas around leaf j (-1 outside the array)
     const int dl = j > 0 ? delta_adj(keys, kbits, j - 1) : -1;
     const int dj = j + 1 < n ? delta_adj(keys, kbits, j) : -1;
@@ -511,7 +542,7 @@ __device__ __forceinline__ void tree_climb(const KeyT* __restrict__ keys, const 
         const bool next_right = (j + 1 == n - 1) || (dr < dj);
         if (next_right) {
             float b1[6];
-            tri_box(vx, vy, vz, tri, __ldg(sidx + j + 1), b1);
+            tri_box(vx, vy, vz, tri, stage, __ldg(sidx + j + 1), b1);
             float* nd = nodes + 16u * j;
             float4* n4 = reinterpret_cast<float4*>(nd);
             n4[0] = make_float4(box[0], box[1], box[2], box[3]);
@@ -558,22 +589,24 @@ __global__ void __launch_bounds__(kTreeBlock) k_build_tree(const KeyT* __restric
                                                            const uint32_t* __restrict__ sidx, uint32_t n, int kbits,
                                                            const float* __restrict__ vx, const float* __restrict__ vy,
                                                            const float* __restrict__ vz, const uint32_t* __restrict__ tri,
+                                                           const float4* __restrict__ stage,
                                                            float* __restrict__ nodes, float4* __restrict__ tris,
                                                            unsigned int* __restrict__ counters,
                                                            uint32_t* __restrict__ karras_idx,
                                                            float* __restrict__ root_box,
                                                            uint32_t* __restrict__ worklist,
                                                            unsigned int* __restrict__ wl_count) {
-    __shared__ int s_d[kTreeBlock + 1];        // delta(k, k+1), k = B-1 .. E
-    __shared__ int s_wmin[2][kTreeBlock / 32];  // per-warp minima of s_d[0..255]
+    __shared__ int s_d[kTreeBlock + 1];           // delta(k, k+1), k = B-1 .. E
+    __shared__ int s_wmin[3][kTreeBlock / 32];     // per warp: prefix min, suffix min from lanes 0 and 1
     __shared__ unsigned char s_local[kTreeBlock];  // node split at B + i lies inside the block
-    __shared__ float s_box[kTreeBlock][2][6];
-    __shared__ uint32_t s_ref[kTreeBlock][2], s_end[kTreeBlock][2];
+    // child slots of the block's nodes: {box min xyz, box max x}, {box max yz, ref, far end}
+    __shared__ __align__(16) float4 s_slot[kTreeBlock][2][2];
     __shared__ unsigned int s_cnt[kTreeBlock];
     const uint32_t B = blockIdx.x * kTreeBlock;
     const uint32_t E = min(B + kTreeBlock - 1, n - 1);
     const int nd = (int)(E - B) + 2;  // entries of s_d (<= kTreeBlock + 1)
     const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
+    const uint32_t j = B + t;
     constexpr int kBig = 0x7FFFFFFF;
     for (int i = t; i < nd; i += kTreeBlock) {
         const int64_t k = (int64_t)B - 1 + i;
@@ -581,8 +614,8 @@ __global__ void __launch_bounds__(kTreeBlock) k_build_tree(const KeyT* __restric
     }
     s_cnt[t] = 0u;
     __syncthreads();
-    // inclusive prefix minimum (pm) and suffix minimum (sm) of s_d[0..255]
-    // by warp shuffles, then across the 8 warps; s_d[256] is the last entry
+    // prefix minimum pm = min(s_d[0..t]) and the suffix minimum from t+2,
+    // by warp shuffles and per-warp minima; s_d[256] (if present) is last
     const int v = t < nd ? s_d[t] : kBig;
     int pm = v, sm = v;
 #pragma unroll
@@ -591,38 +624,44 @@ __global__ void __launch_bounds__(kTreeBlock) k_build_tree(const KeyT* __restric
         if (lane >= o) pm = min(pm, a);
         if (lane + o < 32) sm = min(sm, b);
     }
+    const int sm2 = __shfl_down_sync(0xFFFFFFFFu, sm, 2);
     if (lane == 31) s_wmin[0][warp] = pm;
     if (lane == 0) s_wmin[1][warp] = sm;
+    if (lane == 1) s_wmin[2][warp] = sm;
     __syncthreads();
     for (int w = 0; w < warp; ++w) pm = min(pm, s_wmin[0][w]);
-    for (int w = warp + 1; w < kTreeBlock / 32; ++w) sm = min(sm, s_wmin[1][w]);
-    if (nd == kTreeBlock + 1) sm = min(sm, s_d[kTreeBlock]);
-    // The node split at s = B + t (s_d index i = t + 1) is inside the block when
-    // min(s_d[0..t]) < s_d[t+1] and min(s_d[t+2..]) < s_d[t+1].  The suffix
-    // minimum from t+2 is thread t+2's value: exchange through shared memory.
-    __shared__ int s_sm[kTreeBlock + 2];
-    s_sm[t] = sm;
-    if (t == 0) {
-        s_sm[kTreeBlock] = nd == kTreeBlock + 1 ? s_d[kTreeBlock] : kBig;
-        s_sm[kTreeBlock + 1] = kBig;
+    const int tail = nd == kTreeBlock + 1 ? s_d[kTreeBlock] : kBig;
+    int after = tail;  // min of s_d over the warps after this one
+    for (int w = warp + 1; w < kTreeBlock / 32; ++w) after = min(after, s_wmin[1][w]);
+    int s2;  // min(s_d[t+2 ..])
+    if (lane < 30) {
+        s2 = min(sm2, after);
+    } else if (lane == 30) {
+        s2 = after;
+    } else if (warp + 1 < kTreeBlock / 32) {
+        int after2 = tail;
+        for (int w = warp + 2; w < kTreeBlock / 32; ++w) after2 = min(after2, s_wmin[1][w]);
+        s2 = min(s_wmin[2][warp + 1], after2);
+    } else {
+        s2 = kBig;
     }
-    __syncthreads();
-    if (t + 1 < nd - 1) {  // split B + t < E
+    // the node split at B + t (s_d index t + 1) lies inside the block when a
+    // smaller delta bounds it on both sides within the block's window
+    if (t + 1 < nd - 1) {
         const int ds = s_d[t + 1];
-        s_local[t] = (pm < ds && s_sm[t + 2] < ds) ? 1 : 0;
+        s_local[t] = (pm < ds && s2 < ds) ? 1 : 0;
     }
     __syncthreads();
-    const uint32_t j = B + t;
     auto block_local = [&](uint32_t split) -> bool {
         return split >= B && split < E && s_local[split - B] != 0;
     };
     // leaves: record and box; the box goes to the left neighbour lane, which
     // merges two adjacent leaves whose parent is their own node (no block
-    // barrier here: a warp climbs while the block's other warps still gather)
+    // barrier after this: a warp climbs while the block's other warps gather)
     float box[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
     if (j < n) {
         const uint32_t tj = __ldg(sidx + j);
-        emit_leaf(vx, vy, vz, tri, tj, tj, j, tris, box);
+        emit_leaf(vx, vy, vz, tri, stage, tj, tj, j, tris, box);
     }
     float nbox[6];
 #pragma unroll
@@ -646,7 +685,7 @@ __global__ void __launch_bounds__(kTreeBlock) k_build_tree(const KeyT* __restric
 #pragma unroll
                 for (int k = 0; k < 6; ++k) b1[k] = nbox[k];
             } else {
-                tri_box(vx, vy, vz, tri, __ldg(sidx + j + 1), b1);
+                tri_box(vx, vy, vz, tri, stage, __ldg(sidx + j + 1), b1);
             }
             float4* n4 = reinterpret_cast<float4*>(nodes + 16u * j);
             n4[0] = make_float4(box[0], box[1], box[2], box[3]);
@@ -684,29 +723,23 @@ __global__ void __launch_bounds__(kTreeBlock) k_build_tree(const KeyT* __restric
         uint32_t far_end;
         if (local) {
             const int ls = (int)(split - B);
-#pragma unroll
-            for (int k = 0; k < 6; ++k) s_box[ls][slot][k] = box[k];
-            s_ref[ls][slot] = ref;
-            s_end[ls][slot] = far_in;
+            s_slot[ls][slot][0] = make_float4(box[0], box[1], box[2], box[3]);
+            s_slot[ls][slot][1] = make_float4(box[4], box[5], __uint_as_float(ref), __uint_as_float(far_in));
             if (atomic_add_acq_rel_cta(&s_cnt[ls], 1u) == 0u) return;
-            float b[12];
-#pragma unroll
-            for (int k = 0; k < 6; ++k) {
-                b[k] = s_box[ls][0][k];
-                b[6 + k] = s_box[ls][1][k];
-            }
-            far_end = s_end[ls][1 - slot];
+            const float4 a0 = s_slot[ls][0][0], a1 = s_slot[ls][0][1];
+            const float4 c0 = s_slot[ls][1][0], c1 = s_slot[ls][1][1];
+            far_end = __float_as_uint(slot == 0 ? c1.w : a1.w);
             float4* n4 = reinterpret_cast<float4*>(nodes + 16u * split);
-            n4[0] = make_float4(b[0], b[1], b[2], b[3]);
-            n4[1] = make_float4(b[4], b[5], b[6], b[7]);
-            n4[2] = make_float4(b[8], b[9], b[10], b[11]);
-            n4[3] = make_float4(__uint_as_float(s_ref[ls][0]), __uint_as_float(s_ref[ls][1]),
-                                __uint_as_float(s_end[ls][0]), __uint_as_float(s_end[ls][1]));
-#pragma unroll
-            for (int k = 0; k < 3; ++k) {
-                box[k] = fminf(b[k], b[6 + k]);
-                box[3 + k] = fmaxf(b[3 + k], b[9 + k]);
-            }
+            n4[0] = a0;
+            n4[1] = make_float4(a1.x, a1.y, c0.x, c0.y);
+            n4[2] = make_float4(c0.z, c0.w, c1.x, c1.y);
+            n4[3] = make_float4(a1.z, c1.z, a1.w, c1.w);
+            box[0] = fminf(a0.x, c0.x);
+            box[1] = fminf(a0.y, c0.y);
+            box[2] = fminf(a0.z, c0.z);
+            box[3] = fmaxf(a0.w, c0.w);
+            box[4] = fmaxf(a1.x, c1.x);
+            box[5] = fmaxf(a1.y, c1.y);
         } else {
             // first node across a block edge: deliver this child; the second
             // arrival hands the finished node to k_build_tree_top, so that this
@@ -771,7 +804,7 @@ __global__ void __launch_bounds__(256) k_build_tree_top(const KeyT* __restrict__
 __global__ void k_single(const float* vx, const float* vy, const float* vz, const uint32_t* tri, float4* tris,
                          float* root_box) {
     float box[6];
-    emit_leaf(vx, vy, vz, tri, 0u, 0u, 0u, tris, box);
+    emit_leaf(vx, vy, vz, tri, nullptr, 0u, 0u, 0u, tris, box);
     for (int k = 0; k < 3; ++k) { root_box[k] = box[k]; root_box[4 + k] = box[3 + k]; }
     root_box[3] = __uint_as_float(kLeafBit);
     root_box[7] = 0.f;
@@ -939,7 +972,8 @@ __global__ void __launch_bounds__(256) k_morton_seg(const float* __restrict__ vx
                                                     const uint32_t* __restrict__ off, uint32_t nseg, uint32_t n,
                                                     uint32_t bits, const unsigned int* __restrict__ boxw,
                                                     uint64_t* __restrict__ keys, unsigned int* __restrict__ hist,
-                                                    int npasses, unsigned int* __restrict__ counters) {
+                                                    int npasses, unsigned int* __restrict__ counters,
+                                                    float4* __restrict__ stage) {
     constexpr uint32_t kMask = (1u << kBits) - 1u;
     __shared__ unsigned int sh[kMaxPasses * kRadix];
     for (int i = threadIdx.x; i < npasses * kRadix; i += blockDim.x) sh[i] = 0;
@@ -962,6 +996,7 @@ __global__ void __launch_bounds__(256) k_morton_seg(const float* __restrict__ vx
         }
         const uint64_t key = ((uint64_t)s << (3 * bits)) | make_key<uint64_t>(q[0], q[1], q[2]);
         keys[t] = key;
+        if (stage) stage_tri(stage, t, tv.p);
         counters[t] = 0u;
         for (int p = 0; p < npasses; ++p) atomicAdd(&sh[p * kRadix + (uint32_t)((key >> (kBits * p)) & kMask)], 1u);
     }
@@ -977,7 +1012,8 @@ __global__ void __launch_bounds__(256) k_build_tree_seg(const KeyT* __restrict__
                                                         const uint32_t* __restrict__ off, uint32_t nseg, uint32_t n,
                                                         int kbits, const float* __restrict__ vx,
                                                         const float* __restrict__ vy, const float* __restrict__ vz,
-                                                        const uint32_t* __restrict__ tri, float* __restrict__ nodes,
+                                                        const uint32_t* __restrict__ tri,
+                                                        const float4* __restrict__ stage, float* __restrict__ nodes,
                                                         float4* __restrict__ tris, unsigned int* __restrict__ counters,
                                                         uint32_t* __restrict__ karras_idx,
                                                         float* __restrict__ root_boxes) {
@@ -985,7 +1021,7 @@ __global__ void __launch_bounds__(256) k_build_tree_seg(const KeyT* __restrict__
     if (j >= n) return;
     const uint32_t s = seg_of(off, nseg, j);
     const uint32_t s0 = __ldg(off + s), ns = __ldg(off + s + 1) - s0;
-    tree_climb<KeyT>(keys + s0, sidx + s0, ns, kbits, vx, vy, vz, tri, nodes + 16ull * s0, tris + 3ull * s0,
+    tree_climb<KeyT>(keys + s0, sidx + s0, ns, kbits, vx, vy, vz, tri, stage, nodes + 16ull * s0, tris + 3ull * s0,
                      counters + s0, karras_idx + s0, root_boxes + 8ull * s, j - s0, s0);
 }
 
@@ -999,7 +1035,7 @@ static size_t align_up(size_t v, size_t a) { return (v + a - 1) / a * a; }
 
 // Lays the scratch pool out for `cap` triangles.  Returns its size; assigns
 // the handle's pointers when `base` is non-NULL.
-static size_t pool_layout(clr_lbvh* h, uint32_t cap, char* base) {
+static size_t pool_layout(clr_lbvh* h, uint32_t cap, char* base, bool stage = true) {
     const size_t tiles = div_up(cap ? cap : 1, kMinSortTile) + 1;
     size_t off = 0;
     auto take = [&](size_t bytes) {
@@ -1010,6 +1046,7 @@ static size_t pool_layout(clr_lbvh* h, uint32_t cap, char* base) {
     const size_t o_keys0 = take(8ull * cap), o_keys1 = take(8ull * cap);
     const size_t o_vals0 = take(4ull * cap), o_vals1 = take(4ull * cap);
     const size_t o_kidx = take(4ull * cap), o_cnt = take(4ull * cap);
+    const size_t o_stage = stage ? take(64ull * cap) : 0;
     const size_t o_zero = off;
     const size_t o_hist = take(4ull * kMaxPasses * kRadix);
     const size_t o_status = take(4ull * kMaxPasses * tiles * kRadix);
@@ -1021,6 +1058,7 @@ static size_t pool_layout(clr_lbvh* h, uint32_t cap, char* base) {
         h->vals[0] = reinterpret_cast<uint32_t*>(base + o_vals0);
         h->vals[1] = reinterpret_cast<uint32_t*>(base + o_vals1);
         h->karras_idx = reinterpret_cast<uint32_t*>(base + o_kidx);
+        h->stage = stage ? reinterpret_cast<float4*>(base + o_stage) : nullptr;
         h->counters = reinterpret_cast<unsigned int*>(base + o_cnt);
         h->zero_region = base + o_zero;
         h->zero_bytes = off - o_zero;
@@ -1104,7 +1142,7 @@ static int run_build(clr_lbvh* h, const float* vx, const float* vy, const float*
     timer.done("scene_box");
     KeyT* keys[2] = {static_cast<KeyT*>(h->keys[0]), static_cast<KeyT*>(h->keys[1])};
     k_morton<KeyT><<<grid_stream, 256, 0, st>>>(vx, vy, vz, tri, n, bits, h->boxw, keys[0], h->hist, npasses,
-                                                          h->counters);
+                                                h->counters, h->stage);
     CLR_LAUNCH_CHECK("k_morton");
     timer.done("morton");
     constexpr int kTile = kSortThreads * SortCfg<KeyT>::kItems;
@@ -1134,7 +1172,7 @@ static int run_build(clr_lbvh* h, const float* vx, const float* vy, const float*
         uint32_t* worklist = h->vals[fin ^ 1];
         unsigned int* wl_count = h->tile_ctr + kMaxPasses;
         k_build_tree<KeyT><<<div_up(n, kTreeBlock), kTreeBlock, 0, st>>>(
-            keys[fin], h->vals[fin], n, kbits, vx, vy, vz, tri, reinterpret_cast<float*>(out->nodes), tris,
+            keys[fin], h->vals[fin], n, kbits, vx, vy, vz, tri, h->stage, reinterpret_cast<float*>(out->nodes), tris,
             h->counters, h->karras_idx, out->root_box, worklist, wl_count);
         CLR_LAUNCH_CHECK("k_build_tree");
         k_build_tree_top<KeyT><<<kSmCount * 4, 256, 0, st>>>(keys[fin], n, kbits, reinterpret_cast<float*>(out->nodes),
@@ -1241,13 +1279,13 @@ extern "C" int clr_lbvh_build_batched(clr_lbvh* h, const float* vx, const float*
     const int grid_stream = kSmCount * 8;
     if (radix_bits == 8)
         k_morton_seg<8><<<grid_stream, 256, 0, st>>>(vx, vy, vz, tri, h->seg_off, num_scenes, n, bits_per_dim,
-                                                     h->seg_box, keys[0], h->hist, npasses, h->counters);
+                                                     h->seg_box, keys[0], h->hist, npasses, h->counters, h->stage);
     else if (radix_bits == 7)
         k_morton_seg<7><<<grid_stream, 256, 0, st>>>(vx, vy, vz, tri, h->seg_off, num_scenes, n, bits_per_dim,
-                                                     h->seg_box, keys[0], h->hist, npasses, h->counters);
+                                                     h->seg_box, keys[0], h->hist, npasses, h->counters, h->stage);
     else
         k_morton_seg<6><<<grid_stream, 256, 0, st>>>(vx, vy, vz, tri, h->seg_off, num_scenes, n, bits_per_dim,
-                                                     h->seg_box, keys[0], h->hist, npasses, h->counters);
+                                                     h->seg_box, keys[0], h->hist, npasses, h->counters, h->stage);
     CLR_LAUNCH_CHECK("k_morton_seg");
     timer.done("morton");
     constexpr int kTile = kSortThreads * SortCfg<uint64_t>::kItems;
@@ -1263,7 +1301,7 @@ extern "C" int clr_lbvh_build_batched(clr_lbvh* h, const float* vx, const float*
     const int fin = npasses & 1;
     h->final_buf = fin;
     k_build_tree_seg<uint64_t><<<div_up(n, 256), 256, 0, st>>>(
-        keys[fin], h->vals[fin], h->seg_off, num_scenes, n, kbits, vx, vy, vz, tri, static_cast<float*>(nodes),
+        keys[fin], h->vals[fin], h->seg_off, num_scenes, n, kbits, vx, vy, vz, tri, h->stage, static_cast<float*>(nodes),
         static_cast<float4*>(tris), h->counters, h->karras_idx, root_boxes);
     CLR_LAUNCH_CHECK("k_build_tree_seg");
     timer.done("build_tree");
@@ -1383,9 +1421,9 @@ extern "C" int clr_lbvh_build_noalloc(const float* vx, const float* vy, const fl
     int rc = noalloc_scratch(&base);
     if (rc != CLR_OK) return rc;
     clr_lbvh h{};
-    if (pool_layout(&h, kNoAllocMaxTris, nullptr) > kNoAllocScratchBytes)
+    if (pool_layout(&h, kNoAllocMaxTris, nullptr, false) > kNoAllocScratchBytes)
         return clr_set_error(CLR_ECAPACITY, "clr_lbvh_build_noalloc: scratch layout exceeds the static array");
-    pool_layout(&h, kNoAllocMaxTris, static_cast<char*>(base));
+    pool_layout(&h, kNoAllocMaxTris, static_cast<char*>(base), false);
     h.capacity = kNoAllocMaxTris;
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     if (bits_per_dim <= 10) return run_build<uint32_t>(&h, vx, vy, vz, tri, num_tris, bits_per_dim, out, st);
