@@ -216,7 +216,7 @@ def bench_render(dev, args) -> dict:
     return out
 
 
-def bench_render_terrain(dev, spp=4) -> dict:
+def bench_render_terrain(dev, spp=64) -> dict:
     """Wavefront vs megakernel on the large scene: 2.23 M triangles
     (1024^2 heightfield + 256 spheres), 1024 x 512 sky, 8 bump-mapped
     materials, thin lens 0.02 / 1.5, 1920 x 1080, depth 8; `spp` samples per
@@ -229,7 +229,8 @@ def bench_render_terrain(dev, spp=4) -> dict:
     sc = scenes.terrain_scene()
     ds = DeviceScene(sc, dev)
     w, h = sc.width, sc.height
-    out = {"workload": "terrain 2.23M tris, 1920x1080, depth 8, thin lens", "spp": spp, "samples": w * h * spp}
+    out = {"workload": f"terrain 2.23M tris, 1920x1080, {spp} spp, depth 8, thin lens", "spp": spp,
+           "samples": w * h * spp}
     stream = torch.cuda.current_stream(dev)
     for name, ordered, wf in (("megakernel_ordered", True, False), ("wavefront_exact", False, True),
                               ("wavefront_ordered", True, True)):
