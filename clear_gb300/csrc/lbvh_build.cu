@@ -225,7 +225,7 @@ struct SortCfg<uint64_t> { static constexpr int kItems = 8; };
 
 // kBits-bit digits (6, 7 or 8); the per-digit arrays keep a 256 stride.
 template <typename KeyT, bool kFirst, int kBits = 8>
-__global__ void __launch_bounds__(kSortThreads) k_onesweep(const KeyT* __restrict__ kin,
+__global__ void __launch_bounds__(kSortThreads, 4) k_onesweep(const KeyT* __restrict__ kin,
                                                            const uint32_t* __restrict__ vin,
                                                            KeyT* __restrict__ kout, uint32_t* __restrict__ vout,
                                                            uint32_t n, uint32_t shift,
