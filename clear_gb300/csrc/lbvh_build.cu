@@ -276,7 +276,16 @@ __global__ void __launch_bounds__(kSortThreads, 4) k_onesweep(const KeyT* __rest
         const uint32_t idx = wbase + i * 32 + lane;
         const bool ok = idx < n;
         const unsigned int dig = ok ? (unsigned int)((k[i] >> shift) & kDigitMask) : 0xFFFFFFFFu;
-        const unsigned int peers = __match_any_sync(0xFFFFFFFFu, dig);
+        // lanes holding the same digit: one ballot per digit bit (and one for
+        // validity), AND-combined -- the ballot form of match.any
+        unsigned int peers = __ballot_sync(0xFFFFFFFFu, ok);
+        if (!ok) peers = ~peers;
+#pragma unroll
+        for (int b = 0; b < kBits; ++b) {
+            const bool bit = (dig >> b) & 1u;
+            const unsigned int bal = __ballot_sync(0xFFFFFFFFu, bit);
+            peers &= bit ? bal : ~bal;
+        }
         const int leader = __ffs(peers) - 1;
         unsigned int old = 0;
         if (ok && lane == leader) {
