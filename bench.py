@@ -245,6 +245,30 @@ def bench_render_terrain(dev, spp=64) -> dict:
         ms = e0.elapsed_time(e1)
         out[f"{name}_ms"] = ms
         out[f"{name}_msamples_s"] = w * h * spp / ms / 1e3
+    # the steps either side of the path on the same scene: the 8-bit tone map
+    # of the image (16 B read + 3 B written per pixel) and the rebuild of the
+    # sky's importance distribution (8 B read + 8 B written per texel)
+    from clear_gb300 import postprocess as PP
+
+    peak, _ = measured_peaks()
+    reps = 20
+    e0, e1, e2 = (torch.cuda.Event(enable_timing=True) for _ in range(3))
+    PP.to_ldr(pix, w, h, spp)
+    ds.update_env_distribution()
+    torch.cuda.synchronize()
+    e0.record(stream)
+    for _ in range(reps):
+        PP.to_ldr(pix, w, h, spp)
+    e1.record(stream)
+    for _ in range(reps):
+        ds.update_env_distribution()
+    e2.record(stream)
+    torch.cuda.synchronize()
+    tm_us = 1e3 * e0.elapsed_time(e1) / reps
+    env_us = 1e3 * e1.elapsed_time(e2) / reps
+    ew, eh = ds.env_dist["width"], ds.env_dist["height"]
+    out["tonemap"] = {"us": tm_us, "gbs": 19 * w * h / tm_us / 1e3, "frac_of_hbm": 19 * w * h / tm_us / 1e3 / peak}
+    out["env_distribution"] = {"texels": ew * eh, "us": env_us, "gbs": 16 * ew * eh / env_us / 1e3}
     return out
 
 

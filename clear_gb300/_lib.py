@@ -19,6 +19,7 @@ DEVERR_SORT_TIMEOUT = 0x1
 DEVERR_STACK = 0x2
 DEVERR_REFIT = 0x4
 DEVERR_QUEUE = 0x8
+DEVERR_INPUT = 0x10
 NODE_BYTES = 64
 TRI_BYTES = 48
 REF_NODE_BYTES = 48
@@ -88,6 +89,8 @@ def lib() -> C.CDLL:
             "clr_batch_get_config": [vp, vp],
             "clr_batch_pixels": [vp, C.POINTER(u32)],
             "clr_batch_render": [vp, vp, vp, u32, u32, u32, vp],
+            "clr_postprocess_ldr": [vp, u32, u32, u32, vp, vp],
+            "clr_env_distribution_update": [vp, u32, vp, u32, u32, vp, vp],
             "clr_lbvh_pass_times": [vp, C.POINTER(C.c_float), C.POINTER(C.c_char_p), i32, C.POINTER(i32)],
         }
         for name, args in sig.items():

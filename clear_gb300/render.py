@@ -4,6 +4,7 @@ calls ``clr_render`` (the counterpart of enqueueing the reference's
 from __future__ import annotations
 
 import ctypes as C
+import math
 
 import numpy as np
 import torch
@@ -35,6 +36,7 @@ class DeviceScene:
         self.device = torch.device(device)
         b = scene.blobs()
         self.blobs = b
+        self.env_dist = getattr(scene, "env_dist", None)
         self.width, self.height = scene.width, scene.height
         self.t = {k: _dev(b[k], self.device) for k in ("vertices", "normals", "tangents", "uvs", "faces", "lights",
                                                         "materials", "textures", "others")}
@@ -107,6 +109,30 @@ class DeviceScene:
             off = (-buf.data_ptr()) % 256
             self._aws = buf[off:off + int(n.value)]
         return self._aws
+
+    def env_row_weights(self) -> torch.Tensor:
+        """The zenith correction of each environment row as the scene encoder
+        computes it (cos(pi (0.5 - (i + 0.5) / h)), rounded to float)."""
+        h = self.env_dist["height"]
+        w = np.array([math.cos(math.pi * (0.5 - (i + 0.5) / h)) for i in range(h)], dtype=np.float32)
+        return torch.from_numpy(w).to(self.device)
+
+    def update_env_distribution(self, row_weight: torch.Tensor | None = None, encoder_weights: bool = True) -> None:
+        """Rebuilds the environment light's importance distribution on the
+        device from the environment texels now in the textures blob (after an
+        optimisation step changed them).  With encoder_weights the row weights
+        are the scene encoder's, so the result equals re-encoding the scene."""
+        if self.env_dist is None:
+            raise ValueError("the scene has no image-based environment light")
+        if row_weight is None and encoder_weights:
+            row_weight = self.env_row_weights()
+        d = self.env_dist
+        with torch.cuda.device(self.device):
+            _lib.call("clr_env_distribution_update", C.c_void_p(self.t["others"].data_ptr()),
+                      C.c_uint32(d["dist_offset"]), C.c_void_p(self.t["textures"].data_ptr()),
+                      C.c_uint32(d["tex_offset"]), C.c_uint32(d["height"]),
+                      C.c_void_p(row_weight.data_ptr()) if row_weight is not None else None,
+                      C.c_void_p(torch.cuda.current_stream(self.device).cuda_stream))
 
     def workspace(self) -> torch.Tensor:
         if getattr(self, "_ws", None) is None:

@@ -561,6 +561,10 @@ class MaterialCreator:
         distribution (the reference reads the same texels as half floats)."""
         dname = "InternalDistribution2D_" + radiance_tex
         self.continuous_consts_2d_h(dname, rgb, True)
+        h, w = np.asarray(rgb).shape[:2]
+        # where the device rebuild of this distribution finds its inputs
+        self.s.env_dist = {"dist_offset": self.s.other_ref[dname], "tex_offset": self.s.tex_ref[radiance_tex],
+                           "width": w, "height": h}
         self.begin_light_property(name)
         self.num_eedfs += 1
         self.s.materials.align(4)

@@ -44,6 +44,7 @@ enum {
 #define CLR_DEVERR_STACK        0x2u  /* traversal stack full (ray reported as miss) */
 #define CLR_DEVERR_REFIT        0x4u  /* refit climb exceeded the tree depth bound */
 #define CLR_DEVERR_QUEUE        0x8u  /* a wavefront queue or bounded wait failed */
+#define CLR_DEVERR_INPUT        0x10u /* scene data not laid out as the entry point requires */
 
 /* Byte sizes of the records below. */
 #define CLR_NODE_BYTES 64u      /* internal node: both child boxes + child refs */
@@ -227,6 +228,33 @@ CLR_API int clr_render_workspace_bytes(uint32_t width, uint32_t height, uint64_t
 CLR_API int clr_render_wavefront(const clr_scene* scene, uint32_t width, uint32_t height, uint32_t* rand_states,
                                  float* pixels, uint32_t spp, uint32_t max_depth, uint32_t flags, void* workspace,
                                  uint64_t workspace_bytes, void* stream);
+
+/* ----------------------------------------------------- post-processing */
+
+/* Replaces the `scaling` + `toneMapping` kernel pair that turns the
+ * accumulation buffer into the BMP image (OpenCL/post_processing.cl:20-26,
+ * 98-117; main.cpp:526-536), fused into one kernel.  `accum` holds float4 per
+ * pixel (xyz = radiance summed over `spp` samples); `bgr` receives the
+ * reference's BMP pixel array: 8-bit BGR, rows bottom-up, each row
+ * 3 * width + width % 4 bytes (padding written as zero), ready for a BMP
+ * file header (BMPExporter.cpp:14-55). */
+CLR_API int clr_postprocess_ldr(const float* accum, uint32_t width, uint32_t height, uint32_t spp, uint8_t* bgr,
+                                void* stream);
+
+/* Recomputes, on the device and in place, the importance distribution of an
+ * image-based environment light after its texels changed: the
+ * ContinuousConsts2D_H that createContinuousConsts2D_H_FromImageTexture
+ * (OpenCL_PathTracer/CreateFunctions.cpp:246-349) builds on the host, one
+ * stratum per texel, at byte `dist_offset` of the `others` blob, from the
+ * RGBA16F image texture at byte `tex_offset` of the `textures` blob, whose
+ * height is `height`.  `row_weight` (height floats, device) weights each row's
+ * luminance; NULL uses the reference's zenith correction
+ * cos(pi (0.5 - (i + 0.5) / height)) evaluated on the device.  The structure's
+ * headers must already be laid out (by the scene encoder); a mismatch sets
+ * CLR_DEVERR_INPUT. */
+CLR_API int clr_env_distribution_update(uint8_t* others, uint32_t dist_offset, const uint8_t* textures,
+                                        uint32_t tex_offset, uint32_t height, const float* row_weight,
+                                        void* stream);
 
 /* ------------------------------------------------------------- batched */
 

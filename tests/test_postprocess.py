@@ -1,0 +1,54 @@
+"""Post-processing (accumulation -> 8-bit BGR BMP pixels) against the numpy
+restatement of the reference's scaling + toneMapping kernels, and the BMP
+file layout of the reference's saveBMP.  Bar (stated here): every byte within
+1 of the oracle and at least 99 % of bytes equal (exp and pow of two math
+libraries may round differently); the row padding and the header exact."""
+import struct
+
+import numpy as np
+import pytest
+import torch
+
+from clear_gb300 import _lib
+from clear_gb300 import postprocess as PP
+from oracle import postprocess as OP
+
+
+def _hdr(n, seed=3):
+    r = np.random.default_rng(seed)
+    a = np.zeros((n, 4), dtype=np.float32)
+    a[:, :3] = r.lognormal(0.0, 2.0, size=(n, 3)).astype(np.float32)
+    special = [(0.0, 0.0, 0.0),      # black: Y = 0 branch
+               (1e6, 1e6, 1e6),      # saturates at the threshold
+               (0.0, 5.0, 0.0)]
+    for i, v in enumerate(special[:n]):
+        a[i, :3] = v
+    return a
+
+
+def test_oracle_layout_and_header():
+    w, h = 5, 3
+    acc = _hdr(w * h)
+    px = OP.tonemap(acc, w, h, 4)
+    assert px.size == h * OP.byte_width(w) == h * (3 * w + 1)
+    rows = px.reshape(h, -1)
+    assert np.all(rows[:, 3 * w:] == 0)
+    assert tuple(rows[h - 1, 0:3]) == (0, 0, 0)  # pixel 0 (black) is the first pixel of the last row
+    b = PP.bmp_bytes(px, w, h)
+    assert b[:2] == b"BM" and len(b) == 54 + px.size
+    size, _, _, off, info, ww, hh, planes, bits = struct.unpack_from("<IHHIIIIHH", b, 2)
+    assert (size, off, info, ww, hh, planes, bits) == (54 + px.size, 54, 40, w, h, 1, 24)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("w,h,spp", [(1920, 1080, 64), (33, 7, 1), (1, 1, 3)])
+def test_postprocess_matches_oracle(cuda, w, h, spp):
+    acc = _hdr(w * h, seed=w)
+    got = PP.to_ldr(torch.from_numpy(acc).to(cuda), w, h, spp).cpu().numpy()
+    want = OP.tonemap(acc, w, h, spp)
+    diff = np.abs(got.astype(np.int32) - want.astype(np.int32))
+    assert diff.max() <= 1, diff.max()
+    assert (diff == 0).mean() >= 0.99
+    rows = got.reshape(h, -1)
+    assert np.all(rows[:, 3 * w:] == 0)
+    assert _lib.device_status() == 0
