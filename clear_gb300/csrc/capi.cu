@@ -23,13 +23,15 @@ cudaError_t clr_status_render_wf(unsigned int* v, int clear);
 cudaError_t clr_status_render_adjoint(unsigned int* v, int clear);
 cudaError_t clr_status_render_batch(unsigned int* v, int clear);
 cudaError_t clr_status_env_dist(unsigned int* v, int clear);
+cudaError_t clr_status_bvh_vis(unsigned int* v, int clear);
 
 extern "C" int clr_device_status(uint32_t* bits, int clear) {
     CLR_CUDA_TRY(cudaDeviceSynchronize());
     unsigned int all = 0;
     cudaError_t (*readers[])(unsigned int*, int) = {clr_status_lbvh, clr_status_traverse, clr_status_render,
                                                    clr_status_render_wf, clr_status_render_adjoint,
-                                                   clr_status_render_batch, clr_status_env_dist};
+                                                   clr_status_render_batch, clr_status_env_dist,
+                                                   clr_status_bvh_vis};
     for (auto rd : readers) {
         unsigned int v = 0;
         CLR_CUDA_TRY(rd(&v, clear));

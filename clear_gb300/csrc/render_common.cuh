@@ -65,8 +65,11 @@ struct Hit {
 
 // rayIntersection for the renderer: returns the closest hit with its
 // barycentrics.  kOrdered visits the nearer child first.
-template <bool kOrdered>
-static __device__ bool intersect(const DScene& sc, f3 org, f3 dir, Hit& h, uint2* stack) {
+// Closest hit.  With kCount, *boxes counts the boxes the search accepts,
+// internal and leaf (the reference's numAABBHit of rayIntersectionVis,
+// bvh_traversal.cl:217-254, in its visiting order when !kOrdered).
+template <bool kOrdered, bool kCount = false>
+static __device__ bool intersect_impl(const DScene& sc, f3 org, f3 dir, Hit& h, uint2* stack, uint32_t* boxes) {
     Ray ray{org.x, org.y, org.z, INFINITY, dir.x, dir.y, dir.z};
     const float ix = 1.0f / dir.x, iy = 1.0f / dir.y, iz = 1.0f / dir.z;
     float t = INFINITY;
@@ -93,6 +96,7 @@ static __device__ bool intersect(const DScene& sc, f3 org, f3 dir, Hit& h, uint2
         for (uint32_t guard = 0; sp > 0 && guard < sc.num_tris; ++guard) {
             --sp;
             if (__uint_as_float(stack[sp].y) > t) continue;
+            if (kCount) ++*boxes;
             const NodeBoxes nb = load_node(sc.nodes, stack[sp].x);
             float e0, e1;
             const bool p0 = box_test_fast(nb.b0[0], nb.b0[1], nb.b0[2], nb.b0[3], nb.b0[4], nb.b0[5], ray, ix, iy, iz, e0);
@@ -107,7 +111,10 @@ static __device__ bool intersect(const DScene& sc, f3 org, f3 dir, Hit& h, uint2
                 const bool pass = c ? p1 : p0;
                 const float e = c ? e1 : e0;
                 if (ref & kLeafBit) {
-                    if (pass && !(e > t)) test_leaf(ref & ~kLeafBit);
+                    if (pass && !(e > t)) {
+                        if (kCount) ++*boxes;
+                        test_leaf(ref & ~kLeafBit);
+                    }
                 } else if (pass) {
                     if (sp < kStackSize) stack[sp++] = make_uint2(ref, __float_as_uint(e));
                     else clr_raise(CLR_DEVERR_STACK);
@@ -121,6 +128,11 @@ static __device__ bool intersect(const DScene& sc, f3 org, f3 dir, Hit& h, uint2
     h.b1 = bb1;
     h.b2 = bb2;
     return true;
+}
+
+template <bool kOrdered>
+static __device__ __forceinline__ bool intersect(const DScene& sc, f3 org, f3 dir, Hit& h, uint2* stack) {
+    return intersect_impl<kOrdered, false>(sc, org, dir, h, stack, nullptr);
 }
 
 // Whether the ray hits any triangle at all (environment shadow rays: the
@@ -454,16 +466,17 @@ __device__ __forceinline__ Camera load_camera(const DScene& sc) {
 
 // sampleLensPos + IDFAlloc + sample_We (camera.cl:60-115): the primary ray of
 // pixel (gx, gy), its throughput alpha and direction pdf; consumes 4 randoms.
-__device__ __forceinline__ void camera_ray(const Camera& cam, uint32_t gx, uint32_t gy, Rng& rng, f3& org, f3& dir,
-                                           f3& alpha, float& dirPDF) {
-    const float cu0 = rng.uniform(), cu1 = rng.uniform();
+// The same ray for given samples: lens (cu0, cu1) and pixel position
+// (gx + pu0, gy + pu1).
+__device__ __forceinline__ void camera_ray_at(const Camera& cam, uint32_t gx, uint32_t gy, float cu0, float cu1,
+                                              float pu0, float pu1, f3& org, f3& dir, f3& alpha, float& dirPDF) {
     float ux, uy;
     concentric_disk(cu0, cu1, ux, uy);
     const f3 idfDir = mat_v3(cam.l2w, mk(0.0f, 0.0f, 1.0f));
     const f3 lensLocal = mk(ux * cam.lensRadius, uy * cam.lensRadius, 0.0f);
     org = mat_p3(cam.l2w, lensLocal);
-    const float pxs = gx + rng.uniform();
-    const float pys = gy + rng.uniform();
+    const float pxs = gx + pu0;
+    const float pys = gy + pu1;
     const float* r2c = reinterpret_cast<const float*>(cam.blob + 192);
     float4 pc = make_float4(r2c[0] * pxs + r2c[4] * pys + r2c[8] * 0.0f + r2c[12] * 1.0f,
                             r2c[1] * pxs + r2c[5] * pys + r2c[9] * 0.0f + r2c[13] * 1.0f,
@@ -486,6 +499,13 @@ __device__ __forceinline__ void camera_ray(const Camera& cam, uint32_t gx, uint3
     dirPDF = 1.0f / (powf(-d.z, 3) * cam.virtualPlaneArea);
     alpha = mk(1, 1, 1);
     alpha *= fabsf(dot(idfDir, dir)) / dirPDF;
+}
+
+__device__ __forceinline__ void camera_ray(const Camera& cam, uint32_t gx, uint32_t gy, Rng& rng, f3& org, f3& dir,
+                                           f3& alpha, float& dirPDF) {
+    const float cu0 = rng.uniform(), cu1 = rng.uniform();
+    const float pu0 = rng.uniform(), pu1 = rng.uniform();
+    camera_ray_at(cam, gx, gy, cu0, cu1, pu0, pu1, org, dir, alpha, dirPDF);
 }
 
 // dirToPolarYTop (global.cl:438-441) -> equirectangular uv

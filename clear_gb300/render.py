@@ -110,6 +110,20 @@ class DeviceScene:
             self._aws = buf[off:off + int(n.value)]
         return self._aws
 
+    def visualize_bvh(self, pix: torch.Tensor | None = None):
+        """The reference's BVH visualiser image (the hit material's base colour
+        plus 0.025 per accepted BVH box, one centred ray per pixel) added to
+        `pix`, and the per-pixel box counts.  Returns (pix, visits)."""
+        n = self.width * self.height
+        if pix is None:
+            pix = torch.zeros((n, 4), dtype=torch.float32, device=self.device)
+        visits = torch.zeros(n, dtype=torch.int32, device=self.device)
+        with torch.cuda.device(self.device):
+            _lib.call("clr_bvh_visualize", C.byref(self.c), C.c_uint32(self.width), C.c_uint32(self.height),
+                      C.c_void_p(pix.data_ptr()), C.c_void_p(visits.data_ptr()),
+                      C.c_void_p(torch.cuda.current_stream(self.device).cuda_stream))
+        return pix, visits
+
     def env_row_weights(self) -> torch.Tensor:
         """The zenith correction of each environment row as the scene encoder
         computes it (cos(pi (0.5 - (i + 0.5) / h)), rounded to float)."""

@@ -229,6 +229,16 @@ CLR_API int clr_render_wavefront(const clr_scene* scene, uint32_t width, uint32_
                                  float* pixels, uint32_t spp, uint32_t max_depth, uint32_t flags, void* workspace,
                                  uint64_t workspace_bytes, void* stream);
 
+/* Replaces the `bvh_visualizer` kernel (OpenCL/bvh_visualizer.cl:25-84): one
+ * ray per pixel through the lens centre and pixel centre; adds to `pixels`
+ * (float4 per pixel) the hit material's base colour plus 0.025 per BVH box
+ * the closest-hit search accepts (internal and leaf,
+ * in the reference's visiting order, rayIntersectionVis,
+ * bvh_traversal.cl:217-254).  `visits` (optional, uint32 per pixel) receives
+ * that box count. */
+CLR_API int clr_bvh_visualize(const clr_scene* scene, uint32_t width, uint32_t height, float* pixels,
+                              uint32_t* visits, void* stream);
+
 /* ----------------------------------------------------- post-processing */
 
 /* Replaces the `scaling` + `toneMapping` kernel pair that turns the

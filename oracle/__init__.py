@@ -215,6 +215,17 @@ def ref_trace_closest_mid(vx, vy, vz, tri, n, nodes, rays):
     return ids, ts
 
 
+def ref_bvh_visualizer(scene_blobs: dict, inodes, lnodes, pixels, width, height):
+    """sim::bvh_visualizer over the whole image; pixels (f32[W*H*4]) are
+    updated in place."""
+    b = scene_blobs
+    rs = np.zeros(4 * width * height, dtype=np.uint32)
+    _ref("lbvh").ref_bvh_visualizer(_p(b["vertices"]), _p(b["normals"]), _p(b["tangents"]), _p(b["uvs"]),
+                                    _p(b["faces"]), _p(b["lights"]), _p(b["materials"]), _p(b["textures"]),
+                                    _p(b["others"]), _p(inodes), _p(lnodes), _p(rs), _p(pixels),
+                                    C.c_uint32(width), C.c_uint32(height))
+
+
 def ref_render(scene_blobs: dict, inodes, lnodes, rand_states, pixels, width, height, y0, y1, spp):
     """sim::pathtracing over rows [y0, y1); rand_states (u32[4*W*H]) and
     pixels (f32[W*H*4]) are updated in place."""

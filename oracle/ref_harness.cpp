@@ -17,6 +17,9 @@
 #include <vector>
 
 #include "sim_pathtracer.hpp"
+#ifdef __USE_LBVH
+#include "sim_bvh_visualizer.hpp"
+#endif
 #ifndef __USE_LBVH
 #include "BVH.hpp"
 #endif
@@ -108,6 +111,28 @@ int ref_render(const float* verts, const float* normals, const float* tangents, 
                                  (sim::uchar*)inodes, (sim::uchar*)lnodes, rand_states,
                                  (sim::float3*)pixels);
             }
+    return 0;
+}
+
+/* sim::bvh_visualizer over a width x height image (one NDRange, offset 0). */
+int ref_bvh_visualizer(const float* verts, const float* normals, const float* tangents, const float* uvs,
+                       const uint8_t* faces, const uint8_t* lights, const uint8_t* materials,
+                       const uint8_t* textures, const uint8_t* others, const uint8_t* inodes,
+                       const uint8_t* lnodes, uint32_t* rand_states, float* pixels, uint32_t width,
+                       uint32_t height) {
+    sim::global_sizes[0] = width;
+    sim::global_sizes[1] = height;
+    sim::global_offsets[0] = 0;
+    sim::global_offsets[1] = 0;
+    for (uint32_t y = 0; y < height; ++y)
+        for (uint32_t x = 0; x < width; ++x) {
+            sim::global_ids[0] = x;
+            sim::global_ids[1] = y;
+            sim::bvh_visualizer((sim::float3*)verts, (sim::float3*)normals, (sim::float3*)tangents,
+                                (sim::float2*)uvs, (sim::uchar*)faces, (sim::uint*)lights, (sim::uchar*)materials,
+                                (sim::uchar*)textures, (sim::uchar*)others, (sim::uchar*)inodes,
+                                (sim::uchar*)lnodes, rand_states, (sim::float3*)pixels);
+        }
     return 0;
 }
 #else
