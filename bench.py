@@ -547,6 +547,14 @@ def run_ours(args):
     closest_ms = t0.elapsed_time(t1) / trav_steps
     shadow_ms = t1.elapsed_time(t2) / trav_steps
     ordered_ms = t2.elapsed_time(t3) / trav_steps
+    # visiting statistics of the same query (reference order): the bytes the
+    # exact search gathers per ray, 64 per node loaded and 48 per triangle
+    # tested, plus the 32-byte ray and its 8-byte result
+    _, cnt = lbvh.trace_closest_counted(bvh, crays)
+    nodes_per_ray = float(cnt[:, 0].double().mean().item())
+    tris_per_ray = float(cnt[:, 1].double().mean().item())
+    del cnt
+    fetch_bytes = m * (32 + 8 + 64 * nodes_per_ray + 48 * tris_per_ray)
     ordered_id_mismatch = int((hid != hid2).sum().item())
     ordered_t_mismatch = int((ht != ht2).sum().item())
     render = bench_render(dev, args) if args.render else None
@@ -592,6 +600,8 @@ def run_ours(args):
                       "ordered_vs_exact_id_mismatches": ordered_id_mismatch,
                       "ordered_vs_exact_t_mismatches": ordered_t_mismatch,
                       "closest_ms": closest_ms, "shadow_ms": shadow_ms, "closest_hit_frac": hit_frac,
+                      "closest_nodes_per_ray": nodes_per_ray, "closest_tris_per_ray": tris_per_ray,
+                      "closest_gather_gbs": fetch_bytes / (closest_ms * 1e-3) / 1e9,
                       "shadow_occluded_frac": occ_frac},
         "render": render,
         "render_terrain": render_terrain,

@@ -91,6 +91,7 @@ def lib() -> C.CDLL:
             "clr_batch_render": [vp, vp, vp, u32, u32, u32, vp],
             "clr_postprocess_ldr": [vp, u32, u32, u32, vp, vp],
             "clr_bvh_visualize": [vp, u32, u32, vp, vp, vp],
+            "clr_trace_closest_counted": [C.POINTER(ClrBvh), vp, u32, vp, vp, vp],
             "clr_env_distribution_update": [vp, u32, vp, u32, u32, vp, vp],
             "clr_lbvh_pass_times": [vp, C.POINTER(C.c_float), C.POINTER(C.c_char_p), i32, C.POINTER(i32)],
         }

@@ -34,10 +34,12 @@ __global__ void __launch_bounds__(128) k_bvh_vis(DScene sc, uint32_t width, uint
     float dirPDF;
     camera_ray_at(cam, x, y, 0.5f, 0.5f, 0.5f, 0.5f, org, dir, alpha, dirPDF);
     uint2 stack[kStackSize];
-    uint32_t boxes = 0;
+    uint32_t cnt[2] = {0u, 0u};
     Hit h;
     float4 px = pixels[p];
-    if (intersect_impl<false, true>(sc, org, dir, h, stack, &boxes)) {
+    const bool hit = intersect_impl<false, true>(sc, org, dir, h, stack, cnt);
+    const uint32_t boxes = cnt[0] + cnt[1];
+    if (hit) {
         SurfPt sp;
         surface_point(sc, org, dir, h, sp);
         const Face face = load_face(sc, sp.faceID);
@@ -56,9 +58,44 @@ __global__ void __launch_bounds__(128) k_bvh_vis(DScene sc, uint32_t width, uint
     if (visits) visits[p] = boxes;
 }
 
+// Closest hit of rays {ox,oy,oz,tmax,dx,dy,dz,0} in the reference's order
+// with t unbounded, counting per ray the internal boxes and the leaf boxes
+// the search accepts (counts[2r], counts[2r+1]).
+__global__ void __launch_bounds__(128) k_trace_counted(DScene sc, const float4* __restrict__ rays, uint32_t n,
+                                                       uint32_t* __restrict__ hit_id, uint32_t* __restrict__ counts) {
+    const uint32_t r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= n) return;
+    const float4 a = rays[2u * r], b = rays[2u * r + 1];
+    uint2 stack[kStackSize];
+    uint32_t cnt[2] = {0u, 0u};
+    Hit h;
+    const bool hit = intersect_impl<false, true>(sc, mk(a.x, a.y, a.z), mk(b.x, b.y, b.z), h, stack, cnt);
+    if (hit_id) hit_id[r] = hit ? h.id : kNone32;
+    counts[2u * r] = cnt[0];
+    counts[2u * r + 1] = cnt[1];
+}
+
 }  // namespace clr
 
 using namespace clr;
+
+extern "C" int clr_trace_closest_counted(const clr_bvh* bvh, const float* rays, uint32_t num_rays, uint32_t* hit_id,
+                                         uint32_t* counts, void* stream) {
+    if (!bvh || !counts || (num_rays && !rays))
+        return clr_set_error(CLR_EINVAL, "clr_trace_closest_counted: NULL argument");
+    if (reinterpret_cast<uintptr_t>(rays) & 15u)
+        return clr_set_error(CLR_EINVAL, "clr_trace_closest_counted: rays must be 16-byte aligned");
+    if (num_rays == 0) return CLR_OK;
+    DScene sc{};
+    sc.nodes = static_cast<const float4*>(bvh->nodes);
+    sc.tris = static_cast<const float4*>(bvh->tris);
+    sc.root_box = bvh->root_box;
+    sc.num_tris = bvh->num_tris;
+    k_trace_counted<<<div_up(num_rays, 128u), 128, 0, static_cast<cudaStream_t>(stream)>>>(
+        sc, reinterpret_cast<const float4*>(rays), num_rays, hit_id, counts);
+    CLR_LAUNCH_CHECK("k_trace_counted");
+    return CLR_OK;
+}
 
 extern "C" int clr_bvh_visualize(const clr_scene* scene, uint32_t width, uint32_t height, float* pixels,
                                  uint32_t* visits, void* stream) {

@@ -65,9 +65,10 @@ struct Hit {
 
 // rayIntersection for the renderer: returns the closest hit with its
 // barycentrics.  kOrdered visits the nearer child first.
-// Closest hit.  With kCount, *boxes counts the boxes the search accepts,
-// internal and leaf (the reference's numAABBHit of rayIntersectionVis,
-// bvh_traversal.cl:217-254, in its visiting order when !kOrdered).
+// Closest hit.  With kCount, boxes[0] counts the internal boxes and boxes[1]
+// the leaf boxes the search accepts (their sum is the reference's numAABBHit
+// of rayIntersectionVis, bvh_traversal.cl:217-254, in its visiting order when
+// !kOrdered): the nodes loaded and the triangles tested.
 template <bool kOrdered, bool kCount = false>
 static __device__ bool intersect_impl(const DScene& sc, f3 org, f3 dir, Hit& h, uint2* stack, uint32_t* boxes) {
     Ray ray{org.x, org.y, org.z, INFINITY, dir.x, dir.y, dir.z};
@@ -88,7 +89,8 @@ static __device__ bool intersect_impl(const DScene& sc, f3 org, f3 dir, Hit& h, 
             bb2 = b2;
         }
     };
-    if (sc.num_tris == 1) {
+    if (sc.num_tris == 1) {  // the root box is the leaf's box
+        if (kCount) ++boxes[1];
         test_leaf(0);
     } else if (sc.num_tris >= 2) {
         int sp = 0;
@@ -96,7 +98,7 @@ static __device__ bool intersect_impl(const DScene& sc, f3 org, f3 dir, Hit& h, 
         for (uint32_t guard = 0; sp > 0 && guard < sc.num_tris; ++guard) {
             --sp;
             if (__uint_as_float(stack[sp].y) > t) continue;
-            if (kCount) ++*boxes;
+            if (kCount) ++boxes[0];
             const NodeBoxes nb = load_node(sc.nodes, stack[sp].x);
             float e0, e1;
             const bool p0 = box_test_fast(nb.b0[0], nb.b0[1], nb.b0[2], nb.b0[3], nb.b0[4], nb.b0[5], ray, ix, iy, iz, e0);
@@ -112,7 +114,7 @@ static __device__ bool intersect_impl(const DScene& sc, f3 org, f3 dir, Hit& h, 
                 const float e = c ? e1 : e0;
                 if (ref & kLeafBit) {
                     if (pass && !(e > t)) {
-                        if (kCount) ++*boxes;
+                        if (kCount) ++boxes[1];
                         test_leaf(ref & ~kLeafBit);
                     }
                 } else if (pass) {

@@ -200,3 +200,17 @@ def trace_shadow(bvh: BVH, rays: torch.Tensor, occluded: torch.Tensor | None = N
     with torch.cuda.device(bvh.device):
         call("clr_trace_shadow", C.byref(bvh.c), _ptr(r), C.c_uint32(m), _ptr(occluded), _stream(bvh.device))
     return occluded
+
+
+def trace_closest_counted(bvh: BVH, rays: torch.Tensor):
+    """Closest hit in the reference's order with per-ray visiting counts:
+    returns (hit_id int32, counts int32 (n, 2): internal boxes accepted = nodes
+    loaded, leaf boxes accepted = triangles tested)."""
+    r = _rays(rays, bvh.device)
+    m = r.shape[0]
+    hit_id = torch.empty(m, dtype=torch.int32, device=bvh.device)
+    counts = torch.empty((m, 2), dtype=torch.int32, device=bvh.device)
+    with torch.cuda.device(bvh.device):
+        call("clr_trace_closest_counted", C.byref(bvh.c), _ptr(r), C.c_uint32(m), _ptr(hit_id), _ptr(counts),
+             _stream(bvh.device))
+    return hit_id, counts

@@ -239,6 +239,15 @@ CLR_API int clr_render_wavefront(const clr_scene* scene, uint32_t width, uint32_
 CLR_API int clr_bvh_visualize(const clr_scene* scene, uint32_t width, uint32_t height, float* pixels,
                               uint32_t* visits, void* stream);
 
+/* The visiting statistics of the closest-hit search, the counter of
+ * rayIntersectionVis (bvh_traversal.cl:217-254) per ray: counts[2r] internal
+ * boxes accepted (nodes loaded), counts[2r+1] leaf boxes accepted (triangles
+ * tested), in the reference's order with t starting unbounded (tmax is not
+ * read).  hit_id (optional) receives the closest hit as clr_trace_closest
+ * gives it for tmax = infinity.  For measuring traversal traffic. */
+CLR_API int clr_trace_closest_counted(const clr_bvh* bvh, const float* rays, uint32_t num_rays, uint32_t* hit_id,
+                                      uint32_t* counts, void* stream);
+
 /* ----------------------------------------------------- post-processing */
 
 /* Replaces the `scaling` + `toneMapping` kernel pair that turns the

@@ -98,7 +98,9 @@ def trace_closest(vx, vy, vz, tri, bvh: OracleBVH, rays, stats=False):
     nr = rays.shape[0]
     ids = np.zeros(nr, dtype=np.uint32)
     ts = np.zeros(nr, dtype=np.float32)
-    st = np.zeros((nr, 3), dtype=np.uint32) if stats else None
+    # per ray: internal nodes popped, internal boxes accepted, leaf box tests,
+    # leaf boxes accepted (= triangle tests)
+    st = np.zeros((nr, 4), dtype=np.uint32) if stats else None
     rc = lib().orc_trace_closest(_p(vx), _p(vy), _p(vz), _p(tri), _p(bvh.inodes), _p(bvh.lnodes),
                                  C.c_uint32(len(bvh.lnodes)), _p(rays), C.c_uint32(nr), _p(ids), _p(ts), _p(st))
     if rc != 0:

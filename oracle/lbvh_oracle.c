@@ -323,8 +323,10 @@ static int ray_box(const float* bmin, const float* bmax, v3 org, v3 dir, float t
 /* rays: 8 floats per ray {ox,oy,oz,tmax, dx,dy,dz,unused}.
  * Closest hit, rayIntersection (bvh_traversal.cl:182-215) with t starting at
  * tmax (the reference starts at INFINITY).  Miss: id 0xFFFFFFFF, t = tmax.
- * stats (optional, 3 per ray): internal-node box tests, leaf box tests,
- * triangle tests. */
+ * stats (optional, 4 per ray): internal nodes popped, internal boxes
+ * accepted, leaf box tests, leaf boxes accepted (= triangle tests); the
+ * second plus the fourth is numAABBHit of rayIntersectionVis
+ * (bvh_traversal.cl:217-254). */
 int orc_trace_closest(const float* vx, const float* vy, const float* vz, const uint32_t* tri,
                       const orc_inode* inodes, const orc_lnode* lnodes, uint32_t n,
                       const float* rays, uint32_t nrays, uint32_t* hit_id, float* hit_t,
@@ -335,7 +337,7 @@ int orc_trace_closest(const float* vx, const float* vy, const float* vz, const u
         v3 org = {R[0], R[1], R[2]}, dir = {R[4], R[5], R[6]};
         float t = R[3];
         uint32_t best = 0xFFFFFFFFu;
-        uint32_t s_in = 0, s_leaf = 0, s_tri = 0;
+        uint32_t s_in = 0, s_acc = 0, s_leaf = 0, s_tri = 0;
         if (n == 1) {
             ++s_leaf;
             if (ray_box(lnodes[0].min, lnodes[0].max, org, dir, t)) {
@@ -350,6 +352,7 @@ int orc_trace_closest(const float* vx, const float* vy, const float* vz, const u
                 const orc_inode* in = inodes + stack[--depth];
                 ++s_in;
                 if (!ray_box(in->min, in->max, org, dir, t)) continue;
+                ++s_acc;
                 for (int i = 0; i < 2; ++i) {
                     if (!in->isChild[i]) {
                         if (depth >= ORC_STACK) { status = ORC_ESTACK; continue; }
@@ -366,7 +369,12 @@ int orc_trace_closest(const float* vx, const float* vy, const float* vz, const u
         }
         hit_id[r] = best;
         hit_t[r] = t;
-        if (stats) { stats[3u * r] = s_in; stats[3u * r + 1] = s_leaf; stats[3u * r + 2] = s_tri; }
+        if (stats) {
+            stats[4u * r] = s_in;
+            stats[4u * r + 1] = s_acc;
+            stats[4u * r + 2] = s_leaf;
+            stats[4u * r + 3] = s_tri;
+        }
     }
     return status;
 }

@@ -108,6 +108,25 @@ def test_trace_parity(cuda, n):
     no_device_errors()
 
 
+@pytest.mark.parametrize("n", [1, 2, 5000, 300001])
+def test_trace_counted_matches_oracle_visits(cuda, n):
+    """Per-ray visiting counts in the reference's order: internal boxes
+    accepted and leaf boxes accepted (triangles tested) equal the oracle's,
+    and the hit is the plain closest-hit query's."""
+    vx, vy, vz = W.triangle_soup(n, seed=3000 + n)
+    b, bvh, _ = gpu_build(cuda, vx, vy, vz, None, n, 10)
+    ob = oracle.lbvh_build(vx, vy, vz, None, n, 10)
+    rays = W.closest_rays(20000, seed=n + 5)
+    ids, counts = lbvh.trace_closest_counted(bvh, torch.from_numpy(rays).to(cuda))
+    oids, _, st = oracle.trace_closest(vx, vy, vz, None, ob, rays, stats=True)
+    np.testing.assert_array_equal(ids.cpu().numpy().view(np.uint32), oids)
+    c = counts.cpu().numpy().view(np.uint32)
+    np.testing.assert_array_equal(c[:, 0], st[:, 1])
+    np.testing.assert_array_equal(c[:, 1], st[:, 3])
+    assert (st[:, 1] <= st[:, 0]).all() and (st[:, 3] <= st[:, 2]).all()
+    no_device_errors()
+
+
 def test_trace_ordered_matches_closest_hit(cuda):
     """The nearer-child-first query finds the same closest hit; only exact or
     rounding-level ties may resolve differently (none expected here)."""
