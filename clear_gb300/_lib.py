@@ -36,6 +36,24 @@ class ClrAdjointParams(C.Structure):
                 ("tape", C.c_void_p), ("tape_capacity", C.c_uint32), ("tape_count", C.c_void_p)]
 
 
+class ClrObjGroup(C.Structure):
+    _fields_ = [("first_face", C.c_uint32), ("num_faces", C.c_uint32), ("format", C.c_uint32),
+                ("smooth", C.c_uint32), ("name", C.c_uint32), ("material", C.c_uint32)]
+
+
+class ClrObjMaterial(C.Structure):
+    _fields_ = [("Kd", C.c_float * 3), ("Ks", C.c_float * 3), ("Ka", C.c_float * 3), ("Ns", C.c_float),
+                ("Ni", C.c_float), ("name", C.c_uint32), ("map_Kd", C.c_uint32), ("map_Ks", C.c_uint32),
+                ("map_Ka", C.c_uint32)]
+
+
+class ClrObjCounts(C.Structure):
+    _fields_ = [(k, C.c_uint32) for k in ("num_positions", "num_uvs", "num_normals", "num_faces", "num_groups",
+                                          "num_materials", "num_skipped", "string_bytes")]
+
+
+OBJ_VTN, OBJ_VN, OBJ_VT, OBJ_V, OBJ_NONE = range(5)
+
 _lib = None
 
 
@@ -94,11 +112,16 @@ def lib() -> C.CDLL:
             "clr_trace_closest_counted": [C.POINTER(ClrBvh), vp, u32, vp, vp, vp],
             "clr_env_distribution_update": [vp, u32, vp, u32, u32, vp, vp],
             "clr_lbvh_pass_times": [vp, C.POINTER(C.c_float), C.POINTER(C.c_char_p), i32, C.POINTER(i32)],
+            "clr_obj_parse": [C.c_char_p, C.POINTER(vp)],
+            "clr_obj_counts_of": [vp, C.POINTER(ClrObjCounts)],
+            "clr_obj_data": [vp, *([C.POINTER(vp)] * 7)],
         }
         for name, args in sig.items():
             fn = getattr(L, name)
             fn.argtypes = args
             fn.restype = i32
+        L.clr_obj_free.argtypes = [vp]
+        L.clr_obj_free.restype = None
         _lib = L
     return _lib
 

@@ -1,6 +1,7 @@
 """Compile the CUDA sources into ``clear_gb300/libclear_gb300.so`` (sm_103a).
 
-Each ``csrc/*.cu`` is compiled to an object in parallel, then linked into one
+Each ``csrc/*.cu`` (nvcc) and host-only ``csrc/*.cpp`` (the host compiler) is
+compiled to an object in parallel, then linked into one
 shared library whose exported symbols are the C ABI of
 ``include/clear_cuda.h``.  Only nvcc and the host compiler are needed.
 """
@@ -28,8 +29,13 @@ NVCC_FLAGS = [
 ]
 
 
+CXX = os.environ.get("CXX", "g++")
+# Host-only sources (no device code): the host compiler directly.
+CXX_FLAGS = ["-O2", "-std=c++17", "-fPIC", "-fvisibility=hidden", f"-I{ROOT / 'include'}", f"-I{CSRC}"]
+
+
 def _sources() -> list[Path]:
-    return sorted(CSRC.glob("*.cu"))
+    return sorted(CSRC.glob("*.cu")) + sorted(CSRC.glob("*.cpp"))
 
 
 def _headers() -> list[Path]:
@@ -41,10 +47,13 @@ def _compile(src: Path) -> Path:
     deps = [src, *_headers(), Path(__file__)]
     if obj.exists() and all(obj.stat().st_mtime >= d.stat().st_mtime for d in deps):
         return obj
-    cmd = [NVCC, *NVCC_FLAGS, "-c", str(src), "-o", str(obj)]
+    if src.suffix == ".cpp":
+        cmd = [CXX, *CXX_FLAGS, "-c", str(src), "-o", str(obj)]
+    else:
+        cmd = [NVCC, *NVCC_FLAGS, "-c", str(src), "-o", str(obj)]
     res = subprocess.run(cmd, capture_output=True, text=True)
     if res.returncode != 0:
-        raise RuntimeError(f"nvcc failed for {src.name}:\n{res.stderr}")
+        raise RuntimeError(f"{cmd[0]} failed for {src.name}:\n{res.stderr}")
     return obj
 
 

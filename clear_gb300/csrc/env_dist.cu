@@ -10,9 +10,13 @@
 // offsetCDF} for the parent (rows) and each child (the texels of a row);
 // distribution.cl:85-129 samples it.
 //
-// Row i (one thread): pdf_j = luminance(texel i, j) * w_i (luminance =
-// 0.2126 r + 0.7152 g + 0.0722 b in float; w_i the row weight, by default the
-// zenith correction cos(pi (0.5 - (i + 0.5) / h))), cdf_{j+1} = cdf_j +
+// Row i (one thread): pdf_j = L * w_i, where L is the reference's
+// averageLuminance of a one-texel stratum (CreateFunctions.cpp:159-244): the
+// texel's luminance l = 0.2126 r + 0.7152 g + 0.0722 b, in float, added once
+// per corner of the stratum, ((l + l) + l) + l, over an area of 1; w_i is the
+// row weight, by default the zenith correction cos(pi (0.5 - (i + 0.5) / h))
+// with the device cosf (the host passes the C library's for bit-exactness
+// with the host encoder); cdf_{j+1} = cdf_j +
 // pdf_j * (1 / width) accumulated left to right as the reference's loop does,
 // both normalised by the row's mass cdf_w, which becomes the parent's pdf_i;
 // then the parent's cdf over rows, normalised the same way (one thread).  The
@@ -76,7 +80,8 @@ __global__ void __launch_bounds__(128) k_env_rows(uint8_t* __restrict__ others, 
     for (uint32_t j = 0; j < w; ++j) {
         const float r = __half2float(texel[4 * j]), g = __half2float(texel[4 * j + 1]), b = __half2float(texel[4 * j + 2]);
         const float lum = __fadd_rn(__fadd_rn(__fmul_rn(0.2126f, r), __fmul_rn(0.7152f, g)), __fmul_rn(0.0722f, b));
-        const float pdf = __fmul_rn(lum, corr);
+        const float l4 = __fadd_rn(__fadd_rn(__fadd_rn(lum, lum), lum), lum);
+        const float pdf = __fmul_rn(l4, corr);
         row.pdf[j] = pdf;
         c = __fadd_rn(c, __fmul_rn(pdf, wc));
         row.cdf[j + 1] = c;

@@ -4,13 +4,12 @@ calls ``clr_render`` (the counterpart of enqueueing the reference's
 from __future__ import annotations
 
 import ctypes as C
-import math
 
 import numpy as np
 import torch
 
 from . import _lib, lbvh
-from .scene import Scene
+from .scene import Scene, zenith_weights
 from .scenes import pixel_seeds
 
 RENDER_ORDERED = 0x1
@@ -126,10 +125,8 @@ class DeviceScene:
 
     def env_row_weights(self) -> torch.Tensor:
         """The zenith correction of each environment row as the scene encoder
-        computes it (cos(pi (0.5 - (i + 0.5) / h)), rounded to float)."""
-        h = self.env_dist["height"]
-        w = np.array([math.cos(math.pi * (0.5 - (i + 0.5) / h)) for i in range(h)], dtype=np.float32)
-        return torch.from_numpy(w).to(self.device)
+        computes it (scene.zenith_weights)."""
+        return torch.from_numpy(zenith_weights(self.env_dist["height"])).to(self.device)
 
     def update_env_distribution(self, row_weight: torch.Tensor | None = None, encoder_weights: bool = True) -> None:
         """Rebuilds the environment light's importance distribution on the

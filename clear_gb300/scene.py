@@ -15,14 +15,16 @@ Deliberate differences from the reference's host code, each a defect there:
     8 bytes off.
   * The light-power PMF has numItems entries; the reference's loop writes one
     past the end (Scene.h:281-284).
-  * RGB8 images are stored with a 4-byte texel stride, which is what the
-    kernel's uchar3 reads use (texture.cl:72; OpenCL 3-vectors are 4 wide).
+  * The 2D environment distribution maps a black row (zero mass) to zero PDF
+    and CDF values; the reference multiplies them by 1/0 and stores NaN.
   * createFloatCheckerBoardTexture tags its texture ColorProcedural as the
     reference does (CreateFunctions.cpp:117), so evaluateFloatTexture reads 0
     from it, as in the reference.
 """
 from __future__ import annotations
 
+import ctypes as C
+import ctypes.util
 import math
 import struct
 
@@ -127,6 +129,26 @@ def _colmajor(m) -> bytes:
     return np.asarray(m, dtype=np.float32).T.reshape(-1).tobytes()
 
 
+# --------------------------------------------------- environment rows
+
+_libm = None
+
+
+def zenith_weights(h: int) -> np.ndarray:
+    """Row weights of the environment distribution, as
+    CreateFunctions.cpp:275 computes them: cosf((float)(M_PI * (double)a))
+    with a = 0.5f - (i + 0.5f) / h in float, through the C library's cosf."""
+    global _libm
+    if _libm is None:
+        _libm = C.CDLL(ctypes.util.find_library("m"))
+        _libm.cosf.argtypes = [C.c_float]
+        _libm.cosf.restype = C.c_float
+    i = np.arange(h, dtype=np.float32)
+    a = (np.float32(0.5) - (i + np.float32(0.5)) / np.float32(h)).astype(np.float32)
+    arg = (math.pi * a.astype(np.float64)).astype(np.float32)
+    return np.array([_libm.cosf(float(x)) for x in arg], dtype=np.float32)
+
+
 # ------------------------------------------------------------------- scene
 
 
@@ -166,6 +188,16 @@ class _Rows:
         return self.parts[0]
 
 
+class _NameMap(dict):
+    """Name -> blob offset with the reference's std::map::insert semantics
+    (Scene.h:117-140): registering a name again keeps the first offset (the
+    second record is still written to the blob)."""
+
+    def __setitem__(self, key, value):
+        if key not in self:
+            super().__setitem__(key, value)
+
+
 class Scene:
     def __init__(self):
         self.vertices = _Rows(np.float64, 3)
@@ -178,7 +210,9 @@ class Scene:
         self.materials = Blob()
         self.textures = Blob()
         self.others = Blob(b"\0" * 12)  # offsets of camera, environment, light distribution
-        self.mat_ref, self.light_ref, self.tex_ref, self.other_ref = {}, {}, {}, {}
+        self.mat_ref, self.light_ref, self.tex_ref, self.other_ref = _NameMap(), _NameMap(), _NameMap(), _NameMap()
+        self.tex_files = _NameMap()  # image file -> texture offset (texFilesDatabase)
+        self.models: set = set()     # loaded model files (modelDatabase)
         self.local_to_world = [np.eye(4)]
         self._base = None
         self.mc = MaterialCreator(self)
@@ -259,6 +293,40 @@ class Scene:
         if light != NONE16:
             self.light_infos.append((0, len(self.faces) - 1))
             self.light_powers.append(1.0)
+
+    # bulk forms of the four calls above, for whole arrays ------------------
+    def add_vertices(self, p):
+        """add_vertex for each row of p (n, 3)."""
+        p = np.asarray(p, dtype=np.float64).reshape(-1, 3)
+        vh = np.concatenate([p, np.ones((len(p), 1))], axis=1) @ self.local_to_world[-1].T
+        self.vertices.extend(vh[:, :3] / vh[:, 3:4])
+
+    def add_normals(self, n):
+        """add_normal for each row of n (n, 3)."""
+        n = np.asarray(n, dtype=np.float64).reshape(-1, 3)
+        self.normals.extend(n @ np.linalg.inv(self.local_to_world[-1])[:3, :3])
+
+    def add_uvs(self, uv):
+        self.uvs.extend(np.asarray(uv, dtype=np.float64).reshape(-1, 2))
+
+    def add_faces(self, p, mat, light=NONE16, uv=None, vn=None, alpha_tex=NONE32):
+        """add_face for each row of p (m, 3) (uv, vn likewise, or None), with
+        one material, light and alpha texture for all of them."""
+        bv, bn, bt, bu = self._base or (0, 0, 0, 0)
+        p = np.asarray(p, dtype=np.int64).reshape(-1, 3)
+        f = np.zeros(len(p), dtype=FACE_DTYPE)
+        f["p"] = p + bv
+        f["vn"] = np.asarray(vn, dtype=np.int64).reshape(-1, 3) + bn if vn is not None else NONE32
+        f["vt"] = NONE32
+        f["uv"] = np.asarray(uv, dtype=np.int64).reshape(-1, 3) + bu if uv is not None else NONE32
+        f["alphaTexPtr"] = alpha_tex
+        f["matPtr"] = mat
+        f["lightPtr"] = light
+        first = len(self.faces)
+        self.faces.extend(f)
+        if light != NONE16:
+            self.light_infos.extend((0, first + i) for i in range(len(p)))
+            self.light_powers.extend([1.0] * len(p))
 
     # Scene.h:140-152 -----------------------------------------------------
     def set_camera(self, width, height, cam_to_world, fov_y_deg=30.0, lens_radius=0.0, focus_dist=1.0):
@@ -362,7 +430,9 @@ class MaterialCreator:
         head = t.zeros(16, 4)
         img = t.align(128)
         if kind == "rgb8":
-            px = np.zeros((h, w, 4), dtype=np.uint8)
+            # 4 bytes per texel, the fourth 0xFF, as the reference's PNG reader
+            # stores RGB (ImageLoader.cpp:161-162, png_set_filler)
+            px = np.full((h, w, 4), 0xFF, dtype=np.uint8)
             px[..., :3] = data
             t.b.extend(px.tobytes())
             tt = TEX_RGB8
@@ -382,6 +452,7 @@ class MaterialCreator:
             raise ValueError(kind)
         t.put(head, struct.pack("<B3xIIi", tt, w, h, img - head))
         self.s.tex_ref[name] = head
+        return head
 
     def normal_map_texture(self, name, rgb8: np.ndarray):
         self.image_texture(name, rgb8, "rgb8")
@@ -409,22 +480,6 @@ class MaterialCreator:
         self.s.other_ref[name] = self.s.others.add(struct.pack("<B3xff", FRESNEL_DIELECTRIC, eta_ext, eta_int), 4)
 
     # environment distribution --------------------------------------------
-    def _average_luminance(self, rgb: np.ndarray, x0, x1, y0, y1):
-        """Area-weighted mean luminance of [x0,x1) x [y0,y1) texels,
-        CreateFunctions.cpp:159-244 (float accumulation)."""
-        lum = (np.float32(0.2126) * rgb[..., 0] + np.float32(0.7152) * rgb[..., 1] +
-               np.float32(0.0722) * rgb[..., 2]).astype(np.float32)
-        xl, xr, yt, yb = int(x0), int(math.ceil(x1)) - 1, int(y0), int(math.ceil(y1)) - 1
-        wx = np.ones(xr - xl + 1, dtype=np.float32)
-        wy = np.ones(yb - yt + 1, dtype=np.float32)
-        wx[0] = np.float32(xl + 1 - x0)
-        wx[-1] = np.float32(x1 - xr) if xr > xl else wx[-1]
-        wy[0] = np.float32(yt + 1 - y0)
-        wy[-1] = np.float32(y1 - yb) if yb > yt else wy[-1]
-        block = lum[yt:yb + 1, xl:xr + 1]
-        return float(np.float32((wy[:, None] * wx[None, :] * block).sum(dtype=np.float32) /
-                                np.float32((x1 - x0) * (y1 - y0))))
-
     def continuous_consts_2d_h(self, name, rgb: np.ndarray, zenith_correction=True):
         """ContinuousConsts2D_H over an equirectangular image, one stratum
         per texel, rows weighted by sin(theta) (CreateFunctions.cpp:246-349)."""
@@ -439,9 +494,12 @@ class MaterialCreator:
         rgb = np.asarray(rgb, dtype=np.float32)
         lum = (np.float32(0.2126) * rgb[..., 0] + np.float32(0.7152) * rgb[..., 1] +
                np.float32(0.0722) * rgb[..., 2]).astype(np.float32)
+        # averageLuminance (CreateFunctions.cpp:159-244) of a one-texel stratum:
+        # the texel is added once per corner of the stratum, weight 1 each, and
+        # the sum divided by the stratum's area, 1
+        lum = ((lum + lum) + lum) + lum
         width_c = np.float32(1.0) / np.float32(w)
-        corr = np.array([math.cos(math.pi * (0.5 - (i + 0.5) / h)) if zenith_correction else 1.0 for i in range(h)],
-                        dtype=np.float32)
+        corr = zenith_weights(h) if zenith_correction else np.ones(h, dtype=np.float32)
         pdf = (lum * corr[:, None]).astype(np.float32)
         # running sums in float32, left to right, as the reference's loop
         cdf = np.zeros((h, w + 1), dtype=np.float32)

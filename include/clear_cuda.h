@@ -361,6 +361,53 @@ CLR_API int clr_render_adjoint(const clr_scene* scene, uint32_t width, uint32_t 
                                const clr_adjoint_params* params, void* workspace, uint64_t workspace_bytes,
                                void* stream);
 
+/* ------------------------------------------------------ Wavefront .obj */
+
+/* Parsing half of loadModel / OBJ::load (ModelLoader.cpp:155-495): the
+ * .obj's vertex positions, uvs (stored as 1 - v) and normals, its faces
+ * grouped by runs of `f` lines, and the materials of its .mtl library, with
+ * the reference's line rules (host code; no device work).  Turning this into
+ * scene records -- the `%05u_` material names, matte or glass materials,
+ * textures, faces -- is the caller's part (clear_gb300/model_loader.py). */
+enum { CLR_OBJ_VTN = 0, CLR_OBJ_VN = 1, CLR_OBJ_VT = 2, CLR_OBJ_V = 3, CLR_OBJ_NONE = 4 };
+
+typedef struct clr_obj_group {
+    uint32_t first_face, num_faces; /* range in the face array */
+    uint32_t format;                /* CLR_OBJ_*, fixed by the run's first face */
+    uint32_t smooth;                /* `s` value in effect (0 = off) */
+    uint32_t name;                  /* `g` name, offset in the string table */
+    uint32_t material;              /* `usemtl` name, offset in the string table */
+} clr_obj_group;
+
+typedef struct clr_obj_material { /* OBJ::Material (ModelLoader.cpp:34-51) */
+    float Kd[3], Ks[3], Ka[3];
+    float Ns, Ni;                   /* defaults 100 and 1 */
+    uint32_t name, map_Kd, map_Ks, map_Ka; /* string offsets (0 = none); maps include the .mtl's directory */
+} clr_obj_material;
+
+typedef struct clr_obj_counts {
+    uint32_t num_positions, num_uvs, num_normals, num_faces;
+    uint32_t num_groups, num_materials;
+    uint32_t num_skipped;           /* face lines dropped: no format, or an index outside the lists */
+    uint32_t string_bytes;
+} clr_obj_counts;
+
+typedef struct clr_obj_model clr_obj_model;
+
+/* Parses `path` and the first .mtl of each `mtllib` line.  CLR_EINVAL if the
+ * .obj cannot be opened. */
+CLR_API int clr_obj_parse(const char* path, clr_obj_model** model);
+CLR_API int clr_obj_counts_of(const clr_obj_model* model, clr_obj_counts* counts);
+/* Pointers into the model (valid until clr_obj_free): positions 3 floats and
+ * uvs 2 floats per entry, normals 3 floats, faces 9 uint32 per triangle
+ * (p0 p1 p2, uv0 uv1 uv2, n0 n1 n2; 0-based, UINT32_MAX where the group's
+ * format has no such index), groups, materials, the string table.  Any
+ * output pointer may be NULL. */
+CLR_API int clr_obj_data(const clr_obj_model* model, const float** positions, const float** uvs,
+                         const float** normals, const uint32_t** faces, const clr_obj_group** groups,
+                         const clr_obj_material** materials, const char** strings);
+CLR_API void clr_obj_free(clr_obj_model* model);
+
 /* ----------------------------------------------------------------- misc */
 
 /* Reads (and optionally clears) the device error bits CLR_DEVERR_* of the

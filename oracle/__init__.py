@@ -28,6 +28,7 @@ assert INODE_DTYPE.itemsize == 48 and LNODE_DTYPE.itemsize == 48 and BVHNODE_DTY
 _lib = None
 _ref_lbvh = None
 _ref_mid = None
+_ref_scene = None
 
 
 def _p(a):
@@ -150,10 +151,25 @@ def ref_available() -> bool:
 
 
 def _ref(name):
-    global _ref_lbvh, _ref_mid
+    global _ref_lbvh, _ref_mid, _ref_scene
     libs = {p.name: p for p in build_ref()}
     if not libs:
         raise RuntimeError("reference checkout not available; oracle/_ref not built")
+    if name == "scene":
+        if _ref_scene is None:
+            L = C.CDLL(str(libs["libref_scene.so"]))
+            L.ref_scene_new.restype = C.c_void_p
+            L.ref_scene_free.argtypes = [C.c_void_p]
+            L.ref_scene_exec.argtypes = [C.c_void_p, C.c_char_p]
+            L.ref_scene_exec.restype = C.c_int
+            L.ref_scene_blob.argtypes = [C.c_void_p, C.c_int, C.POINTER(C.c_void_p)]
+            L.ref_scene_blob.restype = C.c_uint64
+            L.ref_scene_names.argtypes = [C.c_void_p, C.c_int, C.c_char_p, C.c_uint64]
+            L.ref_scene_names.restype = C.c_uint64
+            L.ref_scene_next_model_id.argtypes = [C.c_void_p]
+            L.ref_scene_next_model_id.restype = C.c_int64
+            _ref_scene = L
+        return _ref_scene
     if name == "lbvh":
         if _ref_lbvh is None:
             _ref_lbvh = C.CDLL(str(libs["libref_lbvh.so"]))
@@ -237,3 +253,51 @@ def ref_render(scene_blobs: dict, inodes, lnodes, rand_states, pixels, width, he
                             _p(b["others"]), _p(inodes), _p(lnodes), _p(rand_states), _p(pixels),
                             C.c_uint32(width), C.c_uint32(height), C.c_uint32(y0), C.c_uint32(y1),
                             C.c_uint32(spp))
+
+
+SCENE_BLOBS = ("vertices", "normals", "tangents", "uvs", "faces", "lights", "materials", "textures", "others",
+               "light_powers")
+SCENE_NAMES = ("materials", "light_props", "textures", "others", "tex_files")
+
+
+class RefScene:
+    """The reference's Scene + MaterialCreator + loadModel driven by a command
+    script (oracle/ref_scene.cpp lists the commands).  Note the reference's
+    MaterialCreator is a process-wide singleton and its .obj model counter a
+    process-wide static: ``next_model_id`` says which number the next load
+    gets."""
+
+    def __init__(self):
+        self.L = _ref("scene")
+        self.h = self.L.ref_scene_new()
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            self.L.ref_scene_free(self.h)
+            self.h = None
+
+    def exec(self, script: str) -> int:
+        n = self.L.ref_scene_exec(self.h, script.encode())
+        if n < 0:
+            raise ValueError(f"unknown command on line {-n}: {script.splitlines()[-n - 1]!r}")
+        return n
+
+    def blob(self, name: str) -> bytes:
+        p = C.c_void_p()
+        n = self.L.ref_scene_blob(self.h, SCENE_BLOBS.index(name), C.byref(p))
+        return C.string_at(p, n) if n else b""
+
+    def names(self, name: str) -> dict:
+        which = SCENE_NAMES.index(name)
+        n = self.L.ref_scene_names(self.h, which, None, 0)
+        buf = C.create_string_buffer(n)
+        self.L.ref_scene_names(self.h, which, buf, n)
+        out = {}
+        for line in buf.raw[:n].decode().splitlines():
+            k, v = line.rsplit("\t", 1)
+            out[k] = int(v)
+        return out
+
+    @property
+    def next_model_id(self) -> int:
+        return int(self.L.ref_scene_next_model_id(self.h))

@@ -6,9 +6,15 @@
 * ``oracle/_ref/libref_lbvh.so`` and ``oracle/_ref/libref_mid.so`` -- the
   reference's own CPU code (``OpenCL_PathTracer/Equivalent/sim_*.hpp`` and
   ``OpenCL_PathTracer/BVH.hpp``) compiled in place from a reference checkout
-  with the stand-in headers of ``oracle/ref_stubs``.  Built only when the
-  checkout exists (``CLEAR_REFERENCE_DIR``, default ``/root/reference``);
-  nothing is copied out of it.
+  with the stand-in headers of ``oracle/ref_stubs``.
+* ``oracle/_ref/libref_scene.so`` -- the reference's scene encoders and .obj
+  loader (``OpenCL_PathTracer/CreateFunctions.cpp``, ``ModelLoader.cpp``,
+  with ``LinearAlgebra/*.cpp`` for the matrix stack of ``Scene.h``) behind
+  ``oracle/ref_scene.cpp``.
+
+The ``_ref`` libraries are built only when the checkout exists
+(``CLEAR_REFERENCE_DIR``, default ``/root/reference``); nothing is copied out
+of it.
 """
 from __future__ import annotations
 
@@ -60,6 +66,17 @@ def build_ref() -> list[Path]:
             _run(["g++", "-std=c++17", "-w", *CFLAGS, *defs, f"-I{stubs}", f"-I{eq}",
                   f"-I{REF_DIR / 'OpenCL_PathTracer'}", str(src), "-o", str(out)])
         built.append(out)
+    out = outdir / "libref_scene.so"
+    scene_src = HERE / "ref_scene.cpp"
+    if _stale(out, [scene_src, *stubs.iterdir(), Path(__file__)]):
+        pt, la = REF_DIR / "OpenCL_PathTracer", REF_DIR / "LinearAlgebra"
+        srcs = [scene_src, pt / "CreateFunctions.cpp", pt / "ModelLoader.cpp",
+                *(la / f for f in ("Matrix4f.cpp", "Vector4f.cpp", "Vector3f.cpp", "Point3f.cpp"))]
+        # the encoders copy stack structs whose padding they never set:
+        # zero-initialised locals make those bytes zeros instead of garbage
+        _run(["g++", "-std=c++17", "-w", *CFLAGS, "-ftrivial-auto-var-init=zero", f"-I{stubs}", f"-I{pt}",
+              f"-I{la}", *map(str, srcs), "-o", str(out), "-Wl,--no-undefined"])
+    built.append(out)
     return built
 
 

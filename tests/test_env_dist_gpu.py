@@ -61,9 +61,8 @@ def test_env_distribution_matches_encoder(cuda, shape):
     torch.cuda.synchronize()
     assert np.array_equal(o.cpu().numpy(), ref1)
     assert not np.array_equal(ref0, ref1)
-    # the reference's own row weights (cosf of a float argument) evaluated on
-    # the device: near the poles the weight is close to 0, so the float
-    # rounding of the argument moves it by ~1e-5 relative
+    # the default row weights, the same float argument through the device's
+    # cosf instead of the C library's: equal to a few ulps of the weight
     ds.update_env_distribution(encoder_weights=False)
     got = o.cpu().numpy()
     for lo, hi in spans:
