@@ -84,31 +84,144 @@ def _f3(x, y, z) -> bytes:
 
 
 # ---------------------------------------------------------------- matrices
-# Column-major 4x4 like the reference's Matrix4f (matrix.cl reads s048c as
-# the first row).
+# 4x4 float32 matrices m[row, col] with the reference's arithmetic
+# (LinearAlgebra/Matrix4f.hpp, LinearAlgebra.cpp:47-98): every product and sum
+# is rounded to float in the order written there (sums left to right, no
+# fused multiply-add), so that vertices and normals placed by a transform are
+# the reference's bit for bit.  The blobs store them column-major, as the
+# kernels read them (matrix.cl reads s048c as the first row).
+
+_F = np.float32
+
+
+_libm_handle = None
+
+
+def _libm():
+    """The C library's float functions (cosf, sinf, sqrtf), which the
+    reference's host code calls."""
+    global _libm_handle
+    if _libm_handle is None:
+        L = C.CDLL(ctypes.util.find_library("m"))
+        for fn in ("cosf", "sinf", "sqrtf"):
+            getattr(L, fn).argtypes = [C.c_float]
+            getattr(L, fn).restype = C.c_float
+        _libm_handle = L
+    return _libm_handle
+
+
+def identity():
+    return np.eye(4, dtype=np.float32)
 
 
 def translate(x, y, z):
-    m = np.eye(4)
-    m[:3, 3] = (x, y, z)
+    m = identity()
+    m[:3, 3] = (_F(x), _F(y), _F(z))
     return m
 
 
 def scale(x, y, z):
-    return np.diag([x, y, z, 1.0])
+    m = identity()
+    m[0, 0], m[1, 1], m[2, 2] = _F(x), _F(y), _F(z)
+    return m
 
 
 def rotate(angle, ax, ay, az):
-    a = np.array([ax, ay, az], dtype=np.float64)
-    a /= np.linalg.norm(a)
-    c, s = math.cos(angle), math.sin(angle)
-    x, y, z = a
-    r = np.array([[c + x * x * (1 - c), x * y * (1 - c) - z * s, x * z * (1 - c) + y * s],
-                  [y * x * (1 - c) + z * s, c + y * y * (1 - c), y * z * (1 - c) - x * s],
-                  [z * x * (1 - c) - y * s, z * y * (1 - c) + x * s, c + z * z * (1 - c)]])
-    m = np.eye(4)
-    m[:3, :3] = r
+    """RotateMatrix (LinearAlgebra.cpp:73-98): `angle` in radians, rounded to
+    float as the reference's parameter is; cosf/sinf of the C library."""
+    L = _libm()
+    rx, ry, rz = _F(ax), _F(ay), _F(az)
+    length = _F(L.sqrtf(float(rx * rx + ry * ry + rz * rz)))
+    rx, ry, rz = rx / length, ry / length, rz / length
+    a = float(_F(angle))
+    c, s = _F(L.cosf(a)), _F(L.sinf(a))
+    omc = _F(1) - c
+    m = identity()
+    m[0, 0] = rx * rx * omc + c
+    m[1, 0] = rx * ry * omc + rz * s
+    m[2, 0] = rz * rx * omc - ry * s
+    m[0, 1] = rx * ry * omc - rz * s
+    m[1, 1] = ry * ry * omc + c
+    m[2, 1] = ry * rz * omc + rx * s
+    m[0, 2] = rz * rx * omc + ry * s
+    m[1, 2] = ry * rz * omc - rx * s
+    m[2, 2] = rz * rz * omc + c
     return m
+
+
+def mul(*ms):
+    """Product of matrices left to right, each entry dot(row, column) summed
+    left to right in float (Matrix4f::operator*, Matrix4f.hpp:193-213)."""
+    out = np.asarray(ms[0], dtype=np.float32)
+    for m in ms[1:]:
+        m = np.asarray(m, dtype=np.float32)
+        out = ((out[:, 0:1] * m[0:1, :] + out[:, 1:2] * m[1:2, :]) + out[:, 2:3] * m[2:3, :]) + \
+            out[:, 3:4] * m[3:4, :]
+    return out
+
+
+def invert(m):
+    """Matrix4f::Invert (Matrix4f.hpp:81-163): Gauss-Jordan elimination with
+    full pivoting on the transposed matrix, in float; NaNs for a singular
+    matrix."""
+    inv = [[_F(m[j, i]) for j in range(4)] for i in range(4)]  # inverse[i][j] = m_ji
+    col_idx, row_idx, piv = [0] * 4, [0] * 4, [-1] * 4
+    icol = irow = 0
+    for i in range(4):
+        best = _F(0)
+        for j in range(4):
+            if piv[j] != 0:
+                for k in range(4):
+                    if piv[k] == -1:
+                        v = abs(inv[j][k])
+                        if v > best:
+                            best, irow, icol = v, j, k
+                    elif piv[k] > 0:
+                        return np.asarray(m, dtype=np.float32).copy()
+        piv[icol] += 1
+        if irow != icol:
+            inv[irow], inv[icol] = inv[icol], inv[irow]
+        row_idx[i], col_idx[i] = irow, icol
+        pivot = inv[icol][icol]
+        if pivot == 0:
+            return np.full((4, 4), np.nan, dtype=np.float32)
+        one_over = _F(1) / pivot
+        inv[icol][icol] = _F(1)
+        inv[icol] = [x * one_over for x in inv[icol]]
+        for j in range(4):
+            if j != icol:
+                f = inv[j][icol]
+                inv[j][icol] = _F(0)
+                inv[j] = [inv[j][k] - inv[icol][k] * f for k in range(4)]
+    for i in range(3, -1, -1):
+        ir, ic = row_idx[i], col_idx[i]
+        for j in range(4):
+            inv[j][ir], inv[j][ic] = inv[j][ic], inv[j][ir]
+    out = np.empty((4, 4), dtype=np.float32)
+    for c in range(4):
+        for r in range(4):
+            out[r, c] = inv[c][r]
+    return out
+
+
+def transform_points(m, p):
+    """Matrix4f * Point3f (Matrix4f.hpp:247-256) for each row of p (n, 3)."""
+    m = np.asarray(m, dtype=np.float32)
+    p = np.asarray(p, dtype=np.float32).reshape(-1, 3)
+    x, y, z = p[:, 0], p[:, 1], p[:, 2]
+    r = [((m[i, 0] * x + m[i, 1] * y) + m[i, 2] * z) + m[i, 3] for i in range(4)]
+    nw = r[3]
+    out = np.stack(r[:3], axis=1)
+    keep = nw == _F(1)
+    return np.where(keep[:, None], out, out / np.where(keep, _F(1), nw)[:, None])
+
+
+def transform_vectors(m, v):
+    """Matrix4f * Vector3f (Matrix4f.hpp:231-235): the upper 3x3 block."""
+    m = np.asarray(m, dtype=np.float32)
+    v = np.asarray(v, dtype=np.float32).reshape(-1, 3)
+    x, y, z = v[:, 0], v[:, 1], v[:, 2]
+    return np.stack([(m[i, 0] * x + m[i, 1] * y) + m[i, 2] * z for i in range(3)], axis=1)
 
 
 def look_at(eye, target, up):
@@ -131,22 +244,15 @@ def _colmajor(m) -> bytes:
 
 # --------------------------------------------------- environment rows
 
-_libm = None
-
-
 def zenith_weights(h: int) -> np.ndarray:
     """Row weights of the environment distribution, as
     CreateFunctions.cpp:275 computes them: cosf((float)(M_PI * (double)a))
     with a = 0.5f - (i + 0.5f) / h in float, through the C library's cosf."""
-    global _libm
-    if _libm is None:
-        _libm = C.CDLL(ctypes.util.find_library("m"))
-        _libm.cosf.argtypes = [C.c_float]
-        _libm.cosf.restype = C.c_float
+    cosf = _libm().cosf
     i = np.arange(h, dtype=np.float32)
     a = (np.float32(0.5) - (i + np.float32(0.5)) / np.float32(h)).astype(np.float32)
     arg = (math.pi * a.astype(np.float64)).astype(np.float32)
-    return np.array([_libm.cosf(float(x)) for x in arg], dtype=np.float32)
+    return np.array([cosf(float(x)) for x in arg], dtype=np.float32)
 
 
 # ------------------------------------------------------------------- scene
@@ -213,28 +319,34 @@ class Scene:
         self.mat_ref, self.light_ref, self.tex_ref, self.other_ref = _NameMap(), _NameMap(), _NameMap(), _NameMap()
         self.tex_files = _NameMap()  # image file -> texture offset (texFilesDatabase)
         self.models: set = set()     # loaded model files (modelDatabase)
-        self.local_to_world = [np.eye(4)]
+        self.local_to_world = [identity()]
         self._base = None
         self.mc = MaterialCreator(self)
 
     # Scene.h:62-81 -------------------------------------------------------
     def push(self, m=None):
+        """Matrix4fStack::push, then `*= m` (Matrix4fStack.hpp:28-47)."""
         top = self.local_to_world[-1]
-        self.local_to_world.append(top @ m if m is not None else top.copy())
+        self.local_to_world.append(mul(top, m) if m is not None else top.copy())
+
+    def apply(self, m):
+        """Matrix4fStack `*= m`: the top becomes top * m."""
+        self.local_to_world[-1] = mul(self.local_to_world[-1], m)
 
     def pop(self):
-        self.local_to_world.pop()
+        if len(self.local_to_world) > 1:
+            self.local_to_world.pop()
+        else:
+            self.local_to_world[0] = identity()
 
     def add_vertex(self, x, y, z):
-        p = self.local_to_world[-1] @ np.array([x, y, z, 1.0])
-        self.vertices.append(p[:3] / p[3])
+        self.vertices.append(transform_points(self.local_to_world[-1], [x, y, z])[0])
 
     def add_normal(self, x, y, z):
-        n = np.linalg.inv(self.local_to_world[-1]).T @ np.array([x, y, z, 0.0])
-        self.normals.append(n[:3])
+        self.normals.append(transform_vectors(invert(self.local_to_world[-1]).T, [x, y, z])[0])
 
     def add_tangent(self, x, y, z):
-        self.tangents.append((self.local_to_world[-1] @ np.array([x, y, z, 0.0]))[:3])
+        self.tangents.append(transform_vectors(self.local_to_world[-1], [x, y, z])[0])
 
     def add_uv(self, u, v):
         self.uvs.append((u, v))
@@ -250,18 +362,15 @@ class Scene:
         mesh: verts (n,3) in object space (transformed by the current
         matrix), tris (m,3) object-relative vertex indices; uvs and normals,
         if given, are per vertex and indexed like the vertices."""
-        verts = np.asarray(verts, dtype=np.float64)
         m4 = self.local_to_world[-1]
-        vh = np.concatenate([verts, np.ones((len(verts), 1))], axis=1) @ m4.T
         bv, bn, bu = len(self.vertices), len(self.normals), len(self.uvs)
-        self.vertices.extend(vh[:, :3] / vh[:, 3:4])
+        self.vertices.extend(transform_points(m4, verts))
         tris = np.asarray(tris, dtype=np.int64)
         f = np.zeros(len(tris), dtype=FACE_DTYPE)
         f["p"] = tris + bv
         f["vn"] = f["vt"] = f["uv"] = NONE32
         if normals is not None:
-            nm = np.asarray(normals, dtype=np.float64) @ np.linalg.inv(m4)[:3, :3]
-            self.normals.extend(nm)
+            self.normals.extend(transform_vectors(invert(m4).T, normals))
             f["vn"] = tris + bn
         if uvs is not None:
             self.uvs.extend(np.asarray(uvs, dtype=np.float64))
@@ -297,14 +406,11 @@ class Scene:
     # bulk forms of the four calls above, for whole arrays ------------------
     def add_vertices(self, p):
         """add_vertex for each row of p (n, 3)."""
-        p = np.asarray(p, dtype=np.float64).reshape(-1, 3)
-        vh = np.concatenate([p, np.ones((len(p), 1))], axis=1) @ self.local_to_world[-1].T
-        self.vertices.extend(vh[:, :3] / vh[:, 3:4])
+        self.vertices.extend(transform_points(self.local_to_world[-1], p))
 
     def add_normals(self, n):
         """add_normal for each row of n (n, 3)."""
-        n = np.asarray(n, dtype=np.float64).reshape(-1, 3)
-        self.normals.extend(n @ np.linalg.inv(self.local_to_world[-1])[:3, :3])
+        self.normals.extend(transform_vectors(invert(self.local_to_world[-1]).T, n))
 
     def add_uvs(self, uv):
         self.uvs.extend(np.asarray(uv, dtype=np.float64).reshape(-1, 2))

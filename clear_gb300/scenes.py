@@ -20,7 +20,7 @@ from . import scene as S
 
 
 def _box(sc: S.Scene, mat, center, size, angle_deg):
-    m = S.translate(*center) @ S.rotate(math.radians(angle_deg), 0, 1, 0) @ S.scale(*size)
+    m = S.mul(S.translate(*center), S.rotate(math.radians(angle_deg), 0, 1, 0), S.scale(*size))
     sc.push(m)
     sc.begin_object()
     for x in (-0.5, 0.5):

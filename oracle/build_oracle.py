@@ -9,7 +9,7 @@
   with the stand-in headers of ``oracle/ref_stubs``.
 * ``oracle/_ref/libref_scene.so`` -- the reference's scene encoders and .obj
   loader (``OpenCL_PathTracer/CreateFunctions.cpp``, ``ModelLoader.cpp``,
-  with ``LinearAlgebra/*.cpp`` for the matrix stack of ``Scene.h``) behind
+  with ``LinearAlgebra/*.cpp`` for the matrices of ``Scene.h``) behind
   ``oracle/ref_scene.cpp``.
 
 The ``_ref`` libraries are built only when the checkout exists
@@ -71,7 +71,8 @@ def build_ref() -> list[Path]:
     if _stale(out, [scene_src, *stubs.iterdir(), Path(__file__)]):
         pt, la = REF_DIR / "OpenCL_PathTracer", REF_DIR / "LinearAlgebra"
         srcs = [scene_src, pt / "CreateFunctions.cpp", pt / "ModelLoader.cpp",
-                *(la / f for f in ("Matrix4f.cpp", "Vector4f.cpp", "Vector3f.cpp", "Point3f.cpp"))]
+                *(la / f for f in ("LinearAlgebra.cpp", "Matrix4f.cpp", "Vector4f.cpp", "Vector3f.cpp",
+                                 "Point3f.cpp"))]
         # the encoders copy stack structs whose padding they never set:
         # zero-initialised locals make those bytes zeros instead of garbage
         _run(["g++", "-std=c++17", "-w", *CFLAGS, "-ftrivial-auto-var-init=zero", f"-I{stubs}", f"-I{pt}",

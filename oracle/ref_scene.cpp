@@ -12,7 +12,9 @@
  *
  * Driven by a small command script, one command per line, each naming one
  * MaterialCreator / Scene / loadModel call with its arguments (floats in any
- * strtof form, "-" for a null name or an absent override).
+ * strtof form, "-" for a null name or an absent override); push / pop /
+ * translate / scale / rotate act on the scene's local-to-world stack
+ * (`*=` of LinearAlgebra.cpp's matrices).
  *
  * loadImage (ImageLoader.h) is replaced: the reference decodes PNG with
  * libpng and EXR with OpenEXR, neither of which is part of this build.  The
@@ -34,6 +36,7 @@
 
 #include "CreateFunctions.hpp"
 #include "ImageLoader.h"
+#include "LinearAlgebra.h"
 #include "ModelLoader.hpp"
 
 namespace {
@@ -220,6 +223,12 @@ int ref_scene_exec(void* hp, const char* script) {
         else if (c == "normal" && k == 4) sc->addNormal(F(a[1]), F(a[2]), F(a[3]));
         else if (c == "uv" && k == 3) sc->addUV(F(a[1]), F(a[2]));
         else if (c == "light_dist" && k == 1) sc->calcLightPowerDistribution();
+        else if (c == "push" && k == 1) sc->localToWorld.push();
+        else if (c == "pop" && k == 1) sc->localToWorld.pop();
+        else if (c == "translate" && k == 4) sc->localToWorld *= LinearAlgebra::TranslateMatrix(F(a[1]), F(a[2]), F(a[3]));
+        else if (c == "scale" && k == 4) sc->localToWorld *= LinearAlgebra::ScaleMatrix(F(a[1]), F(a[2]), F(a[3]));
+        else if (c == "rotate" && k == 5)
+            sc->localToWorld *= LinearAlgebra::RotateMatrix(F(a[1]), F(a[2]), F(a[3]), F(a[4]));
         else if ((c == "obj" || c == "objn") && k == 4) {
             // obj: overrides as numbers; objn: as a material and a light
             // property name.  OBJ::load numbers the models it finishes

@@ -149,6 +149,25 @@ ibl_light sky env 2.5
     "obj": """obj <obj>/scene1.obj - -
 obj <obj>/scene2.obj - -
 """,
+    "transforms": """push
+translate 0.25 -0.5 1.5
+rotate 0.52359879 0 1 0
+scale 0.25 0.5 0.25
+vertex 1 2 3
+vertex -0 0.1 -7.25
+normal 0 0 1
+normal 0.6 0.8 0
+push
+rotate -0.9424778 0.3 1 0.2
+translate 1 0 0
+scale 1 -2 0.5
+obj <obj>/scene1.obj - -
+pop
+pop
+pop
+vertex 1 2 3
+normal 0.6 0.8 0
+""",
     "obj_override": """f3tex Le 4 4 4
 diffuse_light lamp Le
 ftex s0 0

@@ -9,6 +9,7 @@ One difference is intended and adjusted for: the 2D environment
 distribution's parent PDF/CDF offsets are stored relative to the embedded 1D
 record the kernels add them to, 8 bytes after the reference's base.
 """
+import ctypes
 import json
 import os
 import struct
@@ -19,6 +20,7 @@ import pytest
 
 import oracle
 from clear_gb300 import _lib, model_loader
+from clear_gb300 import scene as S
 from clear_gb300.scene import Scene
 
 HERE = os.path.dirname(os.path.abspath(__file__))
@@ -26,7 +28,14 @@ sys.path.insert(0, os.path.join(HERE, "golden"))
 import make_golden_scene as G  # noqa: E402
 
 GOLDEN = np.load(os.path.join(HERE, "golden", "scene_blobs.npz"))
-F = np.float32
+_libc = ctypes.CDLL(None)
+_libc.strtof.argtypes = [ctypes.c_char_p, ctypes.c_void_p]
+_libc.strtof.restype = ctypes.c_float
+
+
+def F(text) -> np.float32:
+    """A number of a script as the reference's harness reads it (strtof)."""
+    return np.float32(_libc.strtof(str(text).encode(), None))
 
 
 def _texels(s: Scene, name: str) -> np.ndarray:
@@ -39,7 +48,7 @@ def _texels(s: Scene, name: str) -> np.ndarray:
 def run_ours(script: str, objdir: str, model_ids) -> tuple[Scene, list]:
     """Replays a command script (oracle/ref_scene.cpp's commands) through
     this package; returns the scene and the 2D distributions it created."""
-    s, mc, ids, dists = Scene(), None, iter(model_ids), []
+    s, ids, dists = Scene(), iter(model_ids), []
     mc = s.mc
     bump = lambda x: None if x == "-" else x  # noqa: E731
     for line in script.strip().splitlines():
@@ -91,6 +100,16 @@ def run_ours(script: str, objdir: str, model_ids) -> tuple[Scene, list]:
             s.add_uv(*v)
         elif c == "light_dist":
             s.calc_light_power_distribution()
+        elif c == "push":
+            s.push()
+        elif c == "pop":
+            s.pop()
+        elif c == "translate":
+            s.apply(S.translate(*v))
+        elif c == "scale":
+            s.apply(S.scale(*v))
+        elif c == "rotate":
+            s.apply(S.rotate(*v))
         elif c == "obj":
             model_loader.load_model(a[1], s, None, None, model_id=next(ids))
         elif c == "objn":
@@ -189,7 +208,7 @@ def test_parser_reads_the_reference_line_rules():
     assert m.faces[6].tolist()[:3] == [8, 9, 5] and m.faces[6].tolist()[3:6] == [0xFFFFFFFF] * 3
     mats = {x["name"]: x for x in m.materials}
     assert list(mats) == ["red", "textured", "alpha", "glass", "two", "bumpy"]
-    assert mats["red"]["Kd"] == tuple(F([0.63, 0.065, 0.05])) and mats["red"]["Ni"] == 1.0
+    assert mats["red"]["Kd"] == tuple(F(x) for x in ("0.63", "0.065", "0.05")) and mats["red"]["Ni"] == 1.0
     assert mats["alpha"]["Kd"] == (0.0, 0.0, 0.0)  # its Kd line is tab-indented
     assert mats["two"]["Kd"] == (0.0, 0.0, 0.0)    # fewer than three numbers
     assert mats["glass"]["Ni"] == F(1.5) and mats["red"]["Ns"] == 100.0  # Ns is not read
