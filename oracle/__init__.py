@@ -166,6 +166,8 @@ def _ref(name):
             L.ref_scene_blob.restype = C.c_uint64
             L.ref_scene_names.argtypes = [C.c_void_p, C.c_int, C.c_char_p, C.c_uint64]
             L.ref_scene_names.restype = C.c_uint64
+            L.ref_save_bmp.argtypes = [C.c_char_p, C.c_void_p, C.c_uint32, C.c_uint32]
+            L.ref_save_bmp.restype = None
             L.ref_scene_next_model_id.argtypes = [C.c_void_p]
             L.ref_scene_next_model_id.restype = C.c_int64
             _ref_scene = L
@@ -301,3 +303,9 @@ class RefScene:
     @property
     def next_model_id(self) -> int:
         return int(self.L.ref_scene_next_model_id(self.h))
+
+
+def ref_save_bmp(path: str, pixels: np.ndarray, width: int, height: int) -> None:
+    """The reference's saveBMP (BMPExporter.cpp) writing `pixels`."""
+    px = np.ascontiguousarray(pixels, dtype=np.uint8)
+    _ref("scene").ref_save_bmp(str(path).encode(), px.ctypes.data, width, height)

@@ -7,8 +7,9 @@
   reference's own CPU code (``OpenCL_PathTracer/Equivalent/sim_*.hpp`` and
   ``OpenCL_PathTracer/BVH.hpp``) compiled in place from a reference checkout
   with the stand-in headers of ``oracle/ref_stubs``.
-* ``oracle/_ref/libref_scene.so`` -- the reference's scene encoders and .obj
-  loader (``OpenCL_PathTracer/CreateFunctions.cpp``, ``ModelLoader.cpp``,
+* ``oracle/_ref/libref_scene.so`` -- the reference's scene encoders, .obj
+  loader and BMP writer (``OpenCL_PathTracer/CreateFunctions.cpp``,
+  ``ModelLoader.cpp``, ``BMPExporter.cpp``,
   with ``LinearAlgebra/*.cpp`` for the matrices of ``Scene.h``) behind
   ``oracle/ref_scene.cpp``.
 
@@ -70,7 +71,7 @@ def build_ref() -> list[Path]:
     scene_src = HERE / "ref_scene.cpp"
     if _stale(out, [scene_src, *stubs.iterdir(), Path(__file__)]):
         pt, la = REF_DIR / "OpenCL_PathTracer", REF_DIR / "LinearAlgebra"
-        srcs = [scene_src, pt / "CreateFunctions.cpp", pt / "ModelLoader.cpp",
+        srcs = [scene_src, pt / "CreateFunctions.cpp", pt / "ModelLoader.cpp", pt / "BMPExporter.cpp",
                 *(la / f for f in ("LinearAlgebra.cpp", "Matrix4f.cpp", "Vector4f.cpp", "Vector3f.cpp",
                                  "Point3f.cpp"))]
         # the encoders copy stack structs whose padding they never set:

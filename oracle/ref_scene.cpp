@@ -5,8 +5,9 @@
  * the reference checkout with the stand-in headers in oracle/ref_stubs.
  *
  * TEST INFRASTRUCTURE ONLY: it pins the Python scene encoders
- * (clear_gb300/scene.py) and the .obj loader (clear_gb300/model_loader.py)
- * byte for byte against the reference, and generates the golden fixtures
+ * (clear_gb300/scene.py), the .obj loader (clear_gb300/model_loader.py) and
+ * the BMP writer (clear_gb300/postprocess.py, against BMPExporter.cpp) byte
+ * for byte against the reference, and generates the golden fixtures
  * under tests/golden.  Built only where the reference sources are present
  * (oracle/build_oracle.py), into oracle/_ref/.
  *
@@ -34,6 +35,7 @@
 #include <string>
 #include <vector>
 
+#include "BMPExporter.h"
 #include "CreateFunctions.hpp"
 #include "ImageLoader.h"
 #include "LinearAlgebra.h"
@@ -284,6 +286,12 @@ uint64_t ref_scene_names(void* hp, int which, char* buf, uint64_t cap) {
     for (const auto& kv : *m) out += kv.first + "\t" + std::to_string(kv.second) + "\n";
     if (buf && cap) memcpy(buf, out.data(), std::min<uint64_t>(cap, out.size()));
     return out.size();
+}
+
+/* saveBMP (BMPExporter.cpp) of `pixels`, the 3 * width + width % 4 byte
+ * rows the tone-mapping kernel writes. */
+void ref_save_bmp(const char* path, const void* pixels, uint32_t width, uint32_t height) {
+    saveBMP(path, pixels, width, height);
 }
 
 /* The model number the next successful .obj load will use. */

@@ -52,3 +52,16 @@ def test_postprocess_matches_oracle(cuda, w, h, spp):
     rows = got.reshape(h, -1)
     assert np.all(rows[:, 3 * w:] == 0)
     assert _lib.device_status() == 0
+
+
+@pytest.mark.skipif(not __import__("oracle").ref_available(), reason="reference checkout not available")
+@pytest.mark.parametrize("w,h", [(1, 1), (5, 3), (6, 2), (7, 4), (8, 5)])
+def test_bmp_file_matches_reference_writer(tmp_path, w, h):
+    """save_bmp writes the same file as the reference's saveBMP, for every
+    row-padding case (width % 4 = 0 .. 3)."""
+    import oracle
+
+    px = OP.tonemap(_hdr(w * h, seed=w), w, h, 2)
+    oracle.ref_save_bmp(tmp_path / "ref.bmp", px, w, h)
+    PP.save_bmp(str(tmp_path / "ours.bmp"), px, w, h)
+    assert (tmp_path / "ours.bmp").read_bytes() == (tmp_path / "ref.bmp").read_bytes()
