@@ -108,9 +108,10 @@ def lib() -> C.CDLL:
             "clr_batch_pixels": [vp, C.POINTER(u32)],
             "clr_batch_render": [vp, vp, vp, u32, u32, u32, vp],
             "clr_postprocess_ldr": [vp, u32, u32, u32, vp, vp],
+            "clr_postprocess_scales": [vp, u32, u32, u32, vp, vp],
             "clr_bvh_visualize": [vp, u32, u32, vp, vp, vp],
             "clr_trace_closest_counted": [C.POINTER(ClrBvh), vp, u32, vp, vp, vp],
-            "clr_env_distribution_update": [vp, u32, vp, u32, u32, vp, vp],
+            "clr_env_distribution_update": [vp, u32, vp, u32, u32, u32, vp, vp],
             "clr_lbvh_pass_times": [vp, C.POINTER(C.c_float), C.POINTER(C.c_char_p), i32, C.POINTER(i32)],
             "clr_obj_parse": [C.c_char_p, C.POINTER(vp)],
             "clr_obj_counts_of": [vp, C.POINTER(ClrObjCounts)],

@@ -33,6 +33,18 @@ def to_ldr(accum: torch.Tensor, width: int, height: int, spp: int) -> torch.Tens
     return out
 
 
+def tone_scales(accum: torch.Tensor, width: int, height: int, spp: int) -> torch.Tensor:
+    """Per pixel {Y, expf(-Y), scale, 0} as ``to_ldr`` computes them
+    (``clr_postprocess_scales``): (width * height, 4) float32 on the GPU."""
+    out = torch.empty((height * width, 4), dtype=torch.float32, device=accum.device)
+    a = accum.contiguous()
+    with torch.cuda.device(accum.device):
+        _lib.call("clr_postprocess_scales", C.c_void_p(a.data_ptr()), C.c_uint32(width), C.c_uint32(height),
+                  C.c_uint32(spp), C.c_void_p(out.data_ptr()),
+                  C.c_void_p(torch.cuda.current_stream(accum.device).cuda_stream))
+    return out
+
+
 def bmp_bytes(pixels: np.ndarray, width: int, height: int) -> bytes:
     """The file saveBMP writes: a 14 + 40 byte header (24 bits, uncompressed,
     1 pixel per metre) followed by the pixel array."""

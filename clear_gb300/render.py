@@ -125,8 +125,10 @@ class DeviceScene:
 
     def env_row_weights(self) -> torch.Tensor:
         """The zenith correction of each environment row as the scene encoder
-        computes it (scene.zenith_weights)."""
-        return torch.from_numpy(zenith_weights(self.env_dist["height"])).to(self.device)
+        computes it (scene.zenith_weights), on the device (computed once)."""
+        if getattr(self, "_env_weights", None) is None:
+            self._env_weights = torch.from_numpy(zenith_weights(self.env_dist["height"])).to(self.device)
+        return self._env_weights
 
     def update_env_distribution(self, row_weight: torch.Tensor | None = None, encoder_weights: bool = True) -> None:
         """Rebuilds the environment light's importance distribution on the
@@ -141,7 +143,7 @@ class DeviceScene:
         with torch.cuda.device(self.device):
             _lib.call("clr_env_distribution_update", C.c_void_p(self.t["others"].data_ptr()),
                       C.c_uint32(d["dist_offset"]), C.c_void_p(self.t["textures"].data_ptr()),
-                      C.c_uint32(d["tex_offset"]), C.c_uint32(d["height"]),
+                      C.c_uint32(d["tex_offset"]), C.c_uint32(d["height"]), C.c_uint32(d["width"]),
                       C.c_void_p(row_weight.data_ptr()) if row_weight is not None else None,
                       C.c_void_p(torch.cuda.current_stream(self.device).cuda_stream))
 

@@ -260,20 +260,30 @@ CLR_API int clr_trace_closest_counted(const clr_bvh* bvh, const float* rays, uin
 CLR_API int clr_postprocess_ldr(const float* accum, uint32_t width, uint32_t height, uint32_t spp, uint8_t* bgr,
                                 void* stream);
 
+/* The luminance and tone-mapping scale clr_postprocess_ldr computes per
+ * pixel, written as float4 {Y, expf(-Y), scale, 0} to `scales` (16-byte
+ * aligned, width * height entries) instead of the bytes: the check that Y and
+ * scale are exactly the double-precision expressions of the reference's
+ * double literals (Y = (float)(0.2989 r + 0.5866 g + 0.1144 b),
+ * scale = (float)((1 - e) / Y)) although they are computed in float. */
+CLR_API int clr_postprocess_scales(const float* accum, uint32_t width, uint32_t height, uint32_t spp, float* scales,
+                                   void* stream);
+
 /* Recomputes, on the device and in place, the importance distribution of an
  * image-based environment light after its texels changed: the
  * ContinuousConsts2D_H that createContinuousConsts2D_H_FromImageTexture
  * (OpenCL_PathTracer/CreateFunctions.cpp:246-349) builds on the host, one
  * stratum per texel, at byte `dist_offset` of the `others` blob, from the
- * RGBA16F image texture at byte `tex_offset` of the `textures` blob, whose
- * height is `height`.  `row_weight` (height floats, device) weights each row's
- * luminance; NULL uses the reference's zenith correction
- * cos(pi (0.5 - (i + 0.5) / height)) evaluated on the device.  The structure's
- * headers must already be laid out (by the scene encoder); a mismatch sets
+ * RGBA16F image texture at byte `tex_offset` of the `textures` blob, of
+ * `width` x `height` texels (width at most 25,596).  `row_weight` (height
+ * floats, device) weights each row's luminance; NULL uses the reference's
+ * zenith correction cos(pi (0.5 - (i + 0.5) / height)) with the device's
+ * cosf.  The structure's headers must already be laid out (by the scene
+ * encoder); a mismatch with them, or with width / height, sets
  * CLR_DEVERR_INPUT. */
 CLR_API int clr_env_distribution_update(uint8_t* others, uint32_t dist_offset, const uint8_t* textures,
-                                        uint32_t tex_offset, uint32_t height, const float* row_weight,
-                                        void* stream);
+                                        uint32_t tex_offset, uint32_t height, uint32_t width,
+                                        const float* row_weight, void* stream);
 
 /* ------------------------------------------------------------- batched */
 

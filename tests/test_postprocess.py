@@ -54,6 +54,37 @@ def test_postprocess_matches_oracle(cuda, w, h, spp):
     assert _lib.device_status() == 0
 
 
+@pytest.mark.gpu
+def test_tone_scales_are_the_double_expressions(cuda):
+    """Y and the tone-mapping scale, computed in float-float with a double
+    fallback, equal the double-precision expressions exactly (numpy float64),
+    over 4 Mi pixels of a wide radiance distribution and the edge cases:
+    zeros, saturation, subnormal, negative and NaN channels."""
+    w, h, spp = 2048, 2048, 4
+    r = np.random.default_rng(11)
+    acc = np.zeros((w * h, 4), dtype=np.float32)
+    acc[:, :3] = (r.lognormal(0.0, 3.0, size=(w * h, 3)) * spp).astype(np.float32)
+    edge = np.array([[0, 0, 0], [1e9, 1e9, 1e9], [1e-40, 0, 0], [1e-30, 1e-30, 1e-30], [-1.0, 2.0, 3.0],
+                     [np.nan, 1.0, 1.0], [0.0, 0.0, 1e-7], [4.0, 4.0, 4.0], [120.0, 0.0, 0.0]], dtype=np.float32)
+    acc[:len(edge), :3] = edge
+    acc[len(edge):len(edge) + 4096, :3] = r.uniform(0, 1e-6, size=(4096, 3)).astype(np.float32)
+    got = PP.tone_scales(torch.from_numpy(acc).to(cuda), w, h, spp).cpu().numpy()
+    inv = np.float32(1.0) / np.float32(spp)
+    v = (acc[:, :3] * inv).astype(np.float32)
+    sat = np.where(v > np.float32(30.0), np.float32(30.0), v).astype(np.float32)
+    s64 = sat.astype(np.float64)
+    Y = (0.2989 * s64[:, 0] + 0.5866 * s64[:, 1] + 0.1144 * s64[:, 2]).astype(np.float32)
+    assert np.array_equal(got[:, 0], Y, equal_nan=True)
+    e = got[:, 1]
+    fin = np.isfinite(Y)
+    assert np.all(np.abs(e[fin].astype(np.float64) - np.exp(-Y[fin].astype(np.float64))) <= 3e-7 * e[fin])
+    with np.errstate(divide="ignore", invalid="ignore"):
+        scale = ((1.0 - e.astype(np.float64)) / Y.astype(np.float64)).astype(np.float32)
+    scale = np.where(Y == 0.0, np.float32(1.0), scale)
+    assert np.array_equal(got[:, 2], scale, equal_nan=True)
+    assert _lib.device_status() == 0
+
+
 @pytest.mark.skipif(not __import__("oracle").ref_available(), reason="reference checkout not available")
 @pytest.mark.parametrize("w,h", [(1, 1), (5, 3), (6, 2), (7, 4), (8, 5)])
 def test_bmp_file_matches_reference_writer(tmp_path, w, h):
