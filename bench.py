@@ -450,7 +450,7 @@ def run_ours(args):
     import torch
     import torch.distributed as dist
 
-    from clear_gb300 import _lib, lbvh
+    from clear_gb300 import _lib, lbvh, shard
     from clear_gb300 import workloads as W
     from clear_gb300.build import build
 
@@ -574,10 +574,7 @@ def run_ours(args):
     dev_err = _lib.device_status()
 
     # ---- max over ranks
-    vals = torch.tensor([ms_step, e2e_ms, closest_ms, shadow_ms], dtype=torch.float64, device=dev)
-    if world > 1:
-        dist.all_reduce(vals, op=dist.ReduceOp.MAX)
-    ms_step, e2e_ms, closest_ms, shadow_ms = vals.tolist()
+    ms_step, e2e_ms, closest_ms, shadow_ms = shard.max_over_ranks([ms_step, e2e_ms, closest_ms, shadow_ms], dev)
     if rank != 0:
         dist.destroy_process_group()
         return

@@ -98,6 +98,7 @@ def lib() -> C.CDLL:
             "clr_render": [vp, u32, u32, vp, vp, u32, u32, u32, vp],
             "clr_render_workspace_bytes": [u32, u32, C.POINTER(C.c_uint64)],
             "clr_render_wavefront": [vp, u32, u32, vp, vp, u32, u32, u32, vp, C.c_uint64, vp],
+            "clr_render_wavefront_rows": [vp, u32, u32, u32, u32, vp, vp, u32, u32, u32, vp, C.c_uint64, vp],
             "clr_render_adjoint_workspace_bytes": [u32, u32, u32, C.POINTER(C.c_uint64)],
             "clr_render_adjoint": [vp, u32, u32, vp, vp, u32, u32, u32, C.POINTER(ClrAdjointParams), vp,
                                    C.c_uint64, vp],

@@ -65,11 +65,12 @@ __device__ __forceinline__ uint32_t queue_slot(unsigned int* count, bool want) {
     return base + __popc(m & lt);
 }
 
-__device__ __forceinline__ void start_sample(const Camera& cam, WfState& S, uint32_t p, uint32_t width, Rng& rng,
-                                             uint32_t done) {
+// Pixel p of the rendered rows is image pixel (p % width, row0 + p / width).
+__device__ __forceinline__ void start_sample(const Camera& cam, WfState& S, uint32_t p, uint32_t width,
+                                             uint32_t row0, Rng& rng, uint32_t done) {
     f3 org, dir, alpha;
     float dirPDF;
-    camera_ray(cam, p % width, p / width, rng, org, dir, alpha, dirPDF);
+    camera_ray(cam, p % width, row0 + p / width, rng, org, dir, alpha, dirPDF);
     S.org[p] = make_float4(org.x, org.y, org.z, 0.f);
     S.dir[p] = make_float4(dir.x, dir.y, dir.z, dirPDF);
     S.alpha[p] = make_float4(alpha.x, alpha.y, alpha.z, luminance(alpha));
@@ -77,11 +78,11 @@ __device__ __forceinline__ void start_sample(const Camera& cam, WfState& S, uint
 }
 
 __global__ void __launch_bounds__(kWfThreads) k_wf_init(DScene sc, WfState S, uint32_t npix, uint32_t width,
-                                                        uint32_t* __restrict__ rand_states) {
+                                                        uint32_t row0, uint32_t* __restrict__ rand_states) {
     const Camera cam = load_camera(sc);
     for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < npix; p += gridDim.x * blockDim.x) {
         Rng rng = load_rng(rand_states, p);
-        start_sample(cam, S, p, width, rng, 0u);
+        start_sample(cam, S, p, width, row0, rng, 0u);
         store_rng(rand_states, p, rng);
         S.q[0][p] = p;
     }
@@ -107,7 +108,7 @@ __global__ void __launch_bounds__(kWfThreads) k_wf_extend(DScene sc, WfState S, 
     }
 }
 
-__global__ void __launch_bounds__(kWfThreads) k_wf_shade(DScene sc, WfState S, int cur, uint32_t width,
+__global__ void __launch_bounds__(kWfThreads) k_wf_shade(DScene sc, WfState S, int cur, uint32_t width, uint32_t row0,
                                                          uint32_t* __restrict__ rand_states,
                                                          float4* __restrict__ pixels, uint32_t spp,
                                                          uint32_t max_depth) {
@@ -224,7 +225,7 @@ __global__ void __launch_bounds__(kWfThreads) k_wf_shade(DScene sc, WfState S, i
             if (ended) {
                 const uint32_t done = m.z + 1;
                 if (done < spp) {
-                    start_sample(cam, S, p, width, rng, done);
+                    start_sample(cam, S, p, width, row0, rng, done);
                     cont = true;
                 } else {
                     S.misc[p] = make_uint4(depth, sampledType, done, p);
@@ -312,13 +313,17 @@ extern "C" int clr_render_workspace_bytes(uint32_t width, uint32_t height, uint6
     return CLR_OK;
 }
 
-extern "C" int clr_render_wavefront(const clr_scene* scene, uint32_t width, uint32_t height, uint32_t* rand_states,
-                                    float* pixels, uint32_t spp, uint32_t max_depth, uint32_t flags, void* workspace,
-                                    uint64_t workspace_bytes, void* stream) {
+extern "C" int clr_render_wavefront_rows(const clr_scene* scene, uint32_t width, uint32_t height, uint32_t row0,
+                                         uint32_t rows, uint32_t* rand_states, float* pixels, uint32_t spp,
+                                         uint32_t max_depth, uint32_t flags, void* workspace,
+                                         uint64_t workspace_bytes, void* stream) {
     int rc = check_render_args(scene, rand_states, pixels);
     if (rc != CLR_OK) return rc;
-    if (width == 0 || height == 0 || spp == 0) return CLR_OK;
-    const uint32_t npix = width * height;
+    if (row0 > height || rows > height - row0)
+        return clr_set_error(CLR_EINVAL, "clr_render_wavefront_rows: rows [%u, %u) outside the image's %u", row0,
+                             row0 + rows, height);
+    if (width == 0 || rows == 0 || spp == 0) return CLR_OK;
+    const uint32_t npix = width * rows;
     if (!workspace || workspace_bytes < wf_layout(npix, nullptr, nullptr))
         return clr_set_error(CLR_ECAPACITY, "clr_render_wavefront: workspace of %llu bytes is smaller than %zu",
                              (unsigned long long)workspace_bytes, wf_layout(npix, nullptr, nullptr));
@@ -332,7 +337,7 @@ extern "C" int clr_render_wavefront(const clr_scene* scene, uint32_t width, uint
     const bool ordered = (flags & CLR_RENDER_ORDERED) != 0;
     const unsigned int grid = std::min(div_up(npix, kWfThreads), 152u * 16u);
     float4* px = reinterpret_cast<float4*>(pixels);
-    k_wf_init<<<grid, kWfThreads, 0, st>>>(sc, S, npix, width, rand_states);
+    k_wf_init<<<grid, kWfThreads, 0, st>>>(sc, S, npix, width, row0, rand_states);
     CLR_LAUNCH_CHECK("k_wf_init");
     // every iteration advances each unfinished pixel by one path vertex
     const uint64_t max_iters = (uint64_t)spp * (max_depth + 1) + 1;
@@ -341,7 +346,7 @@ extern "C" int clr_render_wavefront(const clr_scene* scene, uint32_t width, uint
         if (ordered) k_wf_extend<true><<<grid, kWfThreads, 0, st>>>(sc, S, cur);
         else k_wf_extend<false><<<grid, kWfThreads, 0, st>>>(sc, S, cur);
         k_wf_reset<<<1, 1, 0, st>>>(S, cur ^ 1);
-        k_wf_shade<<<grid, kWfThreads, 0, st>>>(sc, S, cur, width, rand_states, px, spp, max_depth);
+        k_wf_shade<<<grid, kWfThreads, 0, st>>>(sc, S, cur, width, row0, rand_states, px, spp, max_depth);
         if (ordered) k_wf_shadow<true><<<grid, kWfThreads, 0, st>>>(sc, S, px);
         else k_wf_shadow<false><<<grid, kWfThreads, 0, st>>>(sc, S, px);
         CLR_LAUNCH_CHECK("wavefront iteration");
@@ -354,4 +359,11 @@ extern "C" int clr_render_wavefront(const clr_scene* scene, uint32_t width, uint
         }
     }
     return CLR_OK;
+}
+
+extern "C" int clr_render_wavefront(const clr_scene* scene, uint32_t width, uint32_t height, uint32_t* rand_states,
+                                    float* pixels, uint32_t spp, uint32_t max_depth, uint32_t flags, void* workspace,
+                                    uint64_t workspace_bytes, void* stream) {
+    return clr_render_wavefront_rows(scene, width, height, 0u, height, rand_states, pixels, spp, max_depth, flags,
+                                     workspace, workspace_bytes, stream);
 }

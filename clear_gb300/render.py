@@ -58,11 +58,24 @@ class DeviceScene:
         return rng, pix
 
     def render(self, rng: torch.Tensor, pix: torch.Tensor, spp: int, max_depth: int = 100,
-               ordered: bool = True, wavefront: bool = False) -> None:
+               ordered: bool = True, wavefront: bool = False, rows: tuple[int, int] | None = None) -> None:
         """Adds `spp` samples per pixel to `pix`.  wavefront=True runs the
-        extend/shade/shadow kernel split (same results as the megakernel)."""
+        extend/shade/shadow kernel split (same results as the megakernel).
+        rows=(y0, y1) renders those image rows only (wavefront form): `rng`
+        and `pix` then hold just those rows."""
         stream = C.c_void_p(torch.cuda.current_stream(self.device).cuda_stream)
         flags = C.c_uint32(RENDER_ORDERED if ordered else 0)
+        if rows is not None:
+            y0, y1 = rows
+            if rng.numel() < 4 * self.width * (y1 - y0) or pix.numel() < 4 * self.width * (y1 - y0):
+                raise ValueError("rng / pix hold fewer than the band's pixels")
+            ws = self.workspace()
+            with torch.cuda.device(self.device):
+                _lib.call("clr_render_wavefront_rows", C.byref(self.c), C.c_uint32(self.width), C.c_uint32(self.height),
+                          C.c_uint32(y0), C.c_uint32(y1 - y0), C.c_void_p(rng.data_ptr()), C.c_void_p(pix.data_ptr()),
+                          C.c_uint32(spp), C.c_uint32(max_depth), flags, C.c_void_p(ws.data_ptr()),
+                          C.c_uint64(ws.numel()), stream)
+            return
         args = (C.byref(self.c), C.c_uint32(self.width), C.c_uint32(self.height), C.c_void_p(rng.data_ptr()),
                 C.c_void_p(pix.data_ptr()), C.c_uint32(spp), C.c_uint32(max_depth), flags)
         with torch.cuda.device(self.device):

@@ -229,6 +229,19 @@ CLR_API int clr_render_wavefront(const clr_scene* scene, uint32_t width, uint32_
                                  float* pixels, uint32_t spp, uint32_t max_depth, uint32_t flags, void* workspace,
                                  uint64_t workspace_bytes, void* stream);
 
+/* clr_render_wavefront for the image rows [row0, row0 + rows) only (the
+ * reference renders per 64 x 64 tile, main.cpp:477-494): `rand_states` and
+ * `pixels` hold those rows alone (width * rows entries, row-major from row0),
+ * the camera sees the whole width x height image.  Each pixel's samples
+ * depend only on its own random state, so the rows of a band are
+ * bit-identical to the same rows of a whole-image render: one process per
+ * GPU renders a band and the bands are gathered (clear_gb300/shard.py).  The
+ * workspace holds clr_render_workspace_bytes(width, rows) bytes. */
+CLR_API int clr_render_wavefront_rows(const clr_scene* scene, uint32_t width, uint32_t height, uint32_t row0,
+                                      uint32_t rows, uint32_t* rand_states, float* pixels, uint32_t spp,
+                                      uint32_t max_depth, uint32_t flags, void* workspace, uint64_t workspace_bytes,
+                                      void* stream);
+
 /* Replaces the `bvh_visualizer` kernel (OpenCL/bvh_visualizer.cl:25-84): one
  * ray per pixel through the lens centre and pixel centre; adds to `pixels`
  * (float4 per pixel) the hit material's base colour plus 0.025 per BVH box
