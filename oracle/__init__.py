@@ -309,3 +309,25 @@ def ref_save_bmp(path: str, pixels: np.ndarray, width: int, height: int) -> None
     """The reference's saveBMP (BMPExporter.cpp) writing `pixels`."""
     px = np.ascontiguousarray(pixels, dtype=np.uint8)
     _ref("scene").ref_save_bmp(str(path).encode(), px.ctypes.data, width, height)
+
+
+def ref_cl_lbvh_build(vx, vy, vz, tri, n, bits=10) -> OracleBVH:
+    """The reference's own LBVH kernels (lbvh_construction.cl,
+    generic_kernels.cl) run on the CPU in the order of LBVHBuilder::perform
+    (oracle/ref_lbvh_cl.cpp); n >= 2."""
+    libs = {p.name: p for p in build_ref()}
+    if "libref_lbvh_cl.so" not in libs:
+        raise RuntimeError("reference checkout not available; oracle/_ref not built")
+    L = C.CDLL(str(libs["libref_lbvh_cl.so"]))
+    vx, vy, vz, tri = _f32(vx), _f32(vy), _f32(vz), _u32(tri)
+    inodes = np.zeros(n - 1, dtype=INODE_DTYPE)
+    lnodes = np.zeros(n, dtype=LNODE_DTYPE)
+    parents = np.zeros(2 * n - 1, dtype=np.uint32)
+    sidx = np.zeros(n, dtype=np.uint32)
+    q = np.zeros((n, 4), dtype=np.uint32)
+    box = np.zeros(6, dtype=np.float32)
+    rc = L.ref_cl_lbvh_build(_p(vx), _p(vy), _p(vz), _p(tri), C.c_uint32(n), C.c_uint32(bits), _p(inodes),
+                             _p(lnodes), _p(parents), _p(sidx), _p(q), _p(box))
+    if rc != 0:
+        raise RuntimeError(f"ref_cl_lbvh_build failed: {rc}")
+    return OracleBVH(inodes, lnodes, parents, sidx, np.ascontiguousarray(q[:, :3]), box, bits)

@@ -7,6 +7,9 @@
   reference's own CPU code (``OpenCL_PathTracer/Equivalent/sim_*.hpp`` and
   ``OpenCL_PathTracer/BVH.hpp``) compiled in place from a reference checkout
   with the stand-in headers of ``oracle/ref_stubs``.
+* ``oracle/_ref/libref_lbvh_cl.so`` -- the reference's LBVH construction
+  kernels (``OpenCL/lbvh_construction.cl``, ``CommonSources/OpenCL/
+  generic_kernels.cl``) run on the CPU by ``oracle/ref_lbvh_cl.cpp``.
 * ``oracle/_ref/libref_scene.so`` -- the reference's scene encoders, .obj
   loader and BMP writer (``OpenCL_PathTracer/CreateFunctions.cpp``,
   ``ModelLoader.cpp``, ``BMPExporter.cpp``,
@@ -79,7 +82,38 @@ def build_ref() -> list[Path]:
         _run(["g++", "-std=c++17", "-w", *CFLAGS, "-ftrivial-auto-var-init=zero", f"-I{stubs}", f"-I{pt}",
               f"-I{la}", *map(str, srcs), "-o", str(out), "-Wl,--no-undefined"])
     built.append(out)
+    out = outdir / "libref_lbvh_cl.so"
+    cl_src = HERE / "ref_lbvh_cl.cpp"
+    if _stale(out, [cl_src, *stubs.iterdir(), Path(__file__)]):
+        build_ref_kernels(out, cl_src, stubs)
+    built.append(out)
     return built
+
+
+def build_ref_kernels(out: Path, harness: Path, stubs: Path) -> None:
+    """The reference's LBVH kernels (lbvh_construction.cl, which includes
+    extra_atomics.cl, and generic_kernels.cl) compiled as C++ with the OpenCL C
+    subset of ref_stubs/opencl_c.hpp.  The kernel text is read from the
+    checkout and piped to the compiler: a work-group `local` declaration at
+    the start of a line becomes `static` (work-groups run one at a time, so a
+    function static is the group's local memory); nothing else changes and
+    nothing is written."""
+    import re
+    import tempfile
+
+    cl_dir = REF_DIR / "OpenCL_PathTracer" / "OpenCL"
+    texts = [(cl_dir / "lbvh_construction.cl").read_text(),
+             (REF_DIR / "CommonSources" / "OpenCL" / "generic_kernels.cl").read_text()]
+    src = "\n".join(re.sub(r"(?m)^(\s+)local\s", r"\1static ", t) for t in texts)
+    flags = ["-std=c++17", "-w", "-O2", "-fPIC", "-fsigned-char", "-ffp-contract=off", "-fno-fast-math",
+             f"-I{stubs}"]
+    with tempfile.TemporaryDirectory() as tmp:
+        obj = Path(tmp) / "kernels.o"
+        res = subprocess.run(["g++", *flags, "-include", str(stubs / "opencl_c.hpp"), f"-I{cl_dir}", "-x", "c++",
+                              "-", "-c", "-o", str(obj)], input=src, capture_output=True, text=True)
+        if res.returncode != 0:
+            raise RuntimeError(f"oracle build failed: reference LBVH kernels\n{res.stderr}")
+        _run(["g++", *flags, "-shared", str(harness), str(obj), "-o", str(out), "-Wl,--no-undefined"])
 
 
 if __name__ == "__main__":

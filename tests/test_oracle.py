@@ -2,9 +2,11 @@
 
 The reference has no tests or golden vectors of its own; the fixtures in
 tests/golden come from its CPU code (OpenCL_PathTracer/Equivalent and BVH.hpp)
-compiled in place -- see tests/golden/make_golden.py.
+compiled in place -- see tests/golden/make_golden.py -- and from its LBVH
+construction kernels run on the CPU (tests/golden/make_golden_build.py).
 """
 import os
+import sys
 
 import numpy as np
 import pytest
@@ -13,6 +15,9 @@ import oracle
 from clear_gb300 import workloads as W
 
 GOLDEN = os.path.join(os.path.dirname(__file__), "golden", "lbvh_traversal.npz")
+BUILD_GOLDEN = os.path.join(os.path.dirname(__file__), "golden", "lbvh_build_ref.npz")
+sys.path.insert(0, os.path.join(os.path.dirname(__file__), "golden"))
+import make_golden_build as GB  # noqa: E402
 MISS = 0xFFFFFFFF
 
 
@@ -154,3 +159,29 @@ def test_live_pin_against_reference(n, seed):
     rids, rts = oracle.ref_trace_closest_lbvh(vx, vy, vz, None, n, bvh, rays)
     np.testing.assert_array_equal(ids, rids)
     np.testing.assert_array_equal(ts[rids != MISS], rts[rids != MISS])
+
+
+@pytest.mark.parametrize("case", list(GB.CASES))
+def test_oracle_build_matches_reference_kernels_golden(case):
+    """The restated build equals the reference's own kernels
+    (lbvh_construction.cl, generic_kernels.cl, run on the CPU): Morton codes,
+    sorted order, internal and leaf nodes, parents, scene box -- digests of
+    every output, and the arrays themselves for the small cases."""
+    g = np.load(BUILD_GOLDEN)
+    kind, n, bits, seed = GB.CASES[case]
+    vx, vy, vz, tri = GB.case_inputs(kind, n, seed)
+    got = GB.outputs(oracle.lbvh_build(vx, vy, vz, tri, n, bits))
+    for k, a in got.items():
+        if f"{case}/{k}" in g.files:
+            assert np.array_equal(GB.canonical(k, a, n), GB.canonical(k, g[f"{case}/{k}"], n)), k
+        assert GB.digest(k, a, n) == str(g[f"{case}/{k}_sha256"]), k
+
+
+@pytest.mark.skipif(not oracle.ref_available(), reason="reference checkout not present")
+@pytest.mark.parametrize("n,bits,seed", [(2, 10, 1), (129, 10, 2), (2500, 10, 3), (1500, 21, 4), (600, 1, 5)])
+def test_oracle_build_matches_reference_kernels_live(n, bits, seed):
+    vx, vy, vz = W.triangle_soup(n, seed=seed)
+    ref = GB.outputs(oracle.ref_cl_lbvh_build(vx, vy, vz, None, n, bits))
+    got = GB.outputs(oracle.lbvh_build(vx, vy, vz, None, n, bits))
+    for k in ref:
+        assert np.array_equal(GB.canonical(k, got[k], n), GB.canonical(k, ref[k], n)), k
