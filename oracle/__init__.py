@@ -331,3 +331,16 @@ def ref_cl_lbvh_build(vx, vy, vz, tri, n, bits=10) -> OracleBVH:
     if rc != 0:
         raise RuntimeError(f"ref_cl_lbvh_build failed: {rc}")
     return OracleBVH(inodes, lnodes, parents, sidx, np.ascontiguousarray(q[:, :3]), box, bits)
+
+
+def ref_cl_postprocess(accum, width: int, height: int, spp: int) -> np.ndarray:
+    """The reference's own `clear`, `scaling` and `toneMapping` kernels
+    (post_processing.cl) run on the CPU: the BMP pixel array, padding zero."""
+    libs = {p.name: p for p in build_ref()}
+    if "libref_post_cl.so" not in libs:
+        raise RuntimeError("reference checkout not available; oracle/_ref not built")
+    L = C.CDLL(str(libs["libref_post_cl.so"]))
+    a = np.ascontiguousarray(np.asarray(accum, dtype=np.float32).reshape(width * height, 4))
+    out = np.zeros(height * (3 * width + width % 4), dtype=np.uint8)
+    L.ref_cl_postprocess(_p(a), C.c_uint32(width), C.c_uint32(height), C.c_uint32(spp), _p(out))
+    return out

@@ -7,9 +7,11 @@
   reference's own CPU code (``OpenCL_PathTracer/Equivalent/sim_*.hpp`` and
   ``OpenCL_PathTracer/BVH.hpp``) compiled in place from a reference checkout
   with the stand-in headers of ``oracle/ref_stubs``.
-* ``oracle/_ref/libref_lbvh_cl.so`` -- the reference's LBVH construction
-  kernels (``OpenCL/lbvh_construction.cl``, ``CommonSources/OpenCL/
-  generic_kernels.cl``) run on the CPU by ``oracle/ref_lbvh_cl.cpp``.
+* ``oracle/_ref/libref_lbvh_cl.so`` and ``libref_post_cl.so`` -- the
+  reference's LBVH construction kernels (``OpenCL/lbvh_construction.cl``,
+  ``CommonSources/OpenCL/generic_kernels.cl``) and post-processing kernels
+  (``OpenCL/post_processing.cl``) run on the CPU by ``oracle/ref_lbvh_cl.cpp``
+  and ``oracle/ref_post_cl.cpp`` (executor ``oracle/ref_cl_exec.cpp``).
 * ``oracle/_ref/libref_scene.so`` -- the reference's scene encoders, .obj
   loader and BMP writer (``OpenCL_PathTracer/CreateFunctions.cpp``,
   ``ModelLoader.cpp``, ``BMPExporter.cpp``,
@@ -82,29 +84,36 @@ def build_ref() -> list[Path]:
         _run(["g++", "-std=c++17", "-w", *CFLAGS, "-ftrivial-auto-var-init=zero", f"-I{stubs}", f"-I{pt}",
               f"-I{la}", *map(str, srcs), "-o", str(out), "-Wl,--no-undefined"])
     built.append(out)
-    out = outdir / "libref_lbvh_cl.so"
-    cl_src = HERE / "ref_lbvh_cl.cpp"
-    if _stale(out, [cl_src, *stubs.iterdir(), Path(__file__)]):
-        build_ref_kernels(out, cl_src, stubs)
-    built.append(out)
+    cl_dir = REF_DIR / "OpenCL_PathTracer" / "OpenCL"
+    for lib, harness, kernels in (
+            ("libref_lbvh_cl.so", "ref_lbvh_cl.cpp",
+             [cl_dir / "lbvh_construction.cl", REF_DIR / "CommonSources" / "OpenCL" / "generic_kernels.cl"]),
+            ("libref_post_cl.so", "ref_post_cl.cpp", [cl_dir / "post_processing.cl"])):
+        out = outdir / lib
+        if _stale(out, [HERE / harness, HERE / "ref_cl_exec.cpp", *stubs.iterdir(), Path(__file__)]):
+            build_ref_kernels(out, HERE / harness, kernels, stubs)
+        built.append(out)
     return built
 
 
-def build_ref_kernels(out: Path, harness: Path, stubs: Path) -> None:
-    """The reference's LBVH kernels (lbvh_construction.cl, which includes
-    extra_atomics.cl, and generic_kernels.cl) compiled as C++ with the OpenCL C
-    subset of ref_stubs/opencl_c.hpp.  The kernel text is read from the
-    checkout and piped to the compiler: a work-group `local` declaration at
-    the start of a line becomes `static` (work-groups run one at a time, so a
-    function static is the group's local memory); nothing else changes and
+def build_ref_kernels(out: Path, harness: Path, kernels: list[Path], stubs: Path) -> None:
+    """Reference OpenCL kernels compiled as C++ with the OpenCL C subset of
+    ref_stubs/opencl_c.hpp and linked with `harness` and the executor
+    (ref_cl_exec.cpp).  The kernel text is read from the checkout and piped to
+    the compiler with two spellings changed: a work-group `local` declaration
+    at the start of a line becomes `static` (work-groups run one at a time, so
+    a function static is the group's local memory), and a vector literal
+    `(T)(...)` becomes the functional cast `T(...)`; nothing else changes and
     nothing is written."""
     import re
     import tempfile
 
-    cl_dir = REF_DIR / "OpenCL_PathTracer" / "OpenCL"
-    texts = [(cl_dir / "lbvh_construction.cl").read_text(),
-             (REF_DIR / "CommonSources" / "OpenCL" / "generic_kernels.cl").read_text()]
-    src = "\n".join(re.sub(r"(?m)^(\s+)local\s", r"\1static ", t) for t in texts)
+    def rewrite(text: str) -> str:
+        text = re.sub(r"(?m)^(\s+)local\s", r"\1static ", text)
+        return re.sub(r"\((float3|point3|vector3|uint3|int3|uchar3)\)\(", r"\1(", text)
+
+    src = "\n".join(rewrite(k.read_text()) for k in kernels)
+    cl_dir = kernels[0].parent
     flags = ["-std=c++17", "-w", "-O2", "-fPIC", "-fsigned-char", "-ffp-contract=off", "-fno-fast-math",
              f"-I{stubs}"]
     with tempfile.TemporaryDirectory() as tmp:
@@ -113,7 +122,8 @@ def build_ref_kernels(out: Path, harness: Path, stubs: Path) -> None:
                               "-", "-c", "-o", str(obj)], input=src, capture_output=True, text=True)
         if res.returncode != 0:
             raise RuntimeError(f"oracle build failed: reference LBVH kernels\n{res.stderr}")
-        _run(["g++", *flags, "-shared", str(harness), str(obj), "-o", str(out), "-Wl,--no-undefined"])
+        _run(["g++", *flags, "-shared", str(harness), str(HERE / "ref_cl_exec.cpp"), str(obj), "-o", str(out),
+              "-Wl,--no-undefined"])
 
 
 if __name__ == "__main__":

@@ -14,15 +14,8 @@
  * compiles the kernels from the reference checkout through a pipe: nothing
  * of them is copied), into oracle/_ref/libref_lbvh_cl.so.
  *
- * Execution: an NDRange runs one work-group after another; within a group,
- * kernels with barriers run their work-items as coroutines (ucontext) that
- * yield at every barrier() in turn, so each barrier completes when every
- * work-item of the group has reached it; kernels without barriers run their
- * work-items one after another.  Work-group `local` arrays are function
- * statics, shared by the group and rewritten by each group before use.
+ * Execution: oracle/ref_cl_exec.cpp.
  */
-#include <ucontext.h>
-
 #include <cstdint>
 #include <cstdlib>
 #include <cstring>
@@ -51,84 +44,6 @@ void calcNodeAABBs(uchar* _iNodes, uint* counters, const uchar* _lNodes, uint nu
 void localScan(uint* elements, uint numElements, uint* blockSums);
 void addOffset(const uint* blockOffsets, uint* elements, uint numElements);
 }
-
-namespace clshim {
-Ids* g_cur = nullptr;
-
-namespace {
-struct Coro {
-    ucontext_t ctx;
-    Ids ids;
-    bool done;
-};
-ucontext_t g_sched;
-Coro* g_running = nullptr;
-bool g_in_coro = false;
-void (*g_body)(void*) = nullptr;
-void* g_body_arg = nullptr;
-
-void trampoline() {
-    g_body(g_body_arg);
-    g_running->done = true;
-    swapcontext(&g_running->ctx, &g_sched);
-}
-}  // namespace
-
-void barrier_yield() {
-    if (!g_in_coro) throw std::logic_error("barrier() in a kernel launched without coroutines");
-    swapcontext(&g_running->ctx, &g_sched);
-}
-
-// Runs body(arg) for every work-item of an NDRange of `global` items in
-// groups of `local` (global a multiple of local, offset 0).
-void launch(size_t global_size, size_t local_size, bool barriers, void (*body)(void*), void* arg) {
-    if (local_size == 0 || global_size % local_size) throw std::invalid_argument("NDRange not a multiple of the group");
-    const size_t groups = global_size / local_size;
-    if (!barriers) {
-        Ids ids{};
-        g_cur = &ids;
-        for (size_t g = 0; g < groups; ++g)
-            for (size_t l = 0; l < local_size; ++l) {
-                ids = Ids{g * local_size + l, l, g, groups, local_size, global_size, 0};
-                body(arg);
-            }
-        g_cur = nullptr;
-        return;
-    }
-    constexpr size_t kStack = 64 * 1024;
-    std::vector<Coro> items(local_size);
-    std::vector<char> stacks(kStack * local_size);
-    g_body = body;
-    g_body_arg = arg;
-    g_in_coro = true;
-    for (size_t g = 0; g < groups; ++g) {
-        for (size_t l = 0; l < local_size; ++l) {
-            Coro& c = items[l];
-            c.ids = Ids{g * local_size + l, l, g, groups, local_size, global_size, 0};
-            c.done = false;
-            getcontext(&c.ctx);
-            c.ctx.uc_stack.ss_sp = stacks.data() + l * kStack;
-            c.ctx.uc_stack.ss_size = kStack;
-            c.ctx.uc_link = nullptr;
-            makecontext(&c.ctx, trampoline, 0);
-        }
-        size_t left = local_size;
-        while (left) {  // one round: every unfinished work-item runs to its next barrier or its end
-            for (size_t l = 0; l < local_size; ++l) {
-                Coro& c = items[l];
-                if (c.done) continue;
-                g_running = &c;
-                g_cur = &c.ids;
-                swapcontext(&g_sched, &c.ctx);
-                if (c.done) --left;
-            }
-        }
-    }
-    g_in_coro = false;
-    g_running = nullptr;
-    g_cur = nullptr;
-}
-}  // namespace clshim
 
 namespace {
 

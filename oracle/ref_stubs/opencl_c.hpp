@@ -1,7 +1,8 @@
-/* OpenCL C on the host, for compiling the reference's own LBVH kernels
- * (OpenCL_PathTracer/OpenCL/lbvh_construction.cl, CommonSources/OpenCL/
- * generic_kernels.cl) as C++ and running them on the CPU
- * (oracle/ref_lbvh_cl.cpp).  TEST INFRASTRUCTURE ONLY.
+/* OpenCL C on the host, for compiling the reference's own LBVH and
+ * post-processing kernels (OpenCL_PathTracer/OpenCL/lbvh_construction.cl,
+ * post_processing.cl, CommonSources/OpenCL/generic_kernels.cl) as C++ and
+ * running them on the CPU (oracle/ref_lbvh_cl.cpp, ref_post_cl.cpp).  TEST
+ * INFRASTRUCTURE ONLY.
  *
  * Written from the OpenCL C 1.2 specification for the subset those kernels
  * use: the address-space qualifiers (empty; the build turns the kernels'
@@ -10,10 +11,11 @@
  * byte size and alignment, their component-wise operators with scalar
  * widening, clz / min / max / fmin / fmax, convert_uint3_rtz (round toward
  * zero; NaN and negative inputs, undefined in OpenCL, give 0 as in the
- * oracle's restatement), convert_uchar3, as_uint / as_float, atomic_inc /
- * atomic_cmpxchg, the work-item functions and barrier(), which yields to the
- * next work-item of the group (oracle/ref_lbvh_cl.cpp runs a group's
- * work-items as coroutines). */
+ * oracle's restatement), convert_uchar3(_rtz), as_uint / as_float, exp / pow
+ * / clamp, atomic_inc / atomic_cmpxchg, the work-item functions and barrier(),
+ * which yields to the next work-item of the group (oracle/ref_cl_exec.cpp
+ * runs a group's work-items as coroutines).  Vector literals `(T)(a, b, c)`
+ * reach the compiler as `T(a, b, c)` (oracle/build_oracle.py). */
 #pragma once
 #include <cmath>
 #include <cstdint>
@@ -33,28 +35,36 @@ typedef uint64_t ulong;
 
 // ------------------------------------------------------------ work-items
 namespace clshim {
-struct Ids {
-    size_t gid, lid, grp, ngrp, lsize, gsize, goff;
+struct Ids {  // per dimension 0, 1 (offsets are always 0)
+    size_t gid[2], lid[2], grp[2], ngrp[2], lsize[2], gsize[2];
 };
 extern Ids* g_cur;      // the running work-item's ids
 void barrier_yield();   // suspends the running work-item until the group reaches the barrier
+// 1-D NDRange of global_size items in groups of local_size (oracle/ref_cl_exec.cpp)
+void launch(size_t global_size, size_t local_size, bool barriers, void (*body)(void*), void* arg);
+// 2-D NDRange without barriers, one work-item per group
+void launch2d(size_t gx, size_t gy, void (*body)(void*), void* arg);
 }  // namespace clshim
 
-inline size_t get_global_id(uint) { return clshim::g_cur->gid; }
-inline size_t get_local_id(uint) { return clshim::g_cur->lid; }
-inline size_t get_group_id(uint) { return clshim::g_cur->grp; }
-inline size_t get_num_groups(uint) { return clshim::g_cur->ngrp; }
-inline size_t get_local_size(uint) { return clshim::g_cur->lsize; }
-inline size_t get_global_size(uint) { return clshim::g_cur->gsize; }
-inline size_t get_global_offset(uint) { return clshim::g_cur->goff; }
+inline size_t get_global_id(uint d) { return clshim::g_cur->gid[d]; }
+inline size_t get_local_id(uint d) { return clshim::g_cur->lid[d]; }
+inline size_t get_group_id(uint d) { return clshim::g_cur->grp[d]; }
+inline size_t get_num_groups(uint d) { return clshim::g_cur->ngrp[d]; }
+inline size_t get_local_size(uint d) { return clshim::g_cur->lsize[d]; }
+inline size_t get_global_size(uint d) { return clshim::g_cur->gsize[d]; }
+inline size_t get_global_offset(uint) { return 0; }
 inline void barrier(int) { clshim::barrier_yield(); }
 
 // ------------------------------------------------------------ vector types
+// components by letter (x, y, z, w) or number (s0 .. s3)
 struct alignas(16) float3 {
-    float x, y, z, w;
-    float3() : x(0), y(0), z(0), w(0) {}
-    float3(float v) : x(v), y(v), z(v), w(0) {}  // (float3)(s): every component s
-    float3(float a, float b, float c) : x(a), y(b), z(c), w(0) {}
+    union {
+        struct { float x, y, z, w; };
+        struct { float s0, s1, s2, s3; };
+    };
+    float3() { x = y = z = w = 0.0f; }
+    float3(float v) { x = y = z = v; w = 0.0f; }  // (float3)(s): every component s
+    float3(float a, float b, float c) { x = a; y = b; z = c; w = 0.0f; }
 };
 inline float3 operator+(float3 a, float3 b) { return float3(a.x + b.x, a.y + b.y, a.z + b.z); }
 inline float3 operator-(float3 a, float3 b) { return float3(a.x - b.x, a.y - b.y, a.z - b.z); }
@@ -63,17 +73,31 @@ inline float3 operator/(float3 a, float3 b) { return float3(a.x / b.x, a.y / b.y
 inline float3 operator-(float3 a) { return float3(-a.x, -a.y, -a.z); }
 // a scalar operand is converted to the element type first (OpenCL 6.2.6)
 inline float3 operator*(float3 a, float s) { return a * float3(s); }
+inline float3 operator*(float s, float3 a) { return float3(s) * a; }
 inline float3 operator*(float3 a, uint s) { return a * float3((float)s); }
 inline float3 fmin(float3 a, float3 b) { return float3(fminf(a.x, b.x), fminf(a.y, b.y), fminf(a.z, b.z)); }
 inline float3 fmax(float3 a, float3 b) { return float3(fmaxf(a.x, b.x), fmaxf(a.y, b.y), fmaxf(a.z, b.z)); }
 inline float fmin(float a, float b) { return fminf(a, b); }
 inline float fmax(float a, float b) { return fmaxf(a, b); }
+// float arguments stay in float, as the OpenCL built-ins (the C library's
+// expf / powf)
+inline float exp(float x) { return expf(x); }
+inline float pow(float x, float y) { return powf(x, y); }
+inline float3 pow(float3 a, float y) { return float3(powf(a.x, y), powf(a.y, y), powf(a.z, y)); }
+// clamp(x, lo, hi) = fmin(fmax(x, lo), hi) for floats
+inline float3 clamp(float3 a, float lo, float hi) {
+    return float3(fminf(fmaxf(a.x, lo), hi), fminf(fmaxf(a.y, lo), hi), fminf(fmaxf(a.z, lo), hi));
+}
+inline int clamp(int x, int lo, int hi) { return x < lo ? lo : (x > hi ? hi : x); }
 
 struct alignas(16) uint3 {
-    uint x, y, z, w;
-    uint3() : x(0), y(0), z(0), w(0) {}
-    uint3(uint v) : x(v), y(v), z(v), w(0) {}
-    uint3(uint a, uint b, uint c) : x(a), y(b), z(c), w(0) {}
+    union {
+        struct { uint x, y, z, w; };
+        struct { uint s0, s1, s2, s3; };
+    };
+    uint3() { x = y = z = w = 0u; }
+    uint3(uint v) { x = y = z = v; w = 0u; }
+    uint3(uint a, uint b, uint c) { x = a; y = b; z = c; w = 0u; }
 };
 inline uint3 operator^(uint3 a, uint3 b) { return uint3(a.x ^ b.x, a.y ^ b.y, a.z ^ b.z); }
 inline uint3 operator>>(uint3 a, uint s) { return uint3(a.x >> s, a.y >> s, a.z >> s); }
@@ -81,7 +105,10 @@ inline uint3 operator&(uint3 a, uint s) { return uint3(a.x & s, a.y & s, a.z & s
 inline uint3 operator-(uint3 a, uint s) { return uint3(a.x - s, a.y - s, a.z - s); }
 
 struct uchar3 {
-    uchar x, y, z, w;
+    union {
+        struct { uchar x, y, z, w; };
+        struct { uchar s0, s1, s2, s3; };
+    };
 };
 
 inline uint clz(uint v) { return v ? (uint)__builtin_clz(v) : 32u; }
@@ -102,7 +129,17 @@ inline uint convert_uint_rtz(float f) {
 inline uint3 convert_uint3_rtz(float3 v) {
     return uint3(convert_uint_rtz(v.x), convert_uint_rtz(v.y), convert_uint_rtz(v.z));
 }
-inline uchar3 convert_uchar3(uint3 v) { return uchar3{(uchar)v.x, (uchar)v.y, (uchar)v.z, 0}; }
+inline uchar3 convert_uchar3(uint3 v) {
+    uchar3 r;
+    r.x = (uchar)v.x; r.y = (uchar)v.y; r.z = (uchar)v.z; r.w = 0;
+    return r;
+}
+// round toward zero; used on values already clamped to [0, 255]
+inline uchar3 convert_uchar3_rtz(float3 v) {
+    uchar3 r;
+    r.x = (uchar)(uint)v.x; r.y = (uchar)(uint)v.y; r.z = (uchar)(uint)v.z; r.w = 0;
+    return r;
+}
 
 inline uint as_uint(float f) {
     uint u;
