@@ -594,7 +594,7 @@ __device__ __forceinline__ unsigned int atomic_add_acq_rel_cta(unsigned int* p, 
 }
 
 template <typename KeyT>
-__global__ void __launch_bounds__(kTreeBlock) k_build_tree(const KeyT* __restrict__ keys,
+__global__ void __launch_bounds__(kTreeBlock, 8) k_build_tree(const KeyT* __restrict__ keys,
                                                            const uint32_t* __restrict__ sidx, uint32_t n, int kbits,
                                                            const float* __restrict__ vx, const float* __restrict__ vy,
                                                            const float* __restrict__ vz, const uint32_t* __restrict__ tri,
