@@ -127,12 +127,24 @@ __global__ void __launch_bounds__(256) k_env_rows(uint8_t* __restrict__ others, 
     if (threadIdx.x < nr) {
         const uint32_t r = threadIdx.x;
         const float wc = read_cc1d(head + *reinterpret_cast<const int32_t*>(head + 4) + 28u * (r0 + r)).width;
-        const float* p = spdf + r * stride;
-        float* c = scdf + r * stride;
+        const float* __restrict__ p = spdf + r * stride;
+        float* __restrict__ c = scdf + r * stride;
         float acc = 0.0f;
         c[0] = 0.0f;
-#pragma unroll 8
-        for (uint32_t j = 0; j < w; ++j) {
+        // eight terms loaded ahead of their adds, so the chain waits on the
+        // adds alone
+        uint32_t j = 0;
+        for (; j + 8 <= w; j += 8) {
+            float t[8];
+#pragma unroll
+            for (int k = 0; k < 8; ++k) t[k] = __fmul_rn(p[j + k], wc);
+#pragma unroll
+            for (int k = 0; k < 8; ++k) {
+                acc = __fadd_rn(acc, t[k]);
+                c[j + k + 1] = acc;
+            }
+        }
+        for (; j < w; ++j) {
             acc = __fadd_rn(acc, __fmul_rn(p[j], wc));
             c[j + 1] = acc;
         }
@@ -167,12 +179,24 @@ __global__ void __launch_bounds__(1024) k_env_parent(uint8_t* __restrict__ other
     __syncthreads();
     __shared__ float norm;
     if (threadIdx.x == 0) {
+        const float* __restrict__ m = mass;
+        float* __restrict__ cd = cdf;
         float c = 0.0f;
-        cdf[0] = 0.0f;
-#pragma unroll 8
-        for (uint32_t i = 0; i < h; ++i) {
-            c = __fadd_rn(c, __fmul_rn(mass[i], parent.width));
-            cdf[i + 1] = c;
+        cd[0] = 0.0f;
+        uint32_t i = 0;
+        for (; i + 8 <= h; i += 8) {
+            float t[8];
+#pragma unroll
+            for (int k = 0; k < 8; ++k) t[k] = __fmul_rn(m[i + k], parent.width);
+#pragma unroll
+            for (int k = 0; k < 8; ++k) {
+                c = __fadd_rn(c, t[k]);
+                cd[i + k + 1] = c;
+            }
+        }
+        for (; i < h; ++i) {
+            c = __fadd_rn(c, __fmul_rn(m[i], parent.width));
+            cd[i + 1] = c;
         }
         norm = __fdiv_rn(1.0f, c);
         parent.cdf[0] = 0.0f;
