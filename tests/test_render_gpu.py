@@ -34,6 +34,32 @@ def metrics(img, ref):
     return rel_rmse, mean_err, frac_close
 
 
+def test_obj_scene_encoding_matches_golden():
+    import make_golden_obj_render as GO
+
+    g = np.load(os.path.join(os.path.dirname(__file__), "golden", "render_obj.npz"))
+    assert blob_hash(GO.build_scene().blobs()) == str(g["hash"])
+
+
+@pytest.mark.gpu
+def test_obj_scene_matches_reference_sim(cuda):
+    """A scene loaded from .obj files (matte walls, a glass sphere with uvs and
+    normals, a lamp quad with material and light overrides) rendered on the
+    device against the reference's own CPU renderer on the same blobs."""
+    import make_golden_obj_render as GO
+
+    g = np.load(os.path.join(os.path.dirname(__file__), "golden", "render_obj.npz"))
+    w, h, spp = int(g["width"]), int(g["height"]), int(g["spp"])
+    ds = DeviceScene(GO.build_scene(width=w, height=h), cuda)
+    rng, pix = ds.new_frame()
+    ds.render(rng, pix, spp, max_depth=100, ordered=False)
+    img = pix[:, :3].cpu().numpy()
+    rel_rmse, mean_err, frac_close = metrics(img, g["image"])
+    print(f"obj scene: rel RMSE {rel_rmse:.4g}, mean err {mean_err:.4g}, close {frac_close:.4f}")
+    assert rel_rmse <= 0.02 and mean_err <= 0.005 and frac_close >= 0.90, (rel_rmse, mean_err, frac_close)
+    assert _lib.device_status() == 0
+
+
 def test_scene_encoding_matches_golden():
     g = np.load(GOLDEN)
     w = int(g["width"])
