@@ -15,9 +15,10 @@
 //     so all tiles share one 64x64 block of streams);
 //   * the depth cap is a parameter (the reference hard-codes depth > 99,
 //     pathtracer.cl:166; max_depth = 100 reproduces it);
-//   * shadow visibility is "closest hit is the sampled light face" for area
-//     lights and "no hit" for the environment; the reference compares an
-//     unset face id when nothing is hit (pathtracer.cl:120-122);
+//   * the shadow test is the reference's, light face carried along the path
+//     (shadow_visible), with the values it leaves unset defined: the path's
+//     light face starts as no face, and a missed shadow ray never matches
+//     (the reference compares an unset hit record, pathtracer.cl:120-122);
 //   * samples-per-pixel loop inside the kernel (the reference launches once
 //     per sample); each pixel's contributions are added in the same order.
 #include "render_common.cuh"
@@ -70,10 +71,7 @@ __device__ void trace_path(const DScene& sc, const Camera& cam, uint32_t gx, uin
                     dist2 = 1.0f;
                 }
                 const f3 sorg = sp.p + vinL * kEpsilon;
-                Hit sh;
-                const bool hit = intersect<kOrdered>(sc, sorg, vinL, sh, stack);
-                const bool visible = lpos.atInfinity ? !hit : (hit && sh.id == lpos.faceID);
-                if (visible) {
+                if (shadow_visible<kOrdered>(sc, sorg, vinL, shadow_light_word(lpos), stack)) {
                     const f3 vinLrev = -vinL;
                     const float fsPDF = bsdf_pdf(bsdf, vout, vinL) * edf_abs_cos(edf, vinL) / dist2;
                     MISWeight = (lightPDF * lightPDF) / (lightPDF * lightPDF + fsPDF * fsPDF);

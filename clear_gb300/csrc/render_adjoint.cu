@@ -47,7 +47,7 @@ constexpr uint32_t kTapeWords = 32;
 constexpr uint32_t kTapeSpecular = 0x80000000u;  // BSDF-sample record: specular component index follows
 
 struct AdState {
-    float4* org;     // xyz ray origin
+    float4* org;     // xyz ray origin, w the path's light face (bits; shadow_visible)
     float4* dir;     // xyz direction, w dirPDF
     float4* alpha;   // xyz throughput, w initY
     uint4* misc;     // x depth, y sampledType, z samples done, w pass (0 primal, 1 replay)
@@ -266,7 +266,7 @@ __device__ __forceinline__ void ad_start(const Camera& cam, const AdState& S, ui
     f3 org, dir, alpha;
     float dirPDF;
     camera_ray(cam, p % width, p / width, rng, org, dir, alpha, dirPDF);
-    S.org[p] = make_float4(org.x, org.y, org.z, 0.f);
+    S.org[p] = make_float4(org.x, org.y, org.z, __uint_as_float(kNone32));
     S.dir[p] = make_float4(dir.x, dir.y, dir.z, dirPDF);
     S.alpha[p] = make_float4(alpha.x, alpha.y, alpha.z, luminance(alpha));
     S.misc[p] = make_uint4(0u, 0u, done, pass);
@@ -397,7 +397,8 @@ __device__ __forceinline__ f3 vertex_emission(const DScene& sc, bool escaped, co
 // Next-event estimation at a surface point (pathtracer.cl:216-240): samples a
 // light, returns false when the BSDF has no non-specular component.  Sets the
 // shadow ray, the scalar weight s (MIS * |cos_l| * |cos| / dist^2 / pdf),
-// the light's radiance and the BSDF value toward it.
+// the light's radiance and the BSDF value toward it; light_face is the
+// path's light face (shadow_visible), updated when an area light is sampled.
 struct Nee {
     f3 org, dir, le, fs;
     float s;
@@ -405,12 +406,13 @@ struct Nee {
 };
 
 __device__ __forceinline__ void next_event(const DScene& sc, const BSDF& bsdf, const SurfPt& sp, f3 vout, Rng& rng,
-                                           Nee& n) {
+                                           Nee& n, uint32_t& light_face) {
     const float uL = rng.uniform(), u0 = rng.uniform(), u1 = rng.uniform();
     EDF edf;
     float lightPDF;
-    n.lpos.faceID = kNone32;
+    n.lpos.faceID = light_face;
     sample_light(sc, uL, u0, u1, n.lpos, edf, lightPDF);
+    light_face = n.lpos.faceID;
     f3 vinL = n.lpos.p - sp.p;
     float dist2 = dot(vinL, vinL);
     vinL = vinL * (1.0f / sqrtf(dist2));
@@ -452,12 +454,14 @@ __global__ void __launch_bounds__(kAdThreads) k_ad_primal(DScene sc, AdState S, 
             uint32_t depth = m.x, sampledType = m.y;
             bool ended = false;
             const uint32_t hid = __float_as_uint(h4.x);
+            uint32_t light_face = __float_as_uint(o4.w);
             SurfPt sp;
             Face face;
             if (hid != kNone32) {
                 Hit h{hid, h4.y, h4.z, h4.w};
                 surface_point(sc, org, dir, h, sp);
                 face = load_face(sc, sp.faceID);
+                if (face.light != kNone16) light_face = sp.faceID;  // LightPointFromSurfacePoint
             }
             LightPt lenv;
             float w;
@@ -484,10 +488,10 @@ __global__ void __launch_bounds__(kAdThreads) k_ad_primal(DScene sc, AdState S, 
                     bsdf_alloc(sc, face.mat, sp, bsdf);
                     if (bsdf_has_non_specular(bsdf)) {
                         Nee ne;
-                        next_event(sc, bsdf, sp, vout, rng, ne);
+                        next_event(sc, bsdf, sp, vout, rng, ne, light_face);
                         const f3 c = ne.s * (alpha * ne.le * ne.fs);
                         sh0 = make_float4(ne.org.x, ne.org.y, ne.org.z,
-                                              __uint_as_float(ne.lpos.atInfinity ? kNone32 : ne.lpos.faceID));
+                                              __uint_as_float(shadow_light_word(ne.lpos)));
                         sh1 = make_float4(ne.dir.x, ne.dir.y, ne.dir.z, __uint_as_float(p));
                         sh2 = make_float4(c.x, c.y, c.z, __uint_as_float(1u));  // add to L
                         shadow = true;
@@ -509,7 +513,7 @@ __global__ void __launch_bounds__(kAdThreads) k_ad_primal(DScene sc, AdState S, 
                 ad_start(cam, S, p, width, rng, m.z, 1u);
                 next_pass = 1;
             } else {
-                S.org[p] = make_float4(org.x, org.y, org.z, 0.f);
+                S.org[p] = make_float4(org.x, org.y, org.z, __uint_as_float(light_face));
                 S.dir[p] = make_float4(dir.x, dir.y, dir.z, dirPDF);
                 S.alpha[p] = make_float4(alpha.x, alpha.y, alpha.z, initY);
                 S.misc[p] = make_uint4(depth, sampledType, m.z, 0u);
@@ -571,12 +575,14 @@ __global__ void __launch_bounds__(kAdThreads) k_ad_replay(DScene sc, AdState S, 
             int npend = 0;
             bool ended = false;
             const uint32_t hid = __float_as_uint(h4.x);
+            uint32_t light_face = __float_as_uint(o4.w);
             SurfPt sp;
             Face face;
             if (hid != kNone32) {
                 Hit h{hid, h4.y, h4.z, h4.w};
                 surface_point(sc, org, dir, h, sp);
                 face = load_face(sc, sp.faceID);
+                if (face.light != kNone16) light_face = sp.faceID;  // LightPointFromSurfacePoint
             }
             LightPt lenv;
             float w;
@@ -630,7 +636,7 @@ __global__ void __launch_bounds__(kAdThreads) k_ad_replay(DScene sc, AdState S, 
                     bsdf_alloc(sc, face.mat, sp, bsdf);
                     if (bsdf_has_non_specular(bsdf)) {
                         Nee ne;
-                        next_event(sc, bsdf, sp, vout, rng, ne);
+                        next_event(sc, bsdf, sp, vout, rng, ne, light_face);
                         const f3 c = ne.s * (alpha * ne.le * ne.fs);
                         const uint32_t flags = side_flags(bsdf, vout, ne.dir);
                         const f3 vl = world_to_local(bsdf.s, bsdf.t, bsdf.n, vout);
@@ -668,7 +674,7 @@ __global__ void __launch_bounds__(kAdThreads) k_ad_replay(DScene sc, AdState S, 
                             }
                         }
                         se.e[0] = make_float4(ne.org.x, ne.org.y, ne.org.z,
-                                              __uint_as_float(ne.lpos.atInfinity ? kNone32 : ne.lpos.faceID));
+                                              __uint_as_float(shadow_light_word(ne.lpos)));
                         se.e[1] = make_float4(ne.dir.x, ne.dir.y, ne.dir.z, __uint_as_float(p));
                         se.e[2] = make_float4(c.x, c.y, c.z, __uint_as_float(tflag | 2u));  // bit 0 set below
                         shadow = true;
@@ -728,7 +734,7 @@ __global__ void __launch_bounds__(kAdThreads) k_ad_replay(DScene sc, AdState S, 
                 }
             } else {
                 se.e[2].w = __uint_as_float(__float_as_uint(se.e[2].w) | 1u);
-                S.org[p] = make_float4(org.x, org.y, org.z, 0.f);
+                S.org[p] = make_float4(org.x, org.y, org.z, __uint_as_float(light_face));
                 S.dir[p] = make_float4(dir.x, dir.y, dir.z, dirPDF);
                 S.alpha[p] = make_float4(alpha.x, alpha.y, alpha.z, initY);
                 S.misc[p] = make_uint4(depth, sampledType, done, 1u);
@@ -756,15 +762,8 @@ __global__ void __launch_bounds__(kAdThreads) k_ad_shadow(DScene sc, AdState S, 
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         const float4* e = S.sh + (size_t)kShWords * i;
         const float4 a = e[0], b = e[1], c = e[2];
-        const uint32_t light_face = __float_as_uint(a.w), p = __float_as_uint(b.w), flags = __float_as_uint(c.w);
-        bool visible;
-        if (light_face == kNone32) {
-            visible = !occluded_any<kOrdered>(sc, mk(a.x, a.y, a.z), mk(b.x, b.y, b.z), stack);
-        } else {
-            Hit h;
-            visible = intersect<kOrdered>(sc, mk(a.x, a.y, a.z), mk(b.x, b.y, b.z), h, stack) && h.id == light_face;
-        }
-        if (!visible) continue;
+        const uint32_t p = __float_as_uint(b.w), flags = __float_as_uint(c.w);
+        if (!shadow_visible<kOrdered>(sc, mk(a.x, a.y, a.z), mk(b.x, b.y, b.z), __float_as_uint(a.w), stack)) continue;
         const bool replay = (flags & 2u) != 0;
         if (flags & 1u) {
             float4 L = S.L[p];

@@ -35,14 +35,14 @@ struct BtScene {
 };
 
 struct BtState {
-    float4* org;     // xyz ray origin
+    float4* org;     // xyz ray origin, w the path's light face (bits; shadow_visible)
     float4* dir;     // xyz direction, w dirPDF
     float4* alpha;   // xyz throughput, w initY
     uint4* misc;     // x depth, y sampledType, z samples done, w scene
     float4* hit;     // x id bits, y t, z b1, w b2
     uint32_t* pix;   // global pixel of the slot
     uint32_t* q[2];  // active slots
-    float4* sh;      // shadow entries: org (w light face), dir (w pixel), contribution (w scene)
+    float4* sh;      // shadow entries: org (w shadow_light_word), dir (w pixel), contribution (w scene)
     unsigned int* count;  // [0],[1] active slots, [2] shadow entries, [3] next pixel, [4] iterations run
 };
 
@@ -104,7 +104,7 @@ __device__ __forceinline__ void bt_start(const BtArgs& A, const BtState& S, uint
     f3 org, dir, alpha;
     float dirPDF;
     camera_ray(cam, lp % bs.width, lp / bs.width, rng, org, dir, alpha, dirPDF);
-    S.org[p] = make_float4(org.x, org.y, org.z, 0.f);
+    S.org[p] = make_float4(org.x, org.y, org.z, __uint_as_float(kNone32));
     S.dir[p] = make_float4(dir.x, dir.y, dir.z, dirPDF);
     S.alpha[p] = make_float4(alpha.x, alpha.y, alpha.z, luminance(alpha));
     S.misc[p] = make_uint4(0u, 0u, done, s);
@@ -170,6 +170,7 @@ __global__ void __launch_bounds__(kBtShadeThreads) k_bt_shade(BtArgs A, BtState 
             const float4 px = A.pixels[g];
             f3 pix = mk(px.x, px.y, px.z);
             bool ended = false;
+            uint32_t light_face = __float_as_uint(o4.w);
             const uint32_t hid = __float_as_uint(h4.x);
             if (hid == kNone32) {
                 LightPt lpos;
@@ -192,7 +193,7 @@ __global__ void __launch_bounds__(kBtShadeThreads) k_bt_shade(BtArgs A, BtState 
                 const Face face = load_face(sc, sp.faceID);
                 const f3 vout = -dir;
                 LightPt lpos;
-                lpos.faceID = kNone32;
+                lpos.faceID = light_face;
                 if (face.light != kNone16) {
                     light_from_surface(sp, lpos);
                     EDF edf;
@@ -239,7 +240,7 @@ __global__ void __launch_bounds__(kBtShadeThreads) k_bt_shade(BtArgs A, BtState 
                         const float MISWeight = (lightPDF * lightPDF) / (lightPDF * lightPDF + fsPDF * fsPDF);
                         const f3 c = (MISWeight * edf_abs_cos(edf, vinL) * fabsf(dot(bsdf.n, vinL)) / dist2 / lightPDF) *
                                      (alpha * edf_le(edf, vinLrev) * bsdf_f(bsdf, vout, vinL));
-                        sh0 = make_float4(sorg.x, sorg.y, sorg.z, __uint_as_float(lpos.atInfinity ? kNone32 : lpos.faceID));
+                        sh0 = make_float4(sorg.x, sorg.y, sorg.z, __uint_as_float(shadow_light_word(lpos)));
                         sh1 = make_float4(vinL.x, vinL.y, vinL.z, __uint_as_float(g));
                         sh2 = make_float4(c.x, c.y, c.z, __uint_as_float(s));
                         shadow = true;
@@ -254,6 +255,7 @@ __global__ void __launch_bounds__(kBtShadeThreads) k_bt_shade(BtArgs A, BtState 
                         ++depth;
                     }
                 }
+                light_face = lpos.faceID;
             }
             A.pixels[g] = make_float4(pix.x, pix.y, pix.z, px.w);
             if (ended) {
@@ -265,7 +267,7 @@ __global__ void __launch_bounds__(kBtShadeThreads) k_bt_shade(BtArgs A, BtState 
                     need_pixel = true;
                 }
             } else {
-                S.org[p] = make_float4(org.x, org.y, org.z, 0.f);
+                S.org[p] = make_float4(org.x, org.y, org.z, __uint_as_float(light_face));
                 S.dir[p] = make_float4(dir.x, dir.y, dir.z, dirPDF);
                 S.alpha[p] = make_float4(alpha.x, alpha.y, alpha.z, initY);
                 S.misc[p] = make_uint4(depth, sampledType, m.z, s);
@@ -316,16 +318,9 @@ __global__ void __launch_bounds__(kBtTraceMaxThreads) k_bt_shadow(BtArgs A, BtSt
     uint2 stack[kStackSize];
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         const float4 a = S.sh[3u * i], b = S.sh[3u * i + 1], c = S.sh[3u * i + 2];
-        const uint32_t light_face = __float_as_uint(a.w), g = __float_as_uint(b.w);
+        const uint32_t g = __float_as_uint(b.w);
         const DScene& sc = A.scenes[__float_as_uint(c.w)].sc;
-        bool visible;
-        if (light_face == kNone32) {
-            visible = !occluded_any<kOrdered>(sc, mk(a.x, a.y, a.z), mk(b.x, b.y, b.z), stack);
-        } else {
-            Hit h;
-            visible = intersect<kOrdered>(sc, mk(a.x, a.y, a.z), mk(b.x, b.y, b.z), h, stack) && h.id == light_face;
-        }
-        if (visible) {
+        if (shadow_visible<kOrdered>(sc, mk(a.x, a.y, a.z), mk(b.x, b.y, b.z), __float_as_uint(a.w), stack)) {
             float4 px = A.pixels[g];
             px.x += c.x;
             px.y += c.y;

@@ -137,10 +137,10 @@ static __device__ __forceinline__ bool intersect(const DScene& sc, f3 org, f3 di
     return intersect_impl<kOrdered, false>(sc, org, dir, h, stack, nullptr);
 }
 
-// Whether the ray hits any triangle at all (environment shadow rays: the
-// reference's test "closest hit exists" has the same answer, since any
-// triangle the closest-hit search would accept is also reachable with the
-// bound held at infinity, and vice versa).
+// Whether the ray hits any triangle at all (environment shadow rays of paths
+// that have no light face yet: the reference's test "closest hit exists"
+// has the same answer, since any triangle the closest-hit search would
+// accept is also reachable with the bound held at infinity, and vice versa).
 template <bool kOrdered>
 __device__ bool occluded_any(const DScene& sc, f3 org, f3 dir, uint2* stack) {
     Ray ray{org.x, org.y, org.z, INFINITY, dir.x, dir.y, dir.z};
@@ -403,6 +403,34 @@ __device__ __forceinline__ void sample_light(const DScene& sc, float uL, float u
         lightProp = f.light;
     }
     edf_alloc(sc, lightProp, lp, e);
+}
+
+// The shadow test of next-event estimation (pathtracer.cl:119-122):
+// "closest hit face == lpos.faceID, or the light is at infinity and nothing
+// is hit".  lpos is one variable for the whole path: sampling the
+// environment leaves its faceID as the last area light the path sampled or
+// hit (sampleLightPos and LightPointFromSurfacePoint are its only writers),
+// so an environment shadow ray whose closest hit is that face also counts
+// as unoccluded.  Paths start with faceID = kNone32, a value no face has
+// (the reference leaves it unset).  After a miss the reference compares an
+// unset hit record; a miss never matches here.
+//
+// Shadow entries carry the test as one word: an area light's face, or for
+// the environment kEnvLightBit | the path's light face (kNone32 when there is
+// none; face ids are below 2^30).
+constexpr uint32_t kEnvLightBit = 0x80000000u;
+
+__device__ __forceinline__ uint32_t shadow_light_word(const LightPt& lp) {
+    return lp.atInfinity ? (kEnvLightBit | lp.faceID) : lp.faceID;
+}
+
+template <bool kOrdered>
+__device__ __forceinline__ bool shadow_visible(const DScene& sc, f3 org, f3 dir, uint32_t light, uint2* stack) {
+    if (light == kNone32) return !occluded_any<kOrdered>(sc, org, dir, stack);
+    Hit h;
+    const bool hit = intersect<kOrdered>(sc, org, dir, h, stack);
+    if (light & kEnvLightBit) return !hit || h.id == (light & ~kEnvLightBit);
+    return hit && h.id == light;
 }
 
 // getAreaPDF, light.cl:247-292

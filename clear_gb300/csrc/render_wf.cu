@@ -29,13 +29,13 @@ namespace clr {
 constexpr int kWfThreads = 128;
 
 struct WfState {
-    float4* org;     // xyz ray origin
+    float4* org;     // xyz ray origin, w the path's light face (bits; shadow_visible)
     float4* dir;     // xyz ray direction, w dirPDF
     float4* alpha;   // xyz throughput, w initY
     uint4* misc;     // x depth, y sampledType, z samples done, w pixel
     float4* hit;     // x id bits, y t, z b1, w b2
     uint32_t* q[2];  // active path queues
-    float4* sh;      // shadow entries: org (w light face | 0xFFFFFFFF env), dir (w path), contribution
+    float4* sh;      // shadow entries: org (w shadow_light_word), dir (w path), contribution
     unsigned int* count;  // [0],[1] active counts, [2] shadow count
 };
 
@@ -71,7 +71,7 @@ __device__ __forceinline__ void start_sample(const Camera& cam, WfState& S, uint
     f3 org, dir, alpha;
     float dirPDF;
     camera_ray(cam, p % width, row0 + p / width, rng, org, dir, alpha, dirPDF);
-    S.org[p] = make_float4(org.x, org.y, org.z, 0.f);
+    S.org[p] = make_float4(org.x, org.y, org.z, __uint_as_float(kNone32));
     S.dir[p] = make_float4(dir.x, dir.y, dir.z, dirPDF);
     S.alpha[p] = make_float4(alpha.x, alpha.y, alpha.z, luminance(alpha));
     S.misc[p] = make_uint4(0u, 0u, done, p);
@@ -135,6 +135,7 @@ __global__ void __launch_bounds__(kWfThreads) k_wf_shade(DScene sc, WfState S, i
             const float4 px = pixels[p];
             f3 pix = mk(px.x, px.y, px.z);
             bool ended = false;
+            uint32_t light_face = __float_as_uint(o4.w);
             const uint32_t hid = __float_as_uint(h4.x);
             if (hid == kNone32) {
                 // escaped: environment emission (pathtracer.cl:183-196)
@@ -158,7 +159,7 @@ __global__ void __launch_bounds__(kWfThreads) k_wf_shade(DScene sc, WfState S, i
                 const Face face = load_face(sc, sp.faceID);
                 const f3 vout = -dir;
                 LightPt lpos;
-                lpos.faceID = kNone32;
+                lpos.faceID = light_face;
                 if (face.light != kNone16) {
                     light_from_surface(sp, lpos);
                     EDF edf;
@@ -205,7 +206,7 @@ __global__ void __launch_bounds__(kWfThreads) k_wf_shade(DScene sc, WfState S, i
                         const float MISWeight = (lightPDF * lightPDF) / (lightPDF * lightPDF + fsPDF * fsPDF);
                         const f3 c = (MISWeight * edf_abs_cos(edf, vinL) * fabsf(dot(bsdf.n, vinL)) / dist2 / lightPDF) *
                                      (alpha * edf_le(edf, vinLrev) * bsdf_f(bsdf, vout, vinL));
-                        sh0 = make_float4(sorg.x, sorg.y, sorg.z, __uint_as_float(lpos.atInfinity ? kNone32 : lpos.faceID));
+                        sh0 = make_float4(sorg.x, sorg.y, sorg.z, __uint_as_float(shadow_light_word(lpos)));
                         sh1 = make_float4(vinL.x, vinL.y, vinL.z, __uint_as_float(p));
                         sh2 = make_float4(c.x, c.y, c.z, 0.f);
                         shadow = true;
@@ -220,6 +221,7 @@ __global__ void __launch_bounds__(kWfThreads) k_wf_shade(DScene sc, WfState S, i
                         ++depth;
                     }
                 }
+                light_face = lpos.faceID;
             }
             pixels[p] = make_float4(pix.x, pix.y, pix.z, px.w);
             if (ended) {
@@ -231,7 +233,7 @@ __global__ void __launch_bounds__(kWfThreads) k_wf_shade(DScene sc, WfState S, i
                     S.misc[p] = make_uint4(depth, sampledType, done, p);
                 }
             } else {
-                S.org[p] = make_float4(org.x, org.y, org.z, 0.f);
+                S.org[p] = make_float4(org.x, org.y, org.z, __uint_as_float(light_face));
                 S.dir[p] = make_float4(dir.x, dir.y, dir.z, dirPDF);
                 S.alpha[p] = make_float4(alpha.x, alpha.y, alpha.z, initY);
                 S.misc[p] = make_uint4(depth, sampledType, m.z, p);
@@ -256,15 +258,8 @@ __global__ void __launch_bounds__(kWfThreads) k_wf_shadow(DScene sc, WfState S, 
     uint2 stack[kStackSize];
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         const float4 a = S.sh[3u * i], b = S.sh[3u * i + 1], c = S.sh[3u * i + 2];
-        const uint32_t light_face = __float_as_uint(a.w), p = __float_as_uint(b.w);
-        bool visible;
-        if (light_face == kNone32) {
-            visible = !occluded_any<kOrdered>(sc, mk(a.x, a.y, a.z), mk(b.x, b.y, b.z), stack);
-        } else {
-            Hit h;
-            visible = intersect<kOrdered>(sc, mk(a.x, a.y, a.z), mk(b.x, b.y, b.z), h, stack) && h.id == light_face;
-        }
-        if (visible) {
+        const uint32_t p = __float_as_uint(b.w);
+        if (shadow_visible<kOrdered>(sc, mk(a.x, a.y, a.z), mk(b.x, b.y, b.z), __float_as_uint(a.w), stack)) {
             float4 px = pixels[p];
             px.x += c.x;
             px.y += c.y;

@@ -69,7 +69,12 @@ def build_ref() -> list[Path]:
     for name, defs in (("libref_lbvh.so", ["-D__USE_LBVH"]), ("libref_mid.so", [])):
         out = outdir / name
         if _stale(out, deps):
-            _run(["g++", "-std=c++17", "-w", *CFLAGS, *defs, f"-I{stubs}", f"-I{eq}",
+            # sim::pathtracing reads two locals it may never set: lpos.faceID
+            # before the path's first light face, and the shadow ray's hit
+            # record after a miss (sim_pathtracer.hpp:80, 121-123).  Filling
+            # uninitialised locals with the 0xFE pattern gives both a value
+            # that matches no face instead of stack leftovers.
+            _run(["g++", "-std=c++17", "-w", *CFLAGS, "-ftrivial-auto-var-init=pattern", *defs, f"-I{stubs}", f"-I{eq}",
                   f"-I{REF_DIR / 'OpenCL_PathTracer'}", str(src), "-o", str(out)])
         built.append(out)
     out = outdir / "libref_scene.so"

@@ -5,9 +5,15 @@ sim::pathtracing compiled in place (tests/golden/make_golden_render.py).  The
 GPU renders the same scene blobs with the same per-pixel XORShift128 streams,
 so each pixel's paths consume the same random numbers; paths only part when a
 transcendental (sin, cos, acos, pow, exp ...) rounds differently between the
-CUDA and the host math library and a later decision flips.  Bars (stated
-here): relative RMSE of the image <= 2 % of its mean, mean radiance within
-0.5 %, and >= 90 % of pixels within 1e-3 relative.
+CUDA and the host math library and a later decision flips.  The reference's
+renderer itself moves by at most 2.4e-6 relative RMSE on these scenes when
+its math library is swapped (correctly rounded results, or results one ulp
+off on an eighth of the inputs).  Bars (stated here) for the reference
+traversal order: relative RMSE of the image <= 1e-4 of its mean, mean
+radiance within 1e-5, and >= 99.9 % of pixels within 1e-3 relative; a
+semantic difference (a shadow rule, a pdf) shows as 1e-3 or more.  The
+nearer-child-first order picks other triangles on exact ties, so its paths
+part more often: bars 2 % and 0.5 % for it.
 """
 import numpy as np
 import pytest
@@ -56,7 +62,7 @@ def test_obj_scene_matches_reference_sim(cuda):
     img = pix[:, :3].cpu().numpy()
     rel_rmse, mean_err, frac_close = metrics(img, g["image"])
     print(f"obj scene: rel RMSE {rel_rmse:.4g}, mean err {mean_err:.4g}, close {frac_close:.4f}")
-    assert rel_rmse <= 0.02 and mean_err <= 0.005 and frac_close >= 0.90, (rel_rmse, mean_err, frac_close)
+    assert rel_rmse <= 1e-4 and mean_err <= 1e-5 and frac_close >= 0.999, (rel_rmse, mean_err, frac_close)
     assert _lib.device_status() == 0
 
 
@@ -79,7 +85,7 @@ def test_render_matches_reference_sim(cuda, variant):
     img = pix[:, :3].cpu().numpy()
     rel_rmse, mean_err, frac_close = metrics(img, g[variant])
     print(f"{variant}: rel RMSE {rel_rmse:.4g}, mean err {mean_err:.4g}, close {frac_close:.4f}")
-    assert rel_rmse <= 0.02 and mean_err <= 0.005 and frac_close >= 0.90, (rel_rmse, mean_err, frac_close)
+    assert rel_rmse <= 1e-4 and mean_err <= 1e-5 and frac_close >= 0.999, (rel_rmse, mean_err, frac_close)
     assert _lib.device_status() == 0
 
 
@@ -100,7 +106,7 @@ def test_wavefront_equals_megakernel(cuda, variant):
     assert torch.equal(rng_a, rng_b)
     assert torch.equal(pix_a, pix_b)
     rel_rmse, mean_err, frac_close = metrics(pix_b[:, :3].cpu().numpy(), g[variant])
-    assert rel_rmse <= 0.02 and mean_err <= 0.005 and frac_close >= 0.90
+    assert rel_rmse <= 1e-4 and mean_err <= 1e-5 and frac_close >= 0.999
     assert _lib.device_status() == 0
 
 
