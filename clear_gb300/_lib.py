@@ -87,6 +87,9 @@ def lib() -> C.CDLL:
             "clr_lbvh_create": [u32, C.POINTER(vp)],
             "clr_lbvh_destroy": [vp],
             "clr_lbvh_build": [vp, vp, vp, vp, vp, u32, u32, C.POINTER(ClrBvh), vp],
+            "clr_lbvh_build_host": [vp, vp, vp, vp, vp, u32, u32, u32, C.POINTER(ClrBvh), vp, vp],
+            "clr_lbvh_host_copy_after": [vp, vp],
+            "clr_lbvh_host_copy_wait": [vp],
             "clr_lbvh_build_noalloc": [vp, vp, vp, vp, u32, u32, C.POINTER(ClrBvh), vp],
             "clr_lbvh_build_batched": [vp, vp, vp, vp, vp, C.POINTER(u32), u32, u32, u32, vp, vp, vp, vp],
             "clr_lbvh_export_reference": [vp, C.POINTER(ClrBvh), vp, vp, vp, vp, vp, vp],

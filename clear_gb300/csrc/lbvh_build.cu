@@ -1118,6 +1118,13 @@ extern "C" int clr_lbvh_destroy(clr_lbvh* h) {
     if (h->seg_pool) cudaFree(h->seg_pool);
     for (auto& e : h->ev)
         if (e) cudaEventDestroy(e);
+    for (int s = 0; s < 2; ++s) {
+        if (h->in_buf[s]) cudaFree(h->in_buf[s]);
+        if (h->in_copied[s]) cudaEventDestroy(h->in_copied[s]);
+        if (h->in_consumed[s]) cudaEventDestroy(h->in_consumed[s]);
+    }
+    if (h->copy_gate) cudaEventDestroy(h->copy_gate);
+    if (h->copy_stream) cudaStreamDestroy(h->copy_stream);
     delete h;
     return CLR_OK;
 }
@@ -1212,6 +1219,102 @@ extern "C" int clr_lbvh_build(clr_lbvh* h, const float* vx, const float* vy, con
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     if (bits_per_dim <= 10) return run_build<uint32_t>(h, vx, vy, vz, tri, num_tris, bits_per_dim, out, st);
     return run_build<uint64_t>(h, vx, vy, vz, tri, num_tris, bits_per_dim, out, st);
+}
+
+// ------------------------------------------------- builds from host inputs
+
+// The copy stream and the four buffer events, made on first use.
+static int host_path_init(clr_lbvh* h) {
+    if (h->copy_stream) return CLR_OK;
+    CLR_CUDA_TRY(cudaStreamCreateWithFlags(&h->copy_stream, cudaStreamNonBlocking));
+    for (int s = 0; s < 2; ++s) {
+        CLR_CUDA_TRY(cudaEventCreateWithFlags(&h->in_copied[s], cudaEventDisableTiming));
+        CLR_CUDA_TRY(cudaEventCreateWithFlags(&h->in_consumed[s], cudaEventDisableTiming));
+    }
+    CLR_CUDA_TRY(cudaEventCreateWithFlags(&h->copy_gate, cudaEventDisableTiming));
+    return CLR_OK;
+}
+
+// Input buffer s holds at least `bytes`.  Growing frees the old buffer, which
+// waits for the work that may still read it.
+static int in_buf_grow(clr_lbvh* h, int s, size_t bytes) {
+    if (h->in_buf[s] && bytes <= h->in_bytes[s]) return CLR_OK;
+    if (h->in_buf[s]) {
+        CLR_CUDA_TRY(cudaEventSynchronize(h->in_consumed[s]));
+        CLR_CUDA_TRY(cudaStreamSynchronize(h->copy_stream));
+        cudaFree(h->in_buf[s]);
+        h->in_buf[s] = nullptr;
+        h->in_bytes[s] = 0;
+    }
+    if (cudaMalloc(&h->in_buf[s], bytes) != cudaSuccess) {
+        cudaGetLastError();
+        h->in_buf[s] = nullptr;
+        return clr_set_error(CLR_ENOMEM, "cudaMalloc of a %zu-byte input buffer failed", bytes);
+    }
+    h->in_bytes[s] = bytes;
+    return CLR_OK;
+}
+
+extern "C" int clr_lbvh_build_host(clr_lbvh* h, const float* host_vx, const float* host_vy, const float* host_vz,
+                                   const uint32_t* host_tri, uint32_t num_verts, uint32_t num_tris,
+                                   uint32_t bits_per_dim, clr_bvh* out, float* host_root_box, void* stream) {
+    if (!h || !out) return clr_set_error(CLR_EINVAL, "clr_lbvh_build_host: NULL handle or output");
+    if (bits_per_dim < 1 || bits_per_dim > 21)
+        return clr_set_error(CLR_EINVAL, "clr_lbvh_build_host: bits_per_dim %u outside [1, 21]", bits_per_dim);
+    if (num_tris >= (1u << 30))
+        return clr_set_error(CLR_EINVAL, "clr_lbvh_build_host: %u triangles exceed the 2^30 limit", num_tris);
+    if (!host_tri && num_verts != 3ull * num_tris)
+        return clr_set_error(CLR_EINVAL, "clr_lbvh_build_host: a soup of %u triangles has %llu vertices, not %u",
+                             num_tris, 3ull * num_tris, num_verts);
+    if (num_tris > 0 && (!host_vx || !host_vy || !host_vz || num_verts == 0 || !out->tris || !out->root_box ||
+                         (num_tris > 1 && !out->nodes)))
+        return clr_set_error(CLR_EINVAL, "clr_lbvh_build_host: NULL input or output buffer");
+    if (num_tris == 0) return clr_lbvh_build(h, nullptr, nullptr, nullptr, nullptr, 0, bits_per_dim, out, stream);
+    int rc = host_path_init(h);
+    if (rc != CLR_OK) return rc;
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    const int s = (int)(h->host_calls & 1u);
+    const size_t vbytes = 4ull * num_verts, vstride = align_up(vbytes, 256);
+    rc = in_buf_grow(h, s, 3 * vstride + (host_tri ? 12ull * num_tris : 0));
+    if (rc != CLR_OK) return rc;
+    char* base = static_cast<char*>(h->in_buf[s]);
+    float* d[3] = {reinterpret_cast<float*>(base), reinterpret_cast<float*>(base + vstride),
+                   reinterpret_cast<float*>(base + 2 * vstride)};
+    uint32_t* dtri = host_tri ? reinterpret_cast<uint32_t*>(base + 3 * vstride) : nullptr;
+    // the copy waits for the build that last read this buffer (two calls
+    // back), not for the previous call's build: the two overlap
+    if (h->in_used[s]) CLR_CUDA_TRY(cudaStreamWaitEvent(h->copy_stream, h->in_consumed[s], 0));
+    const float* src[3] = {host_vx, host_vy, host_vz};
+    for (int k = 0; k < 3; ++k)
+        CLR_CUDA_TRY(cudaMemcpyAsync(d[k], src[k], vbytes, cudaMemcpyHostToDevice, h->copy_stream));
+    if (dtri)
+        CLR_CUDA_TRY(cudaMemcpyAsync(dtri, host_tri, 12ull * num_tris, cudaMemcpyHostToDevice, h->copy_stream));
+    CLR_CUDA_TRY(cudaEventRecord(h->in_copied[s], h->copy_stream));
+    CLR_CUDA_TRY(cudaStreamWaitEvent(st, h->in_copied[s], 0));
+    rc = clr_lbvh_build(h, d[0], d[1], d[2], dtri, num_tris, bits_per_dim, out, stream);
+    if (rc != CLR_OK) return rc;
+    CLR_CUDA_TRY(cudaEventRecord(h->in_consumed[s], st));
+    h->in_used[s] = true;
+    ++h->host_calls;
+    if (host_root_box)
+        CLR_CUDA_TRY(cudaMemcpyAsync(host_root_box, out->root_box, 32, cudaMemcpyDeviceToHost, st));
+    return CLR_OK;
+}
+
+extern "C" int clr_lbvh_host_copy_after(clr_lbvh* h, void* stream) {
+    if (!h) return clr_set_error(CLR_EINVAL, "clr_lbvh_host_copy_after: NULL handle");
+    int rc = host_path_init(h);
+    if (rc != CLR_OK) return rc;
+    CLR_CUDA_TRY(cudaEventRecord(h->copy_gate, static_cast<cudaStream_t>(stream)));
+    CLR_CUDA_TRY(cudaStreamWaitEvent(h->copy_stream, h->copy_gate, 0));
+    return CLR_OK;
+}
+
+extern "C" int clr_lbvh_host_copy_wait(clr_lbvh* h) {
+    if (!h) return clr_set_error(CLR_EINVAL, "clr_lbvh_host_copy_wait: NULL handle");
+    if (!h->copy_stream) return CLR_OK;
+    CLR_CUDA_TRY(cudaStreamSynchronize(h->copy_stream));
+    return CLR_OK;
 }
 
 static int seg_grow(clr_lbvh* h, uint32_t nseg) {

@@ -48,6 +48,15 @@ struct clr_lbvh {
     unsigned int* seg_box = nullptr;
     uint32_t last_n = 0, last_bits = 0;
     int final_buf = 0;                       // ping-pong side holding sorted data
+    // builds from host inputs (clr_lbvh_build_host): two device input buffers
+    // used in turn, the copy stream, and per buffer the events "copy done"
+    // and "build that read it done"
+    void* in_buf[2] = {nullptr, nullptr};
+    size_t in_bytes[2] = {0, 0};
+    cudaStream_t copy_stream = nullptr;
+    cudaEvent_t in_copied[2] = {}, in_consumed[2] = {}, copy_gate = nullptr;
+    bool in_used[2] = {false, false};
+    uint32_t host_calls = 0;
     // profiling (clr_lbvh_set_profiling)
     static constexpr int kMaxTimed = 16;
     bool profiling = false;

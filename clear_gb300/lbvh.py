@@ -119,6 +119,48 @@ class LBVHBuilder:
         bvh._inputs = (vx, vy, vz, tri)  # keep alive until the stream has consumed them
         return bvh
 
+    def perform_host(self, vertices, faces, num_faces: int, num_bits_per_dim: int = 10,
+                     out: BVH | None = None, root_host: torch.Tensor | None = None) -> BVH:
+        """Upload and build from HOST arrays (clr_lbvh_build_host): vertices =
+        (vx, vy, vz) contiguous float32 CPU tensors (page-locked for the copy
+        to overlap the previous build), faces = (num_faces, 3) int32 CPU
+        tensor or None for a soup.  root_host (8 float32, CPU) receives the
+        root record.  Keep the host tensors unchanged until host_copy_wait()
+        or a synchronisation of the stream."""
+        vs = []
+        for v in vertices:
+            if v.device.type != "cpu" or v.dtype != torch.float32 or not v.is_contiguous():
+                raise ValueError("perform_host takes contiguous float32 CPU tensors")
+            vs.append(v)
+        nv = int(vs[0].numel())
+        if any(int(v.numel()) != nv for v in vs):
+            raise ValueError("vx, vy, vz differ in length")
+        tri = None
+        if faces is not None:
+            if faces.device.type != "cpu" or faces.dtype != torch.int32 or not faces.is_contiguous():
+                raise ValueError("faces must be a contiguous int32 CPU tensor")
+            tri = faces
+        if root_host is not None and (root_host.device.type != "cpu" or root_host.dtype != torch.float32
+                                      or root_host.numel() < 8):
+            raise ValueError("root_host must be a float32 CPU tensor of 8 elements")
+        n = int(num_faces)
+        bvh = out if out is not None and out.num_tris == n else BVH(n, self.device)
+        with torch.cuda.device(self.device):
+            call("clr_lbvh_build_host", self._h, _ptr(vs[0]), _ptr(vs[1]), _ptr(vs[2]), _ptr(tri), C.c_uint32(nv),
+                 C.c_uint32(n), C.c_uint32(int(num_bits_per_dim)), C.byref(bvh.c), _ptr(root_host),
+                 _stream(self.device))
+        return bvh
+
+    def host_copy_after_stream(self) -> None:
+        """Later perform_host copies start after the work queued on the
+        current stream so far."""
+        with torch.cuda.device(self.device):
+            call("clr_lbvh_host_copy_after", self._h, _stream(self.device))
+
+    def host_copy_wait(self) -> None:
+        """Block until every perform_host copy issued so far is done."""
+        call("clr_lbvh_host_copy_wait", self._h)
+
     def perform_batched(self, vertices, faces, scene_offsets, num_bits_per_dim: int = 10,
                         radix_bits: int = 8) -> "BatchBVH":
         """Build one LBVH per scene in one segmented pass.  vertices and faces

@@ -99,6 +99,40 @@ CLR_API int clr_lbvh_destroy(clr_lbvh* h);
 CLR_API int clr_lbvh_build(clr_lbvh* h, const float* vx, const float* vy, const float* vz, const uint32_t* tri,
                    uint32_t num_tris, uint32_t bits_per_dim, clr_bvh* out, void* stream);
 
+/* Upload and build from host arrays: what the reference host does by
+ * creating the vertex and face buffers from host memory
+ * (CL_MEM_COPY_HOST_PTR, OpenCL_PathTracer/main.cpp:342-343) and then calling
+ * LBVHBuilder::perform (main.cpp:365).  host_vx/vy/vz hold num_verts
+ * vertices (num_verts = 3 * num_tris for a soup, host_tri NULL); host_tri
+ * holds 3 vertex indices per triangle.  Same outputs and results as
+ * clr_lbvh_build on the same data; if host_root_box is not NULL the 8-float
+ * root record (root_box of clr_bvh) is copied back to it on `stream` after
+ * the build.
+ *
+ * For a stream of builds (a scene per frame): the inputs go into one of two
+ * device input buffers owned by the builder, used in turn, on a copy stream
+ * of the builder's own; the build waits on `stream` for that copy.  A copy
+ * waits only for the build that last read its buffer (two calls back), so the
+ * copy of call k+1 runs while call k builds.  Copies are not ordered after
+ * other work on `stream`: clr_lbvh_host_copy_after(h, stream) orders every
+ * later copy after the work queued on `stream` so far.  Page-locked host
+ * arrays (cudaHostAlloc, cudaHostRegister) make the copies asynchronous; the
+ * caller keeps the host arrays unchanged until the copy is done
+ * (clr_lbvh_host_copy_wait, or a synchronisation of `stream`).  The input
+ * buffers grow to the largest call (12 bytes per vertex + 12 per indexed
+ * triangle, each) and are freed by clr_lbvh_destroy. */
+CLR_API int clr_lbvh_build_host(clr_lbvh* h, const float* host_vx, const float* host_vy, const float* host_vz,
+                                const uint32_t* host_tri, uint32_t num_verts, uint32_t num_tris,
+                                uint32_t bits_per_dim, clr_bvh* out, float* host_root_box, void* stream);
+
+/* Later clr_lbvh_build_host copies start after the work queued on `stream`
+ * so far (e.g. after an event that opens a timed region). */
+CLR_API int clr_lbvh_host_copy_after(clr_lbvh* h, void* stream);
+
+/* Blocks the host until every clr_lbvh_build_host copy issued so far is done:
+ * their host arrays may then be changed. */
+CLR_API int clr_lbvh_host_copy_wait(clr_lbvh* h);
+
 /* Allocation-free build, for callers that may not allocate device memory:
  * hosts that give this library a fixed device-memory budget through their own
  * allocator and forbid any other allocation, and per-frame loops where the

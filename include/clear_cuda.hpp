@@ -58,6 +58,21 @@ class LBVHBuilder {
         check(clr_lbvh_build(h_, vx, vy, vz, faces, numFaces, numBitsPerDim, &out, stream));
     }
 
+    // Upload-and-build from host arrays (the reference host's buffers created
+    // from host memory, then perform): numVerts vertices, faces as 3 indices
+    // per triangle or nullptr for a soup (numVerts = 3 * numFaces).  The copy
+    // of a call overlaps the previous call's build; see clr_lbvh_build_host.
+    void performHost(void* stream, const float* hostVx, const float* hostVy, const float* hostVz,
+                     const uint32_t* hostFaces, uint32_t numVerts, uint32_t numFaces, uint32_t numBitsPerDim,
+                     clr_bvh& out, float* hostRootBox = nullptr) {
+        check(clr_lbvh_build_host(h_, hostVx, hostVy, hostVz, hostFaces, numVerts, numFaces, numBitsPerDim, &out,
+                                  hostRootBox, stream));
+    }
+    // Later performHost copies start after the work queued on `stream` so far.
+    void hostCopyAfter(void* stream) { check(clr_lbvh_host_copy_after(h_, stream)); }
+    // Blocks until the host arrays of every performHost so far may change.
+    void hostCopyWait() { check(clr_lbvh_host_copy_wait(h_)); }
+
     // The per-pass device times of the last profiled perform() (ms), in order.
     std::vector<std::pair<std::string, float>> passTimes() const {
         constexpr int kMax = 64;  // more than the passes of any build

@@ -1,6 +1,7 @@
 // Exercises the C++ facade (include/clear_cuda.hpp): on a machine without a
 // GPU the builder's constructor must throw clr::Error with a message; with a
-// GPU, a two-triangle soup is built and one ray finds the nearer triangle.
+// GPU, a two-triangle soup is built and one ray finds the nearer triangle,
+// and the same soup built from host arrays gives the same tree.
 // Prints one line per check; exits 0 when all pass.
 #include <cstdio>
 #include <cstring>
@@ -44,6 +45,24 @@ int main() {
     cudaMemcpy(&ht, t, 4, cudaMemcpyDeviceToHost);
     std::printf("gpu: hit %u at t %g, %zu timed passes\n", hid, ht, passes.size());
     bool ok = hid == 0 && ht == 1.0f && !passes.empty();
+    // the same soup uploaded from host arrays: same tree, root record read back
+    {
+        clr_bvh hb{};
+        cudaMalloc(&hb.nodes, CLR_NODE_BYTES); cudaMalloc(&hb.tris, 2 * CLR_TRI_BYTES);
+        cudaMalloc((void**)&hb.root_box, 32);
+        float root_a[8], root_b[8];
+        clr::LBVHBuilder hbld(2);
+        hbld.performHost(nullptr, hx, hy, hz, nullptr, 6, 2, 10, hb, root_b);
+        hbld.hostCopyWait();
+        cudaDeviceSynchronize();
+        cudaMemcpy(root_a, bvh.root_box, 32, cudaMemcpyDeviceToHost);
+        unsigned char ta[2 * CLR_TRI_BYTES], tb[2 * CLR_TRI_BYTES];
+        cudaMemcpy(ta, bvh.tris, sizeof(ta), cudaMemcpyDeviceToHost);
+        cudaMemcpy(tb, hb.tris, sizeof(tb), cudaMemcpyDeviceToHost);
+        const bool same = std::memcmp(root_a, root_b, 32) == 0 && std::memcmp(ta, tb, sizeof(ta)) == 0;
+        std::printf("gpu: host-input build %s\n", same ? "identical" : "DIFFERS");
+        ok = ok && same;
+    }
     try {
         clr::LBVHBuilder bad(1);
         bad.perform(nullptr, vx, vy, vz, nullptr, 1, 0, bvh);  // bits_per_dim 0 is rejected
