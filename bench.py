@@ -82,6 +82,9 @@ def parse():
     ap.add_argument("--render-only", action="store_true", help="time only the path tracer (for profiling)")
     ap.add_argument("--adjoint-only", action="store_true", help="time only the adjoint renderer (for profiling)")
     ap.add_argument("--batched-only", action="store_true", help="time only the batched form (for profiling)")
+    ap.add_argument("--terrain-only", action="store_true",
+                    help="time only the wavefront (ordered) render of the terrain scene (for profiling)")
+    ap.add_argument("--terrain-spp", type=int, default=64)
     ap.add_argument("--batched-scenes", type=int, default=512)
     ap.add_argument("--adjoint-res", type=int, default=512)
     ap.add_argument("--adjoint-spp", type=int, default=32)
@@ -256,7 +259,7 @@ def bench_render(dev, args) -> dict:
     return out
 
 
-def bench_render_terrain(dev, spp=64) -> dict:
+def bench_render_terrain(dev, spp=64, forms=("megakernel_ordered", "wavefront_exact", "wavefront_ordered")) -> dict:
     """Wavefront vs megakernel on the large scene: 2.23 M triangles
     (1024^2 heightfield + 256 spheres), 1024 x 512 sky, 8 bump-mapped
     materials, thin lens 0.02 / 1.5, 1920 x 1080, depth 8; `spp` samples per
@@ -274,6 +277,8 @@ def bench_render_terrain(dev, spp=64) -> dict:
     stream = torch.cuda.current_stream(dev)
     for name, ordered, wf in (("megakernel_ordered", True, False), ("wavefront_exact", False, True),
                               ("wavefront_ordered", True, True)):
+        if name not in forms:
+            continue
         rng, pix = ds.new_frame()
         ds.render(rng, pix, 1, max_depth=8, ordered=ordered, wavefront=wf)
         torch.cuda.synchronize()
@@ -671,6 +676,15 @@ def main():
         build()
         dev = torch.device("cuda", 0)
         print(json.dumps({"render": bench_render(dev, args), "render_terrain": bench_render_terrain(dev)}), flush=True)
+        return
+    if args.terrain_only:
+        import torch
+
+        from clear_gb300.build import build
+
+        build()
+        print(json.dumps({"render_terrain": bench_render_terrain(torch.device("cuda", 0), args.terrain_spp,
+                                                                 forms=("wavefront_ordered",))}), flush=True)
         return
     if args.batched_only:
         import torch
