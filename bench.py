@@ -56,7 +56,7 @@ UNIT = "ms/Mtri"
 WORKLOAD = "lbvh-build+traversal, 16Mi random triangles (30-bit Morton), 16Mi closest + 16Mi shadow rays"
 
 # Algorithmic bytes per unit (triangle, or internal node ~ triangle) of each
-# build kernel; see DESIGN.md "Roofline".
+# build kernel: the bytes the algorithm must read and write, counted once.
 ALGO_BYTES = {
     "scene_box": 36.0,          # read 9 floats per triangle
     "morton": 108.0,            # read 9 floats; write a 4-byte key, the 64-byte staging record, the 4-byte counter

@@ -1,6 +1,6 @@
 // Wavefront path tracer: the megakernel (render.cu) split into small kernels
-// over path state kept in SoA device buffers (SURVEY: generate / extend /
-// shade / shadow-connect).
+// over path state kept in SoA device buffers (generate / extend / shade /
+// shadow-connect).
 //
 // One path slot per pixel: a pixel's samples are sequential in its own
 // XORShift128 stream (the reference's per-pixel stream), so a finished path
