@@ -226,6 +226,22 @@ def gpu_time_us(fn, stream, reps: int = 20) -> float:
     return 1e3 * e0.elapsed_time(e1) / reps
 
 
+def path_traffic(ds, spp: int, max_depth: int, msamples_s: float, peak: float) -> dict:
+    """Bytes a path sample moves, from the counted megakernel (the same
+    paths as the timed wavefront): per node loaded 64 B (both child boxes),
+    per triangle tested 48 B (its record), per ray 32 B in + 8 B out, per
+    shaded hit 64 B of face and vertex data, per sample 16 B of accumulation;
+    applied to `msamples_s` against the HBM peak.  Most of it is served by
+    L1/L2, so the fraction measures demand, not DRAM traffic."""
+    rng, pix = ds.new_frame()
+    c = ds.render_counted(rng, pix, spp, max_depth=max_depth, ordered=True)
+    n = c["samples"]
+    b = (64 * c["nodes"] + 48 * c["tris"] + 40 * (c["rays"] + c["shadow_rays"]) + 64 * c["hits"] + 16 * n) / n
+    gbs = b * msamples_s * 1e6 / 1e9
+    return {"per_sample": {k: c[k] / n for k in ("rays", "shadow_rays", "nodes", "tris", "hits")},
+            "counted_spp": spp, "bytes_per_sample": b, "gbs_at_wavefront_ordered": gbs, "frac_of_hbm": gbs / peak}
+
+
 def bench_render(dev, args) -> dict:
     """Path tracing throughput on the procedural Cornell box (996 triangles,
     coat-over-diffuse sphere, quad light): 256 x 256 pixels, 16 samples per
@@ -256,6 +272,7 @@ def bench_render(dev, args) -> dict:
         ms = e0.elapsed_time(e1) / reps
         out[f"{name}_ms"] = ms
         out[f"{name}_msamples_s"] = w * h * spp / ms / 1e3
+    out["traffic"] = path_traffic(ds, spp, 5, out["wavefront_ordered_msamples_s"], measured_peaks()[0])
     return out
 
 
@@ -290,6 +307,8 @@ def bench_render_terrain(dev, spp=64, forms=("megakernel_ordered", "wavefront_ex
         ms = e0.elapsed_time(e1)
         out[f"{name}_ms"] = ms
         out[f"{name}_msamples_s"] = w * h * spp / ms / 1e3
+    if "wavefront_ordered_msamples_s" in out:
+        out["traffic"] = path_traffic(ds, 2, 8, out["wavefront_ordered_msamples_s"], measured_peaks()[0])
     # the steps either side of the path on the same scene: the 8-bit tone map
     # of the image (16 B read + 3 B written per pixel) and the rebuild of the
     # sky's importance distribution (8 B read + 8 B written per texel)
@@ -643,6 +662,10 @@ def run_ours(args):
                      "traffic": traffic, "algo_bytes_per_tri": ALGO_BYTES.get(dom),
                      "kernel_ms": dom_ms},
         "build_kernels_ms": kern_ms,
+        # every build pass against the same measured copy bandwidth
+        "build_kernels_roofline": {k: {"gbs": ALGO_BYTES[k] * n / (v * 1e-3) / 1e9,
+                                       "frac": ALGO_BYTES[k] * n / (v * 1e-3) / 1e9 / peak}
+                                   for k, v in kern_ms.items() if k in ALGO_BYTES},
         "traversal": {"closest_mrays_s": m / closest_ms / 1e3, "shadow_mrays_s": m / shadow_ms / 1e3,
                       "closest_ordered_mrays_s": m / ordered_ms / 1e3,
                       "ordered_vs_exact_id_mismatches": ordered_id_mismatch,
@@ -650,6 +673,7 @@ def run_ours(args):
                       "closest_ms": closest_ms, "shadow_ms": shadow_ms, "closest_hit_frac": hit_frac,
                       "closest_nodes_per_ray": nodes_per_ray, "closest_tris_per_ray": tris_per_ray,
                       "closest_gather_gbs": fetch_bytes / (closest_ms * 1e-3) / 1e9,
+                      "closest_gather_frac_of_hbm": fetch_bytes / (closest_ms * 1e-3) / 1e9 / peak,
                       "shadow_occluded_frac": occ_frac},
         "render": render,
         "render_terrain": render_terrain,

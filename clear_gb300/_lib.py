@@ -99,6 +99,7 @@ def lib() -> C.CDLL:
             "clr_device_status": [C.POINTER(u32), i32],
             "clr_lbvh_set_profiling": [vp, i32],
             "clr_render": [vp, u32, u32, vp, vp, u32, u32, u32, vp],
+            "clr_render_counted": [vp, u32, u32, vp, vp, u32, u32, u32, vp, vp],
             "clr_render_workspace_bytes": [u32, u32, C.POINTER(C.c_uint64)],
             "clr_render_wavefront": [vp, u32, u32, vp, vp, u32, u32, u32, vp, C.c_uint64, vp],
             "clr_render_wavefront_rows": [vp, u32, u32, u32, u32, vp, vp, u32, u32, u32, vp, C.c_uint64, vp],

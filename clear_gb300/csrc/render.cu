@@ -29,9 +29,20 @@ namespace clr {
 
 // ----------------------------------------------------------- path tracer
 
-template <bool kOrdered>
+// With kCount, cnt[0] counts the closest-hit rays, cnt[1] the shadow rays,
+// cnt[2] the nodes loaded and cnt[3] the triangles tested by both, and cnt[4]
+// the surface hits shaded (the visiting counts behind the path's bytes).
+template <bool kOrdered, bool kCount = false>
 __device__ void trace_path(const DScene& sc, const Camera& cam, uint32_t gx, uint32_t gy, Rng& rng, f3& pix,
-                           uint32_t max_depth, uint2* stack) {
+                           uint32_t max_depth, uint2* stack, uint32_t* cnt = nullptr) {
+    auto closest = [&](f3 o, f3 d, Hit& hh) {
+        const bool hit = intersect_impl<kOrdered, kCount>(sc, o, d, hh, stack, kCount ? cnt + 2 : nullptr);
+        if (kCount) {
+            ++cnt[0];
+            cnt[4] += hit ? 1u : 0u;
+        }
+        return hit;
+    };
     f3 org, dir, alpha;
     float dirPDF;
     camera_ray(cam, gx, gy, rng, org, dir, alpha, dirPDF);
@@ -48,7 +59,7 @@ __device__ void trace_path(const DScene& sc, const Camera& cam, uint32_t gx, uin
     EDF edf;
     BSDF bsdf;
     Hit h;
-    if (intersect<kOrdered>(sc, org, dir, h, stack)) {
+    if (closest(org, dir, h)) {
         surface_point(sc, org, dir, h, sp);
         Face face = load_face(sc, sp.faceID);
         vout = -dir;
@@ -71,7 +82,9 @@ __device__ void trace_path(const DScene& sc, const Camera& cam, uint32_t gx, uin
                     dist2 = 1.0f;
                 }
                 const f3 sorg = sp.p + vinL * kEpsilon;
-                if (shadow_visible<kOrdered>(sc, sorg, vinL, shadow_light_word(lpos), stack)) {
+                if (kCount) ++cnt[1];
+                if (shadow_visible<kOrdered, kCount>(sc, sorg, vinL, shadow_light_word(lpos), stack,
+                                                     kCount ? cnt + 2 : nullptr)) {
                     const f3 vinLrev = -vinL;
                     const float fsPDF = bsdf_pdf(bsdf, vout, vinL) * edf_abs_cos(edf, vinL) / dist2;
                     MISWeight = (lightPDF * lightPDF) / (lightPDF * lightPDF + fsPDF * fsPDF);
@@ -89,7 +102,7 @@ __device__ void trace_path(const DScene& sc, const Camera& cam, uint32_t gx, uin
             alpha *= fs * (fabsf(dot(bsdf.n, dir)) / dirPDF);
             org = sp.p + dir * kEpsilon;
             ++depth;
-            if (!intersect<kOrdered>(sc, org, dir, h, stack)) break;
+            if (!closest(org, dir, h)) break;
             surface_point(sc, org, dir, h, sp);
             face = load_face(sc, sp.faceID);
             vout = -dir;
@@ -135,10 +148,11 @@ __device__ void trace_path(const DScene& sc, const Camera& cam, uint32_t gx, uin
     }
 }
 
-template <bool kOrdered>
+template <bool kOrdered, bool kCount = false>
 __global__ void __launch_bounds__(128) k_render(DScene sc, uint32_t width, uint32_t height,
                                                 uint32_t* __restrict__ rand_states, float4* __restrict__ pixels,
-                                                uint32_t spp, uint32_t max_depth) {
+                                                uint32_t spp, uint32_t max_depth,
+                                                unsigned long long* __restrict__ counts = nullptr) {
     const uint32_t x = blockIdx.x * 16 + (threadIdx.x & 15), y = blockIdx.y * 8 + (threadIdx.x >> 4);
     if (x >= width || y >= height) return;
     const uint32_t idx = y * width + x;
@@ -152,9 +166,12 @@ __global__ void __launch_bounds__(128) k_render(DScene sc, uint32_t width, uint3
     f3 pix = mk(p.x, p.y, p.z);
     const Camera cam = load_camera(sc);
     uint2 stack[kStackSize];
-    for (uint32_t i = 0; i < spp; ++i) trace_path<kOrdered>(sc, cam, x, y, rng, pix, max_depth, stack);
+    uint32_t cnt[5] = {0, 0, 0, 0, 0};
+    for (uint32_t i = 0; i < spp; ++i) trace_path<kOrdered, kCount>(sc, cam, x, y, rng, pix, max_depth, stack, cnt);
     pixels[idx] = make_float4(pix.x, pix.y, pix.z, p.w);
     reinterpret_cast<uint4*>(rand_states)[idx] = make_uint4(rng.s[0], rng.s[1], rng.s[2], rng.s[3]);
+    if (kCount)
+        for (int k = 0; k < 5; ++k) atomicAdd(counts + k, (unsigned long long)cnt[k]);
 }
 
 }  // namespace clr
@@ -176,6 +193,27 @@ extern "C" int clr_render(const clr_scene* scene, uint32_t width, uint32_t heigh
     else
         k_render<false><<<grid, 128, 0, st>>>(sc, width, height, rand_states, reinterpret_cast<float4*>(pixels), spp,
                                               max_depth);
+    CLR_LAUNCH_CHECK("k_render");
+    return CLR_OK;
+}
+
+extern "C" int clr_render_counted(const clr_scene* scene, uint32_t width, uint32_t height, uint32_t* rand_states,
+                                  float* pixels, uint32_t spp, uint32_t max_depth, uint32_t flags,
+                                  unsigned long long* counts, void* stream) {
+    int rc = check_render_args(scene, rand_states, pixels);
+    if (rc != CLR_OK) return rc;
+    if (!counts) return clr_set_error(CLR_EINVAL, "clr_render_counted: counts is NULL");
+    if (width == 0 || height == 0 || spp == 0) return CLR_OK;
+    if (max_depth == 0) max_depth = 100;
+    const DScene sc = make_dscene(scene);
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    const dim3 grid(div_up(width, 16), div_up(height, 8));
+    if (flags & CLR_RENDER_ORDERED)
+        k_render<true, true><<<grid, 128, 0, st>>>(sc, width, height, rand_states, reinterpret_cast<float4*>(pixels),
+                                                   spp, max_depth, counts);
+    else
+        k_render<false, true><<<grid, 128, 0, st>>>(sc, width, height, rand_states, reinterpret_cast<float4*>(pixels),
+                                                    spp, max_depth, counts);
     CLR_LAUNCH_CHECK("k_render");
     return CLR_OK;
 }

@@ -141,14 +141,17 @@ static __device__ __forceinline__ bool intersect(const DScene& sc, f3 org, f3 di
 // that have no light face yet: the reference's test "closest hit exists"
 // has the same answer, since any triangle the closest-hit search would
 // accept is also reachable with the bound held at infinity, and vice versa).
-template <bool kOrdered>
-__device__ bool occluded_any(const DScene& sc, f3 org, f3 dir, uint2* stack) {
+// With kCount, boxes[0] counts the nodes loaded and boxes[1] the triangles
+// tested, as in intersect_impl.
+template <bool kOrdered, bool kCount = false>
+__device__ bool occluded_any(const DScene& sc, f3 org, f3 dir, uint2* stack, uint32_t* boxes = nullptr) {
     Ray ray{org.x, org.y, org.z, INFINITY, dir.x, dir.y, dir.z};
     const float ix = 1.0f / dir.x, iy = 1.0f / dir.y, iz = 1.0f / dir.z;
     float entry;
     const float* rb = sc.root_box;
     if (!box_test_fast(rb[0], rb[1], rb[2], rb[4], rb[5], rb[6], ray, ix, iy, iz, entry)) return false;
     auto hit_leaf = [&](uint32_t leaf) {
+        if (kCount) ++boxes[1];
         float t = INFINITY;
         return tri_test(__ldg(sc.tris + 3u * leaf), __ldg(sc.tris + 3u * leaf + 1u), __ldg(sc.tris + 3u * leaf + 2u),
                         ray, t);
@@ -158,6 +161,7 @@ __device__ bool occluded_any(const DScene& sc, f3 org, f3 dir, uint2* stack) {
     int sp = 0;
     stack[sp++] = make_uint2(__float_as_uint(rb[3]), 0u);
     for (uint32_t guard = 0; sp > 0 && guard < sc.num_tris; ++guard) {
+        if (kCount) ++boxes[0];
         const NodeBoxes nb = load_node(sc.nodes, stack[--sp].x);
         float e0, e1;
         const bool p0 = box_test_fast(nb.b0[0], nb.b0[1], nb.b0[2], nb.b0[3], nb.b0[4], nb.b0[5], ray, ix, iy, iz, e0);
@@ -424,11 +428,12 @@ __device__ __forceinline__ uint32_t shadow_light_word(const LightPt& lp) {
     return lp.atInfinity ? (kEnvLightBit | lp.faceID) : lp.faceID;
 }
 
-template <bool kOrdered>
-__device__ __forceinline__ bool shadow_visible(const DScene& sc, f3 org, f3 dir, uint32_t light, uint2* stack) {
-    if (light == kNone32) return !occluded_any<kOrdered>(sc, org, dir, stack);
+template <bool kOrdered, bool kCount = false>
+__device__ __forceinline__ bool shadow_visible(const DScene& sc, f3 org, f3 dir, uint32_t light, uint2* stack,
+                                               uint32_t* boxes = nullptr) {
+    if (light == kNone32) return !occluded_any<kOrdered, kCount>(sc, org, dir, stack, boxes);
     Hit h;
-    const bool hit = intersect<kOrdered>(sc, org, dir, h, stack);
+    const bool hit = intersect_impl<kOrdered, kCount>(sc, org, dir, h, stack, boxes);
     if (light & kEnvLightBit) return !hit || h.id == (light & ~kEnvLightBit);
     return hit && h.id == light;
 }

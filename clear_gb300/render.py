@@ -85,6 +85,21 @@ class DeviceScene:
             ws = self.workspace()
             _lib.call("clr_render_wavefront", *args, C.c_void_p(ws.data_ptr()), C.c_uint64(ws.numel()), stream)
 
+    def render_counted(self, rng: torch.Tensor, pix: torch.Tensor, spp: int, max_depth: int = 100,
+                       ordered: bool = True) -> dict:
+        """clr_render (megakernel) that also counts what the paths visit:
+        closest-hit and shadow rays, BVH nodes loaded, triangles tested,
+        surface hits shaded.  Same image and RNG updates as render()."""
+        counts = torch.zeros(5, dtype=torch.int64, device=self.device)
+        stream = C.c_void_p(torch.cuda.current_stream(self.device).cuda_stream)
+        with torch.cuda.device(self.device):
+            _lib.call("clr_render_counted", C.byref(self.c), C.c_uint32(self.width), C.c_uint32(self.height),
+                      C.c_void_p(rng.data_ptr()), C.c_void_p(pix.data_ptr()), C.c_uint32(spp), C.c_uint32(max_depth),
+                      C.c_uint32(RENDER_ORDERED if ordered else 0), C.c_void_p(counts.data_ptr()), stream)
+        c = [int(v) for v in counts.cpu().tolist()]
+        return {"rays": c[0], "shadow_rays": c[1], "nodes": c[2], "tris": c[3], "hits": c[4],
+                "samples": self.width * self.height * int(spp)}
+
     def render_adjoint(self, rng: torch.Tensor, dloss: torch.Tensor, spp: int, max_depth: int,
                        param_tex: torch.Tensor, param_kind: torch.Tensor, grad: torch.Tensor,
                        env_tex: int | None = None, grad_env: torch.Tensor | None = None,

@@ -252,6 +252,17 @@ typedef struct clr_scene {
 CLR_API int clr_render(const clr_scene* scene, uint32_t width, uint32_t height, uint32_t* rand_states, float* pixels,
                        uint32_t spp, uint32_t max_depth, uint32_t flags, void* stream);
 
+/* clr_render that also counts what the paths visit, for the path's traffic
+ * per sample (the reference's visiting counter, rayIntersectionVis in
+ * bvh_traversal.cl:217-254, extended to whole paths).  The same image and
+ * random-number updates as clr_render.  Adds to counts (5 device uint64,
+ * zeroed by the caller): [0] closest-hit rays traced, [1] shadow rays
+ * traced, [2] BVH nodes loaded and [3] triangles tested by both, [4] surface
+ * hits shaded. */
+CLR_API int clr_render_counted(const clr_scene* scene, uint32_t width, uint32_t height, uint32_t* rand_states,
+                               float* pixels, uint32_t spp, uint32_t max_depth, uint32_t flags,
+                               unsigned long long* counts, void* stream);
+
 /* Wavefront form of clr_render: the same paths, random numbers and
  * contributions (identical results), split into extend / shade / shadow
  * kernels over path state in `workspace`, with per-pixel path regeneration.

@@ -133,3 +133,29 @@ def test_render_accumulates_and_advances_rng(cuda):
     torch.cuda.synchronize()
     assert not torch.equal(rng, rng0)
     assert (pix[:, :3] >= a[:, :3]).all()
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("variant", ["plain", "env"])
+def test_counted_render_same_image_and_consistent_counts(cuda, variant):
+    """clr_render_counted gives clr_render's image and random-number states;
+    its counts obey the path structure: a camera ray per sample, at most
+    max_depth more closest-hit rays per sample, a shadow ray only at a shaded
+    hit, and at least one node or triangle test per ray that enters the scene
+    box."""
+    w = h = 64
+    spp, depth = 4, 5
+    ds = DeviceScene(scenes.cornell_box(w, h, env=env_map() if variant == "env" else None), cuda)
+    rng_a, pix_a = ds.new_frame()
+    ds.render(rng_a, pix_a, spp, max_depth=depth, ordered=True)
+    rng_b, pix_b = ds.new_frame()
+    c = ds.render_counted(rng_b, pix_b, spp, max_depth=depth, ordered=True)
+    torch.cuda.synchronize()
+    assert torch.equal(pix_a, pix_b) and torch.equal(rng_a, rng_b)
+    n = c["samples"]
+    assert n == w * h * spp
+    assert n <= c["rays"] <= n * (1 + depth)
+    assert c["hits"] <= c["rays"]
+    assert 0 < c["shadow_rays"] <= c["hits"]
+    assert c["nodes"] + c["tris"] >= c["hits"]
+    assert _lib.device_status() == 0
