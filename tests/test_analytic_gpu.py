@@ -1,0 +1,134 @@
+"""Renders with analytic answers (the reference ships no tests; these pin the
+path tracer to physics, beside its parity with the reference's renderer).
+
+White furnace: a convex, flat-shaded Lambertian sphere of albedo rho under a
+uniform environment of radiance 1 sees only the environment, so its
+radiance is exactly rho.  The reference's camera weight is not 1 per pixel,
+so the check is relative: the same samples rendered without the sphere give
+the environment's value through the same camera weights, and the ratio over
+a disc inside the silhouette must be rho.  The reference's own CPU renderer
+gives 0.4997 and 0.9998 on this scene at 32 x 32 x 64 spp (per-pixel spread
+1.6 % and 3.1 %); bar: within 1 % of rho (about five standard errors).
+
+Emitting quad: a black quad with radiance exactly 1 (M = pi, diffuse
+emission M / pi) filling the view's centre adds, per camera sample, the same
+camera weight times 1 as an escaped ray adds from the environment of 1: at
+one sample per pixel (later samples of a pixel land elsewhere once the
+quad's paths have drawn more random numbers) the covered pixels equal the
+environment-only image bit for bit, as they do in the reference's renderer.
+"""
+import math
+
+import numpy as np
+import pytest
+import torch
+
+from clear_gb300 import _lib
+from clear_gb300 import scene as S
+from clear_gb300.render import DeviceScene
+
+pytestmark = pytest.mark.gpu
+
+W = H = 32
+SPP = 64
+
+
+def _base(albedo: float) -> S.Scene:
+    sc = S.Scene()
+    mc = sc.mc
+    mc.float3_constant_texture("R", albedo, albedo, albedo)
+    mc.float_constant_texture("sigma0", 0.0)
+    mc.matte_material("m", None, "R", "sigma0")
+    return sc
+
+
+def _finish(sc: S.Scene) -> S.Scene:
+    mc = sc.mc
+    rgba = np.full((8, 16, 4), 1.0, dtype=np.float16)
+    mc.image_texture("env", rgba, "rgba16f")
+    mc.image_based_env_light_property("IBL", "env", rgba[..., :3].astype(np.float32), 1.0)
+    sc.set_environment("IBL")
+    sc.set_camera(W, H, S.look_at((0.0, 0.0, 2.0), (0.0, 0.0, 0.0), (0, 1, 0)), fov_y_deg=40.0)
+    sc.build()
+    return sc
+
+
+def furnace_sphere(albedo: float) -> S.Scene:
+    """A flat-shaded (no vertex normals) 24 x 12 UV sphere of radius 0.5."""
+    sc = _base(albedo)
+    nu, nv = 24, 12
+    sc.begin_object()
+    for j in range(nv + 1):
+        th = math.pi * j / nv
+        for i in range(nu):
+            ph = 2 * math.pi * i / nu
+            sc.add_vertex(0.5 * math.sin(th) * math.cos(ph), 0.5 * math.cos(th), 0.5 * math.sin(th) * math.sin(ph))
+    for j in range(nv):
+        for i in range(nu):
+            a, b = j * nu + i, j * nu + (i + 1) % nu
+            c, d = a + nu, b + nu
+            if j > 0:
+                sc.add_face((a, b, c), sc.mat_ref["m"])
+            if j < nv - 1:
+                sc.add_face((b, d, c), sc.mat_ref["m"])
+    sc.end_object()
+    return _finish(sc)
+
+
+def environment_only() -> S.Scene:
+    """One small triangle behind the camera (no camera ray reaches it)."""
+    sc = _base(0.5)
+    sc.begin_object()
+    for v in ((0.0, 0.0, 10.0), (0.1, 0.0, 10.0), (0.0, 0.1, 10.0)):
+        sc.add_vertex(*v)
+    sc.add_face((0, 1, 2), sc.mat_ref["m"])
+    sc.end_object()
+    return _finish(sc)
+
+
+def emitting_quad() -> S.Scene:
+    """A black quad at z = 0 facing the camera, emitting radiance 1."""
+    sc = _base(0.0)
+    sc.mc.float3_constant_texture("M_quad", math.pi, math.pi, math.pi)
+    sc.mc.diffuse_light_property("quad", "M_quad")
+    sc.begin_object()
+    for v in ((-0.4, -0.4, 0.0), (0.4, -0.4, 0.0), (0.4, 0.4, 0.0), (-0.4, 0.4, 0.0)):
+        sc.add_vertex(*v)
+    sc.add_face((0, 1, 2), sc.mat_ref["m"], light=sc.light_ref["quad"])
+    sc.add_face((0, 2, 3), sc.mat_ref["m"], light=sc.light_ref["quad"])
+    sc.end_object()
+    return _finish(sc)
+
+
+def render(sc: S.Scene, cuda, wavefront: bool, spp: int = SPP) -> np.ndarray:
+    ds = DeviceScene(sc, cuda)
+    rng, pix = ds.new_frame()
+    ds.render(rng, pix, spp, max_depth=100, ordered=True, wavefront=wavefront)
+    torch.cuda.synchronize()
+    assert _lib.device_status() == 0
+    return pix[:, :3].cpu().numpy()
+
+
+def _disc(radius: float) -> np.ndarray:
+    yy, xx = np.mgrid[0:H, 0:W]
+    return (((xx + 0.5 - W / 2) ** 2 + (yy + 0.5 - H / 2) ** 2) <= radius ** 2).reshape(-1)
+
+
+@pytest.mark.parametrize("wavefront", [False, True])
+@pytest.mark.parametrize("albedo", [0.5, 1.0])
+def test_white_furnace(cuda, albedo, wavefront):
+    a = render(furnace_sphere(albedo), cuda, wavefront)
+    b = render(environment_only(), cuda, wavefront)
+    inside, outside = _disc(8.0), ~_disc(13.0)
+    ratio = float(a[inside].sum() / b[inside].sum())
+    print(f"albedo {albedo}: ratio {ratio:.5f}")
+    assert abs(ratio - albedo) <= 0.01 * albedo, ratio
+    np.testing.assert_array_equal(a[outside], b[outside])
+
+
+@pytest.mark.parametrize("wavefront", [False, True])
+def test_emitting_quad_matches_environment(cuda, wavefront):
+    a = render(emitting_quad(), cuda, wavefront, spp=1)
+    b = render(environment_only(), cuda, wavefront, spp=1)
+    inside = _disc(5.0)  # the quad spans about 8.8 pixels either side of the centre
+    np.testing.assert_array_equal(a[inside], b[inside])
