@@ -85,6 +85,8 @@ def parse():
     ap.add_argument("--terrain-only", action="store_true",
                     help="time only the wavefront (ordered) render of the terrain scene (for profiling)")
     ap.add_argument("--terrain-spp", type=int, default=64)
+    ap.add_argument("--loader-only", action="store_true",
+                    help="time only the .obj loader on a generated 1 M-triangle mesh (host code)")
     ap.add_argument("--batched-scenes", type=int, default=512)
     ap.add_argument("--adjoint-res", type=int, default=512)
     ap.add_argument("--adjoint-spp", type=int, default=32)
@@ -240,6 +242,33 @@ def path_traffic(ds, spp: int, max_depth: int, msamples_s: float, peak: float) -
     gbs = b * msamples_s * 1e6 / 1e9
     return {"per_sample": {k: c[k] / n for k in ("rays", "shadow_rays", "nodes", "tris", "hits")},
             "counted_spp": spp, "bytes_per_sample": b, "gbs_at_wavefront_ordered": gbs, "frac_of_hbm": gbs / peak}
+
+
+def bench_loader(reps: int = 3) -> dict:
+    """The .obj loader on a generated 1 M-triangle heightfield (93 MB, v/t/n
+    faces): the native parse alone and load_model (parse + scene encoding),
+    best of `reps`, with the host threads it used."""
+    from clear_gb300 import model_loader
+    from clear_gb300 import scene as S
+    from clear_gb300 import workloads as W
+    from clear_gb300.build import build
+
+    build()
+    with tempfile.TemporaryDirectory() as d:
+        path = W.write_grid_obj(d)
+        size = os.path.getsize(path)
+        parse_s, load_s = [], []
+        for _ in range(reps):
+            t0 = time.perf_counter()
+            model_loader.parse_obj(path)
+            parse_s.append(time.perf_counter() - t0)
+            sc = S.Scene()
+            t0 = time.perf_counter()
+            model_loader.load_model(path, sc)
+            load_s.append(time.perf_counter() - t0)
+        faces = len(sc.faces)
+    return {"file_mb": size / 1e6, "triangles": faces, "parse_s": min(parse_s), "parse_mb_s": size / 1e6 / min(parse_s),
+            "load_model_s": min(load_s), "mtri_s": faces / 1e6 / min(load_s), "host_threads": host_threads()}
 
 
 def bench_render(dev, args) -> dict:
@@ -700,6 +729,9 @@ def main():
         build()
         dev = torch.device("cuda", 0)
         print(json.dumps({"render": bench_render(dev, args), "render_terrain": bench_render_terrain(dev)}), flush=True)
+        return
+    if args.loader_only:
+        print(json.dumps({"obj_loader": bench_loader()}), flush=True)
         return
     if args.terrain_only:
         import torch

@@ -29,6 +29,7 @@
 // defined later), missing vertex components read as 0, negative indices count
 // back from the end of the list read so far as the OBJ format defines, and
 // .mtl statements before the first `newmtl` are ignored.
+#include <algorithm>
 #include <cctype>
 #include <cstdint>
 #include <cstdio>
@@ -37,8 +38,8 @@
 #include <fstream>
 #include <memory>
 #include <new>
-#include <sstream>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "clear_cuda.h"
@@ -258,9 +259,98 @@ void check_ranges(clr_obj_model* m) {
     m->faces.resize(out);
 }
 
+// f(lo, hi) over [0, n) in contiguous ranges on the host's threads, at
+// least min_per_thread items each.
+template <typename F>
+void parallel_ranges(size_t n, F f, size_t min_per_thread = 4096) {
+    size_t threads = std::max<size_t>(1, std::thread::hardware_concurrency());
+    threads = std::min(threads, std::max<size_t>(1, n / min_per_thread));
+    if (threads <= 1) {
+        f(size_t(0), n);
+        return;
+    }
+    std::vector<std::thread> pool;
+    pool.reserve(threads);
+    for (size_t t = 0; t < threads; ++t) pool.emplace_back(f, n * t / threads, n * (t + 1) / threads);
+    for (std::thread& th : pool) th.join();
+}
+
+// A whole file read in one piece, its lines NUL-terminated in place: each
+// '\n' becomes a NUL and each line starts after the bytes the reference
+// strips.
+struct FileLines {
+    std::unique_ptr<char[]> data;
+    size_t size = 0;
+    std::vector<size_t> starts;
+};
+
+bool read_buffer(const char* path, FileLines* fl) {
+    std::FILE* f = std::fopen(path, "rb");
+    if (!f) return false;
+    const long end = std::fseek(f, 0, SEEK_END) == 0 ? std::ftell(f) : -1L;
+    if (end < 0 || std::fseek(f, 0, SEEK_SET) != 0) {  // not a regular file
+        std::fclose(f);
+        return false;
+    }
+    size_t n = (size_t)end;
+    fl->data.reset(new char[n + 1]);
+    n = std::fread(fl->data.get(), 1, n, f);
+    std::fclose(f);
+    char* b = fl->data.get();
+    b[n] = '\0';
+    fl->size = n;
+    // newline positions, found in parallel byte ranges and joined in order
+    const size_t chunks = std::max<size_t>(1, std::min<size_t>(64, n >> 20));  // at least 1 MB each
+    std::vector<std::vector<size_t>> nl(chunks);
+    parallel_ranges(
+        chunks,
+        [&](size_t lo, size_t hi) {
+            for (size_t c = lo; c < hi; ++c) {
+                const char* p = b + n * c / chunks;
+                const char* const e = b + n * (c + 1) / chunks;
+                while ((p = static_cast<const char*>(memchr(p, '\n', (size_t)(e - p)))) != nullptr)
+                    nl[c].push_back((size_t)(p++ - b));
+            }
+        },
+        1);
+    size_t lines = 0;
+    for (const auto& v : nl) lines += v.size();
+    std::vector<size_t> ends;
+    ends.reserve(lines + 1);
+    for (const auto& v : nl) ends.insert(ends.end(), v.begin(), v.end());
+    if (ends.empty() ? n > 0 : ends.back() + 1 < n) ends.push_back(n);  // a last line without '\n'
+    fl->starts.resize(ends.size());
+    parallel_ranges(ends.size(), [&](size_t lo, size_t hi) {
+        for (size_t i = lo; i < hi; ++i) {
+            const size_t e = ends[i];
+            size_t k = i == 0 ? 0 : ends[i - 1] + 1;
+            b[e] = '\0';
+            while (k < e && strip_byte((unsigned char)b[k])) ++k;
+            fl->starts[i] = k;
+        }
+    });
+    return true;
+}
+
+// A face line found by the statement pass: where it is, its group's format
+// and the lengths of the three lists when it was read (for negative indices).
+struct FaceLine {
+    size_t at;
+    uint32_t fmt, np, nt, nn;
+};
+
+// Two passes.  The statement pass walks the lines in order with the
+// reference's state (groups, smoothing, materials, face-run boundaries, each
+// group's face format) and only notes where each vertex, uv, normal and face
+// line is; the number pass then converts those lines in parallel into their
+// slots.  A face that does not parse in its group's format is stored with
+// no valid index, so the range check drops and counts it as the reference's
+// loop would.
 int parse_obj(const char* path, clr_obj_model* m) {
-    std::vector<std::string> lines;
-    if (!read_lines(path, &lines)) return clr_set_error(CLR_EINVAL, "clr_obj_parse: cannot open %s", path);
+    FileLines file;
+    if (!read_buffer(path, &file)) return clr_set_error(CLR_EINVAL, "clr_obj_parse: cannot open %s", path);
+    const std::vector<size_t>& starts = file.starts;
+    const char* b = file.data.get();
     const std::string dir = directory_of(path);
     m->strings.push_back('\0');
     std::string group_name, mat_name;
@@ -268,84 +358,114 @@ int parse_obj(const char* path, clr_obj_model* m) {
     bool in_faces = false;
     Format fmt = kVTN;
     bool fmt_ok = false;
-    for (const std::string& line : lines) {
-        const char c0 = line.empty() ? '\0' : line[0];
+    std::vector<size_t> vlines, tlines, nlines;
+    std::vector<FaceLine> flines;
+    for (const size_t at : starts) {
+        const char* line = b + at;
+        const char c0 = line[0];
         if (in_faces && c0 != 'f') in_faces = false;
-        Cursor c{line.c_str()};
+        Cursor c{line};
         std::string w;
         switch (c0) {
             case 'g':
                 if (c.lit('g') && c.word(&w)) group_name = w;
                 break;
             case 's':
-                if (line.compare(0, 5, "s off") == 0) {
+                if (strncmp(line, "s off", 5) == 0) {
                     smooth = 0;
                 } else {
                     long long v;
                     if (c.lit('s') && c.index(&v)) smooth = (uint32_t)v;
                 }
                 break;
-            case 'v': {
-                const char c1 = line.size() > 1 ? line[1] : '\0';
-                float v[3] = {0.0f, 0.0f, 0.0f};
-                if (c1 == ' ') {
-                    c.p += 1;
-                    c.f32(&v[0]) && c.f32(&v[1]) && c.f32(&v[2]);
-                    m->positions.insert(m->positions.end(), v, v + 3);
-                } else if (c1 == 't') {
-                    c.p += 2;
-                    c.f32(&v[0]) && c.f32(&v[1]);
-                    m->uvs.push_back(v[0]);
-                    m->uvs.push_back(1.0f - v[1]);
-                } else if (c1 == 'n') {
-                    c.p += 2;
-                    c.f32(&v[0]) && c.f32(&v[1]) && c.f32(&v[2]);
-                    m->normals.insert(m->normals.end(), v, v + 3);
-                }
+            case 'v':
+                if (line[1] == ' ') vlines.push_back(at);
+                else if (line[1] == 't') tlines.push_back(at);
+                else if (line[1] == 'n') nlines.push_back(at);
                 break;
-            }
             case 'f': {
-                long long idx[9];
                 if (!in_faces) {
                     in_faces = true;
                     clr_obj_group g{};
-                    g.first_face = (uint32_t)(m->faces.size() / 9);
+                    g.first_face = (uint32_t)flines.size();
                     g.smooth = smooth;
                     g.name = intern(m, group_name);
                     g.material = intern(m, mat_name);
+                    long long idx[9];
                     fmt_ok = true;
-                    if (parse_face(line.c_str(), kVTN, idx)) fmt = kVTN;
-                    else if (parse_face(line.c_str(), kVN, idx)) fmt = kVN;
-                    else if (parse_face(line.c_str(), kVT, idx)) fmt = kVT;
-                    else if (parse_face(line.c_str(), kV, idx)) fmt = kV;
+                    if (parse_face(line, kVTN, idx)) fmt = kVTN;
+                    else if (parse_face(line, kVN, idx)) fmt = kVN;
+                    else if (parse_face(line, kVT, idx)) fmt = kVT;
+                    else if (parse_face(line, kV, idx)) fmt = kV;
                     else fmt_ok = false;
                     g.format = fmt_ok ? (uint32_t)fmt : (uint32_t)CLR_OBJ_NONE;
                     m->groups.push_back(g);
                 }
-                if (!fmt_ok || !parse_face(line.c_str(), fmt, idx)) {
+                if (!fmt_ok) {
                     ++m->skipped;
                     break;
                 }
-                uint32_t f[9];
-                for (int k = 0; k < 3; ++k) {
-                    f[k] = resolve(idx[k], m->positions.size() / 3);
-                    f[3 + k] = (fmt == kVTN || fmt == kVT) ? resolve(idx[3 + k], m->uvs.size() / 2) : kNone;
-                    f[6 + k] = (fmt == kVTN || fmt == kVN) ? resolve(idx[6 + k], m->normals.size() / 3) : kNone;
-                }
-                m->faces.insert(m->faces.end(), f, f + 9);
+                flines.push_back(FaceLine{at, (uint32_t)fmt, (uint32_t)vlines.size(), (uint32_t)tlines.size(),
+                                          (uint32_t)nlines.size()});
                 ++m->groups.back().num_faces;
                 break;
             }
             case 'm':
-                if (line.compare(0, 6, "mtllib") == 0 && c.lit("mtllib") && c.word(&w)) parse_mtl(dir + w, m);
+                if (strncmp(line, "mtllib", 6) == 0 && c.lit("mtllib") && c.word(&w)) parse_mtl(dir + w, m);
                 break;
             case 'u':
-                if (line.compare(0, 6, "usemtl") == 0 && c.lit("usemtl") && c.word(&w)) mat_name = w;
+                if (strncmp(line, "usemtl", 6) == 0 && c.lit("usemtl") && c.word(&w)) mat_name = w;
                 break;
             default:  // `o` starts a new object, which changes nothing in the flattened lists
                 break;
         }
     }
+    m->positions.resize(3 * vlines.size());
+    m->uvs.resize(2 * tlines.size());
+    m->normals.resize(3 * nlines.size());
+    m->faces.resize(9 * flines.size());
+    parallel_ranges(vlines.size(), [&](size_t lo, size_t hi) {
+        for (size_t i = lo; i < hi; ++i) {
+            Cursor c{b + vlines[i] + 1};
+            float v[3] = {0.0f, 0.0f, 0.0f};
+            c.f32(&v[0]) && c.f32(&v[1]) && c.f32(&v[2]);
+            memcpy(&m->positions[3 * i], v, sizeof(v));
+        }
+    });
+    parallel_ranges(tlines.size(), [&](size_t lo, size_t hi) {
+        for (size_t i = lo; i < hi; ++i) {
+            Cursor c{b + tlines[i] + 2};
+            float v[2] = {0.0f, 0.0f};
+            c.f32(&v[0]) && c.f32(&v[1]);
+            m->uvs[2 * i] = v[0];
+            m->uvs[2 * i + 1] = 1.0f - v[1];
+        }
+    });
+    parallel_ranges(nlines.size(), [&](size_t lo, size_t hi) {
+        for (size_t i = lo; i < hi; ++i) {
+            Cursor c{b + nlines[i] + 2};
+            float v[3] = {0.0f, 0.0f, 0.0f};
+            c.f32(&v[0]) && c.f32(&v[1]) && c.f32(&v[2]);
+            memcpy(&m->normals[3 * i], v, sizeof(v));
+        }
+    });
+    parallel_ranges(flines.size(), [&](size_t lo, size_t hi) {
+        for (size_t i = lo; i < hi; ++i) {
+            const FaceLine& fl = flines[i];
+            const Format ff = (Format)fl.fmt;
+            uint32_t* f = &m->faces[9 * i];
+            long long idx[9];
+            if (!parse_face(b + fl.at, ff, idx)) {
+                for (int k = 0; k < 9; ++k) f[k] = kNone;
+                continue;
+            }
+            for (int k = 0; k < 3; ++k) {
+                f[k] = resolve(idx[k], fl.np);
+                f[3 + k] = (ff == kVTN || ff == kVT) ? resolve(idx[3 + k], fl.nt) : kNone;
+                f[6 + k] = (ff == kVTN || ff == kVN) ? resolve(idx[6 + k], fl.nn) : kNone;
+            }
+        }
+    });
     check_ranges(m);
     return CLR_OK;
 }

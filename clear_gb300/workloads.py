@@ -58,3 +58,29 @@ def shadow_rays(m: int, seed: int = 3):
     L = np.maximum(L, 1e-12)
     d = d / L[:, None]
     return pack_rays(a.astype(np.float32), d.astype(np.float32), L.astype(np.float32))
+
+
+def write_grid_obj(directory: str, n: int = 708) -> str:
+    """Writes ``grid.obj`` and ``grid.mtl`` into `directory`: an n x n
+    heightfield (2 (n-1)^2 triangles; n = 708 gives about 1 M and 93 MB) with
+    one uv and one normal per vertex, faces in v/t/n form, one material.
+    Returns the .obj path."""
+    import os
+
+    xs = np.linspace(0.0, 1.0, n)
+    x, z = np.meshgrid(xs, xs)
+    y = 0.1 * np.sin(7.0 * x) * np.cos(5.0 * z)
+    path = os.path.join(directory, "grid.obj")
+    with open(path, "w") as fh:
+        fh.write("mtllib grid.mtl\no grid\n")
+        fh.write("".join(f"v {a:.6f} {b:.6f} {c:.6f}\n" for a, b, c in zip(x.ravel(), y.ravel(), z.ravel())))
+        fh.write("".join(f"vt {a:.6f} {c:.6f}\n" for a, c in zip(x.ravel(), z.ravel())))
+        fh.write("vn 0 1 0\n" * (n * n))
+        fh.write("usemtl white\n")
+        j, i = np.meshgrid(np.arange(n - 1), np.arange(n - 1), indexing="ij")
+        a = (j * n + i + 1).ravel()
+        fh.write("".join(f"f {p}/{p}/{p} {q}/{q}/{q} {r}/{r}/{r}\nf {r}/{r}/{r} {q}/{q}/{q} {s}/{s}/{s}\n"
+                         for p, q, r, s in zip(a, a + n, a + 1, a + n + 1)))
+    with open(os.path.join(directory, "grid.mtl"), "w") as fh:
+        fh.write("newmtl white\nKd 0.7 0.7 0.7\n")
+    return path
