@@ -21,6 +21,12 @@
 //     (the reference compares an unset hit record, pathtracer.cl:120-122);
 //   * samples-per-pixel loop inside the kernel (the reference launches once
 //     per sample); each pixel's contributions are added in the same order.
+//
+// The kernel traces from three sites (camera ray, shadow ray, bounce); one
+// out-of-line copy of each search instead of three inlined copies keeps the
+// kernel's instruction footprint down, which this instruction-fetch-bound
+// kernel turns into speed (13.2 -> 20.1 Msamples/s on the Cornell box).
+#define CLR_TRAVERSAL_OUTLINED
 #include "render_common.cuh"
 
 CLR_DEFINE_STATUS_READER(render)

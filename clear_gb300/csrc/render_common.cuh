@@ -69,8 +69,17 @@ struct Hit {
 // the leaf boxes the search accepts (their sum is the reference's numAABBHit
 // of rayIntersectionVis, bvh_traversal.cl:217-254, in its visiting order when
 // !kOrdered): the nodes loaded and the triangles tested.
+// Kernels that trace from several call sites may define
+// CLR_TRAVERSAL_OUTLINED before including this header to keep one copy of
+// each search instead of one inlined copy per site.
+#ifdef CLR_TRAVERSAL_OUTLINED
+#define CLR_TRAVERSAL_ATTR __noinline__
+#else
+#define CLR_TRAVERSAL_ATTR
+#endif
+
 template <bool kOrdered, bool kCount = false>
-static __device__ bool intersect_impl(const DScene& sc, f3 org, f3 dir, Hit& h, uint2* stack, uint32_t* boxes) {
+static __device__ CLR_TRAVERSAL_ATTR bool intersect_impl(const DScene& sc, f3 org, f3 dir, Hit& h, uint2* stack, uint32_t* boxes) {
     Ray ray{org.x, org.y, org.z, INFINITY, dir.x, dir.y, dir.z};
     const float ix = 1.0f / dir.x, iy = 1.0f / dir.y, iz = 1.0f / dir.z;
     float t = INFINITY;
@@ -144,7 +153,7 @@ static __device__ __forceinline__ bool intersect(const DScene& sc, f3 org, f3 di
 // With kCount, boxes[0] counts the nodes loaded and boxes[1] the triangles
 // tested, as in intersect_impl.
 template <bool kOrdered, bool kCount = false>
-__device__ bool occluded_any(const DScene& sc, f3 org, f3 dir, uint2* stack, uint32_t* boxes = nullptr) {
+__device__ CLR_TRAVERSAL_ATTR bool occluded_any(const DScene& sc, f3 org, f3 dir, uint2* stack, uint32_t* boxes = nullptr) {
     Ray ray{org.x, org.y, org.z, INFINITY, dir.x, dir.y, dir.z};
     const float ix = 1.0f / dir.x, iy = 1.0f / dir.y, iz = 1.0f / dir.z;
     float entry;
