@@ -1226,12 +1226,22 @@ extern "C" int clr_lbvh_build(clr_lbvh* h, const float* vx, const float* vy, con
 // The copy stream and the four buffer events, made on first use.
 static int host_path_init(clr_lbvh* h) {
     if (h->copy_stream) return CLR_OK;
-    CLR_CUDA_TRY(cudaStreamCreateWithFlags(&h->copy_stream, cudaStreamNonBlocking));
-    for (int s = 0; s < 2; ++s) {
-        CLR_CUDA_TRY(cudaEventCreateWithFlags(&h->in_copied[s], cudaEventDisableTiming));
-        CLR_CUDA_TRY(cudaEventCreateWithFlags(&h->in_consumed[s], cudaEventDisableTiming));
+    cudaStream_t st = nullptr;
+    cudaEvent_t ev[5] = {};
+    cudaError_t e = cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking);
+    for (int k = 0; k < 5 && e == cudaSuccess; ++k) e = cudaEventCreateWithFlags(&ev[k], cudaEventDisableTiming);
+    if (e != cudaSuccess) {  // nothing half-made stays behind
+        for (cudaEvent_t x : ev)
+            if (x) cudaEventDestroy(x);
+        if (st) cudaStreamDestroy(st);
+        return clr_set_error(CLR_ECUDA, "clr_lbvh_build_host: copy stream or events: %s", cudaGetErrorString(e));
     }
-    CLR_CUDA_TRY(cudaEventCreateWithFlags(&h->copy_gate, cudaEventDisableTiming));
+    h->in_copied[0] = ev[0];
+    h->in_copied[1] = ev[1];
+    h->in_consumed[0] = ev[2];
+    h->in_consumed[1] = ev[3];
+    h->copy_gate = ev[4];
+    h->copy_stream = st;
     return CLR_OK;
 }
 
