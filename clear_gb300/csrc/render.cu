@@ -184,11 +184,17 @@ __global__ void __launch_bounds__(128) k_render(DScene sc, uint32_t width, uint3
 
 using namespace clr;
 
+// The wavefront form on the library's own workspace (render_wf.cu).
+int clr_render_kept_wavefront(const clr_scene* scene, uint32_t width, uint32_t height, uint32_t* rand_states,
+                              float* pixels, uint32_t spp, uint32_t max_depth, uint32_t flags, void* stream);
+
 extern "C" int clr_render(const clr_scene* scene, uint32_t width, uint32_t height, uint32_t* rand_states,
                           float* pixels, uint32_t spp, uint32_t max_depth, uint32_t flags, void* stream) {
     int rc = check_render_args(scene, rand_states, pixels);
     if (rc != CLR_OK) return rc;
     if (width == 0 || height == 0 || spp == 0) return CLR_OK;
+    if (flags & CLR_RENDER_WAVEFRONT)
+        return clr_render_kept_wavefront(scene, width, height, rand_states, pixels, spp, max_depth, flags, stream);
     if (max_depth == 0) max_depth = 100;
     const DScene sc = make_dscene(scene);
     cudaStream_t st = static_cast<cudaStream_t>(stream);
@@ -209,6 +215,8 @@ extern "C" int clr_render_counted(const clr_scene* scene, uint32_t width, uint32
     int rc = check_render_args(scene, rand_states, pixels);
     if (rc != CLR_OK) return rc;
     if (!counts) return clr_set_error(CLR_EINVAL, "clr_render_counted: counts is NULL");
+    if (flags & CLR_RENDER_WAVEFRONT)
+        return clr_set_error(CLR_EINVAL, "clr_render_counted: counts are taken by the megakernel form only");
     if (width == 0 || height == 0 || spp == 0) return CLR_OK;
     if (max_depth == 0) max_depth = 100;
     const DScene sc = make_dscene(scene);

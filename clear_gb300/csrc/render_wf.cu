@@ -20,6 +20,8 @@
 // in the reference's order (a bounce's NEE term lands in the shadow pass,
 // before the next bounce's emission term), so results match the megakernel
 // path for path.
+#include <mutex>
+
 #include "render_common.cuh"
 
 CLR_DEFINE_STATUS_READER(render_wf)
@@ -361,4 +363,53 @@ extern "C" int clr_render_wavefront(const clr_scene* scene, uint32_t width, uint
                                     uint64_t workspace_bytes, void* stream) {
     return clr_render_wavefront_rows(scene, width, height, 0u, height, rand_states, pixels, spp, max_depth, flags,
                                      workspace, workspace_bytes, stream);
+}
+
+// clr_render with CLR_RENDER_WAVEFRONT: the wavefront form on a workspace the
+// library keeps per device until the process exits.  It grows to the largest
+// image rendered (freed and reallocated once the renders queued on it are
+// done), and every render that uses it waits on the GPU for the previous
+// one, so calls on different streams stay correct (they take turns).
+namespace {
+constexpr int kKeptDevices = 64;
+struct KeptWorkspace {
+    void* ptr = nullptr;
+    uint64_t bytes = 0;
+    cudaEvent_t last_use = nullptr;
+};
+std::mutex g_kept_mutex;
+KeptWorkspace g_kept[kKeptDevices];
+}  // namespace
+
+int clr_render_kept_wavefront(const clr_scene* scene, uint32_t width, uint32_t height, uint32_t* rand_states,
+                              float* pixels, uint32_t spp, uint32_t max_depth, uint32_t flags, void* stream) {
+    int dev = 0;
+    CLR_CUDA_TRY(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= kKeptDevices) return clr_set_error(CLR_EINVAL, "clr_render: device %d out of range", dev);
+    uint64_t need = 0;
+    int rc = clr_render_workspace_bytes(width, height, &need);
+    if (rc != CLR_OK) return rc;
+    std::lock_guard<std::mutex> lock(g_kept_mutex);
+    KeptWorkspace& w = g_kept[dev];
+    if (!w.last_use) CLR_CUDA_TRY(cudaEventCreateWithFlags(&w.last_use, cudaEventDisableTiming));
+    if (w.bytes < need) {
+        CLR_CUDA_TRY(cudaEventSynchronize(w.last_use));  // no queued render still uses it
+        if (w.ptr) cudaFree(w.ptr);
+        w.ptr = nullptr;
+        w.bytes = 0;
+        if (cudaMalloc(&w.ptr, need) != cudaSuccess) {
+            cudaGetLastError();
+            w.ptr = nullptr;
+            return clr_set_error(CLR_ENOMEM, "clr_render: cudaMalloc of a %llu-byte workspace failed",
+                                 (unsigned long long)need);
+        }
+        w.bytes = need;
+    }
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    CLR_CUDA_TRY(cudaStreamWaitEvent(st, w.last_use, 0));
+    rc = clr_render_wavefront(scene, width, height, rand_states, pixels, spp, max_depth, flags & ~CLR_RENDER_WAVEFRONT,
+                              w.ptr, w.bytes, stream);
+    if (rc != CLR_OK) return rc;
+    CLR_CUDA_TRY(cudaEventRecord(w.last_use, st));
+    return CLR_OK;
 }

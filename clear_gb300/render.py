@@ -13,6 +13,7 @@ from .scene import Scene, zenith_weights
 from .scenes import pixel_seeds
 
 RENDER_ORDERED = 0x1
+RENDER_WAVEFRONT = 0x2  # clr_render: the wavefront form on the library's own workspace
 NO_TEX = 0xFFFFFFFF
 TAPE_WORDS = 32
 TAPE_VISIBLE = 0x100

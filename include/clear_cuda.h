@@ -240,6 +240,13 @@ typedef struct clr_scene {
 } clr_scene;
 
 #define CLR_RENDER_ORDERED 0x1u  /* trace with nearer-child-first traversal */
+/* clr_render: run the wavefront form (identical results, several times
+ * faster) on a workspace the library keeps per device until the process
+ * exits, grown to the largest image rendered; renders that share it take
+ * turns on the GPU.  Not for stream capture (it may allocate, and it orders
+ * itself after earlier renders through an event).  clr_render_wavefront
+ * takes a caller-owned workspace instead. */
+#define CLR_RENDER_WAVEFRONT 0x2u
 
 /* Replaces the `pathtracing` kernel (OpenCL/pathtracer.cl:25-271) launched
  * once per tile per sample (main.cpp:477-494): adds `spp` path samples per

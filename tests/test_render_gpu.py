@@ -159,3 +159,34 @@ def test_counted_render_same_image_and_consistent_counts(cuda, variant):
     assert 0 < c["shadow_rays"] <= c["hits"]
     assert c["nodes"] + c["tris"] >= c["hits"]
     assert _lib.device_status() == 0
+
+
+@pytest.mark.gpu
+def test_render_flag_wavefront_on_kept_workspace(cuda):
+    """clr_render with CLR_RENDER_WAVEFRONT runs the wavefront form on a
+    workspace the library keeps: the megakernel's image and RNG states; two
+    renders on two streams that share the workspace are both right; a larger
+    image afterwards grows it."""
+    import ctypes as C
+
+    from clear_gb300.render import RENDER_ORDERED, RENDER_WAVEFRONT
+
+    def kept(ds, rng, pix, spp, stream):
+        with torch.cuda.device(cuda):
+            _lib.call("clr_render", C.byref(ds.c), C.c_uint32(ds.width), C.c_uint32(ds.height),
+                      C.c_void_p(rng.data_ptr()), C.c_void_p(pix.data_ptr()), C.c_uint32(spp), C.c_uint32(5),
+                      C.c_uint32(RENDER_ORDERED | RENDER_WAVEFRONT), C.c_void_p(stream.cuda_stream))
+
+    for size in (48, 80):
+        ds = DeviceScene(scenes.cornell_box(size, size, env=env_map()), cuda)
+        rng_a, pix_a = ds.new_frame()
+        ds.render(rng_a, pix_a, 8, max_depth=5, ordered=True)
+        torch.cuda.synchronize()
+        frames = [ds.new_frame() for _ in range(2)]
+        streams = [torch.cuda.Stream(cuda) for _ in range(2)]
+        for (rng, pix), st in zip(frames, streams):
+            kept(ds, rng, pix, 8, st)
+        torch.cuda.synchronize()
+        for rng, pix in frames:
+            assert torch.equal(pix, pix_a) and torch.equal(rng, rng_a)
+    assert _lib.device_status() == 0
