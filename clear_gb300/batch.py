@@ -24,7 +24,7 @@ import torch
 from . import _lib, lbvh
 from . import scene as S
 from . import workloads as W
-from .render import RENDER_ORDERED, ClrScene, DeviceScene
+from .render import RENDER_ORDERED, ClrScene, DeviceScene, scene_flags
 from .scenes import pixel_seeds
 
 BATCH_GRAPH = 0x2
@@ -127,7 +127,8 @@ class BatchRenderer:
         for s in range(len(scenes)):
             p = {k: self.t[k].data_ptr() + self.boff[k][s] for k in BLOB_KEYS}
             arr[s] = ClrScene(p["vertices"], p["normals"], p["tangents"], p["uvs"], p["faces"], p["lights"],
-                              p["materials"], p["textures"], p["others"], C.pointer(self._bvh_c[s].c))
+                              p["materials"], p["textures"], p["others"], C.pointer(self._bvh_c[s].c),
+                              scene_flags(blobs[s]))
         self._arr = arr
         w = (C.c_uint32 * len(scenes))(*[wh[0] for wh in self.sizes])
         h = (C.c_uint32 * len(scenes))(*[wh[1] for wh in self.sizes])

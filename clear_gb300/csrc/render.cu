@@ -38,11 +38,12 @@ namespace clr {
 // With kCount, cnt[0] counts the closest-hit rays, cnt[1] the shadow rays,
 // cnt[2] the nodes loaded and cnt[3] the triangles tested by both, and cnt[4]
 // the surface hits shaded (the visiting counts behind the path's bytes).
-template <bool kOrdered, bool kCount = false>
+// kAlpha: the scene has cutout faces (CLR_SCENE_ALPHA), fixed per launch.
+template <bool kOrdered, bool kCount, bool kAlpha>
 __device__ void trace_path(const DScene& sc, const Camera& cam, uint32_t gx, uint32_t gy, Rng& rng, f3& pix,
                            uint32_t max_depth, uint2* stack, uint32_t* cnt = nullptr) {
     auto closest = [&](f3 o, f3 d, Hit& hh) {
-        const bool hit = intersect_impl<kOrdered, kCount>(sc, o, d, hh, stack, kCount ? cnt + 2 : nullptr);
+        const bool hit = intersect_impl<kOrdered, kCount, kAlpha ? 1 : 0>(sc, o, d, hh, stack, kCount ? cnt + 2 : nullptr);
         if (kCount) {
             ++cnt[0];
             cnt[4] += hit ? 1u : 0u;
@@ -89,8 +90,8 @@ __device__ void trace_path(const DScene& sc, const Camera& cam, uint32_t gx, uin
                 }
                 const f3 sorg = sp.p + vinL * kEpsilon;
                 if (kCount) ++cnt[1];
-                if (shadow_visible<kOrdered, kCount>(sc, sorg, vinL, shadow_light_word(lpos), stack,
-                                                     kCount ? cnt + 2 : nullptr)) {
+                if (shadow_visible<kOrdered, kCount, kAlpha ? 1 : 0>(sc, sorg, vinL, shadow_light_word(lpos), stack,
+                                                                     kCount ? cnt + 2 : nullptr)) {
                     const f3 vinLrev = -vinL;
                     const float fsPDF = bsdf_pdf(bsdf, vout, vinL) * edf_abs_cos(edf, vinL) / dist2;
                     MISWeight = (lightPDF * lightPDF) / (lightPDF * lightPDF + fsPDF * fsPDF);
@@ -154,7 +155,7 @@ __device__ void trace_path(const DScene& sc, const Camera& cam, uint32_t gx, uin
     }
 }
 
-template <bool kOrdered, bool kCount = false>
+template <bool kOrdered, bool kCount, bool kAlpha>
 __global__ void __launch_bounds__(128) k_render(DScene sc, uint32_t width, uint32_t height,
                                                 uint32_t* __restrict__ rand_states, float4* __restrict__ pixels,
                                                 uint32_t spp, uint32_t max_depth,
@@ -173,7 +174,8 @@ __global__ void __launch_bounds__(128) k_render(DScene sc, uint32_t width, uint3
     const Camera cam = load_camera(sc);
     uint2 stack[kStackSize];
     uint32_t cnt[5] = {0, 0, 0, 0, 0};
-    for (uint32_t i = 0; i < spp; ++i) trace_path<kOrdered, kCount>(sc, cam, x, y, rng, pix, max_depth, stack, cnt);
+    for (uint32_t i = 0; i < spp; ++i)
+        trace_path<kOrdered, kCount, kAlpha>(sc, cam, x, y, rng, pix, max_depth, stack, cnt);
     pixels[idx] = make_float4(pix.x, pix.y, pix.z, p.w);
     reinterpret_cast<uint4*>(rand_states)[idx] = make_uint4(rng.s[0], rng.s[1], rng.s[2], rng.s[3]);
     if (kCount)
@@ -183,6 +185,25 @@ __global__ void __launch_bounds__(128) k_render(DScene sc, uint32_t width, uint3
 }  // namespace clr
 
 using namespace clr;
+
+// k_render over the image, instantiated for the traversal order and for
+// whether the scene has cutout faces.
+template <bool kCount>
+static void launch_render(const DScene& sc, uint32_t width, uint32_t height, uint32_t* rand_states, float* pixels,
+                          uint32_t spp, uint32_t max_depth, uint32_t flags, unsigned long long* counts,
+                          cudaStream_t st) {
+    const dim3 grid(div_up(width, 16), div_up(height, 8));
+    float4* px = reinterpret_cast<float4*>(pixels);
+    const bool ordered = (flags & CLR_RENDER_ORDERED) != 0;
+    if (ordered && sc.alpha)
+        k_render<true, kCount, true><<<grid, 128, 0, st>>>(sc, width, height, rand_states, px, spp, max_depth, counts);
+    else if (ordered)
+        k_render<true, kCount, false><<<grid, 128, 0, st>>>(sc, width, height, rand_states, px, spp, max_depth, counts);
+    else if (sc.alpha)
+        k_render<false, kCount, true><<<grid, 128, 0, st>>>(sc, width, height, rand_states, px, spp, max_depth, counts);
+    else
+        k_render<false, kCount, false><<<grid, 128, 0, st>>>(sc, width, height, rand_states, px, spp, max_depth, counts);
+}
 
 // The wavefront form on the library's own workspace (render_wf.cu).
 int clr_render_kept_wavefront(const clr_scene* scene, uint32_t width, uint32_t height, uint32_t* rand_states,
@@ -196,15 +217,8 @@ extern "C" int clr_render(const clr_scene* scene, uint32_t width, uint32_t heigh
     if (flags & CLR_RENDER_WAVEFRONT)
         return clr_render_kept_wavefront(scene, width, height, rand_states, pixels, spp, max_depth, flags, stream);
     if (max_depth == 0) max_depth = 100;
-    const DScene sc = make_dscene(scene);
-    cudaStream_t st = static_cast<cudaStream_t>(stream);
-    const dim3 grid(div_up(width, 16), div_up(height, 8));
-    if (flags & CLR_RENDER_ORDERED)
-        k_render<true><<<grid, 128, 0, st>>>(sc, width, height, rand_states, reinterpret_cast<float4*>(pixels), spp,
-                                             max_depth);
-    else
-        k_render<false><<<grid, 128, 0, st>>>(sc, width, height, rand_states, reinterpret_cast<float4*>(pixels), spp,
-                                              max_depth);
+    launch_render<false>(make_dscene(scene), width, height, rand_states, pixels, spp, max_depth, flags, nullptr,
+                         static_cast<cudaStream_t>(stream));
     CLR_LAUNCH_CHECK("k_render");
     return CLR_OK;
 }
@@ -219,15 +233,8 @@ extern "C" int clr_render_counted(const clr_scene* scene, uint32_t width, uint32
         return clr_set_error(CLR_EINVAL, "clr_render_counted: counts are taken by the megakernel form only");
     if (width == 0 || height == 0 || spp == 0) return CLR_OK;
     if (max_depth == 0) max_depth = 100;
-    const DScene sc = make_dscene(scene);
-    cudaStream_t st = static_cast<cudaStream_t>(stream);
-    const dim3 grid(div_up(width, 16), div_up(height, 8));
-    if (flags & CLR_RENDER_ORDERED)
-        k_render<true, true><<<grid, 128, 0, st>>>(sc, width, height, rand_states, reinterpret_cast<float4*>(pixels),
-                                                   spp, max_depth, counts);
-    else
-        k_render<false, true><<<grid, 128, 0, st>>>(sc, width, height, rand_states, reinterpret_cast<float4*>(pixels),
-                                                    spp, max_depth, counts);
+    launch_render<true>(make_dscene(scene), width, height, rand_states, pixels, spp, max_depth, flags, counts,
+                        static_cast<cudaStream_t>(stream));
     CLR_LAUNCH_CHECK("k_render");
     return CLR_OK;
 }

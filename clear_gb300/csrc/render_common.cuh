@@ -27,6 +27,7 @@ struct DScene {
     const float4* tris;
     const float* root_box;
     uint32_t num_tris;
+    bool alpha;  // CLR_SCENE_ALPHA: cutout test on closest hits
 };
 
 struct Face {
@@ -63,6 +64,39 @@ struct Hit {
     float t, b1, b2;
 };
 
+// evaluateAlphaTexture (texture.cl:124-148): the alpha byte of an RGBA8
+// image, a Gray8 image's value, a procedural float texture; 1 otherwise.
+// Only "reads 0" matters, and k / 255 is 0 only for k = 0.
+static __device__ __noinline__ bool alpha_is_zero(const uint8_t* t, float2 uv) {
+    uint32_t x, y;
+    const uint8_t* d;
+    switch (t[0]) {
+        case kTexRGBA8:
+            image_xy(t, uv, x, y, d);
+            return d[4u * (y * ldb<uint32_t>(t + 4) + x) + 3u] == 0;
+        case kTexGray8:
+            image_xy(t, uv, x, y, d);
+            return d[y * ldb<uint32_t>(t + 4) + x] == 0;
+        case kTexFloatProc:
+            return eval_float_texture(t, uv) == 0.0f;
+        default:
+            return false;
+    }
+}
+
+// rayTriangleIntersection's cutout test (bvh_traversal.cl:94-105) for an
+// accepted hit on face `id` at barycentrics (b1, b2): the face has uvs
+// (uv0 set) and an alpha texture that reads 0 at the interpolated uv.
+static __device__ __noinline__ bool alpha_cutout(const DScene& sc, uint32_t id, float b1, float b2) {
+    const uint32_t* w = reinterpret_cast<const uint32_t*>(sc.faces + 56u * id);
+    const uint32_t tex = __ldg(w + 12), t0 = __ldg(w + 9);
+    if (tex == kNone32 || t0 == kNone32) return false;
+    const float b0 = 1.0f - b1 - b2;
+    const float2 uv0 = __ldg(sc.uvs + t0), uv1 = __ldg(sc.uvs + __ldg(w + 10)), uv2 = __ldg(sc.uvs + __ldg(w + 11));
+    const float2 uv = make_float2(b0 * uv0.x + b1 * uv1.x + b2 * uv2.x, b0 * uv0.y + b1 * uv1.y + b2 * uv2.y);
+    return alpha_is_zero(sc.textures + tex, uv);
+}
+
 // rayIntersection for the renderer: returns the closest hit with its
 // barycentrics.  kOrdered visits the nearer child first.
 // Closest hit.  With kCount, boxes[0] counts the internal boxes and boxes[1]
@@ -78,24 +112,31 @@ struct Hit {
 #define CLR_TRAVERSAL_ATTR
 #endif
 
-template <bool kOrdered, bool kCount = false>
-static __device__ CLR_TRAVERSAL_ATTR bool intersect_impl(const DScene& sc, f3 org, f3 dir, Hit& h, uint2* stack, uint32_t* boxes) {
+// The record returned is the last hit recorded, at its own distance; with
+// kAlpha (scenes with CLR_SCENE_ALPHA) a cutout moves the bound without being
+// recorded (see alpha_cutout).  Whether the bound ended finite is the
+// reference's "hit" for shadow rays.
+template <bool kOrdered, bool kCount, bool kAlpha>
+static __device__ CLR_TRAVERSAL_ATTR uint32_t intersect_search(const DScene& sc, f3 org, f3 dir, Hit& h, uint2* stack,
+                                                               uint32_t* boxes) {
     Ray ray{org.x, org.y, org.z, INFINITY, dir.x, dir.y, dir.z};
     const float ix = 1.0f / dir.x, iy = 1.0f / dir.y, iz = 1.0f / dir.z;
     float t = INFINITY;
     uint32_t best = kNone32;
-    float bb1 = 0.f, bb2 = 0.f;
+    float bb1 = 0.f, bb2 = 0.f, bt = INFINITY;
     float entry;
     const float* rb = sc.root_box;
-    if (!box_test_fast(rb[0], rb[1], rb[2], rb[4], rb[5], rb[6], ray, ix, iy, iz, entry)) return false;
+    if (!box_test_fast(rb[0], rb[1], rb[2], rb[4], rb[5], rb[6], ray, ix, iy, iz, entry)) return 0u;
     auto test_leaf = [&](uint32_t leaf) {
         const float4 a = __ldg(sc.tris + 3u * leaf), b = __ldg(sc.tris + 3u * leaf + 1u),
                      c = __ldg(sc.tris + 3u * leaf + 2u);
         float b1, b2;
         if (tri_test(a, b, c, ray, t, &b1, &b2)) {
+            if (kAlpha && alpha_cutout(sc, __float_as_uint(a.w), b1, b2)) return;
             best = __float_as_uint(a.w);
             bb1 = b1;
             bb2 = b2;
+            bt = t;
         }
     };
     if (sc.num_tris == 1) {  // the root box is the leaf's box
@@ -133,12 +174,31 @@ static __device__ CLR_TRAVERSAL_ATTR bool intersect_impl(const DScene& sc, f3 or
             }
         }
     }
-    if (best == kNone32) return false;
     h.id = best;
-    h.t = t;
+    const uint32_t bound = t < INFINITY ? 2u : 0u;
+    if (best == kNone32) return bound;
+    h.t = bt;
     h.b1 = bb1;
     h.b2 = bb2;
-    return true;
+    return bound | 1u;
+}
+
+// The search with the cutout test compiled in only for scenes that need it:
+// bit 0 set when a hit is recorded, bit 1 when the bound ended finite.
+// kAlpha 0 or 1 fixes the choice at compile time (a kernel instantiated per
+// scene kind); -1 reads the scene's flag at the call.
+template <bool kOrdered, bool kCount = false, int kAlpha = -1>
+static __device__ __forceinline__ uint32_t intersect_status(const DScene& sc, f3 org, f3 dir, Hit& h, uint2* stack,
+                                                            uint32_t* boxes) {
+    if (kAlpha >= 0) return intersect_search<kOrdered, kCount, (kAlpha > 0)>(sc, org, dir, h, stack, boxes);
+    return sc.alpha ? intersect_search<kOrdered, kCount, true>(sc, org, dir, h, stack, boxes)
+                    : intersect_search<kOrdered, kCount, false>(sc, org, dir, h, stack, boxes);
+}
+
+template <bool kOrdered, bool kCount = false, int kAlpha = -1>
+static __device__ __forceinline__ bool intersect_impl(const DScene& sc, f3 org, f3 dir, Hit& h, uint2* stack,
+                                                      uint32_t* boxes) {
+    return (intersect_status<kOrdered, kCount, kAlpha>(sc, org, dir, h, stack, boxes) & 1u) != 0;
 }
 
 template <bool kOrdered>
@@ -437,14 +497,15 @@ __device__ __forceinline__ uint32_t shadow_light_word(const LightPt& lp) {
     return lp.atInfinity ? (kEnvLightBit | lp.faceID) : lp.faceID;
 }
 
-template <bool kOrdered, bool kCount = false>
+template <bool kOrdered, bool kCount = false, int kAlpha = -1>
 __device__ __forceinline__ bool shadow_visible(const DScene& sc, f3 org, f3 dir, uint32_t light, uint2* stack,
                                                uint32_t* boxes = nullptr) {
     if (light == kNone32) return !occluded_any<kOrdered, kCount>(sc, org, dir, stack, boxes);
     Hit h;
-    const bool hit = intersect_impl<kOrdered, kCount>(sc, org, dir, h, stack, boxes);
-    if (light & kEnvLightBit) return !hit || h.id == (light & ~kEnvLightBit);
-    return hit && h.id == light;
+    const uint32_t st = intersect_status<kOrdered, kCount, kAlpha>(sc, org, dir, h, stack, boxes);
+    const bool rec = (st & 1u) != 0, bounded = (st & 2u) != 0;
+    if (light & kEnvLightBit) return !bounded || (rec && h.id == (light & ~kEnvLightBit));
+    return rec && h.id == light;
 }
 
 // getAreaPDF, light.cl:247-292
@@ -574,6 +635,7 @@ static inline DScene make_dscene(const clr_scene* scene) {
     sc.tris = static_cast<const float4*>(scene->bvh->tris);
     sc.root_box = scene->bvh->root_box;
     sc.num_tris = scene->bvh->num_tris;
+    sc.alpha = (scene->flags & CLR_SCENE_ALPHA) != 0;
     return sc;
 }
 

@@ -9,7 +9,7 @@ import numpy as np
 import torch
 
 from . import _lib, lbvh
-from .scene import Scene, zenith_weights
+from .scene import FACE_DTYPE, NONE32, Scene, zenith_weights
 from .scenes import pixel_seeds
 
 RENDER_ORDERED = 0x1
@@ -22,7 +22,17 @@ TAPE_VISIBLE = 0x100
 class ClrScene(C.Structure):
     _fields_ = [("vertices", C.c_void_p), ("normals", C.c_void_p), ("tangents", C.c_void_p), ("uvs", C.c_void_p),
                 ("faces", C.c_void_p), ("lights", C.c_void_p), ("materials", C.c_void_p),
-                ("textures", C.c_void_p), ("others", C.c_void_p), ("bvh", C.POINTER(_lib.ClrBvh))]
+                ("textures", C.c_void_p), ("others", C.c_void_p), ("bvh", C.POINTER(_lib.ClrBvh)),
+                ("flags", C.c_uint32)]
+
+SCENE_ALPHA = 0x1  # CLR_SCENE_ALPHA
+
+
+def scene_flags(blobs: dict) -> int:
+    """CLR_SCENE_* of a scene's blobs: CLR_SCENE_ALPHA when some face has an
+    alpha texture."""
+    faces = np.asarray(blobs["faces"]).view(FACE_DTYPE)
+    return SCENE_ALPHA if bool((faces["alphaTexPtr"] != NONE32).any()) else 0
 
 
 def _dev(a: np.ndarray, device) -> torch.Tensor:
@@ -48,7 +58,7 @@ class DeviceScene:
         self.bvh = self.builder.perform(self.soa, self.tri, self.num_faces, bits_per_dim)
         p = lambda k: self.t[k].data_ptr()  # noqa: E731
         self.c = ClrScene(p("vertices"), p("normals"), p("tangents"), p("uvs"), p("faces"), p("lights"),
-                          p("materials"), p("textures"), p("others"), C.pointer(self.bvh.c))
+                          p("materials"), p("textures"), p("others"), C.pointer(self.bvh.c), scene_flags(b))
 
     def new_frame(self):
         """Fresh per-pixel RNG states (seed = pixel index + 1) and a zeroed

@@ -237,7 +237,18 @@ typedef struct clr_scene {
     const uint8_t* textures;
     const uint8_t* others;
     const clr_bvh* bvh;
+    uint32_t flags;  /* CLR_SCENE_*; 0 when none apply */
 } clr_scene;
+
+/* Some face has an alpha texture (Face::alphaTexPtr).  The closest-hit
+ * searches then apply the reference's cutout test (bvh_traversal.cl:102-105):
+ * a face with uvs whose alpha texture reads 0 at the hit is not recorded,
+ * though the search bound has already moved to its distance, so it still
+ * hides what lies behind it, and a shadow ray counts as blocked by it.  When
+ * a ray's only hits are such cutouts the reference reads an intersection
+ * record it never wrote; here that ray is a miss.  Without the flag alpha
+ * textures are not read. */
+#define CLR_SCENE_ALPHA 0x1u
 
 #define CLR_RENDER_ORDERED 0x1u  /* trace with nearer-child-first traversal */
 /* clr_render: run the wavefront form (identical results, several times
