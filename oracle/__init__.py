@@ -29,6 +29,7 @@ _lib = None
 _ref_lbvh = None
 _ref_mid = None
 _ref_scene = None
+_ref_kbump = None
 
 
 def _p(a):
@@ -151,7 +152,7 @@ def ref_available() -> bool:
 
 
 def _ref(name):
-    global _ref_lbvh, _ref_mid, _ref_scene
+    global _ref_lbvh, _ref_mid, _ref_scene, _ref_kbump
     libs = {p.name: p for p in build_ref()}
     if not libs:
         raise RuntimeError("reference checkout not available; oracle/_ref not built")
@@ -176,6 +177,10 @@ def _ref(name):
         if _ref_lbvh is None:
             _ref_lbvh = C.CDLL(str(libs["libref_lbvh.so"]))
         return _ref_lbvh
+    if name == "lbvh_kbump":
+        if _ref_kbump is None:
+            _ref_kbump = C.CDLL(str(libs["libref_lbvh_kbump.so"]))
+        return _ref_kbump
     if _ref_mid is None:
         _ref_mid = C.CDLL(str(libs["libref_mid.so"]))
         _ref_mid.ref_midbvh_build.restype = C.c_int64
@@ -246,11 +251,14 @@ def ref_bvh_visualizer(scene_blobs: dict, inodes, lnodes, pixels, width, height)
                                     C.c_uint32(width), C.c_uint32(height))
 
 
-def ref_render(scene_blobs: dict, inodes, lnodes, rand_states, pixels, width, height, y0, y1, spp):
+def ref_render(scene_blobs: dict, inodes, lnodes, rand_states, pixels, width, height, y0, y1, spp,
+               bump_as_kernel: bool = False):
     """sim::pathtracing over rows [y0, y1); rand_states (u32[4*W*H]) and
-    pixels (f32[W*H*4]) are updated in place."""
+    pixels (f32[W*H*4]) are updated in place.  bump_as_kernel: the build of
+    the renderer whose bump frame follows the OpenCL kernel
+    (libref_lbvh_kbump, see build_oracle.build_ref_kernel_bump)."""
     b = scene_blobs
-    _ref("lbvh").ref_render(_p(b["vertices"]), _p(b["normals"]), _p(b["tangents"]), _p(b["uvs"]),
+    _ref("lbvh_kbump" if bump_as_kernel else "lbvh").ref_render(_p(b["vertices"]), _p(b["normals"]), _p(b["tangents"]), _p(b["uvs"]),
                             _p(b["faces"]), _p(b["lights"]), _p(b["materials"]), _p(b["textures"]),
                             _p(b["others"]), _p(inodes), _p(lnodes), _p(rand_states), _p(pixels),
                             C.c_uint32(width), C.c_uint32(height), C.c_uint32(y0), C.c_uint32(y1),

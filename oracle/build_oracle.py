@@ -7,6 +7,9 @@
   reference's own CPU code (``OpenCL_PathTracer/Equivalent/sim_*.hpp`` and
   ``OpenCL_PathTracer/BVH.hpp``) compiled in place from a reference checkout
   with the stand-in headers of ``oracle/ref_stubs``.
+* ``oracle/_ref/libref_lbvh_kbump.so`` -- ``libref_lbvh.so`` with the one
+  line where the CPU renderer departs from its OpenCL kernel (the bump frame's
+  axis normalisation, ``OpenCL/reflection.cl:210``) as the kernel has it.
 * ``oracle/_ref/libref_lbvh_cl.so`` and ``libref_post_cl.so`` -- the
   reference's LBVH construction kernels (``OpenCL/lbvh_construction.cl``,
   ``CommonSources/OpenCL/generic_kernels.cl``) and post-processing kernels
@@ -89,6 +92,10 @@ def build_ref() -> list[Path]:
         _run(["g++", "-std=c++17", "-w", *CFLAGS, "-ftrivial-auto-var-init=zero", f"-I{stubs}", f"-I{pt}",
               f"-I{la}", *map(str, srcs), "-o", str(out), "-Wl,--no-undefined"])
     built.append(out)
+    out = outdir / "libref_lbvh_kbump.so"
+    if _stale(out, deps):
+        build_ref_kernel_bump(out, src, stubs, eq)
+    built.append(out)
     cl_dir = REF_DIR / "OpenCL_PathTracer" / "OpenCL"
     for lib, harness, kernels in (
             ("libref_lbvh_cl.so", "ref_lbvh_cl.cpp",
@@ -99,6 +106,28 @@ def build_ref() -> list[Path]:
             build_ref_kernels(out, HERE / harness, kernels, stubs)
         built.append(out)
     return built
+
+
+def build_ref_kernel_bump(out: Path, harness: Path, stubs: Path, eq: Path) -> None:
+    """The LBVH harness over the reference's CPU renderer with the one line
+    where that renderer departs from its OpenCL kernel put back as the kernel
+    has it: the bump frame's rotation axis is normalised before use
+    (OpenCL/reflection.cl:210; Equivalent/sim_reflection.hpp omits it, which
+    turns the frame by the wrong matrix).  sim_reflection.hpp is read from the
+    checkout, changed in memory and piped to the compiler ahead of the
+    harness, whose own #include of it is then a no-op (include guard);
+    nothing is written."""
+    text = (eq / "sim_reflection.hpp").read_text()
+    anchor = "float sinTH = fminf(length(ax), 1.0f);\n            if (sinTH > 0.0001f) {\n"
+    if text.count(anchor) != 1:
+        raise RuntimeError("oracle build: the bump block of sim_reflection.hpp is not where expected")
+    text = text.replace(anchor, anchor + "                ax = normalize(ax);\n")
+    src = "#include <cstdint>\n#include <cstring>\n#include <vector>\n" + text + '\n#include "ref_harness.cpp"\n'
+    res = subprocess.run(["g++", "-std=c++17", "-w", *CFLAGS, "-ftrivial-auto-var-init=pattern", "-D__USE_LBVH",
+                          f"-I{stubs}", f"-I{eq}", f"-I{REF_DIR / 'OpenCL_PathTracer'}", f"-I{harness.parent}",
+                          "-x", "c++", "-", "-o", str(out)], input=src, capture_output=True, text=True)
+    if res.returncode != 0:
+        raise RuntimeError(f"oracle build failed: kernel-bump renderer\n{res.stderr}")
 
 
 def build_ref_kernels(out: Path, harness: Path, kernels: list[Path], stubs: Path) -> None:
