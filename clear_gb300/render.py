@@ -69,9 +69,10 @@ class DeviceScene:
         return rng, pix
 
     def render(self, rng: torch.Tensor, pix: torch.Tensor, spp: int, max_depth: int = 100,
-               ordered: bool = True, wavefront: bool = False, rows: tuple[int, int] | None = None) -> None:
-        """Adds `spp` samples per pixel to `pix`.  wavefront=True runs the
-        extend/shade/shadow kernel split (same results as the megakernel).
+               ordered: bool = True, wavefront: bool = True, rows: tuple[int, int] | None = None) -> None:
+        """Adds `spp` samples per pixel to `pix`.  wavefront=True (the
+        default) runs the extend/shade/shadow kernel split, wavefront=False
+        the megakernel (clr_render); the results are identical.
         rows=(y0, y1) renders those image rows only (wavefront form): `rng`
         and `pix` then hold just those rows."""
         stream = C.c_void_p(torch.cuda.current_stream(self.device).cuda_stream)

@@ -58,7 +58,7 @@ def test_obj_scene_matches_reference_sim(cuda):
     w, h, spp = int(g["width"]), int(g["height"]), int(g["spp"])
     ds = DeviceScene(GO.build_scene(width=w, height=h), cuda)
     rng, pix = ds.new_frame()
-    ds.render(rng, pix, spp, max_depth=100, ordered=False)
+    ds.render(rng, pix, spp, max_depth=100, ordered=False, wavefront=False)
     img = pix[:, :3].cpu().numpy()
     rel_rmse, mean_err, frac_close = metrics(img, g["image"])
     print(f"obj scene: rel RMSE {rel_rmse:.4g}, mean err {mean_err:.4g}, close {frac_close:.4f}")
@@ -81,7 +81,7 @@ def test_render_matches_reference_sim(cuda, variant):
     sc = scenes.cornell_box(w, h, env=env_map() if variant == "env" else None)
     ds = DeviceScene(sc, cuda)
     rng, pix = ds.new_frame()
-    ds.render(rng, pix, spp, max_depth=100, ordered=False)
+    ds.render(rng, pix, spp, max_depth=100, ordered=False, wavefront=False)
     img = pix[:, :3].cpu().numpy()
     rel_rmse, mean_err, frac_close = metrics(img, g[variant])
     print(f"{variant}: rel RMSE {rel_rmse:.4g}, mean err {mean_err:.4g}, close {frac_close:.4f}")
@@ -99,7 +99,7 @@ def test_wavefront_equals_megakernel(cuda, variant):
     w, h, spp = int(g["width"]), int(g["height"]), int(g["spp"])
     ds = DeviceScene(scenes.cornell_box(w, h, env=env_map() if variant == "env" else None), cuda)
     rng_a, pix_a = ds.new_frame()
-    ds.render(rng_a, pix_a, spp, max_depth=100, ordered=False)
+    ds.render(rng_a, pix_a, spp, max_depth=100, ordered=False, wavefront=False)
     rng_b, pix_b = ds.new_frame()
     ds.render(rng_b, pix_b, spp, max_depth=100, ordered=False, wavefront=True)
     torch.cuda.synchronize()
@@ -147,7 +147,7 @@ def test_counted_render_same_image_and_consistent_counts(cuda, variant):
     spp, depth = 4, 5
     ds = DeviceScene(scenes.cornell_box(w, h, env=env_map() if variant == "env" else None), cuda)
     rng_a, pix_a = ds.new_frame()
-    ds.render(rng_a, pix_a, spp, max_depth=depth, ordered=True)
+    ds.render(rng_a, pix_a, spp, max_depth=depth, ordered=True, wavefront=False)
     rng_b, pix_b = ds.new_frame()
     c = ds.render_counted(rng_b, pix_b, spp, max_depth=depth, ordered=True)
     torch.cuda.synchronize()
@@ -180,7 +180,7 @@ def test_render_flag_wavefront_on_kept_workspace(cuda):
     for size in (48, 80):
         ds = DeviceScene(scenes.cornell_box(size, size, env=env_map()), cuda)
         rng_a, pix_a = ds.new_frame()
-        ds.render(rng_a, pix_a, 8, max_depth=5, ordered=True)
+        ds.render(rng_a, pix_a, 8, max_depth=5, ordered=True, wavefront=False)
         torch.cuda.synchronize()
         frames = [ds.new_frame() for _ in range(2)]
         streams = [torch.cuda.Stream(cuda) for _ in range(2)]
