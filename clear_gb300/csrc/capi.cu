@@ -16,6 +16,19 @@ int clr_set_error(int code, const char* fmt, ...) {
 
 extern "C" const char* clr_last_error_string(void) { return t_last_error; }
 
+int clr_sm_count() {
+    constexpr int kMaxDevices = 64;
+    static int sms[kMaxDevices] = {};
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) dev = 0;
+    if (sms[dev] <= 0) {
+        int v = 0;
+        if (cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || v <= 0) v = 1;
+        sms[dev] = v;
+    }
+    return sms[dev];
+}
+
 cudaError_t clr_status_lbvh(unsigned int* v, int clear);
 cudaError_t clr_status_traverse(unsigned int* v, int clear);
 cudaError_t clr_status_render(unsigned int* v, int clear);

@@ -83,3 +83,7 @@ constexpr uint32_t kLeafBit = 0x80000000u;
 }  // namespace clr
 
 static inline unsigned int div_up(unsigned int a, unsigned int b) { return (a + b - 1) / b; }
+
+// Streaming multiprocessors of the current device (capi.cu), queried once per
+// device; grids that fill the GPU once are sized from it.
+int clr_sm_count();

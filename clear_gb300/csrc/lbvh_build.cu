@@ -231,7 +231,8 @@ __global__ void __launch_bounds__(kSortThreads, 4) k_onesweep(const KeyT* __rest
                                                            uint32_t n, uint32_t shift,
                                                            const unsigned int* __restrict__ hist,
                                                            unsigned int* __restrict__ status,
-                                                           unsigned int* __restrict__ tile_ctr) {
+                                                           unsigned int* __restrict__ tile_ctr,
+                                                           unsigned int spin_limit) {
     constexpr int kItems = SortCfg<KeyT>::kItems;
     constexpr unsigned int kR = 1u << kBits, kDigitMask = kR - 1u;
     static_assert(kBits >= 1 && kBits <= 8, "digits of 1..8 bits");
@@ -327,7 +328,7 @@ __global__ void __launch_bounds__(kSortThreads, 4) k_onesweep(const KeyT* __rest
             const unsigned int s = ld_relaxed_gpu(status + (size_t)j * kRadix + d);
             const unsigned int flag = s & kFlagMask;
             if (flag == 0u) {
-                if (++spins > kSpinLimit) {
+                if (++spins > spin_limit) {
                     clr_raise(CLR_DEVERR_SORT_TIMEOUT);
                     break;
                 }
@@ -1044,6 +1045,25 @@ static size_t align_up(size_t v, size_t a) { return (v + a - 1) / a * a; }
 
 // Lays the scratch pool out for `cap` triangles.  Returns its size; assigns
 // the handle's pointers when `base` is non-NULL.
+// Digit histogram (added to a zeroed `hist`, one 256-thread block each) of the
+// low 8 bits of n keys, the stall test's input, and the
+// tile counter set so that the next block to start takes tile 1.
+__global__ void k_debug_hist(const uint32_t* __restrict__ keys, uint32_t n, unsigned int* __restrict__ hist,
+                             unsigned int* __restrict__ tile_ctr) {
+    __shared__ unsigned int h[kRadix];
+    h[threadIdx.x] = 0;
+    __syncthreads();
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+        atomicAdd(&h[keys[i] & 0xFFu], 1u);
+    __syncthreads();
+    if (blockIdx.x == 0 && threadIdx.x == 0) *tile_ctr = 1u;
+    if (h[threadIdx.x]) atomicAdd(&hist[threadIdx.x], h[threadIdx.x]);
+}
+
+// Polls of a look-back before a sort pass gives up (CLR_DEVERR_SORT_TIMEOUT);
+// lowered only by clr_debug_set_wait_limits.
+static unsigned int g_sort_spin_limit = kSpinLimit;
+
 static size_t pool_layout(clr_lbvh* h, uint32_t cap, char* base, bool stage = true) {
     const size_t tiles = div_up(cap ? cap : 1, kMinSortTile) + 1;
     size_t off = 0;
@@ -1150,7 +1170,7 @@ static int run_build(clr_lbvh* h, const float* vx, const float* vy, const float*
                      uint32_t n, uint32_t bits, clr_bvh* out, cudaStream_t st) {
     const int kbits = 3 * (int)bits;
     const int npasses = (kbits + 7) / 8;
-    const int grid_stream = kSmCount * 8;
+    const int grid_stream = clr_sm_count() * 8;
     PassTimer timer(h, st);
     CLR_CUDA_TRY(cudaMemsetAsync(h->zero_region, 0, h->zero_bytes, st));
     k_scene_box<<<grid_stream, 256, 0, st>>>(vx, vy, vz, tri, n, h->boxw);
@@ -1168,11 +1188,11 @@ static int run_build(clr_lbvh* h, const float* vx, const float* vy, const float*
         if (p == 0)
             k_onesweep<KeyT, true><<<tiles, kSortThreads, 0, st>>>(
                 keys[src], nullptr, keys[dst], h->vals[dst], n, 8 * p, h->hist + p * kRadix,
-                h->status + p * h->status_stride, h->tile_ctr + p);
+                h->status + p * h->status_stride, h->tile_ctr + p, g_sort_spin_limit);
         else
             k_onesweep<KeyT, false><<<tiles, kSortThreads, 0, st>>>(
                 keys[src], h->vals[src], keys[dst], h->vals[dst], n, 8 * p, h->hist + p * kRadix,
-                h->status + p * h->status_stride, h->tile_ctr + p);
+                h->status + p * h->status_stride, h->tile_ctr + p, g_sort_spin_limit);
         CLR_LAUNCH_CHECK("k_onesweep");
         timer.done("sort_pass");
     }
@@ -1191,7 +1211,7 @@ static int run_build(clr_lbvh* h, const float* vx, const float* vy, const float*
             keys[fin], h->vals[fin], n, kbits, vx, vy, vz, tri, h->stage, reinterpret_cast<float*>(out->nodes), tris,
             h->counters, h->karras_idx, out->root_box, worklist, wl_count);
         CLR_LAUNCH_CHECK("k_build_tree");
-        k_build_tree_top<KeyT><<<kSmCount * 4, 256, 0, st>>>(keys[fin], n, kbits, reinterpret_cast<float*>(out->nodes),
+        k_build_tree_top<KeyT><<<clr_sm_count() * 4, 256, 0, st>>>(keys[fin], n, kbits, reinterpret_cast<float*>(out->nodes),
                                                              h->counters, h->karras_idx, out->root_box, worklist,
                                                              wl_count);
         CLR_LAUNCH_CHECK("k_build_tree_top");
@@ -1350,11 +1370,11 @@ static void launch_sort_pass(uint64_t* kin, uint32_t* vin, uint64_t* kout, uint3
     if (p == 0)
         k_onesweep<uint64_t, true, kBits><<<tiles, kSortThreads, 0, st>>>(
             kin, nullptr, kout, vout, n, kBits * p, h->hist + p * kRadix, h->status + p * h->status_stride,
-            h->tile_ctr + p);
+            h->tile_ctr + p, g_sort_spin_limit);
     else
         k_onesweep<uint64_t, false, kBits><<<tiles, kSortThreads, 0, st>>>(
             kin, vin, kout, vout, n, kBits * p, h->hist + p * kRadix, h->status + p * h->status_stride,
-            h->tile_ctr + p);
+            h->tile_ctr + p, g_sort_spin_limit);
 }
 
 extern "C" int clr_lbvh_build_batched(clr_lbvh* h, const float* vx, const float* vy, const float* vz,
@@ -1398,7 +1418,7 @@ extern "C" int clr_lbvh_build_batched(clr_lbvh* h, const float* vx, const float*
     CLR_LAUNCH_CHECK("k_seg_box");
     timer.done("scene_box");
     uint64_t* keys[2] = {static_cast<uint64_t*>(h->keys[0]), static_cast<uint64_t*>(h->keys[1])};
-    const int grid_stream = kSmCount * 8;
+    const int grid_stream = clr_sm_count() * 8;
     if (radix_bits == 8)
         k_morton_seg<8><<<grid_stream, 256, 0, st>>>(vx, vy, vz, tri, h->seg_off, num_scenes, n, bits_per_dim,
                                                      h->seg_box, keys[0], h->hist, npasses, h->counters, h->stage);
@@ -1504,23 +1524,53 @@ constexpr int kNoAllocMaxDevices = 64;
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
 
-// Device address of g_noalloc_scratch per device, resolved once per device by
-// the first call made while that device is current.
-static void* g_noalloc_addr[kNoAllocMaxDevices] = {};
+// Device address of g_noalloc_scratch per device, resolved by the first call
+// made while that device is current, together with the CUDA context it was
+// resolved in.  The address is only valid in that context: after a device
+// reset (or with another context made current on the device) the next call
+// resolves it again, so the first call after such a change is again a set-up
+// call and belongs outside any stream capture.
+struct NoAllocAddr {
+    void* ctx = nullptr;
+    void* addr = nullptr;
+};
+static NoAllocAddr g_noalloc_addr[kNoAllocMaxDevices];
 static std::mutex g_noalloc_mutex;
+
+// The current context of the calling thread (cuCtxGetCurrent, reached through
+// the runtime so that the library links no driver stub); null if unavailable.
+static void* current_context() {
+    using CtxGet = int (*)(void**);
+    static CtxGet fn = [] {
+        void* f = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+            q != cudaDriverEntryPointSuccess)
+            f = nullptr;
+        return reinterpret_cast<CtxGet>(f);
+    }();
+    void* ctx = nullptr;
+    if (!fn || fn(&ctx) != 0) return nullptr;
+    return ctx;
+}
 
 static int noalloc_scratch(void** out) {
     int dev = -1;
     CLR_CUDA_TRY(cudaGetDevice(&dev));
     if (dev < 0 || dev >= kNoAllocMaxDevices)
         return clr_set_error(CLR_EINVAL, "clr_lbvh_build_noalloc: device %d out of range", dev);
+    // cudaGetDevice does not create the context; the symbol lookup below
+    // does, so a null context only ever means "not resolved yet"
+    void* ctx = current_context();
     std::lock_guard<std::mutex> lock(g_noalloc_mutex);
-    if (!g_noalloc_addr[dev]) {
+    NoAllocAddr& a = g_noalloc_addr[dev];
+    if (!a.addr || !ctx || a.ctx != ctx) {
         void* p = nullptr;
         CLR_CUDA_TRY(cudaGetSymbolAddress(&p, g_noalloc_scratch));
-        g_noalloc_addr[dev] = p;
+        a.addr = p;
+        a.ctx = current_context();
     }
-    *out = g_noalloc_addr[dev];
+    *out = a.addr;
     return CLR_OK;
 }
 
@@ -1542,12 +1592,56 @@ extern "C" int clr_lbvh_build_noalloc(const float* vx, const float* vy, const fl
     void* base = nullptr;
     int rc = noalloc_scratch(&base);
     if (rc != CLR_OK) return rc;
+    // laid out for this call's triangle count, so that the part cleared per
+    // build (digit histograms and look-back words) covers only the tiles this
+    // build uses; the layout grows with the count and, at the maximum count,
+    // still fits the array
     clr_lbvh h{};
     if (pool_layout(&h, kNoAllocMaxTris, nullptr, false) > kNoAllocScratchBytes)
         return clr_set_error(CLR_ECAPACITY, "clr_lbvh_build_noalloc: scratch layout exceeds the static array");
-    pool_layout(&h, kNoAllocMaxTris, static_cast<char*>(base), false);
-    h.capacity = kNoAllocMaxTris;
+    pool_layout(&h, num_tris, static_cast<char*>(base), false);
+    h.capacity = num_tris;
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     if (bits_per_dim <= 10) return run_build<uint32_t>(&h, vx, vy, vz, tri, num_tris, bits_per_dim, out, st);
     return run_build<uint64_t>(&h, vx, vy, vz, tri, num_tris, bits_per_dim, out, st);
+}
+
+// ============================================================ bounded waits
+//
+// The sort's look-back is the one place where a block of the build waits on
+// another block.  Its wait is bounded: after g_sort_spin_limit polls the block
+// raises CLR_DEVERR_SORT_TIMEOUT, finishes its tile with the prefix it has
+// (its writes stay inside the output, only their order is wrong) and returns.
+
+int clr_batch_set_iteration_cap(uint32_t cap);  // render_batch.cu
+
+extern "C" int clr_debug_set_wait_limits(uint32_t sort_spin_limit, uint32_t batch_iteration_cap) {
+    g_sort_spin_limit = sort_spin_limit ? sort_spin_limit : kSpinLimit;
+    return clr_batch_set_iteration_cap(batch_iteration_cap);
+}
+
+extern "C" int clr_debug_lookback_stall(uint32_t* keys, uint32_t* scratch, uint32_t tile_keys, void* stream) {
+    // One sort pass over two tiles of 32-bit keys in which only the second
+    // tile's block runs: the first tile never publishes its digit counts, so
+    // the second tile's look-back finds no flag and must give up.
+    constexpr int kTile = kSortThreads * SortCfg<uint32_t>::kItems;
+    if (!keys || !scratch) return clr_set_error(CLR_EINVAL, "clr_debug_lookback_stall: NULL argument");
+    if (tile_keys != (uint32_t)kTile)
+        return clr_set_error(CLR_EINVAL, "clr_debug_lookback_stall: tile_keys must be %d", kTile);
+    const uint32_t n = 2u * kTile;
+    // scratch: keys out [n], values out [n], histogram [256], look-back words
+    // [2][256] (zero: nothing published), tile counter [1] = 1
+    uint32_t* kout = scratch;
+    uint32_t* vout = kout + n;
+    unsigned int* hist = vout + n;
+    unsigned int* status = hist + kRadix;
+    unsigned int* tile_ctr = status + 2 * kRadix;
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    CLR_CUDA_TRY(cudaMemsetAsync(hist, 0, 4ull * 3 * kRadix, st));  // histogram and look-back words
+    k_debug_hist<<<div_up(n, 256), 256, 0, st>>>(keys, n, hist, tile_ctr);
+    CLR_LAUNCH_CHECK("k_debug_hist");
+    k_onesweep<uint32_t, true><<<1, kSortThreads, 0, st>>>(keys, nullptr, kout, vout, n, 0, hist, status, tile_ctr,
+                                                          g_sort_spin_limit);
+    CLR_LAUNCH_CHECK("k_onesweep");
+    return CLR_OK;
 }

@@ -8,7 +8,6 @@
 
 namespace clr {
 
-constexpr int kSmCount = 152;        // GB300: 2 dies x 76 SMs
 constexpr int kRadix = 256;          // 8-bit digits
 constexpr int kMaxPasses = 8;        // 63-bit keys (21 bits per axis)
 constexpr int kSortThreads = 256;

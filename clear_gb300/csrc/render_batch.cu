@@ -344,6 +344,12 @@ __global__ void k_bt_continue(BtState S, cudaGraphConditionalHandle h, unsigned 
     cudaGraphSetConditional(h, more ? 1u : 0u);
 }
 
+// After a frame loop run without the graph: paths still in flight when the
+// iteration bound ran out are reported, as the graph's loop does.
+__global__ void k_bt_check_done(BtState S, int next) {
+    if (S.count[next] > 0) clr_raise(CLR_DEVERR_QUEUE);
+}
+
 static size_t bt_layout(uint32_t slots, char* base, BtState* S) {
     size_t off = 0;
     auto take = [&](size_t bytes) {
@@ -393,6 +399,7 @@ struct clr_batch {
     uint32_t* g_rs = nullptr;
     float* g_px = nullptr;
     uint32_t g_spp = 0, g_depth = 0, g_flags = 0;
+    uint64_t g_cap = 0;  // iteration bound the graph was captured with
     clr_batch_config g_cfg{};
 };
 
@@ -524,6 +531,15 @@ static void bt_iteration(const clr_batch* b, const BtArgs& A, int cur, bool orde
     else k_bt_shadow<false><<<gt, tb, 0, st>>>(A, b->S);
 }
 
+// A lower iteration bound set through clr_debug_set_wait_limits (0 = none), so
+// that a test can make the frame loop's bound run out.
+static uint32_t g_iteration_cap = 0;
+
+int clr_batch_set_iteration_cap(uint32_t cap) {
+    g_iteration_cap = cap;
+    return CLR_OK;
+}
+
 static uint64_t bt_max_iters(const clr_batch* b, uint32_t spp, uint32_t max_depth) {
     // every iteration advances every busy slot by one vertex; a pixel takes at
     // most spp * (max_depth + 1) vertices and one succession step.  While
@@ -532,7 +548,8 @@ static uint64_t bt_max_iters(const clr_batch* b, uint32_t spp, uint32_t max_dept
     // one more pixel-length.
     const uint64_t per_pixel = (uint64_t)spp * (max_depth + 1) + 1;
     const uint64_t per_slot = (b->total_pix + b->slots - 1) / b->slots;
-    return (per_slot + 1) * per_pixel + 4;
+    const uint64_t bound = (per_slot + 1) * per_pixel + 4;
+    return (g_iteration_cap && g_iteration_cap < bound) ? g_iteration_cap : bound;
 }
 
 // Builds the frame graph: init kernel -> WHILE (two iterations + continue
@@ -603,7 +620,7 @@ extern "C" int clr_batch_render(clr_batch* b, uint32_t* rand_states, float* pixe
     const uint64_t cap = bt_max_iters(b, spp, max_depth);
     if (flags & CLR_BATCH_GRAPH) {
         if (cap >= 0xFFFFFFFFull) return clr_set_error(CLR_EINVAL, "clr_batch_render: iteration bound too large");
-        const bool same = b->exec && b->g_rs == rand_states && b->g_px == pixels && b->g_spp == spp &&
+        const bool same = b->exec && b->g_rs == rand_states && b->g_px == pixels && b->g_spp == spp && b->g_cap == cap &&
                           b->g_depth == max_depth && b->g_flags == flags && b->g_cfg.trace_block == b->cfg.trace_block &&
                           b->g_cfg.shade_block == b->cfg.shade_block && b->g_cfg.pool_slots == b->cfg.pool_slots;
         if (!same) {
@@ -613,6 +630,7 @@ extern "C" int clr_batch_render(clr_batch* b, uint32_t* rand_states, float* pixe
             b->g_rs = rand_states;
             b->g_px = pixels;
             b->g_spp = spp;
+            b->g_cap = cap;
             b->g_depth = max_depth;
             b->g_flags = flags;
             b->g_cfg = b->cfg;
@@ -630,8 +648,10 @@ extern "C" int clr_batch_render(clr_batch* b, uint32_t* rand_states, float* pixe
             unsigned int left = 0;
             CLR_CUDA_TRY(cudaMemcpyAsync(&left, b->S.count + (cur ^ 1), sizeof(left), cudaMemcpyDeviceToHost, st));
             CLR_CUDA_TRY(cudaStreamSynchronize(st));
-            if (left == 0) break;
+            if (left == 0) return CLR_OK;
         }
     }
+    k_bt_check_done<<<1, 1, 0, st>>>(b->S, (int)(cap & 1));
+    CLR_LAUNCH_CHECK("k_bt_check_done");
     return CLR_OK;
 }

@@ -17,7 +17,6 @@ CLR_DEFINE_STATUS_READER(traverse)
 
 namespace clr {
 
-constexpr int kSmCountFallback = 152;
 constexpr int kTraceThreads = 128;
 
 // Ray-per-lane loops.  Each thread walks the rays r, r + P, r + 2P, ... (P =
@@ -182,13 +181,7 @@ __global__ void __launch_bounds__(kTraceThreads) k_trace_shadow(const float4* __
 // Grid that fills every SM once for a ray-per-lane kernel.
 template <typename K>
 static unsigned int persistent_grid(K kernel, uint32_t nr) {
-    static int sms = 0;
-    if (!sms) {
-        int dev = 0;
-        cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        if (sms <= 0) sms = kSmCountFallback;
-    }
+    const int sms = clr_sm_count();
     int per_sm = 0;
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, kTraceThreads, 0) != cudaSuccess || per_sm <= 0)
         per_sm = 1;

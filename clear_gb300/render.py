@@ -3,6 +3,7 @@ calls ``clr_render`` (the counterpart of enqueueing the reference's
 ``pathtracing`` kernel per tile and sample, main.cpp:477-494)."""
 from __future__ import annotations
 
+import contextlib
 import ctypes as C
 
 import numpy as np
@@ -57,6 +58,7 @@ class DeviceScene:
         self.tri = torch.from_numpy(tri.astype(np.int32)).to(self.device)
         self.bvh = self.builder.perform(self.soa, self.tri, self.num_faces, bits_per_dim)
         p = lambda k: self.t[k].data_ptr()  # noqa: E731
+        self._ws_last_use = None  # torch.cuda.Event recorded after each workspace use
         self.c = ClrScene(p("vertices"), p("normals"), p("tangents"), p("uvs"), p("faces"), p("lights"),
                           p("materials"), p("textures"), p("others"), C.pointer(self.bvh.c), scene_flags(b))
 
@@ -75,14 +77,14 @@ class DeviceScene:
         the megakernel (clr_render); the results are identical.
         rows=(y0, y1) renders those image rows only (wavefront form): `rng`
         and `pix` then hold just those rows."""
-        stream = C.c_void_p(torch.cuda.current_stream(self.device).cuda_stream)
+        cur = torch.cuda.current_stream(self.device)
+        stream = C.c_void_p(cur.cuda_stream)
         flags = C.c_uint32(RENDER_ORDERED if ordered else 0)
         if rows is not None:
             y0, y1 = rows
             if rng.numel() < 4 * self.width * (y1 - y0) or pix.numel() < 4 * self.width * (y1 - y0):
                 raise ValueError("rng / pix hold fewer than the band's pixels")
-            ws = self.workspace()
-            with torch.cuda.device(self.device):
+            with torch.cuda.device(self.device), self._workspace_turn(cur, self.workspace()) as ws:
                 _lib.call("clr_render_wavefront_rows", C.byref(self.c), C.c_uint32(self.width), C.c_uint32(self.height),
                           C.c_uint32(y0), C.c_uint32(y1 - y0), C.c_void_p(rng.data_ptr()), C.c_void_p(pix.data_ptr()),
                           C.c_uint32(spp), C.c_uint32(max_depth), flags, C.c_void_p(ws.data_ptr()),
@@ -94,8 +96,8 @@ class DeviceScene:
             if not wavefront:
                 _lib.call("clr_render", *args, stream)
                 return
-            ws = self.workspace()
-            _lib.call("clr_render_wavefront", *args, C.c_void_p(ws.data_ptr()), C.c_uint64(ws.numel()), stream)
+            with self._workspace_turn(cur, self.workspace()) as ws:
+                _lib.call("clr_render_wavefront", *args, C.c_void_p(ws.data_ptr()), C.c_uint64(ws.numel()), stream)
 
     def render_counted(self, rng: torch.Tensor, pix: torch.Tensor, spp: int, max_depth: int = 100,
                        ordered: bool = True) -> dict:
@@ -130,9 +132,9 @@ class DeviceScene:
             grad_env.data_ptr() if grad_env is not None else None,
             tape.data_ptr() if tape is not None else None, int(tape.shape[0]) if tape is not None else 0,
             tape_count.data_ptr() if tape_count is not None else None)
-        stream = C.c_void_p(torch.cuda.current_stream(self.device).cuda_stream)
-        ws = self.adjoint_workspace(K)
-        with torch.cuda.device(self.device):
+        cur = torch.cuda.current_stream(self.device)
+        stream = C.c_void_p(cur.cuda_stream)
+        with torch.cuda.device(self.device), self._workspace_turn(cur, self.adjoint_workspace(K)) as ws:
             _lib.call("clr_render_adjoint", C.byref(self.c), C.c_uint32(self.width), C.c_uint32(self.height),
                       C.c_void_p(rng.data_ptr()), C.c_void_p(dloss.data_ptr()), C.c_uint32(spp),
                       C.c_uint32(max_depth), C.c_uint32(RENDER_ORDERED if ordered else 0), C.byref(p),
@@ -186,6 +188,23 @@ class DeviceScene:
                       C.c_uint32(d["tex_offset"]), C.c_uint32(d["height"]), C.c_uint32(d["width"]),
                       C.c_void_p(row_weight.data_ptr()) if row_weight is not None else None,
                       C.c_void_p(torch.cuda.current_stream(self.device).cuda_stream))
+
+    @contextlib.contextmanager
+    def _workspace_turn(self, stream: torch.cuda.Stream, ws: torch.Tensor):
+        """Orders the uses of this scene's workspaces across streams: the
+        call on `stream` starts after the last call that used a workspace of
+        this scene (on whatever stream) has finished on the GPU, and the next
+        call waits for this one.  Renders on two streams thus take turns
+        instead of sharing the wavefront queues at the same time."""
+        if self._ws_last_use is None:
+            self._ws_last_use = torch.cuda.Event()
+        else:
+            stream.wait_event(self._ws_last_use)
+        ws.record_stream(stream)
+        try:
+            yield ws
+        finally:
+            self._ws_last_use.record(stream)
 
     def workspace(self) -> torch.Tensor:
         if getattr(self, "_ws", None) is None:

@@ -144,7 +144,10 @@ CLR_API int clr_lbvh_host_copy_wait(clr_lbvh* h);
  * fail with CLR_ECAPACITY), and every GPU that loads the library keeps that
  * 12 MiB array until the process exits.  The first call on a device resolves
  * the array's device address (cudaGetSymbolAddress) with that device current;
- * make that first call before any stream capture.  All calls share the one
+ * make that first call before any stream capture.  A device reset (or another
+ * context made current on the device) gives the array a new address: the
+ * next call resolves it again, so it too belongs outside any stream capture.
+ * All calls share the one
  * array, so calls that overlap on the GPU (different streams or threads)
  * race: serialise them.  Nothing is allocated or freed. */
 CLR_API int clr_lbvh_build_noalloc(const float* vx, const float* vy, const float* vz, const uint32_t* tri,
@@ -502,6 +505,22 @@ CLR_API int clr_device_status(uint32_t* bits, int clear);
 
 /* Thread-local description of the last failure. */
 CLR_API const char* clr_last_error_string(void);
+
+/* ------------------------------------------------------- bounded waits
+ * The reference has no bounded waits (its host catches cl::Error only,
+ * main.cpp:546-551); these two entry points exist to test the ones here. */
+
+/* Lowers the bounds of the two waits that can run out: the polls of a radix
+ * sort pass's look-back (CLR_DEVERR_SORT_TIMEOUT when exceeded) and the
+ * iterations of the batched frame loop (CLR_DEVERR_QUEUE when paths remain).
+ * 0 restores the built-in bound.  Process-wide; for tests. */
+CLR_API int clr_debug_set_wait_limits(uint32_t sort_spin_limit, uint32_t batch_iteration_cap);
+
+/* One sort pass over 2 * tile_keys 32-bit keys (tile_keys = 4096) in which
+ * only the second tile's block runs, so its look-back waits for a tile that
+ * never publishes, runs out of polls, raises CLR_DEVERR_SORT_TIMEOUT and
+ * returns.  scratch holds 4 * (4 * tile_keys + 769) bytes. */
+CLR_API int clr_debug_lookback_stall(uint32_t* keys, uint32_t* scratch, uint32_t tile_keys, void* stream);
 
 #ifdef __cplusplus
 }

@@ -21,9 +21,10 @@
   with ``LinearAlgebra/*.cpp`` for the matrices of ``Scene.h``) behind
   ``oracle/ref_scene.cpp``.
 
-The ``_ref`` libraries are built only when the checkout exists
-(``CLEAR_REFERENCE_DIR``, default ``/root/reference``); nothing is copied out
-of it.
+The ``_ref`` libraries are built only when the reference checkout exists:
+the directory named by ``CLEAR_REFERENCE_DIR``, else a checkout named
+``reference`` beside this repository (``<repo>/../reference``); nothing is
+copied out of it.
 """
 from __future__ import annotations
 
@@ -33,7 +34,7 @@ import sys
 from pathlib import Path
 
 HERE = Path(__file__).resolve().parent
-REF_DIR = Path(os.environ.get("CLEAR_REFERENCE_DIR", "/root/reference"))
+REF_DIR = Path(os.environ.get("CLEAR_REFERENCE_DIR", HERE.parent.parent / "reference"))
 CFLAGS = ["-O2", "-fPIC", "-shared", "-ffp-contract=off", "-fno-fast-math"]
 
 

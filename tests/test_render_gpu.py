@@ -192,6 +192,28 @@ def test_render_flag_wavefront_on_kept_workspace(cuda):
     assert _lib.device_status() == 0
 
 
+@pytest.mark.gpu
+def test_device_scene_default_render_on_two_streams(cuda):
+    """DeviceScene.render's default (wavefront) form uses one workspace per
+    scene; renders of one scene issued on two streams take turns on it and
+    both equal the same calls on one stream."""
+    ds = DeviceScene(scenes.cornell_box(64, 64, env=env_map()), cuda)
+    rng_a, pix_a = ds.new_frame()
+    ds.render(rng_a, pix_a, 4, max_depth=5)
+    ds.render(rng_a, pix_a, 4, max_depth=5)
+    torch.cuda.synchronize()
+    frames = [ds.new_frame() for _ in range(3)]
+    streams = [torch.cuda.Stream(cuda) for _ in range(3)]
+    for (rng, pix), st in zip(frames, streams):
+        with torch.cuda.stream(st):
+            ds.render(rng, pix, 4, max_depth=5)
+            ds.render(rng, pix, 4, max_depth=5)
+    torch.cuda.synchronize()
+    for rng, pix in frames:
+        assert torch.equal(pix, pix_a) and torch.equal(rng, rng_a)
+    assert _lib.device_status() == 0
+
+
 def test_zoo_scene_encoding_matches_golden():
     import make_golden_zoo as GZ
 

@@ -36,16 +36,33 @@ def _same(a: lbvh.BVH, b: lbvh.BVH):
     assert torch.equal(a.root_box, b.root_box)
 
 
-def test_noalloc_matches_allocating_build_twice(cuda):
+@pytest.mark.parametrize("bits", [10, 21])
+def test_noalloc_matches_allocating_build_twice(cuda, bits):
+    """32-bit keys (10 bits per axis) and 64-bit keys (21 bits per axis, eight
+    sort passes, the most look-back words): first a large input, then a
+    smaller one, so stale scratch from the first call would show up if
+    anything were not cleared."""
     builder = lbvh.LBVHBuilder(1, cuda)
-    # first call: a large input; second call: a smaller one, so stale scratch
-    # from the first call would show up if anything were not cleared
     for n, seed in ((200000, 31), (4097, 32)):
         vx, vy, vz = W.triangle_soup(n, seed=seed)
         verts = [torch.from_numpy(a).to(cuda) for a in (vx, vy, vz)]
-        ref = builder.perform(verts, None, n, 10)
-        got = _noalloc_build(cuda, verts, n, 10)
+        ref = builder.perform(verts, None, n, bits)
+        got = _noalloc_build(cuda, verts, n, bits)
         _same(ref, got)
+    assert _lib.device_status() == 0
+
+
+@pytest.mark.parametrize("bits", [10, 21])
+@pytest.mark.parametrize("n", [1, 2, 1 << 18])
+def test_noalloc_edge_sizes(cuda, bits, n):
+    """One triangle (no internal node), two (a single internal node) and the
+    largest count the fixed array takes, each called twice in a row."""
+    builder = lbvh.LBVHBuilder(1, cuda)
+    vx, vy, vz = W.triangle_soup(n, seed=40 + n % 7)
+    verts = [torch.from_numpy(a).to(cuda) for a in (vx, vy, vz)]
+    ref = builder.perform(verts, None, n, bits)
+    for _ in range(2):
+        _same(ref, _noalloc_build(cuda, verts, n, bits))
     assert _lib.device_status() == 0
 
 
