@@ -20,13 +20,13 @@ Reported with it:
   roofline   the build's dominant kernel: algorithmic bytes / its CUDA-event
              duration vs the measured HBM copy bandwidth;
   traversal  closest-hit and shadow throughput (Mrays/s) on the built tree;
-  cpu_baseline  the oracle's restatement of the reference LBVH build on a
-             1 Mi-triangle sample of the same workload, one build per host
-             thread at once.
+  cpu_baseline  the oracle's restatement of the reference LBVH build on the
+             same 16 Mi triangles, run data-parallel on every host core.
 
---impl reference times the reference's algorithm on the host CPU instead (the
-reference's own code is OpenCL and cannot run here; its CPU restatement in
-oracle/ is timed), on the same metric.
+--impl reference times the reference's algorithm on the host CPU instead, on
+the same workload and metric (the reference's own code is OpenCL and cannot
+run here; its restatement in oracle/ runs stage by stage on all host cores, as
+the reference's kernels would on a CPU OpenCL device).
 
 Multi-GPU: the build does not shard; --gpus N runs N independent replicas
 (one process per GPU under torchrun), value = total triangles / max time.
@@ -50,7 +50,6 @@ sys.path.insert(0, ROOT)
 N_TRIS = 1 << 24
 N_RAYS = 1 << 24
 BITS = 10
-CPU_SAMPLE_TRIS = 1 << 20
 METRIC = "LBVH build ms per 1M triangles"
 UNIT = "ms/Mtri"
 WORKLOAD = "lbvh-build+traversal, 16Mi random triangles (30-bit Morton), 16Mi closest + 16Mi shadow rays"
@@ -185,33 +184,56 @@ def host_threads() -> int:
         return os.cpu_count() or 1
 
 
-def cpu_build_round(vx, vy, vz, n: int, threads: int) -> float:
-    """Seconds for `threads` concurrent builds of the n-triangle sample, one
-    per host thread (the C build releases the interpreter lock)."""
+def cpu_build_ms(vx, vy, vz, n: int, steps: int, warmup: int, threads: int) -> list[float]:
+    """Milliseconds per build of the n triangles by the restatement of the
+    reference's LBVH construction run data-parallel on `threads` host threads
+    (oracle/lbvh_oracle.c, orc_lbvh_build_mt; the C code releases the
+    interpreter lock)."""
+    import oracle
+
+    out = []
+    for i in range(warmup + steps):
+        t0 = time.perf_counter()
+        oracle.lbvh_build_mt(vx, vy, vz, None, n, BITS, threads)
+        if i >= warmup:
+            out.append(1e3 * (time.perf_counter() - t0))
+    return out
+
+
+def cpu_trace_mrays(vx, vy, vz, n: int, rays, threads: int) -> float:
+    """Closest-hit rays per second of the restated reference traversal
+    (orc_trace_closest, reference order) over the CPU-built tree, the rays
+    split into one chunk per host thread."""
     import oracle
     from concurrent.futures import ThreadPoolExecutor
 
+    ob = oracle.lbvh_build_mt(vx, vy, vz, None, n, BITS, threads)
+    chunks = np.array_split(rays, threads)
     with ThreadPoolExecutor(max_workers=threads) as ex:
         t0 = time.perf_counter()
-        list(ex.map(lambda _: oracle.lbvh_build(vx, vy, vz, None, n, BITS), range(threads)))
-        return time.perf_counter() - t0
+        list(ex.map(lambda c: oracle.trace_closest(vx, vy, vz, None, ob, c), chunks))
+        dt = time.perf_counter() - t0
+    return rays.shape[0] / dt / 1e6
+
+
+CPU_NOTE = ("the reference's LBVH construction (OpenCL/lbvh_construction.cl driven as LBVHBuilder.cpp:160-375) "
+            "restated in C and run stage by stage on all host cores, as its kernels would run on a CPU OpenCL "
+            "device; the reference's own kernels and CPU code cannot run on this host (no OpenCL driver; its "
+            "sources are not on the GPU host and x86 builds of them do not run on its aarch64 cores)")
 
 
 def cpu_baseline(n: int, budget_s: float = 20.0) -> dict:
+    """The CPU build of the same 16 Mi-triangle workload on every host core,
+    a few builds within `budget_s`."""
     from clear_gb300 import workloads as W
 
     threads = host_threads()
-    vx, vy, vz = W.triangle_soup(n, seed=101)
-    cpu_build_round(vx, vy, vz, n, threads)  # warm
-    times = []
-    t_end = time.perf_counter() + budget_s
-    while time.perf_counter() < t_end and len(times) < 5:
-        times.append(cpu_build_round(vx, vy, vz, n, threads))
-    ms = 1e3 * statistics.median(times)
-    return {"value": ms / (threads * n / 1e6), "unit": UNIT, "cores": threads, "kind": "port",
-            "sample": f"{threads} concurrent builds (one per host thread) of {n} triangles of the same "
-                      f"distribution, oracle/lbvh_oracle.c restatement of lbvh_construction.cl, median of "
-                      f"{len(times)} rounds"}
+    vx, vy, vz = W.triangle_soup(n, seed=1)
+    first = cpu_build_ms(vx, vy, vz, n, 1, 0, threads)[0]
+    reps = max(1, min(5, int(budget_s * 1e3 / max(first, 1.0))))
+    ms = statistics.median(cpu_build_ms(vx, vy, vz, n, reps, 0, threads))
+    return {"value": ms / (n / 1e6), "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": f"{reps} builds of the full {n}-triangle workload (median), {CPU_NOTE}"}
 
 
 def gpu_time_us(fn, stream, reps: int = 20) -> float:
@@ -496,30 +518,44 @@ def bench_batched(dev, num_scenes=512, spp=8, depth=5) -> dict:
 
 
 def run_reference(args):
+    """The reference's build on the host CPU, on this arm's workload: the same
+    16 Mi random triangles (seed 1) and 10 bits per axis, one build per step on
+    every host core.  For information it also times the restated reference
+    traversal on a ray sample and the reference's own CPU builder (the
+    midpoint-split BVH of BVH.hpp, single-threaded as the reference runs it)
+    restated, on a 1 Mi sample."""
     rank, world, _ = dist_env()
     if rank != 0:
         return
     import oracle
     from clear_gb300 import workloads as W
 
-    n = CPU_SAMPLE_TRIS
+    n = args.tris
     threads = host_threads()
-    vx, vy, vz = W.triangle_soup(n, seed=101)
-    oracle.lbvh_build(vx, vy, vz, None, 1024, BITS)  # loads (and if needed builds) the C library
-    for _ in range(args.warmup):
-        cpu_build_round(vx, vy, vz, n, threads)
-    dt = sum(cpu_build_round(vx, vy, vz, n, threads) for _ in range(args.steps)) / args.steps
-    value = 1e3 * dt / (threads * n / 1e6)
+    vx, vy, vz = W.triangle_soup(n, seed=1)
+    oracle.lbvh_build(vx[:9], vy[:9], vz[:9], None, 3, BITS)  # loads (and if needed builds) the C library
+    ms = cpu_build_ms(vx, vy, vz, n, args.steps, args.warmup, threads)
+    ms_step = statistics.mean(ms)
+    value = ms_step / (n / 1e6)
+    rays = W.closest_rays(1 << 18, seed=11)
+    mrays = cpu_trace_mrays(vx, vy, vz, n, rays, threads)
+    m = 1 << 20
+    t0 = time.perf_counter()
+    oracle.midbvh_build(vx[:3 * m], vy[:3 * m], vz[:3 * m], None, m)
+    mid_ms = 1e3 * (time.perf_counter() - t0)
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
-        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * dt, "higher_is_better": False,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": False,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": WORKLOAD, "sample_tris": n, "bits_per_dim": BITS, "host_threads": threads,
-                   "note": "reference LBVH algorithm (lbvh_construction.cl) restated in C, one build per host "
-                           "thread at once; the reference's OpenCL kernels cannot run here"},
+        "config": {"workload": WORKLOAD, "tris_per_gpu": n, "bits_per_dim": BITS, "host_threads": threads,
+                   "same_config": True, "note": CPU_NOTE},
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
-                         "sample": f"{threads} concurrent builds of a {n}-triangle sample per step"},
+                         "sample": f"one build of the full {n}-triangle workload per step on {threads} threads"},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "traversal": {"closest_mrays_s": mrays, "rays": int(rays.shape[0]), "threads": threads,
+                      "form": "restated reference order (bvh_traversal.cl:182-215) over the CPU-built tree"},
+        "midpoint_bvh_build": {"ms_per_mtri": mid_ms / (m / 1e6), "tris": m, "threads": 1,
+                               "form": "restated BVH::build (BVH.hpp:140-175), the reference's CPU builder"},
     }
     print(json.dumps(line), flush=True)
 
@@ -626,16 +662,18 @@ def run_ours(args):
     occ = torch.empty(m, dtype=torch.uint8, device=dev)
     trav_steps = max(3, args.steps // 4)
     for _ in range(2):
-        lbvh.trace_closest(bvh, crays, hid, ht)
+        lbvh.trace_closest(bvh, crays, hid, ht, ordered=False)
         lbvh.trace_shadow(bvh, srays, occ)
     torch.cuda.synchronize()
     hid2 = torch.empty(m, dtype=torch.int32, device=dev)
     ht2 = torch.empty(m, dtype=torch.float32, device=dev)
+    lbvh.trace_replays(clear=True)
     lbvh.trace_closest(bvh, crays, hid2, ht2, ordered=True)
+    replayed = lbvh.trace_replays(clear=True)
     t0, t1, t2, t3 = (torch.cuda.Event(enable_timing=True) for _ in range(4))
     t0.record(stream)
     for _ in range(trav_steps):
-        lbvh.trace_closest(bvh, crays, hid, ht)
+        lbvh.trace_closest(bvh, crays, hid, ht, ordered=False)
     t1.record(stream)
     for _ in range(trav_steps):
         lbvh.trace_shadow(bvh, srays, occ)
@@ -644,12 +682,13 @@ def run_ours(args):
         lbvh.trace_closest(bvh, crays, hid2, ht2, ordered=True)
     t3.record(stream)
     torch.cuda.synchronize()
-    closest_ms = t0.elapsed_time(t1) / trav_steps
+    lbvh.trace_replays(clear=True)
+    refo_ms = t0.elapsed_time(t1) / trav_steps
     shadow_ms = t1.elapsed_time(t2) / trav_steps
-    ordered_ms = t2.elapsed_time(t3) / trav_steps
-    # visiting statistics of the same query (reference order): the bytes the
-    # exact search gathers per ray, 64 per node loaded and 48 per triangle
-    # tested, plus the 32-byte ray and its 8-byte result
+    closest_ms = t2.elapsed_time(t3) / trav_steps
+    # visiting statistics of the reference-order query: the bytes that search
+    # gathers per ray, 64 per node loaded and 48 per triangle tested, plus the
+    # 32-byte ray and its 8-byte result
     _, cnt = lbvh.trace_closest_counted(bvh, crays)
     nodes_per_ray = float(cnt[:, 0].double().mean().item())
     tris_per_ray = float(cnt[:, 1].double().mean().item())
@@ -704,13 +743,16 @@ def run_ours(args):
                                            "frac": b * n / (kern_ms[k] * 1e-3) / 1e9 / peak}
                                        for k, b in DESIGN_BYTES.items() if k in kern_ms},
         "traversal": {"closest_mrays_s": m / closest_ms / 1e3, "shadow_mrays_s": m / shadow_ms / 1e3,
-                      "closest_ordered_mrays_s": m / ordered_ms / 1e3,
-                      "ordered_vs_exact_id_mismatches": ordered_id_mismatch,
-                      "ordered_vs_exact_t_mismatches": ordered_t_mismatch,
-                      "closest_ms": closest_ms, "shadow_ms": shadow_ms, "closest_hit_frac": hit_frac,
-                      "closest_nodes_per_ray": nodes_per_ray, "closest_tris_per_ray": tris_per_ray,
-                      "closest_gather_gbs": fetch_bytes / (closest_ms * 1e-3) / 1e9,
-                      "closest_gather_frac_of_hbm": fetch_bytes / (closest_ms * 1e-3) / 1e9 / peak,
+                      "closest_form": "nearer-first with replay of order-dependent rays (bit-exact)",
+                      "closest_replayed_frac": replayed / m,
+                      "closest_reference_order_mrays_s": m / refo_ms / 1e3,
+                      "fast_vs_reference_order_id_mismatches": ordered_id_mismatch,
+                      "fast_vs_reference_order_t_mismatches": ordered_t_mismatch,
+                      "closest_ms": closest_ms, "closest_reference_order_ms": refo_ms, "shadow_ms": shadow_ms,
+                      "closest_hit_frac": hit_frac,
+                      "reference_order_nodes_per_ray": nodes_per_ray, "reference_order_tris_per_ray": tris_per_ray,
+                      "reference_order_gather_gbs": fetch_bytes / (refo_ms * 1e-3) / 1e9,
+                      "reference_order_gather_frac_of_hbm": fetch_bytes / (refo_ms * 1e-3) / 1e9 / peak,
                       "shadow_occluded_frac": occ_frac},
         "render": render,
         "render_terrain": render_terrain,
@@ -721,7 +763,7 @@ def run_ours(args):
         "device_error_bits": dev_err,
     }
     if not args.no_cpu_baseline:
-        line["cpu_baseline"] = cpu_baseline(CPU_SAMPLE_TRIS)
+        line["cpu_baseline"] = cpu_baseline(n)
     print(json.dumps(line), flush=True)
     if world > 1:
         dist.destroy_process_group()

@@ -116,70 +116,158 @@ static __device__ __noinline__ bool alpha_cutout(const DScene& sc, uint32_t id, 
 // kAlpha (scenes with CLR_SCENE_ALPHA) a cutout moves the bound without being
 // recorded (see alpha_cutout).  Whether the bound ended finite is the
 // reference's "hit" for shadow rays.
-template <bool kOrdered, bool kCount, bool kAlpha>
-static __device__ CLR_TRAVERSAL_ATTR uint32_t intersect_search(const DScene& sc, f3 org, f3 dir, Hit& h, uint2* stack,
-                                                               uint32_t* boxes) {
-    Ray ray{org.x, org.y, org.z, INFINITY, dir.x, dir.y, dir.z};
-    const float ix = 1.0f / dir.x, iy = 1.0f / dir.y, iz = 1.0f / dir.z;
+// kOrdered runs the nearer-first search and replays the ray in the
+// reference's order when its answer could depend on the order (traverse.cuh),
+// so both forms return the reference's record.  Scenes with cutouts are always
+// searched in the reference's order: a cutout moves the bound without a
+// record, which makes the record depend on the order in ways the replay test
+// does not cover.
+// What a search leaves: its final bound and the leaf (sorted position) of the
+// triangle it recorded.  The record's distance and barycentrics are computed
+// again from that leaf afterwards (the same arithmetic gives the same values),
+// which keeps them out of the registers the search loop holds.
+struct SearchResult {
+    float t;
+    uint32_t leaf;
+};
+
+// The reference's order (bvh_traversal.cl:191-208).
+template <bool kCount, bool kAlpha>
+static __device__ CLR_TRAVERSAL_ATTR SearchResult search_reference_order(const DScene& sc, const Ray& ray, float ix,
+                                                                         float iy, float iz, float root_entry,
+                                                                         uint2* stack, uint32_t* boxes) {
     float t = INFINITY;
     uint32_t best = kNone32;
-    float bb1 = 0.f, bb2 = 0.f, bt = INFINITY;
-    float entry;
-    const float* rb = sc.root_box;
-    if (!box_test_fast(rb[0], rb[1], rb[2], rb[4], rb[5], rb[6], ray, ix, iy, iz, entry)) return 0u;
-    auto test_leaf = [&](uint32_t leaf) {
-        const float4 a = __ldg(sc.tris + 3u * leaf), b = __ldg(sc.tris + 3u * leaf + 1u),
-                     c = __ldg(sc.tris + 3u * leaf + 2u);
-        float b1, b2;
-        if (tri_test(a, b, c, ray, t, &b1, &b2)) {
-            if (kAlpha && alpha_cutout(sc, __float_as_uint(a.w), b1, b2)) return;
-            best = __float_as_uint(a.w);
-            bb1 = b1;
-            bb2 = b2;
-            bt = t;
-        }
-    };
-    if (sc.num_tris == 1) {  // the root box is the leaf's box
-        if (kCount) ++boxes[1];
-        test_leaf(0);
-    } else if (sc.num_tris >= 2) {
-        int sp = 0;
-        stack[sp++] = make_uint2(__float_as_uint(rb[3]), __float_as_uint(entry));
-        for (uint32_t guard = 0; sp > 0 && guard < sc.num_tris; ++guard) {
-            --sp;
-            if (__uint_as_float(stack[sp].y) > t) continue;
-            if (kCount) ++boxes[0];
-            const NodeBoxes nb = load_node(sc.nodes, stack[sp].x);
-            float e0, e1;
-            const bool p0 = box_test_fast(nb.b0[0], nb.b0[1], nb.b0[2], nb.b0[3], nb.b0[4], nb.b0[5], ray, ix, iy, iz, e0);
-            const bool p1 = box_test_fast(nb.b1[0], nb.b1[1], nb.b1[2], nb.b1[3], nb.b1[4], nb.b1[5], ray, ix, iy, iz, e1);
-            const bool leaf0 = (nb.ref0 & kLeafBit) != 0, leaf1 = (nb.ref1 & kLeafBit) != 0;
-            const bool swap = kOrdered && (e1 < e0);
+    int sp = 0;
+    stack[sp++] = make_uint2(__float_as_uint(sc.root_box[3]), __float_as_uint(root_entry));
+    for (uint32_t guard = 0; sp > 0 && guard < sc.num_tris; ++guard) {
+        --sp;
+        if (__uint_as_float(stack[sp].y) > t) continue;
+        if (kCount) ++boxes[0];
+        const NodeBoxes nb = load_node(sc.nodes, stack[sp].x);
+        float e0, e1;
+        const bool p0 = box_test_fast(nb.b0[0], nb.b0[1], nb.b0[2], nb.b0[3], nb.b0[4], nb.b0[5], ray, ix, iy, iz, e0);
+        const bool p1 = box_test_fast(nb.b1[0], nb.b1[1], nb.b1[2], nb.b1[3], nb.b1[4], nb.b1[5], ray, ix, iy, iz, e1);
 #pragma unroll
-            for (int k = 0; k < 2; ++k) {
-                int c = k;
-                if (kOrdered) c = (!leaf0 && !leaf1) ? (swap ? k : 1 - k) : (swap ? 1 - k : k);
-                const uint32_t ref = c ? nb.ref1 : nb.ref0;
-                const bool pass = c ? p1 : p0;
-                const float e = c ? e1 : e0;
-                if (ref & kLeafBit) {
-                    if (pass && !(e > t)) {
-                        if (kCount) ++boxes[1];
-                        test_leaf(ref & ~kLeafBit);
-                    }
-                } else if (pass) {
-                    if (sp < kStackSize) stack[sp++] = make_uint2(ref, __float_as_uint(e));
-                    else clr_raise(CLR_DEVERR_STACK);
+        for (int c = 0; c < 2; ++c) {
+            const uint32_t ref = c ? nb.ref1 : nb.ref0;
+            if (!(c ? p1 : p0)) continue;
+            const float e = c ? e1 : e0;
+            if (ref & kLeafBit) {
+                if (e > t) continue;
+                if (kCount) ++boxes[1];
+                const uint32_t leaf = ref & ~kLeafBit;
+                const float4 a = __ldg(sc.tris + 3u * leaf);
+                float b1, b2;
+                if (tri_test(a, __ldg(sc.tris + 3u * leaf + 1u), __ldg(sc.tris + 3u * leaf + 2u), ray, t, &b1, &b2)) {
+                    if (kAlpha && alpha_cutout(sc, __float_as_uint(a.w), b1, b2)) continue;
+                    best = leaf;
                 }
+            } else if (sp < kStackSize) {
+                stack[sp++] = make_uint2(ref, __float_as_uint(e));
+            } else {
+                clr_raise(CLR_DEVERR_STACK);
             }
         }
     }
-    h.id = best;
-    const uint32_t bound = t < INFINITY ? 2u : 0u;
-    if (best == kNone32) return bound;
-    h.t = bt;
-    h.b1 = bb1;
-    h.b2 = bb2;
+    return SearchResult{t, best};
+}
+
+// The nearer-first search with the bookkeeping of the replay decision
+// (traverse.cuh); sets `replay` when the ray must be searched again in the
+// reference's order.  Not for scenes with cutouts.
+template <bool kCount>
+static __device__ CLR_TRAVERSAL_ATTR SearchResult search_nearer_first(const DScene& sc, const Ray& ray, float ix,
+                                                                      float iy, float iz, float root_entry,
+                                                                      uint2* stack, uint32_t* boxes, bool& replay) {
+    float t = INFINITY, tr = INFINITY;  // the bound and its relaxed form
+    uint32_t best = kNone32;
+    float gbest = -INFINITY, t2 = INFINITY;
+    int sp = 0;
+    stack[sp++] = make_uint2(__float_as_uint(sc.root_box[3]), __float_as_uint(root_entry));
+    for (uint32_t guard = 0; sp > 0 && guard < sc.num_tris; ++guard) {
+        --sp;
+        const float key = __uint_as_float(stack[sp].y);
+        if (key > tr) continue;
+        if (kCount) ++boxes[0];
+        const NodeBoxes nb = load_node(sc.nodes, stack[sp].x);
+        float e0, e1;
+        const bool p0 = box_test_fast(nb.b0[0], nb.b0[1], nb.b0[2], nb.b0[3], nb.b0[4], nb.b0[5], ray, ix, iy, iz, e0);
+        const bool p1 = box_test_fast(nb.b1[0], nb.b1[1], nb.b1[2], nb.b1[3], nb.b1[4], nb.b1[5], ray, ix, iy, iz, e1);
+        const bool both_internal = !(nb.ref0 & kLeafBit) && !(nb.ref1 & kLeafBit);
+        const bool swap = e1 < e0;
+#pragma unroll
+        for (int k = 0; k < 2; ++k) {
+            // leaves: near first; internal: far pushed first
+            const int c = both_internal ? (swap ? k : 1 - k) : (swap ? 1 - k : k);
+            const uint32_t ref = c ? nb.ref1 : nb.ref0;
+            if (!(c ? p1 : p0)) continue;
+            const float kc = fmaxf(c ? e1 : e0, key);
+            if (ref & kLeafBit) {
+                if (kc > tr) continue;
+                if (kCount) ++boxes[1];
+                const uint32_t leaf = ref & ~kLeafBit;
+                float tt, b1, b2;
+                if (!tri_eval(__ldg(sc.tris + 3u * leaf), __ldg(sc.tris + 3u * leaf + 1u),
+                              __ldg(sc.tris + 3u * leaf + 2u), ray, tt, b1, b2))
+                    continue;
+                if (tt < t || (tt == t && best == kNone32)) {
+                    if (best != kNone32) t2 = fminf(t2, t);
+                    t = tt;
+                    tr = relaxed_bound(tt, replay_scale(sc.root_box));
+                    best = leaf;
+                    gbest = kc;
+                } else {
+                    t2 = fminf(t2, tt);
+                }
+            } else if (sp < kStackSize) {
+                stack[sp++] = make_uint2(ref, __float_as_uint(kc));
+            } else {
+                clr_raise(CLR_DEVERR_STACK);
+            }
+        }
+    }
+    replay = needs_replay(t, gbest, t2, replay_scale(sc.root_box));
+    return SearchResult{t, best};
+}
+
+// The record returned is the last hit recorded, at its own distance; with
+// kAlpha (scenes with CLR_SCENE_ALPHA) a cutout moves the bound without being
+// recorded (see alpha_cutout).  Whether the bound ended finite is the
+// reference's "hit" for shadow rays.
+// kOrdered runs the nearer-first search and replays the ray in the
+// reference's order when its answer could depend on the order (traverse.cuh),
+// so both forms return the reference's record.  Scenes with cutouts are always
+// searched in the reference's order: a cutout moves the bound without a
+// record, which makes the record depend on the order in ways the replay test
+// does not cover.
+template <bool kOrdered, bool kCount, bool kAlpha>
+static __device__ __forceinline__ uint32_t intersect_search(const DScene& sc, f3 org, f3 dir, Hit& h, uint2* stack,
+                                                            uint32_t* boxes) {
+    const Ray ray{org.x, org.y, org.z, INFINITY, dir.x, dir.y, dir.z};
+    const float ix = 1.0f / dir.x, iy = 1.0f / dir.y, iz = 1.0f / dir.z;
+    float entry;
+    const float* rb = sc.root_box;
+    if (!box_test_fast(rb[0], rb[1], rb[2], rb[4], rb[5], rb[6], ray, ix, iy, iz, entry)) return 0u;
+    SearchResult r{INFINITY, kNone32};
+    if (sc.num_tris == 1) {  // the root box is the leaf's box
+        if (kCount) ++boxes[1];
+        float b1, b2;
+        const float4 a = __ldg(sc.tris);
+        if (tri_test(a, __ldg(sc.tris + 1u), __ldg(sc.tris + 2u), ray, r.t, &b1, &b2) &&
+            !(kAlpha && alpha_cutout(sc, __float_as_uint(a.w), b1, b2)))
+            r.leaf = 0;
+    } else if (sc.num_tris >= 2) {
+        bool replay = true;
+        if (kOrdered && !kAlpha) r = search_nearer_first<kCount>(sc, ray, ix, iy, iz, entry, stack, boxes, replay);
+        if (replay) r = search_reference_order<kCount, kAlpha>(sc, ray, ix, iy, iz, entry, stack, boxes);
+    }
+    const uint32_t bound = r.t < INFINITY ? 2u : 0u;
+    h.id = kNone32;
+    if (r.leaf == kNone32) return bound;
+    const float4 a = __ldg(sc.tris + 3u * r.leaf);
+    tri_eval(a, __ldg(sc.tris + 3u * r.leaf + 1u), __ldg(sc.tris + 3u * r.leaf + 2u), ray, h.t, h.b1, h.b2);
+    h.id = __float_as_uint(a.w);
     return bound | 1u;
 }
 

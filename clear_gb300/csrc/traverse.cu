@@ -1,15 +1,18 @@
 // BVH traversal on sm_103a: closest-hit and shadow (any-hit) queries.
 //
-// The root node index is root_box[3] (bit pattern).  The closest-hit kernel
-// visits nodes in the reference's order
-// (OpenCL/bvh_traversal.cl:182-215): pop a node, handle child 0 then child 1,
-// a leaf child is box-tested and its triangle tested at once, an internal
-// child is pushed (so child 1's subtree is explored before child 0's).
-// The reference tests a popped node's box against the current t; here both
-// child boxes are tested when their parent is loaded (one 64-byte node fetch)
-// and the entry distance rides on the stack, compared with t at pop time.
-// The bound-independent half of the test does not depend on t, so the set of
-// boxes accepted, and with it the hit, is the reference's.
+// The root node index is root_box[3] (bit pattern).  clr_trace_closest
+// visits nodes in the reference's order (OpenCL/bvh_traversal.cl:182-215):
+// pop a node, handle child 0 then child 1, a leaf child is box-tested and its
+// triangle tested at once, an internal child is pushed (so child 1's subtree
+// is explored before child 0's).  The reference tests a popped node's box
+// against the current t; here both child boxes are tested when their parent
+// is loaded (one 64-byte node fetch) and the entry distance rides on the
+// stack, compared with t at pop time.  The bound-independent half of the test
+// does not depend on t, so the set of boxes accepted, and with it the hit, is
+// the reference's.
+// clr_trace_closest_ordered visits the nearer child first and replays, in the
+// reference's order, every ray whose answer could depend on the order
+// (traverse.cuh): the same ids and distances, with far fewer nodes visited.
 #include "common.cuh"
 #include "traverse.cuh"
 
@@ -30,70 +33,99 @@ struct ClosestState {
     float ix, iy, iz;
     float t;
     uint32_t best;
+    float tr;         // fast search: the relaxed bound of t,
+    float gbest, t2;  // G(best) and the other candidates' smallest tt
     int sp;
+    bool exact;  // searching in the reference's order
 };
 
 __device__ __forceinline__ void closest_begin(ClosestState& s, const float4* __restrict__ rays, uint32_t r,
                                               const float* __restrict__ root_box, uint32_t n,
-                                              const float4* __restrict__ tris, uint2* stack) {
+                                              const float4* __restrict__ tris, uint2* stack, bool exact) {
     s.ray = load_ray(rays, r);
     s.ix = 1.0f / s.ray.dx;
     s.iy = 1.0f / s.ray.dy;
     s.iz = 1.0f / s.ray.dz;
     s.t = s.ray.tmax;
+    s.tr = relaxed_bound(s.t, replay_scale(root_box));
     s.best = 0xFFFFFFFFu;
+    s.gbest = -INFINITY;
+    s.t2 = INFINITY;
     s.sp = 0;
+    s.exact = exact || n < 2;  // one triangle: no order to depend on
     float entry;
-    const bool root_ok = box_test_fast(__ldg(root_box + 0), __ldg(root_box + 1), __ldg(root_box + 2),
-                                       __ldg(root_box + 4), __ldg(root_box + 5), __ldg(root_box + 6), s.ray, s.ix,
-                                       s.iy, s.iz, entry) &&
-                         !(entry > s.t);
-    if (!root_ok) return;
-    if (n == 1) tri_hit(tris, 0, s.ray, s.t, s.best);
-    else if (n >= 2) stack[s.sp++] = make_uint2(__float_as_uint(__ldg(root_box + 3)), __float_as_uint(entry));
+    if (!box_test_fast(__ldg(root_box + 0), __ldg(root_box + 1), __ldg(root_box + 2), __ldg(root_box + 4),
+                       __ldg(root_box + 5), __ldg(root_box + 6), s.ray, s.ix, s.iy, s.iz, entry))
+        return;
+    if (n == 1) {
+        if (!(entry > s.t)) tri_hit(tris, 0, s.ray, s.t, s.best);
+    } else if (n >= 2) {
+        // the pop-time bound test applies the root's entry (both modes)
+        stack[s.sp++] = make_uint2(__float_as_uint(__ldg(root_box + 3)), __float_as_uint(entry));
+    }
 }
 
-// One pop of rayIntersection's loop (bvh_traversal.cl:191-208).  kOrdered
-// visits the nearer child first (by box entry distance) instead of the
-// reference's fixed child order: fewer nodes per ray, same closest t up to
-// ties and rounding-level near-ties (which the reference resolves by its
-// visiting order).
-template <bool kOrdered>
+// One pop of rayIntersection's loop (bvh_traversal.cl:191-208).
+// Reference order (s.exact): children in the fixed order, internal ones
+// pushed with their own entry distance, compared with t when popped.
+// Fast search: nearer child first, boxes keyed by the path maximum of entry
+// distances and culled against the relaxed bound, every reached leaf tested
+// with the bookkeeping of the replay decision (traverse.cuh).
 __device__ __forceinline__ void closest_step(ClosestState& s, const float4* __restrict__ nodes,
-                                             const float4* __restrict__ tris, uint2* stack) {
+                                             const float4* __restrict__ tris, uint2* stack, float S) {
     --s.sp;
     const uint32_t node = stack[s.sp].x;
-    if (__uint_as_float(stack[s.sp].y) > s.t) return;  // the reference's bound test at pop
+    const float key = __uint_as_float(stack[s.sp].y);
+    if (key > (s.exact ? s.t : s.tr)) return;  // the reference's bound test at pop
     const NodeBoxes nb = load_node(nodes, node);
     float e0, e1;
     const bool p0 = box_test_fast(nb.b0[0], nb.b0[1], nb.b0[2], nb.b0[3], nb.b0[4], nb.b0[5], s.ray, s.ix, s.iy, s.iz, e0);
     const bool p1 = box_test_fast(nb.b1[0], nb.b1[1], nb.b1[2], nb.b1[3], nb.b1[4], nb.b1[5], s.ray, s.ix, s.iy, s.iz, e1);
     // reference order: child 0 then child 1 (internal children pushed, so
-    // child 1's subtree pops first).  Ordered: far child handled first so the
+    // child 1's subtree pops first).  Fast: far child handled first so the
     // near internal child is popped first; near leaf tested first.
-    const bool swap = kOrdered && (e1 < e0);
+    const bool swap = !s.exact && (e1 < e0);
+    const bool both_internal = !(nb.ref0 & kLeafBit) && !(nb.ref1 & kLeafBit);
 #pragma unroll
     for (int k = 0; k < 2; ++k) {
-        int c = k;
-        if (kOrdered) {
-            const bool leaf0 = (nb.ref0 & kLeafBit) != 0, leaf1 = (nb.ref1 & kLeafBit) != 0;
-            // leaves: near first; internal: far pushed first
-            const bool both_internal = !leaf0 && !leaf1;
-            c = both_internal ? (swap ? k : 1 - k) : (swap ? 1 - k : k);
-        }
+        const int c = s.exact ? k : (both_internal ? (swap ? k : 1 - k) : (swap ? 1 - k : k));
         const uint32_t ref = c ? nb.ref1 : nb.ref0;
-        const bool pass = c ? p1 : p0;
+        if (!(c ? p1 : p0)) continue;
         const float e = c ? e1 : e0;
+        const float kc = s.exact ? e : fmaxf(e, key);
         if (ref & kLeafBit) {
-            if (pass && !(e > s.t)) tri_hit(tris, ref & ~kLeafBit, s.ray, s.t, s.best);
-        } else if (pass) {
-            if (s.sp < kStackSize) stack[s.sp++] = make_uint2(ref, __float_as_uint(e));
+            if (s.exact) {
+                if (!(e > s.t)) tri_hit(tris, ref & ~kLeafBit, s.ray, s.t, s.best);
+                continue;
+            }
+            if (kc > s.tr) continue;
+            const uint32_t leaf = ref & ~kLeafBit;
+            const float4 a = __ldg(tris + 3u * leaf), b = __ldg(tris + 3u * leaf + 1u), cc = __ldg(tris + 3u * leaf + 2u);
+            float tt, b1, b2;
+            if (!tri_eval(a, b, cc, s.ray, tt, b1, b2)) continue;
+            if (tt < s.t || (tt == s.t && s.best == 0xFFFFFFFFu)) {
+                if (s.best != 0xFFFFFFFFu) s.t2 = fminf(s.t2, s.t);
+                s.t = tt;
+                s.tr = relaxed_bound(tt, S);
+                s.best = __float_as_uint(a.w);
+                s.gbest = kc;
+            } else {
+                s.t2 = fminf(s.t2, tt);
+            }
+        } else {
+            if (s.sp < kStackSize) stack[s.sp++] = make_uint2(ref, __float_as_uint(kc));
             else clr_raise(CLR_DEVERR_STACK);
         }
     }
 }
 
-template <bool kOrdered>
+// Rays searched again in the reference's order, summed over launches
+// (clr_trace_replays).
+static __device__ unsigned long long g_replays = 0;
+
+// kFast: the nearer-first search with replay; otherwise the reference's order.
+// Both give the reference's ids and distances.
+template <bool kFast>
 __global__ void __launch_bounds__(kTraceThreads) k_trace_closest(const float4* __restrict__ nodes,
                                                                  const float4* __restrict__ tris,
                                                                  const float* __restrict__ root_box, uint32_t n,
@@ -103,15 +135,23 @@ __global__ void __launch_bounds__(kTraceThreads) k_trace_closest(const float4* _
     const uint32_t P = gridDim.x * blockDim.x;
     uint32_t r = blockIdx.x * blockDim.x + threadIdx.x;
     if (r >= nr) return;
+    const float S = replay_scale(root_box);
     uint2 stack[kStackSize];
     ClosestState s;
-    closest_begin(s, rays, r, root_box, n, tris, stack);
-    // a valid tree pops each internal node at most once per ray
+    closest_begin(s, rays, r, root_box, n, tris, stack, !kFast);
+    unsigned int replays = 0;
+    // a valid tree pops each internal node at most once per ray and search
     uint32_t guard = 0;
     for (;;) {
         if (s.sp > 0 && guard < n) {
-            closest_step<kOrdered>(s, nodes, tris, stack);
+            closest_step(s, nodes, tris, stack, S);
             ++guard;
+            continue;
+        }
+        if (kFast && !s.exact && needs_replay(s.t, s.gbest, s.t2, S)) {
+            ++replays;
+            guard = 0;
+            closest_begin(s, rays, r, root_box, n, tris, stack, true);
             continue;
         }
         hit_id[r] = s.best;
@@ -119,8 +159,9 @@ __global__ void __launch_bounds__(kTraceThreads) k_trace_closest(const float4* _
         r += P;
         if (r >= nr) break;
         guard = 0;
-        closest_begin(s, rays, r, root_box, n, tris, stack);
+        closest_begin(s, rays, r, root_box, n, tris, stack, !kFast);
     }
+    if (kFast && replays) atomicAdd(&g_replays, (unsigned long long)replays);
 }
 
 // Any-hit: the bound stays at tmax, so the accepted set of boxes does not
@@ -204,14 +245,14 @@ static int check_trace_args(const clr_bvh* bvh, const float* rays, uint32_t num_
     return CLR_OK;
 }
 
-template <bool kOrdered>
+template <bool kFast>
 static int trace_closest(const clr_bvh* bvh, const float* rays, uint32_t num_rays, uint32_t* hit_id, float* hit_t,
                          void* stream) {
     int rc = check_trace_args(bvh, rays, num_rays, hit_id);
     if (rc != CLR_OK || num_rays == 0) return rc;
     if (!hit_t) return clr_set_error(CLR_EINVAL, "clr_trace_closest: hit_t is NULL");
     cudaStream_t st = static_cast<cudaStream_t>(stream);
-    k_trace_closest<kOrdered><<<persistent_grid(k_trace_closest<kOrdered>, num_rays), kTraceThreads, 0, st>>>(
+    k_trace_closest<kFast><<<persistent_grid(k_trace_closest<kFast>, num_rays), kTraceThreads, 0, st>>>(
         static_cast<const float4*>(bvh->nodes), static_cast<const float4*>(bvh->tris), bvh->root_box, bvh->num_tris,
         reinterpret_cast<const float4*>(rays), num_rays, hit_id, hit_t);
     CLR_LAUNCH_CHECK("k_trace_closest");
@@ -226,6 +267,18 @@ extern "C" int clr_trace_closest(const clr_bvh* bvh, const float* rays, uint32_t
 extern "C" int clr_trace_closest_ordered(const clr_bvh* bvh, const float* rays, uint32_t num_rays, uint32_t* hit_id,
                                          float* hit_t, void* stream) {
     return trace_closest<true>(bvh, rays, num_rays, hit_id, hit_t, stream);
+}
+
+extern "C" int clr_trace_replays(uint64_t* count, int clear) {
+    if (!count) return clr_set_error(CLR_EINVAL, "clr_trace_replays: NULL count");
+    unsigned long long v = 0;
+    CLR_CUDA_TRY(cudaMemcpyFromSymbol(&v, g_replays, sizeof(v)));
+    if (clear) {
+        const unsigned long long z = 0;
+        CLR_CUDA_TRY(cudaMemcpyToSymbol(g_replays, &z, sizeof(z)));
+    }
+    *count = v;
+    return CLR_OK;
 }
 
 extern "C" int clr_trace_shadow(const clr_bvh* bvh, const float* rays, uint32_t num_rays, uint8_t* occluded,

@@ -97,10 +97,11 @@ __device__ __forceinline__ bool box_test_fast(float mnx, float mny, float mnz, f
 }
 
 // rayTriangleIntersection (OpenCL/bvh_traversal.cl:54-108), Moller-Trumbore
-// with |det| < 1e-6 rejected and a hit at tt > t rejected (so an equal-t hit
-// tested later wins).  Record = {p0, id}, {p1-p0}, {p2-p0}.
-__device__ __forceinline__ bool tri_test(const float4 a, const float4 e1, const float4 e2, const Ray& r, float& t,
-                                         float* b1_out = nullptr, float* b2_out = nullptr) {
+// with |det| < 1e-6 rejected: whether the ray meets the triangle at some
+// tt >= 0, and tt with its barycentrics, before any comparison with the
+// current bound.  Record = {p0, id}, {p1-p0}, {p2-p0}.
+__device__ __forceinline__ bool tri_eval(const float4 a, const float4 e1, const float4 e2, const Ray& r, float& tt,
+                                         float& b1, float& b2) {
     const float px = fsub(fmul(r.dy, e2.z), fmul(r.dz, e2.y));
     const float py = fsub(fmul(r.dz, e2.x), fmul(r.dx, e2.z));
     const float pz = fsub(fmul(r.dx, e2.y), fmul(r.dy, e2.x));
@@ -108,15 +109,23 @@ __device__ __forceinline__ bool tri_test(const float4 a, const float4 e1, const 
     if (det > -0.000001f && det < 0.000001f) return false;
     const float invDet = fdiv(1.0f, det);
     const float dx = fsub(r.ox, a.x), dy = fsub(r.oy, a.y), dz = fsub(r.oz, a.z);
-    const float b1 = fmul(dot3(dx, dy, dz, px, py, pz), invDet);
+    b1 = fmul(dot3(dx, dy, dz, px, py, pz), invDet);
     if (b1 < 0.0f || b1 > 1.0f) return false;
     const float qx = fsub(fmul(dy, e1.z), fmul(dz, e1.y));
     const float qy = fsub(fmul(dz, e1.x), fmul(dx, e1.z));
     const float qz = fsub(fmul(dx, e1.y), fmul(dy, e1.x));
-    const float b2 = fmul(dot3(r.dx, r.dy, r.dz, qx, qy, qz), invDet);
+    b2 = fmul(dot3(r.dx, r.dy, r.dz, qx, qy, qz), invDet);
     if (b2 < 0.0f || fadd(b1, b2) > 1.0f) return false;
-    const float tt = fmul(dot3(e2.x, e2.y, e2.z, qx, qy, qz), invDet);
-    if (tt < 0.0f || tt > t) return false;
+    tt = fmul(dot3(e2.x, e2.y, e2.z, qx, qy, qz), invDet);
+    return !(tt < 0.0f);
+}
+
+// The reference's test against the current bound t: a hit at tt > t is
+// rejected (so an equal-t hit tested later wins), an accepted one moves t.
+__device__ __forceinline__ bool tri_test(const float4 a, const float4 e1, const float4 e2, const Ray& r, float& t,
+                                         float* b1_out = nullptr, float* b2_out = nullptr) {
+    float tt, b1, b2;
+    if (!tri_eval(a, e1, e2, r, tt, b1, b2) || tt > t) return false;
     t = tt;
     if (b1_out) *b1_out = b1;
     if (b2_out) *b2_out = b2;
@@ -147,6 +156,57 @@ __device__ __forceinline__ NodeBoxes load_node(const float4* __restrict__ nodes,
     nb.ref0 = __float_as_uint(d.x);
     nb.ref1 = __float_as_uint(d.y);
     return nb;
+}
+
+// ---------------------------------------------- nearer-first with replay
+//
+// The reference's closest-hit search (bvh_traversal.cl:182-215) visits the
+// children of a node in a fixed order and keeps the LAST triangle accepted at
+// the smallest t; which triangle that is, on ties and near-ties, depends on the
+// visiting order.  The fast search visits the nearer child first and decides,
+// per ray, whether its answer is necessarily the reference's; if not, the ray
+// is searched again in the reference's order (a "replay").
+//
+// Notation for one ray: a candidate is a triangle whose Moller-Trumbore test
+// passes with tt >= 0 and whose boxes, leaf box and ancestors, pass the part
+// of Woo's test that does not depend on the bound; G(j) is the largest entry
+// distance over candidate j's boxes.  Exact arithmetic gives G(j) <= tt(j);
+// with rounding G(j) can exceed tt(j) by a few ulp ("inversion").
+//
+// The fast search culls a box when its path maximum of entries, pm, exceeds
+// the relaxed bound t + kReplayDelta (|t| + S) (S: the scene box's largest
+// extent / 16), tests every leaf it reaches, and records
+//   T, B      the smallest tt and the triangle that first reached it,
+//   G(B)      the path maximum of B's boxes,
+//   t2        the smallest tt of every other candidate it tested.
+// With V = max(T, G(B)), the answer (T, B) is final unless
+//   t2 <= V                                   (a tie or near-tie), or
+//   G(B) > T + kReplayDelta / 4 (|T| + S)     (B's own boxes lie well past it).
+// Proof sketch, assuming no inversion exceeds kReplayDelta / 4 (|tt| + S):
+// every other candidate then has tt > V.  Tested ones by t2 > V.  A culled
+// one lies under a box whose pm exceeded the relaxed bound of a t >= T, so
+// its G > T + kReplayDelta (|T| + S) >= V + kReplayDelta / 4 (|V| + S) (as
+// G(B) is within kReplayDelta / 4 (|T| + S) of T), and its tt > V by the
+// inversion bound.  In the reference's search, before B is tested t holds
+// only tt values > V >= every entry on B's path, so B is reached and
+// accepted, and no later candidate (tt > V >= T) is; the reference returns
+// (T, B) with the same barycentrics.  Inversions measured on the
+// random-triangle, terrain and Cornell scenes stay below 2^-21 relative; the
+// bound assumed is 2^-14.
+constexpr float kReplayDelta = 0x1p-12f;
+
+__device__ __forceinline__ float replay_scale(const float* root_box) {
+    const float ex = __ldg(root_box + 4) - __ldg(root_box + 0), ey = __ldg(root_box + 5) - __ldg(root_box + 1),
+                ez = __ldg(root_box + 6) - __ldg(root_box + 2);
+    const float m = fmaxf(ex, fmaxf(ey, ez));
+    return (m < INFINITY) ? m * 0.0625f : 0.0f;
+}
+
+__device__ __forceinline__ float relaxed_bound(float t, float S) { return t + kReplayDelta * (fabsf(t) + S); }
+
+__device__ __forceinline__ bool needs_replay(float t, float gbest, float t2, float S) {
+    const float V = fmaxf(t, gbest);
+    return (t2 < INFINITY && t2 <= V) || (gbest > t + 0.25f * kReplayDelta * (fabsf(t) + S));
 }
 
 }  // namespace clr

@@ -217,10 +217,12 @@ def _rays(rays: torch.Tensor, device) -> torch.Tensor:
 
 
 def trace_closest(bvh: BVH, rays: torch.Tensor, hit_id: torch.Tensor | None = None,
-                  hit_t: torch.Tensor | None = None, ordered: bool = False):
+                  hit_t: torch.Tensor | None = None, ordered: bool = True):
     """Closest hit for rays packed {ox,oy,oz,tmax,dx,dy,dz,0}.  Returns
-    (hit_id int32 [-1 = miss], hit_t float32).  ordered=True visits the nearer
-    child first (faster; ids may differ from the reference on exact ties)."""
+    (hit_id int32 [-1 = miss], hit_t float32), the reference's answer in both
+    forms: ordered=True (default) visits the nearer child first and replays in
+    the reference's order the rays whose answer could depend on the order;
+    ordered=False searches every ray in the reference's order."""
     r = _rays(rays, bvh.device)
     m = r.shape[0]
     if hit_id is None:
@@ -231,6 +233,14 @@ def trace_closest(bvh: BVH, rays: torch.Tensor, hit_id: torch.Tensor | None = No
         call("clr_trace_closest_ordered" if ordered else "clr_trace_closest", C.byref(bvh.c), _ptr(r),
              C.c_uint32(m), _ptr(hit_id), _ptr(hit_t), _stream(bvh.device))
     return hit_id, hit_t
+
+
+def trace_replays(clear: bool = True) -> int:
+    """Rays the nearer-first closest-hit query searched again in the
+    reference's order, summed over its launches since the last clear."""
+    v = C.c_uint64(0)
+    call("clr_trace_replays", C.byref(v), 1 if clear else 0)
+    return int(v.value)
 
 
 def trace_shadow(bvh: BVH, rays: torch.Tensor, occluded: torch.Tensor | None = None):

@@ -201,14 +201,19 @@ CLR_API int clr_lbvh_pass_times(clr_lbvh* h, float* ms, const char** names, int 
 CLR_API int clr_trace_closest(const clr_bvh* bvh, const float* rays, uint32_t num_rays, uint32_t* hit_id, float* hit_t,
                       void* stream);
 
-/* Closest hit visiting the nearer child first (by box entry distance): same
- * boxes, triangles tests and arithmetic, fewer node visits.  The closest t is
- * the same; when two triangles are hit at exactly the same t (or within the
- * rounding of a box test) the reference's answer depends on its fixed child
- * order, which this query does not follow, so the id may differ there.  For
- * renderers; clr_trace_closest is the bit-exact drop-in. */
+/* The same query (same ids and distances, bit for bit) visiting the nearer
+ * child first, by box entry distance: about a quarter of the node visits.
+ * Where the reference's answer depends on its fixed child order -- two
+ * triangles hit at the same t, or a box whose rounded entry distance lies a
+ * few ulp past a hit inside it -- the ray is detected and searched again in
+ * the reference's order; clr_trace_replays counts those rays. */
 CLR_API int clr_trace_closest_ordered(const clr_bvh* bvh, const float* rays, uint32_t num_rays, uint32_t* hit_id,
                                       float* hit_t, void* stream);
+
+/* Rays that clr_trace_closest_ordered searched again in the reference's order
+ * on the current device, summed over its launches (synchronous read; clear
+ * resets the count). */
+CLR_API int clr_trace_replays(uint64_t* count, int clear);
 
 /* Shadow (any-hit) query; the reference shoots a closest-hit ray for this
  * (OpenCL/pathtracer.cl:119-122).  occluded[r] = 1 when a triangle is hit at
@@ -253,7 +258,11 @@ typedef struct clr_scene {
  * textures are not read. */
 #define CLR_SCENE_ALPHA 0x1u
 
-#define CLR_RENDER_ORDERED 0x1u  /* trace with nearer-child-first traversal */
+/* Trace with nearer-child-first traversal, replaying in the reference's order
+ * the rays whose hit could depend on the order (see clr_trace_closest_ordered):
+ * the same image as without the flag, faster.  Scenes with CLR_SCENE_ALPHA are
+ * always traced in the reference's order. */
+#define CLR_RENDER_ORDERED 0x1u
 /* clr_render: run the wavefront form (identical results, several times
  * faster) on a workspace the library keeps per device until the process
  * exits, grown to the largest image rendered; renders that share it take

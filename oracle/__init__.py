@@ -29,7 +29,7 @@ _lib = None
 _ref_lbvh = None
 _ref_mid = None
 _ref_scene = None
-_ref_kbump = None
+_ref_kbump = {}
 
 
 def _p(a):
@@ -41,6 +41,7 @@ def lib():
     if _lib is None:
         _lib = C.CDLL(str(build_oracle()))
         _lib.orc_lbvh_build.restype = C.c_int
+        _lib.orc_lbvh_build_mt.restype = C.c_int
         _lib.orc_trace_closest.restype = C.c_int
         _lib.orc_trace_shadow.restype = C.c_int
         _lib.orc_midbvh_build.restype = C.c_int64
@@ -92,6 +93,22 @@ def lbvh_build(vx, vy, vz, tri, n, bits=10) -> OracleBVH:
     if rc != 0:
         raise RuntimeError(f"orc_lbvh_build failed: {rc}")
     return OracleBVH(inodes, lnodes, parents, sidx, q, box, bits)
+
+
+def lbvh_build_mt(vx, vy, vz, tri, n, bits=10, threads=0) -> OracleBVH:
+    """lbvh_build on all host cores (threads <= 0) or `threads`; identical
+    outputs (the per-triangle quantised coordinates are not returned)."""
+    vx, vy, vz, tri = _f32(vx), _f32(vy), _f32(vz), _u32(tri)
+    inodes = np.zeros(max(n - 1, 0), dtype=INODE_DTYPE)
+    lnodes = np.zeros(n, dtype=LNODE_DTYPE)
+    parents = np.zeros(max(2 * n - 1, 0), dtype=np.uint32)
+    sidx = np.zeros(n, dtype=np.uint32)
+    box = np.zeros(6, dtype=np.float32)
+    rc = lib().orc_lbvh_build_mt(_p(vx), _p(vy), _p(vz), _p(tri), C.c_uint32(n), C.c_uint32(bits), _p(inodes),
+                                 _p(lnodes), _p(parents), _p(sidx), _p(box), C.c_int(int(threads)))
+    if rc != 0:
+        raise RuntimeError(f"orc_lbvh_build_mt failed: {rc}")
+    return OracleBVH(inodes, lnodes, parents, sidx, None, box, bits)
 
 
 def trace_closest(vx, vy, vz, tri, bvh: OracleBVH, rays, stats=False):
@@ -177,10 +194,10 @@ def _ref(name):
         if _ref_lbvh is None:
             _ref_lbvh = C.CDLL(str(libs["libref_lbvh.so"]))
         return _ref_lbvh
-    if name == "lbvh_kbump":
-        if _ref_kbump is None:
-            _ref_kbump = C.CDLL(str(libs["libref_lbvh_kbump.so"]))
-        return _ref_kbump
+    if name in ("lbvh_kbump", "lbvh_kbump_ulp"):
+        if name not in _ref_kbump:
+            _ref_kbump[name] = C.CDLL(str(libs[f"lib{name.replace('lbvh', 'ref_lbvh')}.so"]))
+        return _ref_kbump[name]
     if _ref_mid is None:
         _ref_mid = C.CDLL(str(libs["libref_mid.so"]))
         _ref_mid.ref_midbvh_build.restype = C.c_int64
@@ -252,13 +269,20 @@ def ref_bvh_visualizer(scene_blobs: dict, inodes, lnodes, pixels, width, height)
 
 
 def ref_render(scene_blobs: dict, inodes, lnodes, rand_states, pixels, width, height, y0, y1, spp,
-               bump_as_kernel: bool = False):
+               bump_as_kernel: bool = False, max_depth: int = 100, perturb_math: bool = False):
     """sim::pathtracing over rows [y0, y1); rand_states (u32[4*W*H]) and
     pixels (f32[W*H*4]) are updated in place.  bump_as_kernel: the build of
-    the renderer whose bump frame follows the OpenCL kernel
-    (libref_lbvh_kbump, see build_oracle.build_ref_kernel_bump)."""
+    the renderer whose bump frame follows the OpenCL kernel and whose depth
+    cap is max_depth (libref_lbvh_kbump, see build_oracle.build_ref_kernel_bump);
+    perturb_math: that build with the transcendentals one ulp off on an eighth
+    of the inputs."""
     b = scene_blobs
-    _ref("lbvh_kbump" if bump_as_kernel else "lbvh").ref_render(_p(b["vertices"]), _p(b["normals"]), _p(b["tangents"]), _p(b["uvs"]),
+    if max_depth != 100 or perturb_math:
+        bump_as_kernel = True
+    L = _ref(("lbvh_kbump_ulp" if perturb_math else "lbvh_kbump") if bump_as_kernel else "lbvh")
+    if bump_as_kernel:
+        L.ref_set_max_depth(C.c_uint32(max_depth))
+    L.ref_render(_p(b["vertices"]), _p(b["normals"]), _p(b["tangents"]), _p(b["uvs"]),
                             _p(b["faces"]), _p(b["lights"]), _p(b["materials"]), _p(b["textures"]),
                             _p(b["others"]), _p(inodes), _p(lnodes), _p(rand_states), _p(pixels),
                             C.c_uint32(width), C.c_uint32(height), C.c_uint32(y0), C.c_uint32(y1),

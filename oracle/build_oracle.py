@@ -9,7 +9,11 @@
   with the stand-in headers of ``oracle/ref_stubs``.
 * ``oracle/_ref/libref_lbvh_kbump.so`` -- ``libref_lbvh.so`` with the one
   line where the CPU renderer departs from its OpenCL kernel (the bump frame's
-  axis normalisation, ``OpenCL/reflection.cl:210``) as the kernel has it.
+  axis normalisation, ``OpenCL/reflection.cl:210``) as the kernel has it, and
+  its path-length cap settable (``ref_set_max_depth``);
+  ``libref_lbvh_kbump_ulp.so`` the same with the transcendental functions'
+  results one ulp off on an eighth of the inputs (the reference's own
+  sensitivity to its math library, the floor of the image bars).
 * ``oracle/_ref/libref_lbvh_cl.so`` and ``libref_post_cl.so`` -- the
   reference's LBVH construction kernels (``OpenCL/lbvh_construction.cl``,
   ``CommonSources/OpenCL/generic_kernels.cl``) and post-processing kernels
@@ -55,7 +59,12 @@ def build_oracle() -> Path:
     out = HERE / "liboracle.so"
     src = HERE / "lbvh_oracle.c"
     if _stale(out, [src, Path(__file__)]):
-        _run(["gcc", "-std=c11", *CFLAGS, str(src), "-o", str(out), "-lm"])
+        # OpenMP runs orc_lbvh_build_mt on all host cores; without it (no
+        # libgomp) the same function runs on one thread
+        try:
+            _run(["gcc", "-std=c11", *CFLAGS, "-fopenmp", str(src), "-o", str(out), "-lm"])
+        except RuntimeError:
+            _run(["gcc", "-std=c11", *CFLAGS, str(src), "-o", str(out), "-lm"])
     return out
 
 
@@ -93,10 +102,11 @@ def build_ref() -> list[Path]:
         _run(["g++", "-std=c++17", "-w", *CFLAGS, "-ftrivial-auto-var-init=zero", f"-I{stubs}", f"-I{pt}",
               f"-I{la}", *map(str, srcs), "-o", str(out), "-Wl,--no-undefined"])
     built.append(out)
-    out = outdir / "libref_lbvh_kbump.so"
-    if _stale(out, deps):
-        build_ref_kernel_bump(out, src, stubs, eq)
-    built.append(out)
+    for lib, perturb in (("libref_lbvh_kbump.so", False), ("libref_lbvh_kbump_ulp.so", True)):
+        out = outdir / lib
+        if _stale(out, deps):
+            build_ref_kernel_bump(out, src, stubs, eq, perturb_math=perturb)
+        built.append(out)
     cl_dir = REF_DIR / "OpenCL_PathTracer" / "OpenCL"
     for lib, harness, kernels in (
             ("libref_lbvh_cl.so", "ref_lbvh_cl.cpp",
@@ -109,21 +119,71 @@ def build_ref() -> list[Path]:
     return built
 
 
-def build_ref_kernel_bump(out: Path, harness: Path, stubs: Path, eq: Path) -> None:
-    """The LBVH harness over the reference's CPU renderer with the one line
-    where that renderer departs from its OpenCL kernel put back as the kernel
-    has it: the bump frame's rotation axis is normalised before use
-    (OpenCL/reflection.cl:210; Equivalent/sim_reflection.hpp omits it, which
-    turns the frame by the wrong matrix).  sim_reflection.hpp is read from the
-    checkout, changed in memory and piped to the compiler ahead of the
-    harness, whose own #include of it is then a no-op (include guard);
-    nothing is written."""
+# Wrappers that move the results of the transcendental functions the
+# reference's renderer calls by one ulp on about an eighth of the inputs
+# (chosen by a hash of the argument): the reference rebuilt with them shows how
+# far its own images move when only the math library's rounding changes.
+MATH_ULP_PRELUDE = r"""
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+static inline float clr_ulp_off(float r, float x) {
+    uint32_t u;
+    std::memcpy(&u, &x, 4);
+    u ^= u >> 15; u *= 0x2c1b3c6du; u ^= u >> 12; u *= 0x297a2d39u; u ^= u >> 15;
+    if ((u & 7u) != 0u) return r;
+    return std::nextafter(r, (u & 8u) ? INFINITY : -INFINITY);
+}
+static inline float clr_sinf(float x) { return clr_ulp_off(::sinf(x), x); }
+static inline float clr_cosf(float x) { return clr_ulp_off(::cosf(x), x); }
+static inline float clr_asinf(float x) { return clr_ulp_off(::asinf(x), x); }
+static inline float clr_acosf(float x) { return clr_ulp_off(::acosf(x), x); }
+static inline float clr_atanf(float x) { return clr_ulp_off(::atanf(x), x); }
+static inline float clr_atan2f(float y, float x) { return clr_ulp_off(::atan2f(y, x), x + y); }
+static inline float clr_expf(float x) { return clr_ulp_off(::expf(x), x); }
+static inline float clr_logf(float x) { return clr_ulp_off(::logf(x), x); }
+static inline float clr_powf(float x, float y) { return clr_ulp_off(::powf(x, y), x * y); }
+#define sinf clr_sinf
+#define cosf clr_cosf
+#define asinf clr_asinf
+#define acosf clr_acosf
+#define atanf clr_atanf
+#define atan2f clr_atan2f
+#define expf clr_expf
+#define logf clr_logf
+#define powf clr_powf
+"""
+
+
+def build_ref_kernel_bump(out: Path, harness: Path, stubs: Path, eq: Path, perturb_math: bool = False) -> None:
+    """The LBVH harness over the reference's CPU renderer with two changes:
+    * the one line where that renderer departs from its OpenCL kernel is put
+      back as the kernel has it: the bump frame's rotation axis is normalised
+      before use (OpenCL/reflection.cl:210; Equivalent/sim_reflection.hpp
+      omits it, which turns the frame by the wrong matrix);
+    * the path-length cap (ray.depth > 99, sim_pathtracer.hpp:167; the
+      kernel's pathtracer.cl:166) reads a variable, set by ref_set_max_depth,
+      so that the renderer can run at the benchmarked depths (5 and 8);
+      it starts at the reference's 99.
+    sim_reflection.hpp and sim_pathtracer.hpp are read from the checkout,
+    changed in memory and piped to the compiler ahead of the harness (whose
+    own include of sim_pathtracer.hpp is then skipped, and whose include of
+    sim_reflection.hpp is a no-op by its include guard); nothing is written.
+    perturb_math prepends MATH_ULP_PRELUDE (the floor measurement build)."""
     text = (eq / "sim_reflection.hpp").read_text()
     anchor = "float sinTH = fminf(length(ax), 1.0f);\n            if (sinTH > 0.0001f) {\n"
     if text.count(anchor) != 1:
         raise RuntimeError("oracle build: the bump block of sim_reflection.hpp is not where expected")
     text = text.replace(anchor, anchor + "                ax = normalize(ax);\n")
-    src = "#include <cstdint>\n#include <cstring>\n#include <vector>\n" + text + '\n#include "ref_harness.cpp"\n'
+    pt = (eq / "sim_pathtracer.hpp").read_text()
+    cap = "if (ray.depth > 99) {"
+    if pt.count(cap) != 1:
+        raise RuntimeError("oracle build: the depth cap of sim_pathtracer.hpp is not where expected")
+    pt = pt.replace(cap, "if (ray.depth > clr_ref_depth_cap) {")
+    src = ((MATH_ULP_PRELUDE if perturb_math else "") +
+           "#include <cstdint>\n#include <cstring>\n#include <vector>\n"
+           "static int clr_ref_depth_cap = 99;\n#define CLR_REF_PIPED_PATHTRACER 1\n" + text + "\n" + pt +
+           '\n#include "ref_harness.cpp"\n')
     res = subprocess.run(["g++", "-std=c++17", "-w", *CFLAGS, "-ftrivial-auto-var-init=pattern", "-D__USE_LBVH",
                           f"-I{stubs}", f"-I{eq}", f"-I{REF_DIR / 'OpenCL_PathTracer'}", f"-I{harness.parent}",
                           "-x", "c++", "-", "-o", str(out)], input=src, capture_output=True, text=True)

@@ -263,6 +263,212 @@ int orc_lbvh_build(const float* vx, const float* vy, const float* vz, const uint
     return ORC_OK;
 }
 
+/* ------------------------------------------ the same build on all host cores
+ *
+ * orc_lbvh_build_mt is orc_lbvh_build run data-parallel, stage by stage, the
+ * way the reference's kernels run on an OpenCL device: calcAABBs and
+ * calcMortonCodes per triangle, unifyAABBs as a reduction, each of the b
+ * sort rounds as a stable split on its 3-bit digit (per-thread digit counts
+ * over contiguous chunks, a scan over digit-major (digit, chunk) pairs, a
+ * scatter: the blockwiseSort / calcBlockwiseHistograms / GlobalScan /
+ * globalScatter round of LBVHBuilder.cpp:263-287), constructBinaryRadixTree
+ * per internal node, and calcNodeAABBs as the reference's bottom-up climb with
+ * an atomic arrival counter per node (lbvh_construction.cl:415-492).  Every
+ * stage computes the serial build's values, so the outputs are identical.
+ * It is the CPU baseline of the build (the reference's OpenCL kernels cannot
+ * run on a host without an OpenCL driver); `threads` <= 0 uses all cores. */
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+static void karras_node(const uint32_t* q, const uint32_t* idx, uint32_t n, uint32_t bits, uint32_t g,
+                        orc_inode* inodes, uint32_t* parents) {
+    const uint32_t* qi = q + 3u * idx[g];
+    const int64_t gi = (int64_t)g, nn = (int64_t)n;
+    int8_t commonR = num_common_bits(q, idx, nn, bits, qi, gi, gi + 1);
+    int8_t commonL = num_common_bits(q, idx, nn, bits, qi, gi, gi - 1);
+    int8_t d = sign8((int)commonR - (int)commonL);
+    int8_t minNum = d > 0 ? commonL : commonR;
+    int64_t lMax = 2;
+    while (num_common_bits(q, idx, nn, bits, qi, gi, gi + lMax * d) > minNum) lMax <<= 1;
+    int64_t l = 0;
+    for (int64_t t = lMax >> 1; t >= 1; t >>= 1)
+        if (num_common_bits(q, idx, nn, bits, qi, gi, gi + (l + t) * d) > minNum) l += t;
+    int64_t otherEnd = gi + l * d;
+    int8_t numNode = num_common_bits(q, idx, nn, bits, qi, gi, otherEnd);
+    int64_t split = 0;
+    float scale = 0.5f;
+    for (;;) {
+        uint32_t t = (uint32_t)ceilf((float)(uint32_t)l * scale);
+        if (num_common_bits(q, idx, nn, bits, qi, gi, gi + (split + (int64_t)t) * d) > numNode) split += t;
+        if (t <= 1) break;
+        scale *= 0.5f;
+    }
+    int64_t splitPos = gi + split * d + (d < 0 ? d : 0);
+    orc_inode* in = inodes + g;
+    memset(in, 0, sizeof(*in));
+    int64_t lo = gi < otherEnd ? gi : otherEnd, hi = gi < otherEnd ? otherEnd : gi;
+    int leftIsLeaf = lo == splitPos, rightIsLeaf = hi == splitPos + 1;
+    in->isChild[0] = (uint8_t)leftIsLeaf;
+    in->c[0] = (uint32_t)splitPos;
+    parents[leftIsLeaf ? (uint32_t)splitPos : n + (uint32_t)splitPos] = g;
+    in->isChild[1] = (uint8_t)rightIsLeaf;
+    in->c[1] = (uint32_t)(splitPos + 1);
+    parents[rightIsLeaf ? (uint32_t)(splitPos + 1) : n + (uint32_t)(splitPos + 1)] = g;
+}
+
+int orc_lbvh_build_mt(const float* vx, const float* vy, const float* vz, const uint32_t* tri,
+                      uint32_t n, uint32_t bits,
+                      orc_inode* inodes, orc_lnode* lnodes, uint32_t* parents,
+                      uint32_t* sorted_idx, float* scene_box, int threads) {
+    if (bits < 1 || bits > 21) return ORC_EINVAL;
+    if (n == 0) return ORC_OK;
+    int nt = 1;
+#ifdef _OPENMP
+    nt = threads > 0 ? threads : omp_get_max_threads();
+#else
+    (void)threads;
+#endif
+    float* box = (float*)malloc(sizeof(float) * 9u * n);
+    uint32_t* q = (uint32_t*)malloc(sizeof(uint32_t) * 3u * n);
+    uint32_t* idx = (uint32_t*)malloc(sizeof(uint32_t) * n);
+    uint32_t* tmp = (uint32_t*)malloc(sizeof(uint32_t) * n);
+    uint32_t* cnt = (uint32_t*)malloc(sizeof(uint32_t) * 8u * (uint32_t)nt);
+    uint32_t* arrivals = (uint32_t*)calloc(n > 1 ? n - 1 : 1, sizeof(uint32_t));
+    float* red = (float*)malloc(sizeof(float) * 6u * (uint32_t)nt);
+    if (!box || !q || !idx || !tmp || !cnt || !arrivals || !red) {
+        free(box); free(q); free(idx); free(tmp); free(cnt); free(arrivals); free(red);
+        return ORC_ENOMEM;
+    }
+    const int64_t N = (int64_t)n;
+    const uint32_t numDivs = 1u << bits;
+    float smin[3], smax[3], ssize[3];
+#ifdef _OPENMP
+#pragma omp parallel num_threads(nt)
+#endif
+    {
+        int tid = 0, T = 1;
+#ifdef _OPENMP
+        tid = omp_get_thread_num();
+        T = omp_get_num_threads();
+#endif
+        const int64_t c0 = N * tid / T, c1 = N * (tid + 1) / T;  /* this thread's chunk */
+        /* calcAABBs, lbvh_construction.cl:81-96; unifyAABBs per chunk */
+        float mn3[3] = {INFINITY, INFINITY, INFINITY}, mx3[3] = {-INFINITY, -INFINITY, -INFINITY};
+        for (int64_t t = c0; t < c1; ++t) {
+            uint32_t a = vidx(tri, (uint32_t)t, 0), b = vidx(tri, (uint32_t)t, 1), c = vidx(tri, (uint32_t)t, 2);
+            const float p0[3] = {vx[a], vy[a], vz[a]}, p1[3] = {vx[b], vy[b], vz[b]}, p2[3] = {vx[c], vy[c], vz[c]};
+            for (int k = 0; k < 3; ++k) {
+                float mn = fminf(p0[k], fminf(p1[k], p2[k]));
+                float mx = fmaxf(p0[k], fmaxf(p1[k], p2[k]));
+                box[9u * t + k] = mn;
+                box[9u * t + 3 + k] = mx;
+                box[9u * t + 6 + k] = (mn + mx) * 0.5f;
+                mn3[k] = fminf(mn3[k], mn);
+                mx3[k] = fmaxf(mx3[k], mx);
+            }
+        }
+        for (int k = 0; k < 3; ++k) { red[6 * tid + k] = mn3[k]; red[6 * tid + 3 + k] = mx3[k]; }
+#ifdef _OPENMP
+#pragma omp barrier
+#pragma omp single
+#endif
+        {
+            for (int k = 0; k < 3; ++k) { smin[k] = INFINITY; smax[k] = -INFINITY; }
+            for (int u = 0; u < T; ++u)
+                for (int k = 0; k < 3; ++k) {
+                    smin[k] = fminf(smin[k], red[6 * u + k]);
+                    smax[k] = fmaxf(smax[k], red[6 * u + 3 + k]);
+                }
+            for (int k = 0; k < 3; ++k) ssize[k] = smax[k] - smin[k];
+        }
+        /* calcMortonCodes, lbvh_construction.cl:169-181 */
+        for (int64_t t = c0; t < c1; ++t) {
+            for (int k = 0; k < 3; ++k) {
+                float normPos = (box[9u * t + 6 + k] - smin[k]) / ssize[k];
+                uint32_t v = cvt_rtz_u32(normPos * (float)numDivs);
+                q[3u * t + k] = v < numDivs - 1u ? v : numDivs - 1u;
+            }
+            idx[t] = (uint32_t)t;
+        }
+        /* b rounds of a stable split on the round's 3-bit digit */
+        uint32_t *src = idx, *dst = tmp;
+        for (uint32_t bit = 0; bit < bits; ++bit) {
+#ifdef _OPENMP
+#pragma omp barrier
+#endif
+            uint32_t c8[8] = {0};
+            for (int64_t i = c0; i < c1; ++i) {
+                const uint32_t* qq = q + 3u * src[i];
+                c8[((qq[0] >> bit) & 1u) | (((qq[1] >> bit) & 1u) << 1) | (((qq[2] >> bit) & 1u) << 2)]++;
+            }
+            for (int d = 0; d < 8; ++d) cnt[8 * tid + d] = c8[d];
+#ifdef _OPENMP
+#pragma omp barrier
+#endif
+            /* offset of (digit d, chunk tid) = all smaller digits + digit d of earlier chunks */
+            uint32_t off[8];
+            uint32_t base = 0;
+            for (int d = 0; d < 8; ++d) {
+                uint32_t before = 0, total = 0;
+                for (int u = 0; u < T; ++u) {
+                    if (u < tid) before += cnt[8 * u + d];
+                    total += cnt[8 * u + d];
+                }
+                off[d] = base + before;
+                base += total;
+            }
+            for (int64_t i = c0; i < c1; ++i) {
+                const uint32_t* qq = q + 3u * src[i];
+                uint32_t d = ((qq[0] >> bit) & 1u) | (((qq[1] >> bit) & 1u) << 1) | (((qq[2] >> bit) & 1u) << 2);
+                dst[off[d]++] = src[i];
+            }
+            uint32_t* sw = src; src = dst; dst = sw;
+        }
+#ifdef _OPENMP
+#pragma omp barrier
+#endif
+        /* leaves, then constructBinaryRadixTree (lbvh_construction.cl:342-410) */
+        for (int64_t g = c0; g < c1; ++g) {
+            uint32_t objIdx = src[g];
+            orc_lnode* ln = lnodes + g;
+            memset(ln, 0, sizeof(*ln));
+            for (int k = 0; k < 3; ++k) { ln->min[k] = box[9u * objIdx + k]; ln->max[k] = box[9u * objIdx + 3 + k]; }
+            ln->objIdx = objIdx;
+            sorted_idx[g] = objIdx;
+        }
+        for (int64_t g = c0; g < c1; ++g)
+            if (g < N - 1) karras_node(q, src, n, bits, (uint32_t)g, inodes, parents);
+#ifdef _OPENMP
+#pragma omp barrier
+#endif
+        /* calcNodeAABBs: from each leaf, climb; the second child to arrive at
+         * a node (acquire-release counter) merges both boxes and goes on */
+        if (n >= 2)
+            for (int64_t g = c0; g < c1; ++g) {
+                uint32_t node = parents[g];
+                for (;;) {
+                    if (__atomic_fetch_add(&arrivals[node], 1u, __ATOMIC_ACQ_REL) == 0) break;
+                    orc_inode* in = inodes + node;
+                    const float *amin, *amax, *bmin, *bmax;
+                    if (in->isChild[0]) { amin = lnodes[in->c[0]].min; amax = lnodes[in->c[0]].max; }
+                    else { amin = inodes[in->c[0]].min; amax = inodes[in->c[0]].max; }
+                    if (in->isChild[1]) { bmin = lnodes[in->c[1]].min; bmax = lnodes[in->c[1]].max; }
+                    else { bmin = inodes[in->c[1]].min; bmax = inodes[in->c[1]].max; }
+                    for (int k = 0; k < 3; ++k) {
+                        in->min[k] = fminf(amin[k], bmin[k]);
+                        in->max[k] = fmaxf(amax[k], bmax[k]);
+                    }
+                    if (node == 0) break;
+                    node = parents[n + node];
+                }
+            }
+    }
+    if (scene_box) for (int k = 0; k < 3; ++k) { scene_box[k] = smin[k]; scene_box[3 + k] = smax[k]; }
+    free(box); free(q); free(idx); free(tmp); free(cnt); free(arrivals); free(red);
+    return ORC_OK;
+}
+
 /* ---------------------------------------------------------------- traversal */
 
 typedef struct { float x, y, z; } v3;

@@ -16,7 +16,9 @@
 #include <cstring>
 #include <vector>
 
+#ifndef CLR_REF_PIPED_PATHTRACER  // else its text was piped ahead of this file
 #include "sim_pathtracer.hpp"
+#endif
 #ifdef __USE_LBVH
 #include "sim_bvh_visualizer.hpp"
 #endif
@@ -113,6 +115,15 @@ int ref_render(const float* verts, const float* normals, const float* tangents, 
             }
     return 0;
 }
+
+#ifdef CLR_REF_PIPED_PATHTRACER
+/* The depth cap of the piped renderer: a path stops after max_depth bounces
+ * (the reference's constant, ray.depth > 99, is max_depth = 100). */
+int ref_set_max_depth(uint32_t max_depth) {
+    clr_ref_depth_cap = (int)max_depth - 1;
+    return 0;
+}
+#endif
 
 /* sim::bvh_visualizer over a width x height image (one NDRange, offset 0). */
 int ref_bvh_visualizer(const float* verts, const float* normals, const float* tangents, const float* uvs,

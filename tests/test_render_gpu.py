@@ -12,8 +12,9 @@ off on an eighth of the inputs).  Bars (stated here) for the reference
 traversal order: relative RMSE of the image <= 1e-4 of its mean, mean
 radiance within 1e-5, and >= 99.9 % of pixels within 1e-3 relative; a
 semantic difference (a shadow rule, a pdf) shows as 1e-3 or more.  The
-nearer-child-first order picks other triangles on exact ties, so its paths
-part more often: bars 2 % and 0.5 % for it.
+nearer-child-first traversal replays in the reference's order every ray whose
+hit could depend on the order, so its images equal the reference order's
+bit for bit.
 """
 import numpy as np
 import pytest
@@ -111,15 +112,24 @@ def test_wavefront_equals_megakernel(cuda, variant):
 
 
 @pytest.mark.gpu
-def test_render_ordered_traversal_agrees(cuda):
-    """Nearer-child-first traversal in the renderer: same image statistics."""
+@pytest.mark.parametrize("variant", ["plain", "env"])
+@pytest.mark.parametrize("wavefront", [False, True])
+def test_render_ordered_traversal_agrees(cuda, variant, wavefront):
+    """Nearer-child-first traversal with replay in the renderer: the image and
+    random states are identical to the reference-order traversal's, so the
+    same bars against the reference's own renderer hold."""
     g = np.load(GOLDEN)
     w, h, spp = int(g["width"]), int(g["height"]), int(g["spp"])
-    ds = DeviceScene(scenes.cornell_box(w, h), cuda)
-    rng, pix = ds.new_frame()
-    ds.render(rng, pix, spp, max_depth=100, ordered=True)
-    rel_rmse, mean_err, frac_close = metrics(pix[:, :3].cpu().numpy(), g["plain"])
-    assert rel_rmse <= 0.02 and mean_err <= 0.005, (rel_rmse, mean_err, frac_close)
+    ds = DeviceScene(scenes.cornell_box(w, h, env=env_map() if variant == "env" else None), cuda)
+    rng_a, pix_a = ds.new_frame()
+    ds.render(rng_a, pix_a, spp, max_depth=100, ordered=False, wavefront=wavefront)
+    rng_b, pix_b = ds.new_frame()
+    ds.render(rng_b, pix_b, spp, max_depth=100, ordered=True, wavefront=wavefront)
+    torch.cuda.synchronize()
+    assert torch.equal(pix_a, pix_b) and torch.equal(rng_a, rng_b)
+    rel_rmse, mean_err, frac_close = metrics(pix_b[:, :3].cpu().numpy(), g[variant])
+    assert rel_rmse <= 1e-4 and mean_err <= 1e-5 and frac_close >= 0.999, (rel_rmse, mean_err, frac_close)
+    assert _lib.device_status() == 0
 
 
 @pytest.mark.gpu
