@@ -29,7 +29,10 @@ run here; its restatement in oracle/ runs stage by stage on all host cores, as
 the reference's kernels would on a CPU OpenCL device).
 
 Multi-GPU: the build does not shard; --gpus N runs N independent replicas
-(one process per GPU under torchrun), value = total triangles / max time.
+(one process per GPU, started through torchrun by this script itself when no
+launcher started it), value = total triangles / max time.  With more than one
+process the terrain render is also split into row bands, one per GPU, and
+gathered on rank 0 (render_bands).
 """
 from __future__ import annotations
 
@@ -94,6 +97,8 @@ def parse():
     ap.add_argument("--batched-scenes", type=int, default=512)
     ap.add_argument("--adjoint-res", type=int, default=512)
     ap.add_argument("--adjoint-spp", type=int, default=32)
+    ap.add_argument("--band-spp", type=int, default=16,
+                    help="samples per pixel of the row-band terrain render (more than one process)")
     return ap.parse_args()
 
 
@@ -378,6 +383,34 @@ def bench_render_terrain(dev, spp=64, forms=("megakernel_ordered", "wavefront_ex
     out["env_distribution"] = {"texels": ew * eh, "us": env_us, "gbs": 16 * ew * eh / env_us / 1e3,
                                "frac_of_hbm": 16 * ew * eh / env_us / 1e3 / peak}
     return out
+
+
+def bench_render_bands(dev, spp: int) -> dict:
+    """The terrain image split into row bands, one per process (each GPU
+    renders its band with the wavefront form, clr_render_wavefront_rows), and
+    gathered on rank 0; the timed region holds the renders and the gather.
+    Whole-job Msamples/s over all processes."""
+    import torch
+
+    from clear_gb300 import scenes, shard
+    from clear_gb300.render import DeviceScene
+
+    sc = scenes.terrain_scene()
+    ds = DeviceScene(sc, dev)
+    w, h = sc.width, sc.height
+    rng_all, _ = ds.new_frame()
+
+    def render_band(y0, y1):
+        rng = rng_all.view(h * w, 4)[y0 * w:y1 * w].clone()
+        pix = torch.zeros(((y1 - y0) * w, 4), dtype=torch.float32, device=dev)
+        ds.render(rng, pix, spp, max_depth=8, ordered=True, rows=(y0, y1))
+        return pix
+
+    shard.timed_band_render(render_band, h, w, steps=1)  # warm-up
+    dt, img = shard.timed_band_render(render_band, h, w, steps=1)
+    return {"workload": f"terrain 2.23M tris, 1920x1080, {spp} spp, depth 8, row bands + gather to rank 0",
+            "samples": w * h * spp, "s_per_frame": dt, "msamples_s": w * h * spp / dt / 1e6,
+            "gathered_pixels": None if img is None else int(img.shape[0])}
 
 
 def bench_adjoint(dev, spp=32, res=512) -> dict:
@@ -700,6 +733,7 @@ def run_ours(args):
     render_terrain = bench_render_terrain(dev) if args.render else None
     adjoint = bench_adjoint(dev) if args.render else None
     batched = bench_batched(dev, args.batched_scenes) if args.render else None
+    bands = bench_render_bands(dev, args.band_spp) if args.render and world > 1 else None
     hit_frac = float((hid >= 0).float().mean().item())
     occ_frac = float(occ.float().mean().item())
     clk = clocks.stop()
@@ -758,6 +792,7 @@ def run_ours(args):
         "render_terrain": render_terrain,
         "adjoint": adjoint,
         "batched": batched,
+        "render_bands": bands,
         "gpu_launches": launches_per_build * args.steps,
         "clocks": clk,
         "device_error_bits": dev_err,
@@ -771,6 +806,11 @@ def run_ours(args):
 
 def main():
     args = parse()
+    if args.gpus > 1 and "WORLD_SIZE" not in os.environ:
+        # started without a launcher: one process per GPU of this node
+        from clear_gb300 import shard
+
+        sys.exit(shard.launch_local(args.gpus, os.path.abspath(__file__), sys.argv[1:]))
     if args.render_only:
         import torch
 

@@ -295,7 +295,7 @@ __global__ void __launch_bounds__(kAdThreads) k_ad_init(DScene sc, AdState S, ui
 
 // Closest hit of every queued path of both passes.
 template <bool kOrdered>
-__global__ void __launch_bounds__(kAdThreads) k_ad_extend(DScene sc, AdState S, int cur) {
+__global__ void __launch_bounds__(kAdThreads, 8) k_ad_extend(DScene sc, AdState S, int cur) {
     const uint32_t n0 = S.count[2 * cur], n = n0 + S.count[2 * cur + 1];
     const uint32_t* q0 = queue(S, cur, 0);
     const uint32_t* q1 = queue(S, cur, 1);
@@ -430,9 +430,13 @@ __device__ __forceinline__ void next_event(const DScene& sc, const BSDF& bsdf, c
 }
 
 // Primal pass: the forward path tracer (render_wf.cu k_wf_shade) summing the
-// sample's radiance into L.  A finished sample is queued for its replay.
+// sample's radiance into L.  A finished sample is queued for its replay,
+// unless its pixel's loss weight is zero: its replay would add nothing to any
+// gradient, and the random-number state after the primal pass is the state
+// the replay would end in, so the pixel goes on with its next sample.
 __global__ void __launch_bounds__(kAdThreads) k_ad_primal(DScene sc, AdState S, int cur, uint32_t width,
-                                                          uint32_t* __restrict__ rand_states, uint32_t max_depth) {
+                                                          uint32_t* __restrict__ rand_states, uint32_t max_depth,
+                                                          const float4* __restrict__ dloss, uint32_t spp) {
     const uint32_t n = S.count[2 * cur];
     const uint32_t* qin = queue(S, cur, 0);
     const Camera cam = load_camera(sc);
@@ -507,7 +511,17 @@ __global__ void __launch_bounds__(kAdThreads) k_ad_primal(DScene sc, AdState S, 
                     }
                 }
             }
-            if (ended) {
+            cont = true;
+            const float4 g = __ldg(dloss + p);
+            if (ended && g.x == 0.0f && g.y == 0.0f && g.z == 0.0f) {
+                if (m.z + 1 < spp) {
+                    S.rng0[p] = rng_bits(rng);
+                    ad_start(cam, S, p, width, rng, m.z + 1, 0u);
+                } else {
+                    S.misc[p] = make_uint4(depth, sampledType, m.z + 1, 1u);
+                    cont = false;
+                }
+            } else if (ended) {
                 // replay the sample from its first random number
                 rng = rng_from(S.rng0[p]);
                 ad_start(cam, S, p, width, rng, m.z, 1u);
@@ -518,7 +532,6 @@ __global__ void __launch_bounds__(kAdThreads) k_ad_primal(DScene sc, AdState S, 
                 S.alpha[p] = make_float4(alpha.x, alpha.y, alpha.z, initY);
                 S.misc[p] = make_uint4(depth, sampledType, m.z, 0u);
             }
-            cont = true;
             S.L[p] = make_float4(L.x, L.y, L.z, 0.f);
             reinterpret_cast<uint4*>(rand_states)[p] = rng_bits(rng);
         }
@@ -754,7 +767,7 @@ __global__ void __launch_bounds__(kAdThreads) k_ad_replay(DScene sc, AdState S, 
 }
 
 template <bool kOrdered>
-__global__ void __launch_bounds__(kAdThreads) k_ad_shadow(DScene sc, AdState S, AdParams P) {
+__global__ void __launch_bounds__(kAdThreads, 8) k_ad_shadow(DScene sc, AdState S, AdParams P) {
     const uint32_t n = S.count[4];
     if (blockIdx.x * blockDim.x >= n) return;
     const GradSink sink = sink_begin(P);
@@ -933,7 +946,7 @@ extern "C" int clr_render_adjoint(const clr_scene* scene, uint32_t width, uint32
         if (ordered) k_ad_extend<true><<<grid, kAdThreads, 0, st>>>(sc, S, cur);
         else k_ad_extend<false><<<grid, kAdThreads, 0, st>>>(sc, S, cur);
         k_ad_reset<<<1, 1, 0, st>>>(S, cur ^ 1);
-        k_ad_primal<<<grid, kAdThreads, 0, st>>>(sc, S, cur, width, rand_states, max_depth);
+        k_ad_primal<<<grid, kAdThreads, 0, st>>>(sc, S, cur, width, rand_states, max_depth, P.dloss, spp);
         if (tape) k_ad_replay<true><<<grid, kAdThreads, smem, st>>>(sc, S, P, cur, width, rand_states, spp, max_depth);
         else k_ad_replay<false><<<grid, kAdThreads, smem, st>>>(sc, S, P, cur, width, rand_states, spp, max_depth);
         if (ordered) k_ad_shadow<true><<<grid, kAdThreads, smem, st>>>(sc, S, P);

@@ -130,7 +130,7 @@ __global__ void __launch_bounds__(kBtTraceMaxThreads) k_bt_init(BtArgs A, BtStat
 }
 
 template <bool kOrdered>
-__global__ void __launch_bounds__(kBtTraceMaxThreads) k_bt_extend(BtArgs A, BtState S, int cur) {
+__global__ void __launch_bounds__(kBtTraceMaxThreads, 4) k_bt_extend(BtArgs A, BtState S, int cur) {
     const uint32_t n = S.count[cur];
     uint2 stack[kStackSize];
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
@@ -313,7 +313,7 @@ __global__ void __launch_bounds__(kBtShadeThreads) k_bt_shade(BtArgs A, BtState 
 }
 
 template <bool kOrdered>
-__global__ void __launch_bounds__(kBtTraceMaxThreads) k_bt_shadow(BtArgs A, BtState S) {
+__global__ void __launch_bounds__(kBtTraceMaxThreads, 4) k_bt_shadow(BtArgs A, BtState S) {
     const uint32_t n = S.count[2];
     uint2 stack[kStackSize];
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {

@@ -133,9 +133,9 @@ struct SearchResult {
 
 // The reference's order (bvh_traversal.cl:191-208).
 template <bool kCount, bool kAlpha>
-static __device__ CLR_TRAVERSAL_ATTR SearchResult search_reference_order(const DScene& sc, const Ray& ray, float ix,
-                                                                         float iy, float iz, float root_entry,
-                                                                         uint2* stack, uint32_t* boxes) {
+static __device__ __forceinline__ SearchResult search_reference_order(const DScene& sc, const Ray& ray, float ix,
+                                                                     float iy, float iz, float root_entry,
+                                                                     uint2* stack, uint32_t* boxes) {
     float t = INFINITY;
     uint32_t best = kNone32;
     int sp = 0;
@@ -177,9 +177,9 @@ static __device__ CLR_TRAVERSAL_ATTR SearchResult search_reference_order(const D
 // (traverse.cuh); sets `replay` when the ray must be searched again in the
 // reference's order.  Not for scenes with cutouts.
 template <bool kCount>
-static __device__ CLR_TRAVERSAL_ATTR SearchResult search_nearer_first(const DScene& sc, const Ray& ray, float ix,
-                                                                      float iy, float iz, float root_entry,
-                                                                      uint2* stack, uint32_t* boxes, bool& replay) {
+static __device__ __forceinline__ SearchResult search_nearer_first(const DScene& sc, const Ray& ray, float ix,
+                                                                   float iy, float iz, float root_entry,
+                                                                   uint2* stack, uint32_t* boxes, bool& replay) {
     float t = INFINITY, tr = INFINITY;  // the bound and its relaxed form
     uint32_t best = kNone32;
     float gbest = -INFINITY, t2 = INFINITY;
@@ -187,8 +187,7 @@ static __device__ CLR_TRAVERSAL_ATTR SearchResult search_nearer_first(const DSce
     stack[sp++] = make_uint2(__float_as_uint(sc.root_box[3]), __float_as_uint(root_entry));
     for (uint32_t guard = 0; sp > 0 && guard < sc.num_tris; ++guard) {
         --sp;
-        const float key = __uint_as_float(stack[sp].y);
-        if (key > tr) continue;
+        if (__uint_as_float(stack[sp].y) > tr) continue;
         if (kCount) ++boxes[0];
         const NodeBoxes nb = load_node(sc.nodes, stack[sp].x);
         float e0, e1;
@@ -202,9 +201,9 @@ static __device__ CLR_TRAVERSAL_ATTR SearchResult search_nearer_first(const DSce
             const int c = both_internal ? (swap ? k : 1 - k) : (swap ? 1 - k : k);
             const uint32_t ref = c ? nb.ref1 : nb.ref0;
             if (!(c ? p1 : p0)) continue;
-            const float kc = fmaxf(c ? e1 : e0, key);
+            const float e = c ? e1 : e0;
             if (ref & kLeafBit) {
-                if (kc > tr) continue;
+                if (e > tr) continue;
                 if (kCount) ++boxes[1];
                 const uint32_t leaf = ref & ~kLeafBit;
                 float tt, b1, b2;
@@ -216,12 +215,12 @@ static __device__ CLR_TRAVERSAL_ATTR SearchResult search_nearer_first(const DSce
                     t = tt;
                     tr = relaxed_bound(tt, replay_scale(sc.root_box));
                     best = leaf;
-                    gbest = kc;
+                    gbest = e;
                 } else {
                     t2 = fminf(t2, tt);
                 }
             } else if (sp < kStackSize) {
-                stack[sp++] = make_uint2(ref, __float_as_uint(kc));
+                stack[sp++] = make_uint2(ref, __float_as_uint(e));
             } else {
                 clr_raise(CLR_DEVERR_STACK);
             }
@@ -242,8 +241,8 @@ static __device__ CLR_TRAVERSAL_ATTR SearchResult search_nearer_first(const DSce
 // record, which makes the record depend on the order in ways the replay test
 // does not cover.
 template <bool kOrdered, bool kCount, bool kAlpha>
-static __device__ __forceinline__ uint32_t intersect_search(const DScene& sc, f3 org, f3 dir, Hit& h, uint2* stack,
-                                                            uint32_t* boxes) {
+static __device__ CLR_TRAVERSAL_ATTR uint32_t intersect_search(const DScene& sc, f3 org, f3 dir, Hit& h, uint2* stack,
+                                                               uint32_t* boxes) {
     const Ray ray{org.x, org.y, org.z, INFINITY, dir.x, dir.y, dir.z};
     const float ix = 1.0f / dir.x, iy = 1.0f / dir.y, iz = 1.0f / dir.z;
     float entry;

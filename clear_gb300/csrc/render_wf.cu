@@ -96,7 +96,7 @@ __global__ void __launch_bounds__(kWfThreads) k_wf_init(DScene sc, WfState S, ui
 }
 
 template <bool kOrdered>
-__global__ void __launch_bounds__(kWfThreads) k_wf_extend(DScene sc, WfState S, int cur) {
+__global__ void __launch_bounds__(kWfThreads, 8) k_wf_extend(DScene sc, WfState S, int cur) {
     const uint32_t n = S.count[cur];
     uint2 stack[kStackSize];
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
@@ -255,7 +255,7 @@ __global__ void __launch_bounds__(kWfThreads) k_wf_shade(DScene sc, WfState S, i
 }
 
 template <bool kOrdered>
-__global__ void __launch_bounds__(kWfThreads) k_wf_shadow(DScene sc, WfState S, float4* __restrict__ pixels) {
+__global__ void __launch_bounds__(kWfThreads, 8) k_wf_shadow(DScene sc, WfState S, float4* __restrict__ pixels) {
     const uint32_t n = S.count[2];
     uint2 stack[kStackSize];
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {

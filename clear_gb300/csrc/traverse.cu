@@ -34,7 +34,7 @@ struct ClosestState {
     float t;
     uint32_t best;
     float tr;         // fast search: the relaxed bound of t,
-    float gbest, t2;  // G(best) and the other candidates' smallest tt
+    float gbest, t2;  // the winner's leaf-box entry and the other candidates' smallest tt
     int sp;
     bool exact;  // searching in the reference's order
 };
@@ -68,9 +68,9 @@ __device__ __forceinline__ void closest_begin(ClosestState& s, const float4* __r
 // One pop of rayIntersection's loop (bvh_traversal.cl:191-208).
 // Reference order (s.exact): children in the fixed order, internal ones
 // pushed with their own entry distance, compared with t when popped.
-// Fast search: nearer child first, boxes keyed by the path maximum of entry
-// distances and culled against the relaxed bound, every reached leaf tested
-// with the bookkeeping of the replay decision (traverse.cuh).
+// Fast search: nearer child first, boxes culled against the relaxed bound,
+// every reached leaf tested with the bookkeeping of the replay decision
+// (traverse.cuh).
 __device__ __forceinline__ void closest_step(ClosestState& s, const float4* __restrict__ nodes,
                                              const float4* __restrict__ tris, uint2* stack, float S) {
     --s.sp;
@@ -92,13 +92,12 @@ __device__ __forceinline__ void closest_step(ClosestState& s, const float4* __re
         const uint32_t ref = c ? nb.ref1 : nb.ref0;
         if (!(c ? p1 : p0)) continue;
         const float e = c ? e1 : e0;
-        const float kc = s.exact ? e : fmaxf(e, key);
         if (ref & kLeafBit) {
             if (s.exact) {
                 if (!(e > s.t)) tri_hit(tris, ref & ~kLeafBit, s.ray, s.t, s.best);
                 continue;
             }
-            if (kc > s.tr) continue;
+            if (e > s.tr) continue;
             const uint32_t leaf = ref & ~kLeafBit;
             const float4 a = __ldg(tris + 3u * leaf), b = __ldg(tris + 3u * leaf + 1u), cc = __ldg(tris + 3u * leaf + 2u);
             float tt, b1, b2;
@@ -108,12 +107,12 @@ __device__ __forceinline__ void closest_step(ClosestState& s, const float4* __re
                 s.t = tt;
                 s.tr = relaxed_bound(tt, S);
                 s.best = __float_as_uint(a.w);
-                s.gbest = kc;
+                s.gbest = e;
             } else {
                 s.t2 = fminf(s.t2, tt);
             }
         } else {
-            if (s.sp < kStackSize) stack[s.sp++] = make_uint2(ref, __float_as_uint(kc));
+            if (s.sp < kStackSize) stack[s.sp++] = make_uint2(ref, __float_as_uint(e));
             else clr_raise(CLR_DEVERR_STACK);
         }
     }

@@ -173,18 +173,22 @@ __device__ __forceinline__ NodeBoxes load_node(const float4* __restrict__ nodes,
 // distance over candidate j's boxes.  Exact arithmetic gives G(j) <= tt(j);
 // with rounding G(j) can exceed tt(j) by a few ulp ("inversion").
 //
-// The fast search culls a box when its path maximum of entries, pm, exceeds
-// the relaxed bound t + kReplayDelta (|t| + S) (S: the scene box's largest
-// extent / 16), tests every leaf it reaches, and records
+// The fast search culls a box when its entry distance exceeds the relaxed
+// bound t + kReplayDelta (|t| + S) (S: the scene box's largest extent / 16),
+// tests every leaf it reaches, and records
 //   T, B      the smallest tt and the triangle that first reached it,
-//   G(B)      the path maximum of B's boxes,
+//   G(B)      the largest entry distance over B's boxes, which is its leaf
+//             box's: an ancestor's entry that is >= 0 comes from an axis on
+//             which the origin lies outside the ancestor's slab, hence outside
+//             the leaf's slab on the same side with the leaf's plane no nearer,
+//             and (plane - o) / d is monotone in the plane under rounding,
 //   t2        the smallest tt of every other candidate it tested.
 // With V = max(T, G(B)), the answer (T, B) is final unless
 //   t2 <= V                                   (a tie or near-tie), or
 //   G(B) > T + kReplayDelta / 4 (|T| + S)     (B's own boxes lie well past it).
 // Proof sketch, assuming no inversion exceeds kReplayDelta / 4 (|tt| + S):
 // every other candidate then has tt > V.  Tested ones by t2 > V.  A culled
-// one lies under a box whose pm exceeded the relaxed bound of a t >= T, so
+// one lies under a box whose entry exceeded the relaxed bound of a t >= T, so
 // its G > T + kReplayDelta (|T| + S) >= V + kReplayDelta / 4 (|V| + S) (as
 // G(B) is within kReplayDelta / 4 (|T| + S) of T), and its tt > V by the
 // inversion bound.  In the reference's search, before B is tested t holds

@@ -15,11 +15,21 @@ split the work without any exchange until the end:
 * each process builds its own BVH (the build is a small fraction of a
   render).
 
-``max_over_ranks`` is the timing reduction (the slowest rank sets the time).
-Every function works with any ``torch.distributed`` backend: NCCL between
-GPUs, gloo on the host.
+``max_over_ranks`` is the timing reduction (the slowest rank sets the time);
+``timed_band_render`` times one band render per rank plus the gather, with
+barriers and device synchronisation around the timed region;
+``launch_local`` starts one process per GPU of this node for a script that
+was run without a launcher.  Every collective works with any
+``torch.distributed`` backend: NCCL between GPUs, gloo on the host.
 """
 from __future__ import annotations
+
+import os
+import socket
+import subprocess
+import sys
+import time
+from typing import Callable
 
 import torch
 import torch.distributed as dist
@@ -88,3 +98,53 @@ def max_over_ranks(values: list[float], device: torch.device | str = "cpu", grou
     if dist.is_initialized() and dist.get_world_size(group) > 1:
         dist.all_reduce(t, op=dist.ReduceOp.MAX, group=group)
     return t.tolist()
+
+
+def timed_band_render(render_band: Callable[[int, int], torch.Tensor], height: int, width: int,
+                      steps: int = 1, group=None) -> tuple[float, torch.Tensor | None]:
+    """Each rank renders its row band `steps` times (render_band(y0, y1)
+    returns the band's accumulation buffer, (y1 - y0) * width pixel rows) and
+    rank 0 gathers the last one; the timed region -- between barriers, with
+    the device synchronised on both sides -- holds the renders and the
+    gather.  Returns (seconds per step, the slowest rank's; the whole image on
+    rank 0, else None)."""
+    world = dist.get_world_size(group) if dist.is_initialized() else 1
+    rank = dist.get_rank(group) if dist.is_initialized() else 0
+    bands = row_bands(height, world)
+    y0, y1 = bands[rank]
+    cuda = torch.cuda.is_available()
+
+    def sync():
+        if cuda:
+            torch.cuda.synchronize()
+        if world > 1:
+            dist.barrier(group=group)
+
+    sync()
+    t0 = time.perf_counter()
+    band = None
+    for _ in range(steps):
+        band = render_band(y0, y1)
+    img = gather_rows(band, bands, width, group=group) if world > 1 else band
+    sync()
+    dt = (time.perf_counter() - t0) / max(steps, 1)
+    dev = band.device if band is not None else "cpu"
+    return max_over_ranks([dt], dev, group)[0], img
+
+
+def _free_port() -> int:
+    with socket.socket() as s_:
+        s_.bind(("127.0.0.1", 0))
+        return s_.getsockname()[1]
+
+
+def launch_local(nprocs: int, script: str, args: list[str], timeout: float | None = None) -> int:
+    """Runs `script` with `args` as `nprocs` processes of one node through
+    torch.distributed.run (rendezvous on 127.0.0.1, a free port); each
+    process reads RANK / LOCAL_RANK / WORLD_SIZE from its environment.
+    Returns the launcher's exit status."""
+    cmd = [sys.executable, "-m", "torch.distributed.run", "--nnodes=1", f"--nproc-per-node={int(nprocs)}",
+           "--master-addr=127.0.0.1", f"--master-port={_free_port()}", script, *args]
+    env = dict(os.environ)
+    env.setdefault("OMP_NUM_THREADS", "1")
+    return subprocess.run(cmd, env=env, timeout=timeout).returncode

@@ -37,7 +37,7 @@ def _setup(dev, width=W, height=H, **kw):
     return sc, info, ds, tex, kind
 
 
-def _target(dev, info, width=W, height=H, seed=11):
+def _target(dev, info, width=W, height=H, seed=11, spp=SPP):
     """Image rendered with perturbed parameters (albedo + N(0, 0.1) clamped to
     [0.01, 0.99], roughness + N(0, 0.05) (x lognormal(0, 0.05) for the
     Ashikhmin exponent), env x lognormal(0, 0.3))."""
@@ -50,14 +50,42 @@ def _target(dev, info, width=W, height=H, seed=11):
     sc, _ = scenes.cornell_adjoint(width, height, albedo=alb, roughness=rough, env=env)
     ds = DeviceScene(sc, dev)
     rng, pix = ds.new_frame()
-    ds.render(rng, pix, SPP, DEPTH, wavefront=True)
-    return pix[:, :3] / SPP
+    ds.render(rng, pix, spp, DEPTH, wavefront=True)
+    return pix[:, :3] / spp
 
 
-def _dloss(pix, target):
+def _dloss(pix, target, spp=SPP):
     d = torch.zeros_like(pix)
-    d[:, :3] = 2.0 * (pix[:, :3] / SPP - target) / SPP
+    d[:, :3] = 2.0 * (pix[:, :3] / spp - target) / spp
     return d
+
+
+def _check_groups(fp, P, info, g, ge, base, seed=2024):
+    """Adjoint against FP64 central differences per parameter group: all 24
+    albedo channels, all 8 roughness values and 32 environment texel channels
+    drawn by a seeded generator among the texels the recorded paths read
+    (chosen from the tape alone, so a texel whose adjoint gradient is wrongly
+    zero is as likely to be drawn as any)."""
+    groups = {"albedo": [], "roughness": [], "env": []}
+    for i, off in enumerate(info["albedo_tex"]):
+        for c in range(3):
+            groups["albedo"].append((g[i, c], fp.fd_texture(P, off, c, H_FD, base)))
+    for i, off in enumerate(info["rough_tex"]):
+        groups["roughness"].append((g[8 + i, 0], fp.fd_texture(P, off, 0, H_FD, base)))
+    read = np.unique(fp.texel[fp.texel >= 0])
+    assert read.size >= 32
+    pick = np.random.default_rng(seed).choice(read.size * 3, size=32, replace=False)
+    for k in pick:
+        texel, c = int(read[k // 3]), int(k % 3)
+        groups["env"].append((ge[texel, c], fp.fd_env(P, texel, c, H_FD, base)))
+    assert sum(len(v) for v in groups.values()) == 64
+    for name, pairs in groups.items():
+        a = np.array([p[0] for p in pairs])
+        b = np.array([p[1] for p in pairs])
+        rel = np.linalg.norm(a - b) / np.linalg.norm(b)
+        print(f"{name}: relative gradient error {rel:.3e} over {len(pairs)} parameters (|fd| {np.linalg.norm(b):.3e})")
+        assert np.linalg.norm(b) > 0
+        assert rel <= 1e-3, (name, rel)
 
 
 class AdjointRender(torch.autograd.Function):
@@ -130,27 +158,49 @@ def test_adjoint_matches_fp64_finite_differences(cuda):
     assert np.sqrt(((img - ref) ** 2).mean()) <= 1e-5 * ref.mean()
 
     base = fp.factors(P)
-    g = grad.double().cpu().numpy()
-    ge = genv.double().cpu().numpy()
-    groups = {"albedo": [], "roughness": [], "env": []}
-    for i, off in enumerate(info["albedo_tex"]):
-        for c in range(3):
-            groups["albedo"].append((g[i, c], fp.fd_texture(P, off, c, H_FD, base)))
-    for i, off in enumerate(info["rough_tex"]):
-        groups["roughness"].append((g[8 + i, 0], fp.fd_texture(P, off, 0, H_FD, base)))
-    # 32 environment texel channels: those with the largest adjoint gradients
-    flat = np.argsort(-np.abs(ge[:, :3]).reshape(-1))[:32]
-    for k in flat:
-        texel, c = divmod(int(k), 3)
-        groups["env"].append((ge[texel, c], fp.fd_env(P, texel, c, H_FD, base)))
-    assert sum(len(v) for v in groups.values()) == 64
-    for name, pairs in groups.items():
-        a = np.array([p[0] for p in pairs])
-        b = np.array([p[1] for p in pairs])
-        rel = np.linalg.norm(a - b) / np.linalg.norm(b)
-        print(f"{name}: relative gradient error {rel:.3e} over {len(pairs)} parameters (|fd| {np.linalg.norm(b):.3e})")
-        assert np.linalg.norm(b) > 0
-        assert rel <= 1e-3, (name, rel)
+    _check_groups(fp, P, info, grad.double().cpu().numpy(), genv.double().cpu().numpy(), base)
+
+
+@pytest.mark.gpu
+def test_adjoint_at_the_benchmark_configuration(cuda):
+    """The differentiable-render benchmark's configuration: 512 x 512, 32
+    samples per pixel, depth 5, the target from parameters perturbed as the
+    benchmark perturbs them.  The loss is kept on a seeded 24 x 24 window of
+    pixels (the weight elsewhere is zero, so only the window's 18,432 samples
+    are replayed and taped; the others still run their forward pass and
+    advance their random numbers)."""
+    w = h = 512
+    spp = 32
+    sc, info, ds, tex, kind = _setup(cuda, w, h)
+    target = _target(cuda, info, w, h, spp=spp)
+    rng, pix = ds.new_frame()
+    seeds = rng.clone()
+    ds.render(rng, pix, spp, DEPTH, wavefront=True)
+    full = _dloss(pix, target, spp)
+    r = np.random.default_rng(17)
+    x0, y0 = (int(v) for v in r.integers(0, w - 24, size=2))
+    win = torch.zeros((h, w), dtype=torch.bool, device=cuda)
+    win[y0:y0 + 24, x0:x0 + 24] = True
+    dloss = torch.where(win.view(-1, 1), full, torch.zeros_like(full))
+    grad = torch.zeros((16, 4), dtype=torch.float32, device=cuda)
+    T = info["env"].shape[0] * info["env"].shape[1]
+    genv = torch.zeros((T, 4), dtype=torch.float32, device=cuda)
+    tape = torch.zeros((TAPE_CAP, 32), dtype=torch.int32, device=cuda)
+    count = torch.zeros(1, dtype=torch.int32, device=cuda)
+    rng_adj = seeds.clone()
+    ds.render_adjoint(rng_adj, dloss, spp, DEPTH, tex, kind, grad, info["env_tex"], genv, tape, count)
+    torch.cuda.synchronize()
+    assert _lib.device_status() == 0
+    assert torch.equal(rng_adj, rng)
+    n = int(count.item())
+    assert 0 < n <= TAPE_CAP
+    blobs = sc.blobs()
+    fp = FD.FrozenPaths(tape[:n].cpu().numpy().view(np.uint32), blobs, dloss.cpu().numpy())
+    P = FD.Params(blobs["textures"], env=info["env"])
+    img = fp.image(P, w * h)[win.view(-1).cpu().numpy()]
+    ref = pix[:, :3][win.view(-1)].double().cpu().numpy()
+    assert np.sqrt(((img - ref) ** 2).mean()) <= 1e-5 * ref.mean()
+    _check_groups(fp, P, info, grad.double().cpu().numpy(), genv.double().cpu().numpy(), fp.factors(P))
 
 
 @pytest.mark.gpu

@@ -93,6 +93,24 @@ def test_oracle_tree_properties(n, bits):
     check_tree(bvh, n)
 
 
+@pytest.mark.parametrize("n", [1, 2, 3, 1000, 65537])
+@pytest.mark.parametrize("bits", [10, 20])
+@pytest.mark.parametrize("threads", [1, 3, 8])
+def test_parallel_oracle_build_equals_serial(n, bits, threads):
+    """The data-parallel build (the CPU baseline of the benchmark) gives the
+    serial restatement's nodes, parents, order and scene box byte for byte,
+    on unindexed and indexed inputs, whatever the thread count."""
+    vx, vy, vz = W.triangle_soup(n, seed=n + 7 * bits)
+    tris = [None]
+    if n > 2:
+        tris.append(np.random.default_rng(n).permutation(3 * n).astype(np.uint32))
+    for tri in tris:
+        a = oracle.lbvh_build(vx, vy, vz, tri, n, bits)
+        b = oracle.lbvh_build_mt(vx, vy, vz, tri, n, bits, threads)
+        for k in ("inodes", "lnodes", "parents", "sorted_idx", "scene_box"):
+            np.testing.assert_array_equal(getattr(a, k).view(np.uint8), getattr(b, k).view(np.uint8), err_msg=k)
+
+
 def test_oracle_duplicate_keys_and_planar_scene():
     # many triangles with identical centres (equal keys) and a zero-extent z
     # axis (0/0 quantises to 0): the index extension of the Karras search and

@@ -117,3 +117,59 @@ def test_band_renders_equal_the_whole_image(cuda, world):
     assert torch.equal(torch.cat(parts_pix), pix)
     assert torch.equal(torch.cat(parts_rng).view(-1), rng.view(-1))
     assert _lib.device_status() == 0
+
+
+def _band_worker(rank, world, port, out):
+    os.environ["MASTER_ADDR"] = "127.0.0.1"
+    os.environ["MASTER_PORT"] = str(port)
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    try:
+        width, height = 6, 11
+
+        def render_band(y0, y1):  # pixel (x, y) holds y * width + x + 1
+            idx = torch.arange(y0 * width, y1 * width, dtype=torch.float32) + 1
+            return torch.stack([idx, idx, idx, idx], dim=1)
+
+        dt, img = shard.timed_band_render(render_band, height, width, steps=2)
+        out.put((rank, dt, None if img is None else img.numpy()))
+    finally:
+        dist.destroy_process_group()
+
+
+def test_timed_band_render_over_gloo_ranks():
+    """The band-render timing of the multi-process benchmark: every rank gets
+    the same (slowest) time, rank 0 the whole image in row order."""
+    world = 2
+    ctx = mp.get_context("spawn")
+    out = ctx.SimpleQueue()
+    port = _free_port()
+    procs = [ctx.Process(target=_band_worker, args=(r, world, port, out)) for r in range(world)]
+    for p in procs:
+        p.start()
+    res = {}
+    for _ in range(world):
+        rank, dt, img = out.get()
+        res[rank] = (dt, img)
+    for p in procs:
+        p.join(timeout=60)
+        assert p.exitcode == 0
+    assert res[0][0] == res[1][0] and res[0][0] > 0
+    assert np.array_equal(res[0][1][:, 0], np.arange(66, dtype=np.float32) + 1)
+    assert res[1][1] is None
+
+
+def test_launch_local_starts_one_process_per_rank(tmp_path):
+    """launch_local (what `bench.py --gpus N` uses when no launcher started
+    it) runs N processes that see their rank and world size and can form a
+    process group (gloo here)."""
+    script = tmp_path / "probe.py"
+    script.write_text(
+        "import os, sys, torch.distributed as dist\n"
+        "dist.init_process_group('gloo')\n"
+        "r, w = dist.get_rank(), dist.get_world_size()\n"
+        "open(os.path.join(sys.argv[1], f'rank{r}'), 'w').write(f'{r} {w} {os.environ[\"LOCAL_RANK\"]}')\n"
+        "dist.barrier()\n"
+        "dist.destroy_process_group()\n")
+    rc = shard.launch_local(2, str(script), [str(tmp_path)], timeout=120)
+    assert rc == 0
+    assert sorted((tmp_path / f"rank{r}").read_text() for r in range(2)) == ["0 2 0", "1 2 1"]
