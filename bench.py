@@ -70,10 +70,10 @@ ALGO_BYTES = {
     "build_tree": 156.0,
 }
 # Bytes the kernels of this design move beyond the algorithmic ones: the Morton
-# pass also writes each triangle's 64-byte staging record (read back in sorted
+# pass also writes each triangle's 48-byte staging record (read back in sorted
 # order by the tree pass instead of three 12-byte vertex gathers) and its
 # 4-byte arrival counter.
-DESIGN_BYTES = {"morton": 108.0}
+DESIGN_BYTES = {"morton": 92.0}
 
 
 def parse():
@@ -95,6 +95,8 @@ def parse():
     ap.add_argument("--loader-only", action="store_true",
                     help="time only the .obj loader on a generated 1 M-triangle mesh (host code)")
     ap.add_argument("--batched-scenes", type=int, default=512)
+    ap.add_argument("--batched-graph", type=int, default=1,
+                    help="0: launch the batched frame loop kernel by kernel (profiling)")
     ap.add_argument("--adjoint-res", type=int, default=512)
     ap.add_argument("--adjoint-spp", type=int, default=32)
     ap.add_argument("--band-spp", type=int, default=16,
@@ -473,7 +475,7 @@ def bench_adjoint(dev, spp=32, res=512) -> dict:
             "grad_norm": float(torch.linalg.norm(grad).item()), "env_grad_norm": float(torch.linalg.norm(genv).item())}
 
 
-def bench_batched(dev, num_scenes=512, spp=8, depth=5) -> dict:
+def bench_batched(dev, num_scenes=512, spp=8, depth=5, graph=True) -> dict:
     """Many scenes per launch: `num_scenes` scenes with log-uniform 1k-200k
     random triangles plus a quad light, square resolutions from {128, 256,
     384, 512}, `spp` samples, depth `depth`.  Batched form: one segmented LBVH
@@ -496,18 +498,18 @@ def bench_batched(dev, num_scenes=512, spp=8, depth=5) -> dict:
     ev = [torch.cuda.Event(enable_timing=True) for _ in range(8)]
 
     br = BatchRenderer(scenes, dev)
-    tuned = autotune.tune(br, depth, use_cache=False)
+    tuned = autotune.tune(br, depth, use_cache=False, graph=graph)
     seeds, pix = br.new_frame()
     # warm-up (also captures the graph for this spp)
     rng = seeds.clone()
-    br.render(rng, pix, spp, depth, graph=True)
+    br.render(rng, pix, spp, depth, graph=graph)
     torch.cuda.synchronize()
     pix.zero_()
     rng.copy_(seeds)
     ev[0].record(stream)
     br.rebuild_into_current()
     ev[1].record(stream)
-    br.render(rng, pix, spp, depth, graph=True)
+    br.render(rng, pix, spp, depth, graph=graph)
     ev[2].record(stream)
     torch.cuda.synchronize()
     b_build, b_render = ev[0].elapsed_time(ev[1]), ev[1].elapsed_time(ev[2])
@@ -838,7 +840,8 @@ def main():
         from clear_gb300.build import build
 
         build()
-        print(json.dumps({"batched": bench_batched(torch.device("cuda", 0), args.batched_scenes)}), flush=True)
+        print(json.dumps({"batched": bench_batched(torch.device("cuda", 0), args.batched_scenes,
+                                                   graph=bool(args.batched_graph))}), flush=True)
         return
     if args.adjoint_only:
         import torch

@@ -97,6 +97,9 @@ def lib() -> C.CDLL:
             "clr_trace_closest_ordered": [C.POINTER(ClrBvh), vp, u32, vp, vp, vp],
             "clr_trace_shadow": [C.POINTER(ClrBvh), vp, u32, vp, vp],
             "clr_device_status": [C.POINTER(u32), i32],
+            "clr_trace_replays": [C.POINTER(C.c_uint64), i32],
+            "clr_debug_set_wait_limits": [u32, u32],
+            "clr_debug_lookback_stall": [vp, vp, u32, vp],
             "clr_lbvh_set_profiling": [vp, i32],
             "clr_render": [vp, u32, u32, vp, vp, u32, u32, u32, vp],
             "clr_render_counted": [vp, u32, u32, vp, vp, u32, u32, u32, vp, vp],

@@ -38,18 +38,19 @@ def _events(n):
     return [torch.cuda.Event(enable_timing=True) for _ in range(n)]
 
 
-def time_render(br, config: dict, max_depth: int, seeds: torch.Tensor, spp: int = 1) -> float:
-    """ms of one `spp`-sample graph render of the whole batch with `config`
-    (after a warm-up render that also captures the graph)."""
+def time_render(br, config: dict, max_depth: int, seeds: torch.Tensor, spp: int = 1, graph: bool = True) -> float:
+    """ms of one `spp`-sample render of the whole batch with `config` (after a
+    warm-up render that also captures the graph); graph=False times the
+    frame loop launched kernel by kernel."""
     br.set_config(config)
     pix = torch.zeros((br.total_pixels, 4), dtype=torch.float32, device=br.device)
     rng = seeds.clone()
-    br.render(rng, pix, spp, max_depth, graph=True)
+    br.render(rng, pix, spp, max_depth, graph=graph)
     rng.copy_(seeds)
     e0, e1 = _events(2)
     stream = torch.cuda.current_stream(br.device)
     e0.record(stream)
-    br.render(rng, pix, spp, max_depth, graph=True)
+    br.render(rng, pix, spp, max_depth, graph=graph)
     e1.record(stream)
     torch.cuda.synchronize(br.device)
     return e0.elapsed_time(e1)
@@ -67,9 +68,10 @@ def time_build(br, radix_bits: int, reps: int = 3) -> float:
     return e0.elapsed_time(e1) / reps
 
 
-def tune(br, max_depth: int = 5, use_cache: bool = True) -> dict:
+def tune(br, max_depth: int = 5, use_cache: bool = True, graph: bool = True) -> dict:
     """Tunes `br` (a BatchRenderer), applies the best configuration and
-    returns it with the trial timings."""
+    returns it with the trial timings (renders timed as graphs, or kernel by
+    kernel with graph=False)."""
     key = signature(br, max_depth)
     path = cache_path()
     cache = {}
@@ -91,7 +93,7 @@ def tune(br, max_depth: int = 5, use_cache: bool = True) -> dict:
         best_v, best_ms = cfg[field], None
         for v in values:
             c = dict(cfg, **{field: v})
-            ms = time_render(br, c, max_depth, seeds)
+            ms = time_render(br, c, max_depth, seeds, graph=graph)
             trials.append({"config": c, "ms": ms})
             if best_ms is None or ms < best_ms:
                 best_v, best_ms = v, ms

@@ -70,15 +70,15 @@ __device__ __forceinline__ uint64_t make_key<uint64_t>(uint32_t qx, uint32_t qy,
     return spread3_21(qx) | (spread3_21(qy) << 1) | (spread3_21(qz) << 2);
 }
 
-// 64-byte staging record of triangle t in input order: p0, p1, p2 as float4
-// and a zero pad, so that the tree pass gathers one DRAM atom per leaf
-// instead of three scattered 12-byte runs of the SoA arrays.
+// 48-byte staging record of triangle t in input order: the nine vertex floats
+// p0, p1, p2 packed into three float4 (and three zeros), so that the tree
+// pass gathers two DRAM sectors per leaf instead of three scattered 12-byte
+// runs of the SoA arrays.
 __device__ __forceinline__ void stage_tri(float4* stage, uint32_t t, const float P[3][3]) {
-    float4* r = stage + 4ull * t;
-    r[0] = make_float4(P[0][0], P[0][1], P[0][2], 0.f);
-    r[1] = make_float4(P[1][0], P[1][1], P[1][2], 0.f);
-    r[2] = make_float4(P[2][0], P[2][1], P[2][2], 0.f);
-    r[3] = make_float4(0.f, 0.f, 0.f, 0.f);
+    float4* r = stage + 3ull * t;
+    r[0] = make_float4(P[0][0], P[0][1], P[0][2], P[1][0]);
+    r[1] = make_float4(P[1][1], P[1][2], P[2][0], P[2][1]);
+    r[2] = make_float4(P[2][2], 0.f, 0.f, 0.f);
 }
 
 __device__ __forceinline__ uint32_t tri_vertex(const uint32_t* tri, uint32_t t, uint32_t k) {
@@ -104,9 +104,37 @@ __global__ void __launch_bounds__(256) k_scene_box(const float* __restrict__ vx,
     float mn[3] = {INFINITY, INFINITY, INFINITY}, mx[3] = {-INFINITY, -INFINITY, -INFINITY};
     const uint32_t stride = gridDim.x * blockDim.x;
     if (tri == nullptr) {
-        // unindexed soup: every vertex belongs to a triangle
+        // unindexed soup: every vertex belongs to a triangle; with 16-byte
+        // aligned arrays four vertices per load and array, two loads in
+        // flight per array and thread
         const uint64_t nv = 3ull * n;
-        for (uint64_t i = blockIdx.x * blockDim.x + threadIdx.x; i < nv; i += stride) {
+        const uint64_t first = blockIdx.x * blockDim.x + threadIdx.x;
+        uint64_t scalar_from = 0;
+        if (((reinterpret_cast<uintptr_t>(vx) | reinterpret_cast<uintptr_t>(vy) | reinterpret_cast<uintptr_t>(vz)) &
+             15u) == 0u) {
+            const float4* x4 = reinterpret_cast<const float4*>(vx);
+            const float4* y4 = reinterpret_cast<const float4*>(vy);
+            const float4* z4 = reinterpret_cast<const float4*>(vz);
+            const uint64_t nv4 = nv / 4;
+            auto take = [&](const float4 x, const float4 y, const float4 z) {
+                mn[0] = fminf(mn[0], fminf(fminf(x.x, x.y), fminf(x.z, x.w)));
+                mx[0] = fmaxf(mx[0], fmaxf(fmaxf(x.x, x.y), fmaxf(x.z, x.w)));
+                mn[1] = fminf(mn[1], fminf(fminf(y.x, y.y), fminf(y.z, y.w)));
+                mx[1] = fmaxf(mx[1], fmaxf(fmaxf(y.x, y.y), fmaxf(y.z, y.w)));
+                mn[2] = fminf(mn[2], fminf(fminf(z.x, z.y), fminf(z.z, z.w)));
+                mx[2] = fmaxf(mx[2], fmaxf(fmaxf(z.x, z.y), fmaxf(z.z, z.w)));
+            };
+            uint64_t i = first;
+            for (; i + stride < nv4; i += 2 * (uint64_t)stride) {
+                const float4 xa = __ldg(x4 + i), ya = __ldg(y4 + i), za = __ldg(z4 + i);
+                const float4 xb = __ldg(x4 + i + stride), yb = __ldg(y4 + i + stride), zb = __ldg(z4 + i + stride);
+                take(xa, ya, za);
+                take(xb, yb, zb);
+            }
+            if (i < nv4) take(__ldg(x4 + i), __ldg(y4 + i), __ldg(z4 + i));
+            scalar_from = 4 * nv4;
+        }
+        for (uint64_t i = scalar_from + first; i < nv; i += stride) {
             float x = __ldg(vx + i), y = __ldg(vy + i), z = __ldg(vz + i);
             mn[0] = fminf(mn[0], x); mx[0] = fmaxf(mx[0], x);
             mn[1] = fminf(mn[1], y); mx[1] = fmaxf(mx[1], y);
@@ -389,8 +417,9 @@ struct TriVerts {
     float p[3][3];
 };
 
-// Triangle t's vertices: from its 64-byte staging record (p0, p1, p2 as three
-// float4, one DRAM atom) when the build staged them, else from the SoA arrays.
+// Triangle t's vertices: from its 48-byte staging record (the nine floats
+// packed in three float4, two DRAM sectors) when the build staged them, else
+// from the SoA arrays.
 __device__ __forceinline__ TriVerts load_tri_staged(const float* vx, const float* vy, const float* vz,
                                                     const uint32_t* tri, const float4* stage, uint32_t t);
 
@@ -409,11 +438,11 @@ __device__ __forceinline__ TriVerts load_tri(const float* vx, const float* vy, c
 __device__ __forceinline__ TriVerts load_tri_staged(const float* vx, const float* vy, const float* vz,
                                                     const uint32_t* tri, const float4* stage, uint32_t t) {
     if (stage == nullptr) return load_tri(vx, vy, vz, tri, t);
-    const float4 a = __ldg(stage + 4ull * t), b = __ldg(stage + 4ull * t + 1), c = __ldg(stage + 4ull * t + 2);
+    const float4 a = __ldg(stage + 3ull * t), b = __ldg(stage + 3ull * t + 1), c = __ldg(stage + 3ull * t + 2);
     TriVerts tv;
     tv.p[0][0] = a.x; tv.p[0][1] = a.y; tv.p[0][2] = a.z;
-    tv.p[1][0] = b.x; tv.p[1][1] = b.y; tv.p[1][2] = b.z;
-    tv.p[2][0] = c.x; tv.p[2][1] = c.y; tv.p[2][2] = c.z;
+    tv.p[1][0] = a.w; tv.p[1][1] = b.x; tv.p[1][2] = b.y;
+    tv.p[2][0] = b.z; tv.p[2][1] = b.w; tv.p[2][2] = c.x;
     return tv;
 }
 
@@ -1075,7 +1104,7 @@ static size_t pool_layout(clr_lbvh* h, uint32_t cap, char* base, bool stage = tr
     const size_t o_keys0 = take(8ull * cap), o_keys1 = take(8ull * cap);
     const size_t o_vals0 = take(4ull * cap), o_vals1 = take(4ull * cap);
     const size_t o_kidx = take(4ull * cap), o_cnt = take(4ull * cap);
-    const size_t o_stage = stage ? take(64ull * cap) : 0;
+    const size_t o_stage = stage ? take(48ull * cap) : 0;
     const size_t o_zero = off;
     const size_t o_hist = take(4ull * kMaxPasses * kRadix);
     const size_t o_status = take(4ull * kMaxPasses * tiles * kRadix);

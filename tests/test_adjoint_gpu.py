@@ -269,8 +269,10 @@ def test_adjoint_rejects_bad_arguments(cuda):
     tape = torch.zeros((8, 32), dtype=torch.int32, device=cuda)
     with pytest.raises(_lib.ClrError):  # tape without a counter
         ds.render_adjoint(rng, dloss, 1, DEPTH, tex, kind, grad, None, None, tape, None)
-    # a tape too small keeps counting and drops the rest
+    # a tape too small keeps counting and drops the rest (a nonzero loss
+    # weight: pixels with weight zero are not replayed, hence not taped)
     count = torch.zeros(1, dtype=torch.int32, device=cuda)
+    dloss[:, :3] = 1.0
     ds.render_adjoint(rng, dloss, 1, DEPTH, tex, kind, grad, None, None, tape, count)
     torch.cuda.synchronize()
     assert int(count.item()) > 8
