@@ -688,6 +688,30 @@ def run_ours(args):
     barrier()
     e2e_ms = e2.elapsed_time(e3) / args.steps
 
+    # ---- the same build at the other sizes of the microbenchmark (1 Mi, 4 Mi)
+    sizes = {}
+    for ns in (1 << 20, 1 << 22):
+        sx, sy, sz = W.triangle_soup(ns, seed=1 + rank)
+        sv = [torch.from_numpy(a).to(dev) for a in (sx, sy, sz)]
+        sb = lbvh.LBVHBuilder(ns, dev)
+        sbvh = lbvh.BVH(ns, dev)
+        for _ in range(3):
+            sb.perform(sv, None, ns, BITS, out=sbvh)
+        torch.cuda.synchronize()
+        a0, a1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a0.record(stream)
+        for _ in range(args.steps):
+            sb.perform(sv, None, ns, BITS, out=sbvh)
+        a1.record(stream)
+        torch.cuda.synchronize()
+        sms = a0.elapsed_time(a1) / args.steps
+        sb.set_profiling(True)
+        sb.perform(sv, None, ns, BITS, out=sbvh)
+        sizes[str(ns)] = {"ms_per_build": sms, "ms_per_mtri": sms / (ns / 1e6),
+                          "kernels_ms": {f"{i}:{k}": v for i, (k, v) in enumerate(sb.pass_times())}}
+        sb.close()
+        del sv, sbvh
+
     # ---- traversal throughput on the built tree
     m = args.rays
     crays = torch.from_numpy(W.closest_rays(m, seed=11 + rank)).to(dev)
@@ -771,6 +795,7 @@ def run_ours(args):
                      "traffic": traffic, "algo_bytes_per_tri": ALGO_BYTES.get(dom),
                      "kernel_ms": dom_ms},
         "build_kernels_ms": kern_ms,
+        "build_other_sizes": sizes,
         # every build pass against the same measured copy bandwidth
         "build_kernels_roofline": {k: {"gbs": ALGO_BYTES[k] * n / (v * 1e-3) / 1e9,
                                        "frac": ALGO_BYTES[k] * n / (v * 1e-3) / 1e9 / peak}

@@ -1105,11 +1105,14 @@ static size_t pool_layout(clr_lbvh* h, uint32_t cap, char* base, bool stage = tr
     const size_t o_vals0 = take(4ull * cap), o_vals1 = take(4ull * cap);
     const size_t o_kidx = take(4ull * cap), o_cnt = take(4ull * cap);
     const size_t o_stage = stage ? take(48ull * cap) : 0;
+    // the region cleared per build: histograms, tile counters and scene box
+    // first, then the look-back words, of which a build clears only the
+    // passes and tiles it uses (zero_prefix_bytes)
     const size_t o_zero = off;
     const size_t o_hist = take(4ull * kMaxPasses * kRadix);
-    const size_t o_status = take(4ull * kMaxPasses * tiles * kRadix);
     const size_t o_tiles = take(4ull * (kMaxPasses + 1));  // + the tree pass's worklist count
     const size_t o_box = take(4ull * 8);
+    const size_t o_status = take(4ull * kMaxPasses * tiles * kRadix);
     if (base) {
         h->keys[0] = base + o_keys0;
         h->keys[1] = base + o_keys1;
@@ -1123,6 +1126,7 @@ static size_t pool_layout(clr_lbvh* h, uint32_t cap, char* base, bool stage = tr
         h->hist = reinterpret_cast<unsigned int*>(base + o_hist);
         h->status = reinterpret_cast<unsigned int*>(base + o_status);
         h->status_stride = tiles * kRadix;
+        h->zero_prefix_bytes = o_status - o_zero;
         h->tile_ctr = reinterpret_cast<unsigned int*>(base + o_tiles);
         h->boxw = reinterpret_cast<unsigned int*>(base + o_box);
         h->pool_bytes = off;
@@ -1194,6 +1198,15 @@ struct PassTimer {
     }
 };
 
+// Clears what a build of n keys reads before writing: the digit histograms,
+// tile counters and scene box, and the look-back words of the passes and
+// tiles it uses, laid out with a stride of its own tile count.
+static cudaError_t clear_for_build(clr_lbvh* h, uint32_t n, int items, int npasses, cudaStream_t st) {
+    const size_t tiles = div_up(n ? n : 1, (unsigned int)(kSortThreads * items));
+    h->status_stride = tiles * kRadix;
+    return cudaMemsetAsync(h->zero_region, 0, h->zero_prefix_bytes + 4ull * npasses * h->status_stride, st);
+}
+
 template <typename KeyT>
 static int run_build(clr_lbvh* h, const float* vx, const float* vy, const float* vz, const uint32_t* tri,
                      uint32_t n, uint32_t bits, clr_bvh* out, cudaStream_t st) {
@@ -1201,7 +1214,7 @@ static int run_build(clr_lbvh* h, const float* vx, const float* vy, const float*
     const int npasses = (kbits + 7) / 8;
     const int grid_stream = clr_sm_count() * 8;
     PassTimer timer(h, st);
-    CLR_CUDA_TRY(cudaMemsetAsync(h->zero_region, 0, h->zero_bytes, st));
+    CLR_CUDA_TRY(clear_for_build(h, n, SortCfg<KeyT>::kItems, npasses, st));
     k_scene_box<<<grid_stream, 256, 0, st>>>(vx, vy, vz, tri, n, h->boxw);
     CLR_LAUNCH_CHECK("k_scene_box");
     timer.done("scene_box");
@@ -1441,7 +1454,7 @@ extern "C" int clr_lbvh_build_batched(clr_lbvh* h, const float* vx, const float*
     h->last_n = 0;  // the reference-layout export covers single-scene builds only
     PassTimer timer(h, st);
     CLR_CUDA_TRY(cudaMemcpyAsync(h->seg_off, scene_offsets, 4ull * (num_scenes + 1), cudaMemcpyHostToDevice, st));
-    CLR_CUDA_TRY(cudaMemsetAsync(h->zero_region, 0, h->zero_bytes, st));
+    CLR_CUDA_TRY(clear_for_build(h, n, SortCfg<uint64_t>::kItems, npasses, st));
     CLR_CUDA_TRY(cudaMemsetAsync(h->seg_box, 0, 24ull * num_scenes, st));
     k_seg_box<<<div_up(n, kSegBoxChunk), 256, 0, st>>>(vx, vy, vz, tri, h->seg_off, num_scenes, n, h->seg_box);
     CLR_LAUNCH_CHECK("k_seg_box");

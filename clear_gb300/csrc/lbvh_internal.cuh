@@ -33,11 +33,12 @@ struct clr_lbvh {
     uint32_t* karras_idx = nullptr;          // node (at its split) -> reference index
     float4* stage = nullptr;                 // 64-byte vertex record per triangle (input order), or null
     unsigned int* counters = nullptr;        // tree-pass arrival counters
-    void* zero_region = nullptr;             // cleared once per build:
-    size_t zero_bytes = 0;                   //   hist, status, tile_ctr, boxw
+    void* zero_region = nullptr;             // cleared per build: hist, tile_ctr, boxw,
+    size_t zero_bytes = 0;                   //   then the used part of status
+    size_t zero_prefix_bytes = 0;            // hist, tile_ctr and boxw (status follows)
     unsigned int* hist = nullptr;            // [pass][256] digit counts
     unsigned int* status = nullptr;          // [pass][tile][256] look-back words
-    size_t status_stride = 0;
+    size_t status_stride = 0;                // words per pass: the build's tiles x 256
     unsigned int* tile_ctr = nullptr;        // [pass] dynamic tile counter
     unsigned int* boxw = nullptr;            // scene box, ordered-uint encoded
     // batched builds: scene offsets and per-scene boxes (own allocation)
