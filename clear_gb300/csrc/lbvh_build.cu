@@ -70,6 +70,25 @@ __device__ __forceinline__ uint64_t make_key<uint64_t>(uint32_t qx, uint32_t qy,
     return spread3_21(qx) | (spread3_21(qy) << 1) | (spread3_21(qz) << 2);
 }
 
+// One 64-byte internal node written as two 32-byte stores when the node array
+// is 32-byte aligned (whole DRAM sectors per store), else as four 16-byte ones.
+__device__ __forceinline__ void st_node(float* nn, bool wide, float4 a, float4 b, float4 c, float4 d) {
+    if (wide) {
+        asm volatile("st.global.v8.f32 [%0], {%1,%2,%3,%4,%5,%6,%7,%8};" ::"l"(nn), "f"(a.x), "f"(a.y), "f"(a.z),
+                     "f"(a.w), "f"(b.x), "f"(b.y), "f"(b.z), "f"(b.w)
+                     : "memory");
+        asm volatile("st.global.v8.f32 [%0], {%1,%2,%3,%4,%5,%6,%7,%8};" ::"l"(nn + 8), "f"(c.x), "f"(c.y), "f"(c.z),
+                     "f"(c.w), "f"(d.x), "f"(d.y), "f"(d.z), "f"(d.w)
+                     : "memory");
+    } else {
+        float4* n4 = reinterpret_cast<float4*>(nn);
+        n4[0] = a;
+        n4[1] = b;
+        n4[2] = c;
+        n4[3] = d;
+    }
+}
+
 // 48-byte staging record of triangle t in input order: the nine vertex floats
 // p0, p1, p2 packed into three float4 (and three zeros), so that the tree
 // pass gathers two DRAM sectors per leaf instead of three scattered 12-byte
@@ -612,7 +631,7 @@ __device__ __forceinline__ void tree_climb(const KeyT* __restrict__ keys, const 
 // second writes the whole 64-byte node.  A node that crosses a block edge is
 // reached by threads of two blocks and uses the device-scope protocol of
 // tree_climb; so are all its ancestors.
-constexpr int kTreeBlock = 256;
+constexpr int kTreeBlock = 128;
 
 __device__ __forceinline__ unsigned int atomic_add_acq_rel_cta(unsigned int* p, unsigned int v) {
     unsigned int old;
@@ -623,8 +642,8 @@ __device__ __forceinline__ unsigned int atomic_add_acq_rel_cta(unsigned int* p, 
     return old;
 }
 
-template <typename KeyT>
-__global__ void __launch_bounds__(kTreeBlock, 8) k_build_tree(const KeyT* __restrict__ keys,
+template <typename KeyT, bool kWide>
+__global__ void __launch_bounds__(kTreeBlock, 16) k_build_tree(const KeyT* __restrict__ keys,
                                                            const uint32_t* __restrict__ sidx, uint32_t n, int kbits,
                                                            const float* __restrict__ vx, const float* __restrict__ vy,
                                                            const float* __restrict__ vz, const uint32_t* __restrict__ tri,
@@ -726,12 +745,10 @@ __global__ void __launch_bounds__(kTreeBlock, 8) k_build_tree(const KeyT* __rest
             } else {
                 tri_box(vx, vy, vz, tri, stage, __ldg(sidx + j + 1), b1);
             }
-            float4* n4 = reinterpret_cast<float4*>(nodes + 16u * j);
-            n4[0] = make_float4(box[0], box[1], box[2], box[3]);
-            n4[1] = make_float4(box[4], box[5], b1[0], b1[1]);
-            n4[2] = make_float4(b1[2], b1[3], b1[4], b1[5]);
-            n4[3] = make_float4(__uint_as_float(j | kLeafBit), __uint_as_float((j + 1) | kLeafBit),
-                                __uint_as_float(j), __uint_as_float(j + 1));
+            st_node(nodes + 16u * j, kWide, make_float4(box[0], box[1], box[2], box[3]),
+                    make_float4(box[4], box[5], b1[0], b1[1]), make_float4(b1[2], b1[3], b1[4], b1[5]),
+                    make_float4(__uint_as_float(j | kLeafBit), __uint_as_float((j + 1) | kLeafBit),
+                                __uint_as_float(j), __uint_as_float(j + 1)));
 #pragma unroll
             for (int k = 0; k < 3; ++k) {
                 box[k] = fminf(box[k], b1[k]);
@@ -768,11 +785,8 @@ __global__ void __launch_bounds__(kTreeBlock, 8) k_build_tree(const KeyT* __rest
             const float4 a0 = s_slot[ls][0][0], a1 = s_slot[ls][0][1];
             const float4 c0 = s_slot[ls][1][0], c1 = s_slot[ls][1][1];
             far_end = __float_as_uint(slot == 0 ? c1.w : a1.w);
-            float4* n4 = reinterpret_cast<float4*>(nodes + 16u * split);
-            n4[0] = a0;
-            n4[1] = make_float4(a1.x, a1.y, c0.x, c0.y);
-            n4[2] = make_float4(c0.z, c0.w, c1.x, c1.y);
-            n4[3] = make_float4(a1.z, c1.z, a1.w, c1.w);
+            st_node(nodes + 16u * split, kWide, a0, make_float4(a1.x, a1.y, c0.x, c0.y),
+                    make_float4(c0.z, c0.w, c1.x, c1.y), make_float4(a1.z, c1.z, a1.w, c1.w));
             box[0] = fminf(a0.x, c0.x);
             box[1] = fminf(a0.y, c0.y);
             box[2] = fminf(a0.z, c0.z);
@@ -1249,9 +1263,15 @@ static int run_build(clr_lbvh* h, const float* vx, const float* vy, const float*
         // worklist of the block-crossing nodes: the sort's free ping-pong side
         uint32_t* worklist = h->vals[fin ^ 1];
         unsigned int* wl_count = h->tile_ctr + kMaxPasses;
-        k_build_tree<KeyT><<<div_up(n, kTreeBlock), kTreeBlock, 0, st>>>(
-            keys[fin], h->vals[fin], n, kbits, vx, vy, vz, tri, h->stage, reinterpret_cast<float*>(out->nodes), tris,
-            h->counters, h->karras_idx, out->root_box, worklist, wl_count);
+        const bool wide = (reinterpret_cast<uintptr_t>(out->nodes) & 31u) == 0u;  // 32-byte node stores
+        if (wide)
+            k_build_tree<KeyT, true><<<div_up(n, kTreeBlock), kTreeBlock, 0, st>>>(
+                keys[fin], h->vals[fin], n, kbits, vx, vy, vz, tri, h->stage, reinterpret_cast<float*>(out->nodes),
+                tris, h->counters, h->karras_idx, out->root_box, worklist, wl_count);
+        else
+            k_build_tree<KeyT, false><<<div_up(n, kTreeBlock), kTreeBlock, 0, st>>>(
+                keys[fin], h->vals[fin], n, kbits, vx, vy, vz, tri, h->stage, reinterpret_cast<float*>(out->nodes),
+                tris, h->counters, h->karras_idx, out->root_box, worklist, wl_count);
         CLR_LAUNCH_CHECK("k_build_tree");
         k_build_tree_top<KeyT><<<clr_sm_count() * 4, 256, 0, st>>>(keys[fin], n, kbits, reinterpret_cast<float*>(out->nodes),
                                                              h->counters, h->karras_idx, out->root_box, worklist,
