@@ -31,7 +31,7 @@ struct clr_lbvh {
     void* keys[2] = {nullptr, nullptr};     // sort ping-pong (up to 8 B per key)
     uint32_t* vals[2] = {nullptr, nullptr};  // triangle ids riding with the keys
     uint32_t* karras_idx = nullptr;          // node (at its split) -> reference index
-    float4* stage = nullptr;                 // 64-byte vertex record per triangle (input order), or null
+    float4* stage = nullptr;                 // 48-byte vertex record per triangle (input order), or null
     unsigned int* counters = nullptr;        // tree-pass arrival counters
     void* zero_region = nullptr;             // cleared per build: hist, tile_ctr, boxw,
     size_t zero_bytes = 0;                   //   then the used part of status
