@@ -849,7 +849,7 @@ __global__ void __launch_bounds__(256) k_ad_reduce(const float* __restrict__ par
     }
 }
 
-static uint32_t ad_grid(uint32_t npix) { return std::min(div_up(npix, kAdThreads), 152u * 16u); }
+static uint32_t ad_grid(uint32_t npix) { return std::min(div_up(npix, kAdThreads), (unsigned int)clr_sm_count() * 16u); }
 
 static size_t ad_layout(uint32_t npix, uint32_t num_params, char* base, AdState* S) {
     size_t off = 0;

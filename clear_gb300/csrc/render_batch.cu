@@ -516,7 +516,7 @@ extern "C" int clr_batch_pixels(const clr_batch* b, uint32_t* total) {
 }
 
 static unsigned int bt_grid(uint32_t work, uint32_t block) {
-    return std::max(1u, std::min(div_up(work, block), 152u * (2048u / block)));
+    return std::max(1u, std::min(div_up(work, block), (unsigned int)clr_sm_count() * (2048u / block)));
 }
 
 // One iteration's kernels (parity cur).

@@ -37,8 +37,9 @@ struct WfState {
     uint4* misc;     // x depth, y sampledType, z samples done, w pixel
     float4* hit;     // x id bits, y t, z b1, w b2
     uint32_t* q[2];  // active path queues
+    uint32_t* qs;    // the extended paths for shade: escaped first, hits from the end
     float4* sh;      // shadow entries: org (w shadow_light_word), dir (w path), contribution
-    unsigned int* count;  // [0],[1] active counts, [2] shadow count
+    unsigned int* count;  // [0],[1] active counts, [2] shadow count, [3] escaped, [4] hits
 };
 
 __device__ __forceinline__ Rng load_rng(const uint32_t* rs, uint32_t p) {
@@ -92,6 +93,8 @@ __global__ void __launch_bounds__(kWfThreads) k_wf_init(DScene sc, WfState S, ui
         S.count[0] = npix;
         S.count[1] = 0;
         S.count[2] = 0;
+        S.count[3] = 0;
+        S.count[4] = 0;
     }
 }
 
@@ -110,6 +113,28 @@ __global__ void __launch_bounds__(kWfThreads, 8) k_wf_extend(DScene sc, WfState 
     }
 }
 
+// The extended paths partitioned for shade: escaped paths (the environment
+// branch) to the front of S.qs, paths that hit something to its end, so that
+// shade's warps mostly run one of the two branches instead of both.  The
+// order in which paths are shaded changes no path's result.  (A separate pass:
+// votes inside the extend loop would hold every lane of a warp to the
+// slowest ray's traversal.)
+__global__ void __launch_bounds__(kWfThreads) k_wf_partition(WfState S, const uint32_t* __restrict__ q, int cur) {
+    const uint32_t n = S.count[cur];
+    const uint32_t n_round = (n + 31u) & ~31u;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n_round; i += gridDim.x * blockDim.x) {
+        uint32_t p = 0;
+        bool hit = false;
+        if (i < n) {
+            p = q[i];
+            hit = __float_as_uint(S.hit[p].x) != kNone32;
+        }
+        const uint32_t ms = queue_slot(S.count + 3, i < n && !hit);
+        const uint32_t hs = queue_slot(S.count + 4, hit);
+        if (i < n) S.qs[hit ? n - 1u - hs : ms] = p;
+    }
+}
+
 __global__ void __launch_bounds__(kWfThreads) k_wf_shade(DScene sc, WfState S, int cur, uint32_t width, uint32_t row0,
                                                          uint32_t* __restrict__ rand_states,
                                                          float4* __restrict__ pixels, uint32_t spp,
@@ -125,7 +150,7 @@ __global__ void __launch_bounds__(kWfThreads) k_wf_shade(DScene sc, WfState S, i
         uint32_t p = 0;
         float4 sh0, sh1, sh2;
         if (i < n) {
-            p = S.q[cur][i];
+            p = S.qs[i];
             Rng rng = load_rng(rand_states, p);
             const float4 o4 = S.org[p], d4 = S.dir[p], a4 = S.alpha[p];
             uint4 m = S.misc[p];
@@ -271,9 +296,13 @@ __global__ void __launch_bounds__(kWfThreads, 8) k_wf_shadow(DScene sc, WfState 
     }
 }
 
+// After the partition: the counts the shade pass appends to, and the
+// partition's own counts for the next iteration.
 __global__ void k_wf_reset(WfState S, int next) {
     S.count[next] = 0;
     S.count[2] = 0;
+    S.count[3] = 0;
+    S.count[4] = 0;
 }
 
 static size_t wf_layout(uint32_t npix, char* base, WfState* S) {
@@ -285,7 +314,7 @@ static size_t wf_layout(uint32_t npix, char* base, WfState* S) {
     };
     const size_t o_org = take(16ull * npix), o_dir = take(16ull * npix), o_alpha = take(16ull * npix),
                  o_misc = take(16ull * npix), o_hit = take(16ull * npix), o_q0 = take(4ull * npix),
-                 o_q1 = take(4ull * npix), o_sh = take(48ull * npix), o_cnt = take(16);
+                 o_q1 = take(4ull * npix), o_qs = take(4ull * npix), o_sh = take(48ull * npix), o_cnt = take(32);
     if (base && S) {
         S->org = reinterpret_cast<float4*>(base + o_org);
         S->dir = reinterpret_cast<float4*>(base + o_dir);
@@ -294,6 +323,7 @@ static size_t wf_layout(uint32_t npix, char* base, WfState* S) {
         S->hit = reinterpret_cast<float4*>(base + o_hit);
         S->q[0] = reinterpret_cast<uint32_t*>(base + o_q0);
         S->q[1] = reinterpret_cast<uint32_t*>(base + o_q1);
+        S->qs = reinterpret_cast<uint32_t*>(base + o_qs);
         S->sh = reinterpret_cast<float4*>(base + o_sh);
         S->count = reinterpret_cast<unsigned int*>(base + o_cnt);
     }
@@ -332,7 +362,7 @@ extern "C" int clr_render_wavefront_rows(const clr_scene* scene, uint32_t width,
     wf_layout(npix, static_cast<char*>(workspace), &S);
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     const bool ordered = (flags & CLR_RENDER_ORDERED) != 0;
-    const unsigned int grid = std::min(div_up(npix, kWfThreads), 152u * 16u);
+    const unsigned int grid = std::min(div_up(npix, kWfThreads), (unsigned int)clr_sm_count() * 16u);
     float4* px = reinterpret_cast<float4*>(pixels);
     k_wf_init<<<grid, kWfThreads, 0, st>>>(sc, S, npix, width, row0, rand_states);
     CLR_LAUNCH_CHECK("k_wf_init");
@@ -342,6 +372,7 @@ extern "C" int clr_render_wavefront_rows(const clr_scene* scene, uint32_t width,
         const int cur = (int)(it & 1);
         if (ordered) k_wf_extend<true><<<grid, kWfThreads, 0, st>>>(sc, S, cur);
         else k_wf_extend<false><<<grid, kWfThreads, 0, st>>>(sc, S, cur);
+        k_wf_partition<<<grid, kWfThreads, 0, st>>>(S, S.q[cur], cur);
         k_wf_reset<<<1, 1, 0, st>>>(S, cur ^ 1);
         k_wf_shade<<<grid, kWfThreads, 0, st>>>(sc, S, cur, width, row0, rand_states, px, spp, max_depth);
         if (ordered) k_wf_shadow<true><<<grid, kWfThreads, 0, st>>>(sc, S, px);
