@@ -135,21 +135,27 @@ __global__ void __launch_bounds__(kWfThreads) k_wf_partition(WfState S, const ui
     }
 }
 
+// kHit = false shades the escaped paths (S.qs[0, count[3])), kHit = true
+// the paths that hit a surface (S.qs[count[3], n)): two kernels, each with
+// only its branch's code.
+template <bool kHit>
 __global__ void __launch_bounds__(kWfThreads) k_wf_shade(DScene sc, WfState S, int cur, uint32_t width, uint32_t row0,
                                                          uint32_t* __restrict__ rand_states,
                                                          float4* __restrict__ pixels, uint32_t spp,
                                                          uint32_t max_depth) {
-    const uint32_t n = S.count[cur];
+    const uint32_t n = S.count[cur], nm = S.count[3];
+    const uint32_t lo = kHit ? nm : 0u, hi = kHit ? n : nm;
     const Camera cam = load_camera(sc);
     const uint32_t stride = gridDim.x * blockDim.x;
     // whole warps iterate together so the queue appends can use warp votes
-    const uint32_t n_round = (n + 31u) & ~31u;
-    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n_round; i += stride) {
+    const uint32_t n_round = (hi - lo + 31u) & ~31u;
+    for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < n_round; j += stride) {
+        const uint32_t i = lo + j;
         bool cont = false;      // path goes on to the next extend
         bool shadow = false;    // a shadow entry is written
         uint32_t p = 0;
         float4 sh0, sh1, sh2;
-        if (i < n) {
+        if (i < hi) {
             p = S.qs[i];
             Rng rng = load_rng(rand_states, p);
             const float4 o4 = S.org[p], d4 = S.dir[p], a4 = S.alpha[p];
@@ -164,7 +170,7 @@ __global__ void __launch_bounds__(kWfThreads) k_wf_shade(DScene sc, WfState S, i
             bool ended = false;
             uint32_t light_face = __float_as_uint(o4.w);
             const uint32_t hid = __float_as_uint(h4.x);
-            if (hid == kNone32) {
+            if (!kHit) {
                 // escaped: environment emission (pathtracer.cl:183-196)
                 LightPt lpos;
                 lpos.atInfinity = true;
@@ -296,8 +302,8 @@ __global__ void __launch_bounds__(kWfThreads, 8) k_wf_shadow(DScene sc, WfState 
     }
 }
 
-// After the partition: the counts the shade pass appends to, and the
-// partition's own counts for the next iteration.
+// After the extend: the counts the shade kernels append to and the
+// partition's counts.
 __global__ void k_wf_reset(WfState S, int next) {
     S.count[next] = 0;
     S.count[2] = 0;
@@ -328,6 +334,94 @@ static size_t wf_layout(uint32_t npix, char* base, WfState* S) {
         S->count = reinterpret_cast<unsigned int*>(base + o_cnt);
     }
     return off;
+}
+
+// One block of kWfBlockIters iterations (the first of parity 0).
+constexpr int kWfBlockIters = 8;
+
+struct WfArgs {
+    DScene sc;
+    WfState S;
+    uint32_t width, row0, spp, max_depth;
+    uint32_t* rand_states;
+    float4* px;
+    bool ordered;
+    unsigned int grid;
+};
+
+static void wf_block(const WfArgs& a, cudaStream_t st) {
+    for (int k = 0; k < kWfBlockIters; ++k) {
+        const int cur = k & 1;
+        if (a.ordered) k_wf_extend<true><<<a.grid, kWfThreads, 0, st>>>(a.sc, a.S, cur);
+        else k_wf_extend<false><<<a.grid, kWfThreads, 0, st>>>(a.sc, a.S, cur);
+        k_wf_reset<<<1, 1, 0, st>>>(a.S, cur ^ 1);
+        k_wf_partition<<<a.grid, kWfThreads, 0, st>>>(a.S, a.S.q[cur], cur);
+        k_wf_shade<false><<<a.grid, kWfThreads, 0, st>>>(a.sc, a.S, cur, a.width, a.row0, a.rand_states, a.px, a.spp,
+                                                         a.max_depth);
+        k_wf_shade<true><<<a.grid, kWfThreads, 0, st>>>(a.sc, a.S, cur, a.width, a.row0, a.rand_states, a.px, a.spp,
+                                                        a.max_depth);
+        if (a.ordered) k_wf_shadow<true><<<a.grid, kWfThreads, 0, st>>>(a.sc, a.S, a.px);
+        else k_wf_shadow<false><<<a.grid, kWfThreads, 0, st>>>(a.sc, a.S, a.px);
+    }
+}
+
+static bool same_args(const WfArgs& x, const WfArgs& y) {
+    const DScene &a = x.sc, &b = y.sc;
+    return a.vertices == b.vertices && a.normals == b.normals && a.tangents == b.tangents && a.uvs == b.uvs &&
+           a.faces == b.faces && a.lights == b.lights && a.materials == b.materials && a.textures == b.textures &&
+           a.others == b.others && a.nodes == b.nodes && a.tris == b.tris && a.root_box == b.root_box &&
+           a.num_tris == b.num_tris && a.alpha == b.alpha && x.S.org == y.S.org && x.S.count == y.S.count &&
+           x.S.qs == y.S.qs && x.width == y.width && x.row0 == y.row0 && x.spp == y.spp &&
+           x.max_depth == y.max_depth && x.rand_states == y.rand_states && x.px == y.px &&
+           x.ordered == y.ordered && x.grid == y.grid;
+}
+
+// The block as a CUDA graph, captured on a stream of the calling thread and
+// kept (per thread and device) for the last argument set: its 48 launches
+// otherwise cost more than the kernels of a small image.  Returns null when
+// capture is not possible; the caller then launches the kernels itself.
+constexpr int kWfGraphDevices = 64;
+struct WfGraph {
+    cudaStream_t cap = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    WfArgs args{};
+};
+thread_local WfGraph t_wf_graph[kWfGraphDevices];
+
+static cudaGraphExec_t wf_block_graph(const WfArgs& a) {
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kWfGraphDevices) return nullptr;
+    WfGraph& g = t_wf_graph[dev];
+    if (g.exec && same_args(g.args, a)) return g.exec;
+    if (!g.cap && cudaStreamCreateWithFlags(&g.cap, cudaStreamNonBlocking) != cudaSuccess) {
+        g.cap = nullptr;
+        return nullptr;
+    }
+    if (g.exec) {
+        cudaGraphExecDestroy(g.exec);
+        g.exec = nullptr;
+    }
+    cudaGraph_t graph = nullptr;
+    if (cudaStreamBeginCapture(g.cap, cudaStreamCaptureModeThreadLocal) != cudaSuccess) return nullptr;
+    wf_block(a, g.cap);
+    if (cudaStreamEndCapture(g.cap, &graph) != cudaSuccess || !graph) return nullptr;
+    const cudaError_t e = cudaGraphInstantiate(&g.exec, graph, 0);
+    cudaGraphDestroy(graph);
+    if (e != cudaSuccess) {
+        g.exec = nullptr;
+        return nullptr;
+    }
+    g.args = a;
+    return g.exec;
+}
+
+// Forgets the calling thread's graph for the current device (a launch of it
+// failed, e.g. after a device reset).
+static void wf_block_graph_drop() {
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kWfGraphDevices) return;
+    t_wf_graph[dev].exec = nullptr;
+    t_wf_graph[dev].cap = nullptr;
 }
 
 }  // namespace clr
@@ -366,25 +460,25 @@ extern "C" int clr_render_wavefront_rows(const clr_scene* scene, uint32_t width,
     float4* px = reinterpret_cast<float4*>(pixels);
     k_wf_init<<<grid, kWfThreads, 0, st>>>(sc, S, npix, width, row0, rand_states);
     CLR_LAUNCH_CHECK("k_wf_init");
-    // every iteration advances each unfinished pixel by one path vertex
+    const WfArgs a{sc, S, width, row0, spp, max_depth, rand_states, px, ordered, grid};
+    cudaGraphExec_t exec = wf_block_graph(a);
+    cudaGetLastError();  // a failed capture leaves no error behind: the kernels are launched directly
+    // every iteration advances each unfinished pixel by one path vertex; a
+    // block ends with the next iteration's queue count in count[0]
     const uint64_t max_iters = (uint64_t)spp * (max_depth + 1) + 1;
-    for (uint64_t it = 0; it < max_iters; ++it) {
-        const int cur = (int)(it & 1);
-        if (ordered) k_wf_extend<true><<<grid, kWfThreads, 0, st>>>(sc, S, cur);
-        else k_wf_extend<false><<<grid, kWfThreads, 0, st>>>(sc, S, cur);
-        k_wf_partition<<<grid, kWfThreads, 0, st>>>(S, S.q[cur], cur);
-        k_wf_reset<<<1, 1, 0, st>>>(S, cur ^ 1);
-        k_wf_shade<<<grid, kWfThreads, 0, st>>>(sc, S, cur, width, row0, rand_states, px, spp, max_depth);
-        if (ordered) k_wf_shadow<true><<<grid, kWfThreads, 0, st>>>(sc, S, px);
-        else k_wf_shadow<false><<<grid, kWfThreads, 0, st>>>(sc, S, px);
-        CLR_LAUNCH_CHECK("wavefront iteration");
-        // stop once no path is left (checked every 8 iterations)
-        if ((it & 7) == 7) {
-            unsigned int left = 0;
-            CLR_CUDA_TRY(cudaMemcpyAsync(&left, S.count + (cur ^ 1), sizeof(left), cudaMemcpyDeviceToHost, st));
-            CLR_CUDA_TRY(cudaStreamSynchronize(st));
-            if (left == 0) break;
+    for (uint64_t it = 0; it < max_iters; it += kWfBlockIters) {
+        if (exec && cudaGraphLaunch(exec, st) != cudaSuccess) {
+            cudaGetLastError();
+            wf_block_graph_drop();
+            exec = nullptr;
         }
+        if (!exec) wf_block(a, st);
+        CLR_LAUNCH_CHECK("wavefront iterations");
+        // stop once no path is left
+        unsigned int left = 0;
+        CLR_CUDA_TRY(cudaMemcpyAsync(&left, S.count, sizeof(left), cudaMemcpyDeviceToHost, st));
+        CLR_CUDA_TRY(cudaStreamSynchronize(st));
+        if (left == 0) break;
     }
     return CLR_OK;
 }

@@ -295,10 +295,15 @@ CLR_API int clr_render_counted(const clr_scene* scene, uint32_t width, uint32_t 
 
 /* Wavefront form of clr_render: the same paths, random numbers and
  * contributions (identical results), split into extend / shade / shadow
- * kernels over path state in `workspace`, with per-pixel path regeneration.
+ * kernels over path state in `workspace`, with per-pixel path regeneration;
+ * escaped and surface-hit paths are shaded by separate kernels.
  * The caller provides a 256-byte aligned device workspace of at least
  * clr_render_workspace_bytes(width, height) bytes.  Waits on `stream` every
- * few iterations to stop once every pixel has its spp samples. */
+ * eight iterations to stop once every pixel has its spp samples.  Those
+ * eight iterations are launched as one CUDA graph, captured on a stream of
+ * the calling thread and kept per thread and device for the last argument
+ * set (scene, workspace, states, pixels, sizes, flags); a call with other
+ * arguments captures anew.  Not for stream capture (it synchronises). */
 CLR_API int clr_render_workspace_bytes(uint32_t width, uint32_t height, uint64_t* bytes);
 CLR_API int clr_render_wavefront(const clr_scene* scene, uint32_t width, uint32_t height, uint32_t* rand_states,
                                  float* pixels, uint32_t spp, uint32_t max_depth, uint32_t flags, void* workspace,
