@@ -499,17 +499,13 @@ __device__ __forceinline__ int delta_adj(const KeyT* __restrict__ keys, int kbit
 // when delta(hi, hi+1) > delta(lo-1, lo), else to the left (split = lo-1,
 // child 1).  The two deltas never tie for distinct extended keys.  So each
 // leaf thread climbs: it writes its box, reference and far range end into the
-// parent's child slot, and the second of the two children to arrive (atomic
-// counter, device fences) merges both boxes and continues upwards, exactly as
-// calcNodeAABBs (:415-492) climbs.  Internal nodes are stored at index =
-// split position; the reference's index of a node (its hi if it is child 0,
-// its lo if child 1, 0 for the root) is recorded for the reference-layout
-// export, and children and visiting order are the reference's.
-__device__ __forceinline__ unsigned int atomic_add_acq_rel(unsigned int* p, unsigned int v) {
-    unsigned int old;
-    asm volatile("atom.add.acq_rel.gpu.global.u32 %0, [%1], %2;" : "=r"(old) : "l"(p), "r"(v) : "memory");
-    return old;
-}
+// parent's child slot, and the second of the two children to arrive (an
+// arrival word per node, acquire / release ordered) merges both boxes and
+// continues upwards, exactly as calcNodeAABBs (:415-492) climbs.  Internal
+// nodes are stored at index = split position; the reference's index of a node
+// (its hi if it is child 0, its lo if child 1, 0 for the root) is recorded for
+// the reference-layout export, and children and visiting order are the
+// reference's.
 
 __device__ __forceinline__ void tri_box(const float* vx, const float* vy, const float* vz, const uint32_t* tri,
                                         const float4* stage, uint32_t t, float box[6]) {
@@ -520,14 +516,50 @@ __device__ __forceinline__ void tri_box(const float* vx, const float* vy, const 
     }
 }
 
+// Arrival word of a node whose children finish in different blocks (the
+// tree pass's `counters`, zeroed by the Morton pass): bits 0-1 count the
+// children delivered, kArrReady says the first child's slot is written, and
+// bits 16-23 hold delta + 1 at the first child's far range end.  The first
+// arrival writes its slot and then publishes it with a release-ordered OR;
+// the second arrival's acquiring add usually finds the slot published
+// already, so a level of the climb costs one atomic and one slot load.
+constexpr unsigned int kArrReady = 0x100u;
+
+__device__ __forceinline__ unsigned int atom_add_acquire_gpu(unsigned int* p, unsigned int v) {
+    unsigned int old;
+    asm volatile("atom.add.acquire.gpu.global.u32 %0, [%1], %2;" : "=r"(old) : "l"(p), "r"(v) : "memory");
+    return old;
+}
+__device__ __forceinline__ void red_or_release_gpu(unsigned int* p, unsigned int v) {
+    asm volatile("red.release.gpu.global.or.b32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+__device__ __forceinline__ unsigned int ld_acquire_gpu(const unsigned int* p) {
+    unsigned int v;
+    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+
+// Child slot `slot` of node `nd`: box, reference, the child's far range end.
+__device__ __forceinline__ void write_slot(float* nd, int slot, const float box[6], uint32_t ref, uint32_t far_in) {
+    float2* b2 = reinterpret_cast<float2*>(nd + 6 * slot);
+    __stcg(b2 + 0, make_float2(box[0], box[1]));
+    __stcg(b2 + 1, make_float2(box[2], box[3]));
+    __stcg(b2 + 2, make_float2(box[4], box[5]));
+    unsigned int* w = reinterpret_cast<unsigned int*>(nd);
+    __stcg(w + 12 + slot, ref);
+    __stcg(w + 14 + slot, far_in);
+}
+
 // The device-scope climb from a finished node [lo, hi] (reference `ref`, box
-// `box`): write into the parent's child slot, count the arrival (acq_rel),
-// and continue with the merged parent if this was the second arrival.
+// `box`, d_lo = delta(lo-1, lo) and d_hi = delta(hi, hi+1), -1 past the
+// array's ends): deliver into the parent's child slot; the second arrival
+// merges the sibling's box and continues with the parent.
 template <typename KeyT>
 __device__ __forceinline__ void climb_global(const KeyT* __restrict__ keys, uint32_t n, int kbits,
                                              float* __restrict__ nodes, unsigned int* __restrict__ counters,
                                              uint32_t* __restrict__ karras_idx, float* __restrict__ root_box,
-                                             uint32_t lo, uint32_t hi, uint32_t ref, float box[6]) {
+                                             uint32_t lo, uint32_t hi, int d_lo, int d_hi, uint32_t ref,
+                                             float box[6]) {
     // every level up adds at least one common bit of the (3b + 32)-bit key
     for (int step = 0; step <= kMaxDepth; ++step) {
         if (lo == 0 && hi == n - 1) {
@@ -537,35 +569,61 @@ __device__ __forceinline__ void climb_global(const KeyT* __restrict__ keys, uint
             root_box[7] = 0.f;
             return;
         }
-        const bool left = (lo == 0) || (hi != n - 1 && delta_adj(keys, kbits, hi) > delta_adj(keys, kbits, lo - 1));
+        // the parent extends towards the larger adjacent delta (lo == 0 and
+        // hi == n - 1 give -1 on their side)
+        const bool left = d_hi > d_lo;
         const uint32_t split = left ? hi : lo - 1;
         const int slot = left ? 0 : 1;
         float* nd = nodes + 16u * split;
-        float2* b2 = reinterpret_cast<float2*>(nd + 6 * slot);
-        __stcg(b2 + 0, make_float2(box[0], box[1]));
-        __stcg(b2 + 1, make_float2(box[2], box[3]));
-        __stcg(b2 + 2, make_float2(box[4], box[5]));
-        unsigned int* w = reinterpret_cast<unsigned int*>(nd);
-        __stcg(w + 12 + slot, ref);
-        __stcg(w + 14 + slot, left ? lo : hi);
-        // release: this child's slot is visible before the arrival counts;
-        // acquire: the sibling's slot is visible to the second arrival
-        if (atomic_add_acq_rel(counters + split, 1u) == 0u) return;
-        float b[12];
+        unsigned int* ctr = counters + split;
+        const unsigned int old = atom_add_acquire_gpu(ctr, 1u);
+        write_slot(nd, slot, box, ref, left ? lo : hi);
+        if ((old & 3u) == 0u) {
+            red_or_release_gpu(ctr, kArrReady | ((unsigned int)((left ? d_lo : d_hi) + 1) << 16));
+            return;
+        }
+        unsigned int word = old;
+        for (unsigned int spins = 0; !(word & kArrReady); ++spins) {
+            if (spins > kSpinLimit) {  // the sibling never published: report, never read its slot
+                clr_raise(CLR_DEVERR_REFIT);
+                return;
+            }
+            if (spins > 64) __nanosleep(32);
+            word = ld_acquire_gpu(ctr);
+        }
+        const int d_sib = (int)((word >> 16) & 0xFFu) - 1;
+        const float* sb = nd + 6 * (1 - slot);
+        float b[6];
 #pragma unroll
-        for (int k = 0; k < 12; ++k) b[k] = __ldcg(nd + k);
-        const uint32_t far_end = __ldcg(w + 14 + (1 - slot));
+        for (int k = 0; k < 6; ++k) b[k] = __ldcg(sb + k);
+        const uint32_t far_end = __ldcg(reinterpret_cast<const unsigned int*>(nd) + 14 + (1 - slot));
 #pragma unroll
         for (int k = 0; k < 3; ++k) {
-            box[k] = fminf(b[k], b[6 + k]);
-            box[3 + k] = fmaxf(b[3 + k], b[9 + k]);
+            box[k] = fminf(box[k], b[k]);
+            box[3 + k] = fmaxf(box[3 + k], b[3 + k]);
         }
-        if (left) hi = far_end;
-        else lo = far_end;
+        if (left) {
+            hi = far_end;
+            d_hi = d_sib;
+        } else {
+            lo = far_end;
+            d_lo = d_sib;
+        }
         if (lo > hi || hi >= n) break;  // corrupt slot: report, never index out of range
         ref = split;
     }
     clr_raise(CLR_DEVERR_REFIT);
+}
+
+// The same, from a node whose outer deltas are read from the keys.
+template <typename KeyT>
+__device__ __forceinline__ void climb_global_from(const KeyT* __restrict__ keys, uint32_t n, int kbits,
+                                                  float* __restrict__ nodes, unsigned int* __restrict__ counters,
+                                                  uint32_t* __restrict__ karras_idx, float* __restrict__ root_box,
+                                                  uint32_t lo, uint32_t hi, uint32_t ref, float box[6]) {
+    const int d_lo = lo == 0 ? -1 : delta_adj(keys, kbits, lo - 1);
+    const int d_hi = hi + 1 >= n ? -1 : delta_adj(keys, kbits, hi);
+    climb_global<KeyT>(keys, n, kbits, nodes, counters, karras_idx, root_box, lo, hi, d_lo, d_hi, ref, box);
 }
 
 // Leaf j's climb over one tree of n leaves.  All arrays are the tree's own
@@ -617,7 +675,7 @@ __device__ __forceinline__ void tree_climb(const KeyT* __restrict__ keys, const 
             ref = j;
         }
     }
-    climb_global<KeyT>(keys, n, kbits, nodes, counters, karras_idx, root_box, lo, hi, ref, box);
+    climb_global_from<KeyT>(keys, n, kbits, nodes, counters, karras_idx, root_box, lo, hi, ref, box);
 }
 
 // The same climb with block-local merging.  Block b owns leaves [B, E]
@@ -796,16 +854,16 @@ __global__ void __launch_bounds__(kTreeBlock, 16) k_build_tree(const KeyT* __res
         } else {
             // first node across a block edge: deliver this child; the second
             // arrival hands the finished node to k_build_tree_top, so that this
-            // block retires instead of waiting on device-scope climbs
-            float* nd_ = nodes + 16u * split;
-            float2* b2 = reinterpret_cast<float2*>(nd_ + 6 * slot);
-            __stcg(b2 + 0, make_float2(box[0], box[1]));
-            __stcg(b2 + 1, make_float2(box[2], box[3]));
-            __stcg(b2 + 2, make_float2(box[4], box[5]));
-            unsigned int* w = reinterpret_cast<unsigned int*>(nd_);
-            __stcg(w + 12 + slot, ref);
-            __stcg(w + 14 + slot, far_in);
-            if (atomic_add_acq_rel(counters + split, 1u) == 0u) return;
+            // block retires instead of waiting on device-scope climbs.  Both
+            // slots are read only after this kernel, so no ordering is needed
+            // here; the first arrival's word still carries kArrReady and its
+            // far-end delta for a second arrival in k_build_tree_top.
+            const unsigned int old = atomicAdd(counters + split, 1u);
+            write_slot(nodes + 16u * split, slot, box, ref, far_in);
+            if ((old & 3u) == 0u) {
+                atomicOr(counters + split, kArrReady | ((unsigned int)((left ? d_lo : d_hi) + 1) << 16));
+                return;
+            }
             worklist[atomicAdd(wl_count, 1u)] = split;
             return;
         }
@@ -848,7 +906,7 @@ __global__ void __launch_bounds__(256) k_build_tree_top(const KeyT* __restrict__
             clr_raise(CLR_DEVERR_REFIT);
             continue;
         }
-        climb_global<KeyT>(keys, n, kbits, nodes, counters, karras_idx, root_box, lo, hi, split, box);
+        climb_global_from<KeyT>(keys, n, kbits, nodes, counters, karras_idx, root_box, lo, hi, split, box);
     }
 }
 
