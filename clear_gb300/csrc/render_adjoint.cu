@@ -434,7 +434,7 @@ __device__ __forceinline__ void next_event(const DScene& sc, const BSDF& bsdf, c
 // unless its pixel's loss weight is zero: its replay would add nothing to any
 // gradient, and the random-number state after the primal pass is the state
 // the replay would end in, so the pixel goes on with its next sample.
-__global__ void __launch_bounds__(kAdThreads) k_ad_primal(DScene sc, AdState S, int cur, uint32_t width,
+__global__ void __launch_bounds__(kAdThreads, 4) k_ad_primal(DScene sc, AdState S, int cur, uint32_t width,
                                                           uint32_t* __restrict__ rand_states, uint32_t max_depth,
                                                           const float4* __restrict__ dloss, uint32_t spp) {
     const uint32_t n = S.count[2 * cur];
@@ -545,7 +545,7 @@ __global__ void __launch_bounds__(kAdThreads) k_ad_primal(DScene sc, AdState S, 
 // Replay pass: the same vertex, subtracting each term from L and adding the
 // derivatives.  A finished replay starts the pixel's next sample (primal).
 template <bool kTape>
-__global__ void __launch_bounds__(kAdThreads) k_ad_replay(DScene sc, AdState S, AdParams P, int cur, uint32_t width,
+__global__ void __launch_bounds__(kAdThreads, 4) k_ad_replay(DScene sc, AdState S, AdParams P, int cur, uint32_t width,
                                                           uint32_t* __restrict__ rand_states, uint32_t spp,
                                                           uint32_t max_depth) {
     const uint32_t n = S.count[2 * cur + 1];
@@ -882,6 +882,52 @@ static size_t ad_layout(uint32_t npix, uint32_t num_params, char* base, AdState*
     return off;
 }
 
+// One block of kAdBlockIters iterations (the first of parity 0), launched as a
+// CUDA graph kept per thread and device (render_common.cuh BlockGraphCache).
+constexpr int kAdBlockIters = 8;
+
+struct AdArgs {
+    DScene sc;
+    AdState S;
+    AdParams P;
+    uint32_t width, spp, max_depth;
+    uint32_t* rand_states;
+    bool ordered, tape;
+    unsigned int grid;
+    size_t smem;
+};
+
+static void ad_block(const AdArgs& a, cudaStream_t st) {
+    for (int k = 0; k < kAdBlockIters; ++k) {
+        const int cur = k & 1;
+        if (a.ordered) k_ad_extend<true><<<a.grid, kAdThreads, 0, st>>>(a.sc, a.S, cur);
+        else k_ad_extend<false><<<a.grid, kAdThreads, 0, st>>>(a.sc, a.S, cur);
+        k_ad_reset<<<1, 1, 0, st>>>(a.S, cur ^ 1);
+        k_ad_primal<<<a.grid, kAdThreads, 0, st>>>(a.sc, a.S, cur, a.width, a.rand_states, a.max_depth, a.P.dloss,
+                                                    a.spp);
+        if (a.tape)
+            k_ad_replay<true><<<a.grid, kAdThreads, a.smem, st>>>(a.sc, a.S, a.P, cur, a.width, a.rand_states, a.spp,
+                                                                  a.max_depth);
+        else
+            k_ad_replay<false><<<a.grid, kAdThreads, a.smem, st>>>(a.sc, a.S, a.P, cur, a.width, a.rand_states, a.spp,
+                                                                   a.max_depth);
+        if (a.ordered) k_ad_shadow<true><<<a.grid, kAdThreads, a.smem, st>>>(a.sc, a.S, a.P);
+        else k_ad_shadow<false><<<a.grid, kAdThreads, a.smem, st>>>(a.sc, a.S, a.P);
+    }
+}
+
+static bool same_ad_args(const AdArgs& x, const AdArgs& y) {
+    const AdParams &p = x.P, &q = y.P;
+    return same_scene(x.sc, y.sc) && x.S.org == y.S.org && x.S.count == y.S.count && x.S.partial == y.S.partial &&
+           p.pt.tex == q.pt.tex && p.pt.kind == q.pt.kind && p.pt.k == q.pt.k && p.grad == q.grad &&
+           p.env_tex == q.env_tex && p.grad_env == q.grad_env && p.dloss == q.dloss && p.tape.rec == q.tape.rec &&
+           p.tape.cap == q.tape.cap && p.tape.count == q.tape.count && x.width == y.width && x.spp == y.spp &&
+           x.max_depth == y.max_depth && x.rand_states == y.rand_states && x.ordered == y.ordered &&
+           x.tape == y.tape && x.grid == y.grid && x.smem == y.smem;
+}
+
+thread_local BlockGraphCache<AdArgs> t_ad_graphs;
+
 }  // namespace clr
 
 using namespace clr;
@@ -940,24 +986,33 @@ extern "C" int clr_render_adjoint(const clr_scene* scene, uint32_t width, uint32
     // every iteration advances each unfinished path by one vertex; a sample
     // takes at most (max_depth + 1) vertices per pass
     const uint64_t max_iters = 2ull * spp * (max_depth + 1) + 2;
-    const bool tape = A.tape != nullptr;
-    for (uint64_t it = 0; it < max_iters; ++it) {
-        const int cur = (int)(it & 1);
-        if (ordered) k_ad_extend<true><<<grid, kAdThreads, 0, st>>>(sc, S, cur);
-        else k_ad_extend<false><<<grid, kAdThreads, 0, st>>>(sc, S, cur);
-        k_ad_reset<<<1, 1, 0, st>>>(S, cur ^ 1);
-        k_ad_primal<<<grid, kAdThreads, 0, st>>>(sc, S, cur, width, rand_states, max_depth, P.dloss, spp);
-        if (tape) k_ad_replay<true><<<grid, kAdThreads, smem, st>>>(sc, S, P, cur, width, rand_states, spp, max_depth);
-        else k_ad_replay<false><<<grid, kAdThreads, smem, st>>>(sc, S, P, cur, width, rand_states, spp, max_depth);
-        if (ordered) k_ad_shadow<true><<<grid, kAdThreads, smem, st>>>(sc, S, P);
-        else k_ad_shadow<false><<<grid, kAdThreads, smem, st>>>(sc, S, P);
-        CLR_LAUNCH_CHECK("adjoint iteration");
-        if ((it & 7) == 7) {
-            unsigned int left[2] = {0, 0};
-            CLR_CUDA_TRY(cudaMemcpyAsync(left, S.count + 2 * (cur ^ 1), sizeof(left), cudaMemcpyDeviceToHost, st));
-            CLR_CUDA_TRY(cudaStreamSynchronize(st));
-            if (left[0] + left[1] == 0) break;
+    AdArgs a{};
+    a.sc = sc;
+    a.S = S;
+    a.P = P;
+    a.width = width;
+    a.spp = spp;
+    a.max_depth = max_depth;
+    a.rand_states = rand_states;
+    a.ordered = ordered;
+    a.tape = A.tape != nullptr;
+    a.grid = grid;
+    a.smem = smem;
+    cudaGraphExec_t exec = t_ad_graphs.get(a, ad_block, same_ad_args);
+    cudaGetLastError();  // a failed capture leaves no error behind: the kernels are launched directly
+    // a block ends with the next iteration's queue counts in count[0..1]
+    for (uint64_t it = 0; it < max_iters; it += kAdBlockIters) {
+        if (exec && cudaGraphLaunch(exec, st) != cudaSuccess) {
+            cudaGetLastError();
+            t_ad_graphs.drop();
+            exec = nullptr;
         }
+        if (!exec) ad_block(a, st);
+        CLR_LAUNCH_CHECK("adjoint iterations");
+        unsigned int left[2] = {0, 0};
+        CLR_CUDA_TRY(cudaMemcpyAsync(left, S.count, sizeof(left), cudaMemcpyDeviceToHost, st));
+        CLR_CUDA_TRY(cudaStreamSynchronize(st));
+        if (left[0] + left[1] == 0) break;
     }
     if (S.partial) {
         k_ad_reduce<<<A.num_params, 256, 0, st>>>(S.partial, grid, A.num_params, A.param_kind, A.grad_params);

@@ -726,6 +726,64 @@ static inline DScene make_dscene(const clr_scene* scene) {
     return sc;
 }
 
+static inline bool same_scene(const DScene& a, const DScene& b) {
+    return a.vertices == b.vertices && a.normals == b.normals && a.tangents == b.tangents && a.uvs == b.uvs &&
+           a.faces == b.faces && a.lights == b.lights && a.materials == b.materials && a.textures == b.textures &&
+           a.others == b.others && a.nodes == b.nodes && a.tris == b.tris && a.root_box == b.root_box &&
+           a.num_tris == b.num_tris && a.alpha == b.alpha;
+}
+
+// A block of a render loop's iterations as a CUDA graph, captured on a
+// stream of the calling thread and kept per thread and device for the last
+// argument set (`same` compares two sets): the loops launch several kernels
+// per iteration, and their launch gaps cost more than the kernels of a small
+// image.  Returns null when capture is not possible; the caller then launches
+// the kernels itself.  `drop` forgets the graph after a failed launch.
+template <typename Args>
+struct BlockGraphCache {
+    static constexpr int kDevices = 64;
+    struct Entry {
+        cudaStream_t cap = nullptr;
+        cudaGraphExec_t exec = nullptr;
+        Args args{};
+    };
+    Entry e[kDevices];
+
+    template <typename Launch, typename Same>
+    cudaGraphExec_t get(const Args& a, Launch launch, Same same) {
+        int dev = 0;
+        if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kDevices) return nullptr;
+        Entry& g = e[dev];
+        if (g.exec && same(g.args, a)) return g.exec;
+        if (!g.cap && cudaStreamCreateWithFlags(&g.cap, cudaStreamNonBlocking) != cudaSuccess) {
+            g.cap = nullptr;
+            return nullptr;
+        }
+        if (g.exec) {
+            cudaGraphExecDestroy(g.exec);
+            g.exec = nullptr;
+        }
+        cudaGraph_t graph = nullptr;
+        if (cudaStreamBeginCapture(g.cap, cudaStreamCaptureModeThreadLocal) != cudaSuccess) return nullptr;
+        launch(a, g.cap);
+        if (cudaStreamEndCapture(g.cap, &graph) != cudaSuccess || !graph) return nullptr;
+        const cudaError_t err = cudaGraphInstantiate(&g.exec, graph, 0);
+        cudaGraphDestroy(graph);
+        if (err != cudaSuccess) {
+            g.exec = nullptr;
+            return nullptr;
+        }
+        g.args = a;
+        return g.exec;
+    }
+    void drop() {
+        int dev = 0;
+        if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kDevices) return;
+        e[dev].exec = nullptr;
+        e[dev].cap = nullptr;
+    }
+};
+
 static inline int check_render_args(const clr_scene* scene, uint32_t* rand_states, float* pixels) {
     if (!scene || !scene->bvh) return clr_set_error(CLR_EINVAL, "clr_render: NULL scene or bvh");
     if (!rand_states || !pixels || !scene->vertices || !scene->faces || !scene->lights || !scene->materials ||

@@ -366,63 +366,12 @@ static void wf_block(const WfArgs& a, cudaStream_t st) {
 }
 
 static bool same_args(const WfArgs& x, const WfArgs& y) {
-    const DScene &a = x.sc, &b = y.sc;
-    return a.vertices == b.vertices && a.normals == b.normals && a.tangents == b.tangents && a.uvs == b.uvs &&
-           a.faces == b.faces && a.lights == b.lights && a.materials == b.materials && a.textures == b.textures &&
-           a.others == b.others && a.nodes == b.nodes && a.tris == b.tris && a.root_box == b.root_box &&
-           a.num_tris == b.num_tris && a.alpha == b.alpha && x.S.org == y.S.org && x.S.count == y.S.count &&
-           x.S.qs == y.S.qs && x.width == y.width && x.row0 == y.row0 && x.spp == y.spp &&
-           x.max_depth == y.max_depth && x.rand_states == y.rand_states && x.px == y.px &&
-           x.ordered == y.ordered && x.grid == y.grid;
+    return same_scene(x.sc, y.sc) && x.S.org == y.S.org && x.S.count == y.S.count && x.S.qs == y.S.qs &&
+           x.width == y.width && x.row0 == y.row0 && x.spp == y.spp && x.max_depth == y.max_depth &&
+           x.rand_states == y.rand_states && x.px == y.px && x.ordered == y.ordered && x.grid == y.grid;
 }
 
-// The block as a CUDA graph, captured on a stream of the calling thread and
-// kept (per thread and device) for the last argument set: its 48 launches
-// otherwise cost more than the kernels of a small image.  Returns null when
-// capture is not possible; the caller then launches the kernels itself.
-constexpr int kWfGraphDevices = 64;
-struct WfGraph {
-    cudaStream_t cap = nullptr;
-    cudaGraphExec_t exec = nullptr;
-    WfArgs args{};
-};
-thread_local WfGraph t_wf_graph[kWfGraphDevices];
-
-static cudaGraphExec_t wf_block_graph(const WfArgs& a) {
-    int dev = 0;
-    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kWfGraphDevices) return nullptr;
-    WfGraph& g = t_wf_graph[dev];
-    if (g.exec && same_args(g.args, a)) return g.exec;
-    if (!g.cap && cudaStreamCreateWithFlags(&g.cap, cudaStreamNonBlocking) != cudaSuccess) {
-        g.cap = nullptr;
-        return nullptr;
-    }
-    if (g.exec) {
-        cudaGraphExecDestroy(g.exec);
-        g.exec = nullptr;
-    }
-    cudaGraph_t graph = nullptr;
-    if (cudaStreamBeginCapture(g.cap, cudaStreamCaptureModeThreadLocal) != cudaSuccess) return nullptr;
-    wf_block(a, g.cap);
-    if (cudaStreamEndCapture(g.cap, &graph) != cudaSuccess || !graph) return nullptr;
-    const cudaError_t e = cudaGraphInstantiate(&g.exec, graph, 0);
-    cudaGraphDestroy(graph);
-    if (e != cudaSuccess) {
-        g.exec = nullptr;
-        return nullptr;
-    }
-    g.args = a;
-    return g.exec;
-}
-
-// Forgets the calling thread's graph for the current device (a launch of it
-// failed, e.g. after a device reset).
-static void wf_block_graph_drop() {
-    int dev = 0;
-    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kWfGraphDevices) return;
-    t_wf_graph[dev].exec = nullptr;
-    t_wf_graph[dev].cap = nullptr;
-}
+thread_local BlockGraphCache<WfArgs> t_wf_graphs;
 
 }  // namespace clr
 
@@ -461,7 +410,7 @@ extern "C" int clr_render_wavefront_rows(const clr_scene* scene, uint32_t width,
     k_wf_init<<<grid, kWfThreads, 0, st>>>(sc, S, npix, width, row0, rand_states);
     CLR_LAUNCH_CHECK("k_wf_init");
     const WfArgs a{sc, S, width, row0, spp, max_depth, rand_states, px, ordered, grid};
-    cudaGraphExec_t exec = wf_block_graph(a);
+    cudaGraphExec_t exec = t_wf_graphs.get(a, wf_block, same_args);
     cudaGetLastError();  // a failed capture leaves no error behind: the kernels are launched directly
     // every iteration advances each unfinished pixel by one path vertex; a
     // block ends with the next iteration's queue count in count[0]
@@ -469,7 +418,7 @@ extern "C" int clr_render_wavefront_rows(const clr_scene* scene, uint32_t width,
     for (uint64_t it = 0; it < max_iters; it += kWfBlockIters) {
         if (exec && cudaGraphLaunch(exec, st) != cudaSuccess) {
             cudaGetLastError();
-            wf_block_graph_drop();
+            t_wf_graphs.drop();
             exec = nullptr;
         }
         if (!exec) wf_block(a, st);
