@@ -257,3 +257,65 @@ def test_material_zoo_matches_reference_sim(cuda, wavefront):
     print(f"zoo: rel RMSE {rel_rmse:.4g}, mean err {mean_err:.4g}, close {frac_close:.4f}")
     assert rel_rmse <= 1e-3 and mean_err <= 1e-5 and frac_close >= 0.999, (rel_rmse, mean_err, frac_close)
     assert _lib.device_status() == 0
+
+
+def _megakernel_reference(ds, spp, depth, ordered):
+    rng, pix = ds.new_frame()
+    ds.render(rng, pix, spp, max_depth=depth, ordered=ordered, wavefront=False)
+    return rng, pix
+
+
+@pytest.mark.gpu
+def test_wavefront_graph_follows_changing_arguments(cuda):
+    """The wavefront form launches its iterations as a CUDA graph kept for the
+    last argument set; calls that alternate scenes, sample counts, depths,
+    traversal orders and frames (new state and pixel buffers) must each give
+    the megakernel's image and random states bit for bit."""
+    a = DeviceScene(scenes.cornell_box(64, 64), cuda)
+    b = DeviceScene(scenes.cornell_box(48, 40, env=env_map()), cuda)
+    calls = [(a, 3, 5, True), (b, 2, 4, True), (a, 5, 5, True), (a, 3, 5, False), (b, 2, 4, True), (a, 3, 5, True)]
+    for ds, spp, depth, ordered in calls:
+        rng, pix = ds.new_frame()
+        ds.render(rng, pix, spp, max_depth=depth, ordered=ordered, wavefront=True)
+        ref_rng, ref_pix = _megakernel_reference(ds, spp, depth, ordered)
+        torch.cuda.synchronize()
+        assert torch.equal(pix, ref_pix) and torch.equal(rng, ref_rng), (spp, depth, ordered)
+    assert _lib.device_status() == 0
+
+
+@pytest.mark.gpu
+def test_wavefront_renders_from_two_host_threads(cuda):
+    """Two host threads render their own scenes on their own streams at the
+    same time (each thread keeps its own iteration graphs): every image equals
+    the megakernel's."""
+    import threading
+
+    dss = [DeviceScene(scenes.cornell_box(64, 64), cuda), DeviceScene(scenes.cornell_box(56, 48, env=env_map()), cuda)]
+    refs = [[_megakernel_reference(ds, spp, 5, True) for spp in (2, 3, 4)] for ds in dss]
+    torch.cuda.synchronize()
+    out = [[None] * 3 for _ in dss]
+    errors = []
+
+    def work(k):
+        try:
+            st = torch.cuda.Stream(cuda)
+            with torch.cuda.device(cuda), torch.cuda.stream(st):
+                for j, spp in enumerate((2, 3, 4)):
+                    rng, pix = dss[k].new_frame()
+                    dss[k].render(rng, pix, spp, max_depth=5, ordered=True, wavefront=True)
+                    out[k][j] = (rng, pix)
+            st.synchronize()
+        except Exception as e:  # reported on the main thread
+            errors.append(e)
+
+    threads = [threading.Thread(target=work, args=(k,)) for k in range(2)]
+    for t in threads:
+        t.start()
+    for t in threads:
+        t.join()
+    assert not errors, errors
+    torch.cuda.synchronize()
+    for k in range(2):
+        for j in range(3):
+            assert torch.equal(out[k][j][1], refs[k][j][1]) and torch.equal(out[k][j][0], refs[k][j][0]), (k, j)
+    assert _lib.device_status() == 0
