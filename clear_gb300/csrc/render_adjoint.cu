@@ -20,7 +20,9 @@
 //                 shadow pass has removed vertex k's next-event term.  Emission
 //                 and next-event terms add their own BSDF / environment-texel
 //                 derivatives.
-// Nothing of a path is stored between its passes but its RNG state.
+// Between its passes a path keeps its RNG state and, for its first kAdCache
+// vertices, the primal's hit records and next-event visibilities, so that the
+// replay traces only what lies deeper (the same rays give the same answers).
 //
 // Gradients of the material parameters are summed per block in shared memory
 // and kept per block in the workspace; one reduction adds them to the caller's
@@ -40,6 +42,14 @@ namespace clr {
 constexpr int kAdThreads = 128;
 constexpr uint32_t kSmemParams = 1024;  // parameters summed in shared memory (K * 16 B)
 constexpr int kShWords = 4 + kMaxGrad;  // float4s per shadow entry
+// The replay pass traces the primal pass's rays again (same random numbers,
+// same arithmetic), so the primal's answers are kept for the replay: the hit
+// record of each of a path's first kAdCache vertices, and per vertex whether
+// its next-event ray was unoccluded.  A shadow entry's path word carries the
+// vertex depth in its top bits (kShDepthShift), for images below 2^27 pixels.
+constexpr uint32_t kAdCache = 8;
+constexpr uint32_t kShDepthShift = 27;
+constexpr uint32_t kShPixMask = (1u << kShDepthShift) - 1u;
 
 // Tape record kinds (word 3, bits 0-7); bit 8 marks a visible next-event record.
 enum : uint32_t { kTapeCam = 0, kTapeEmit = 1, kTapeRR = 2, kTapeNee = 3, kTapeSample = 4, kTapeVisible = 0x100 };
@@ -59,6 +69,8 @@ struct AdState {
     float4* sh;      // kShWords float4s per shadow entry
     unsigned int* count;  // [2 * parity + pass] queued paths, [4] shadow entries
     float* partial;  // per-block parameter gradients (grid x K x 4), or null
+    float4* hitc;    // kAdCache per path: the primal pass's hit record at each vertex
+    uint32_t* visc;  // per path: bit k = the primal's next-event ray at vertex k was unoccluded
 };
 
 struct Tape {
@@ -302,6 +314,13 @@ __global__ void __launch_bounds__(kAdThreads, 8) k_ad_extend(DScene sc, AdState 
     uint2 stack[kStackSize];
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         const uint32_t p = i < n0 ? q0[i] : q1[i - n0];
+        if (i >= n0) {  // replay pass: the primal found this vertex's hit already
+            const uint32_t depth = S.misc[p].x;
+            if (depth < kAdCache) {
+                S.hit[p] = S.hitc[(size_t)kAdCache * p + depth];
+                continue;
+            }
+        }
         const float4 o = S.org[p], d = S.dir[p];
         Hit h;
         if (intersect<kOrdered>(sc, mk(o.x, o.y, o.z), mk(d.x, d.y, d.z), h, stack))
@@ -457,6 +476,7 @@ __global__ void __launch_bounds__(kAdThreads, 4) k_ad_primal(DScene sc, AdState 
             const float initY = a4.w;
             uint32_t depth = m.x, sampledType = m.y;
             bool ended = false;
+            if (depth < kAdCache) S.hitc[(size_t)kAdCache * p + depth] = h4;  // for the replay pass
             const uint32_t hid = __float_as_uint(h4.x);
             uint32_t light_face = __float_as_uint(o4.w);
             SurfPt sp;
@@ -496,7 +516,8 @@ __global__ void __launch_bounds__(kAdThreads, 4) k_ad_primal(DScene sc, AdState 
                         const f3 c = ne.s * (alpha * ne.le * ne.fs);
                         sh0 = make_float4(ne.org.x, ne.org.y, ne.org.z,
                                               __uint_as_float(shadow_light_word(ne.lpos)));
-                        sh1 = make_float4(ne.dir.x, ne.dir.y, ne.dir.z, __uint_as_float(p));
+                        sh1 = make_float4(ne.dir.x, ne.dir.y, ne.dir.z,
+                                          __uint_as_float(p | (min(depth, 31u) << kShDepthShift)));
                         sh2 = make_float4(c.x, c.y, c.z, __uint_as_float(1u));  // add to L
                         shadow = true;
                     }
@@ -688,7 +709,8 @@ __global__ void __launch_bounds__(kAdThreads, 4) k_ad_replay(DScene sc, AdState 
                         }
                         se.e[0] = make_float4(ne.org.x, ne.org.y, ne.org.z,
                                               __uint_as_float(shadow_light_word(ne.lpos)));
-                        se.e[1] = make_float4(ne.dir.x, ne.dir.y, ne.dir.z, __uint_as_float(p));
+                        se.e[1] = make_float4(ne.dir.x, ne.dir.y, ne.dir.z,
+                                              __uint_as_float(p | (min(depth, 31u) << kShDepthShift)));
                         se.e[2] = make_float4(c.x, c.y, c.z, __uint_as_float(tflag | 2u));  // bit 0 set below
                         shadow = true;
                     }
@@ -775,9 +797,19 @@ __global__ void __launch_bounds__(kAdThreads, 8) k_ad_shadow(DScene sc, AdState 
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         const float4* e = S.sh + (size_t)kShWords * i;
         const float4 a = e[0], b = e[1], c = e[2];
-        const uint32_t p = __float_as_uint(b.w), flags = __float_as_uint(c.w);
-        if (!shadow_visible<kOrdered>(sc, mk(a.x, a.y, a.z), mk(b.x, b.y, b.z), __float_as_uint(a.w), stack)) continue;
+        const uint32_t pw = __float_as_uint(b.w), flags = __float_as_uint(c.w);
+        const uint32_t p = pw & kShPixMask, depth = pw >> kShDepthShift;
         const bool replay = (flags & 2u) != 0;
+        bool visible;
+        if (replay && depth < kAdCache) {
+            visible = (S.visc[p] >> depth) & 1u;  // the primal traced this ray
+        } else {
+            visible = shadow_visible<kOrdered>(sc, mk(a.x, a.y, a.z), mk(b.x, b.y, b.z), __float_as_uint(a.w), stack);
+            // one entry per path per launch: this is the bit's only writer
+            if (!replay && depth < kAdCache)
+                S.visc[p] = (S.visc[p] & ~(1u << depth)) | ((visible ? 1u : 0u) << depth);
+        }
+        if (!visible) continue;
         if (flags & 1u) {
             float4 L = S.L[p];
             if (replay) {
@@ -861,7 +893,8 @@ static size_t ad_layout(uint32_t npix, uint32_t num_params, char* base, AdState*
     const size_t n = npix;
     const size_t o_org = take(16 * n), o_dir = take(16 * n), o_alpha = take(16 * n), o_misc = take(16 * n),
                  o_hit = take(16 * n), o_L = take(16 * n), o_rng0 = take(16 * n), o_pd = take(16 * kMaxGrad * n),
-                 o_q = take(16 * n), o_sh = take(16 * kShWords * n), o_cnt = take(32);
+                 o_q = take(16 * n), o_sh = take(16 * kShWords * n), o_cnt = take(32),
+                 o_hitc = take(16 * kAdCache * n), o_visc = take(4 * n);
     const int mode = sink_mode(num_params);
     const bool use_partial = mode == kSinkPrivate || mode == kSinkShared;
     const size_t o_part = use_partial ? take((size_t)ad_grid(npix) * num_params * 16) : 0;
@@ -878,6 +911,8 @@ static size_t ad_layout(uint32_t npix, uint32_t num_params, char* base, AdState*
         S->sh = reinterpret_cast<float4*>(base + o_sh);
         S->count = reinterpret_cast<unsigned int*>(base + o_cnt);
         S->partial = use_partial ? reinterpret_cast<float*>(base + o_part) : nullptr;
+        S->hitc = reinterpret_cast<float4*>(base + o_hitc);
+        S->visc = reinterpret_cast<uint32_t*>(base + o_visc);
     }
     return off;
 }
@@ -956,6 +991,8 @@ extern "C" int clr_render_adjoint(const clr_scene* scene, uint32_t width, uint32
          reinterpret_cast<uintptr_t>(A.tape)) & 15u)
         return clr_set_error(CLR_EINVAL, "clr_render_adjoint: gradient and tape buffers must be 16-byte aligned");
     if (width == 0 || height == 0 || spp == 0) return CLR_OK;
+    if ((uint64_t)width * height > kShPixMask)
+        return clr_set_error(CLR_EINVAL, "clr_render_adjoint: %u x %u pixels exceed 2^27 - 1", width, height);
     const uint32_t npix = width * height;
     const size_t need = ad_layout(npix, A.num_params, nullptr, nullptr);
     if (!workspace || workspace_bytes < need)

@@ -456,7 +456,10 @@ typedef struct clr_adjoint_params {
  * sampling decisions, pdfs, MIS weights and roulette probabilities held
  * constant.  rand_states advance exactly as in the forward render.  The
  * workspace (256-byte aligned) holds at least
- * clr_render_adjoint_workspace_bytes(width, height, num_params) bytes. */
+ * clr_render_adjoint_workspace_bytes(width, height, num_params) bytes
+ * (including 132 bytes per pixel in which the primal pass keeps the hit
+ * records and next-event visibilities of each path's first 8 vertices for the
+ * replay pass).  width * height must stay below 2^27 (CLR_EINVAL). */
 CLR_API int clr_render_adjoint_workspace_bytes(uint32_t width, uint32_t height, uint32_t num_params,
                                                uint64_t* bytes);
 CLR_API int clr_render_adjoint(const clr_scene* scene, uint32_t width, uint32_t height, uint32_t* rand_states,
