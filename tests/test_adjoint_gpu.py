@@ -128,12 +128,15 @@ def _write_params(ds, info, albedo, roughness, env):
 
 
 @pytest.mark.gpu
-def test_adjoint_matches_fp64_finite_differences(cuda):
+# depth 12: the replay pass takes the primal's hit records and next-event
+# visibilities for a path's first 8 vertices and traces the deeper ones
+@pytest.mark.parametrize("depth", [DEPTH, 12])
+def test_adjoint_matches_fp64_finite_differences(cuda, depth):
     sc, info, ds, tex, kind = _setup(cuda)
     target = _target(cuda, info)
     rng, pix = ds.new_frame()
     seeds = rng.clone()
-    ds.render(rng, pix, SPP, DEPTH, wavefront=True)
+    ds.render(rng, pix, SPP, depth, wavefront=True)
     dloss = _dloss(pix, target)
     grad = torch.zeros((16, 4), dtype=torch.float32, device=cuda)
     T = info["env"].shape[0] * info["env"].shape[1]
@@ -141,7 +144,7 @@ def test_adjoint_matches_fp64_finite_differences(cuda):
     tape = torch.zeros((TAPE_CAP, 32), dtype=torch.int32, device=cuda)
     count = torch.zeros(1, dtype=torch.int32, device=cuda)
     rng_adj = seeds.clone()
-    ds.render_adjoint(rng_adj, dloss, SPP, DEPTH, tex, kind, grad, info["env_tex"], genv, tape, count)
+    ds.render_adjoint(rng_adj, dloss, SPP, depth, tex, kind, grad, info["env_tex"], genv, tape, count)
     torch.cuda.synchronize()
     assert _lib.device_status() == 0
     assert torch.equal(rng_adj, rng), "the adjoint must consume the forward render's random numbers"
