@@ -740,11 +740,31 @@ def run_ours(args):
     for _ in range(trav_steps):
         lbvh.trace_closest(bvh, crays, hid2, ht2, ordered=True)
     t3.record(stream)
+    # the same searches with the rays sorted by origin first (the sort inside
+    # the timed region)
+    hid3 = torch.empty(m, dtype=torch.int32, device=dev)
+    ht3 = torch.empty(m, dtype=torch.float32, device=dev)
+    occ3 = torch.empty(m, dtype=torch.uint8, device=dev)
+    lbvh.trace_closest(bvh, crays, hid3, ht3, sort=True)
+    lbvh.trace_shadow(bvh, srays, occ3, sort=True)
+    t4, t5, t6 = (torch.cuda.Event(enable_timing=True) for _ in range(3))
+    t4.record(stream)
+    for _ in range(trav_steps):
+        lbvh.trace_closest(bvh, crays, hid3, ht3, sort=True)
+    t5.record(stream)
+    for _ in range(trav_steps):
+        lbvh.trace_shadow(bvh, srays, occ3, sort=True)
+    t6.record(stream)
     torch.cuda.synchronize()
     lbvh.trace_replays(clear=True)
     refo_ms = t0.elapsed_time(t1) / trav_steps
     shadow_ms = t1.elapsed_time(t2) / trav_steps
     closest_ms = t2.elapsed_time(t3) / trav_steps
+    closest_sorted_ms = t4.elapsed_time(t5) / trav_steps
+    shadow_sorted_ms = t5.elapsed_time(t6) / trav_steps
+    sorted_mismatches = int((hid3 != hid2).sum().item() + (ht3.view(torch.int32) != ht2.view(torch.int32)).sum().item()
+                            + (occ3 != occ).sum().item())
+    del hid3, ht3, occ3
     # visiting statistics of the reference-order query: the bytes that search
     # gathers per ray, 64 per node loaded and 48 per triangle tested, plus the
     # 32-byte ray and its 8-byte result
@@ -766,8 +786,8 @@ def run_ours(args):
     dev_err = _lib.device_status()
 
     # ---- max over ranks
-    ms_step, e2e_ms, e2e_serial_ms, closest_ms, shadow_ms = shard.max_over_ranks(
-        [ms_step, e2e_ms, e2e_serial_ms, closest_ms, shadow_ms], dev)
+    ms_step, e2e_ms, e2e_serial_ms, closest_ms, shadow_ms, closest_sorted_ms, shadow_sorted_ms = shard.max_over_ranks(
+        [ms_step, e2e_ms, e2e_serial_ms, closest_ms, shadow_ms, closest_sorted_ms, shadow_sorted_ms], dev)
     if rank != 0:
         dist.destroy_process_group()
         return
@@ -810,6 +830,11 @@ def run_ours(args):
                       "fast_vs_reference_order_id_mismatches": ordered_id_mismatch,
                       "fast_vs_reference_order_t_mismatches": ordered_t_mismatch,
                       "closest_ms": closest_ms, "closest_reference_order_ms": refo_ms, "shadow_ms": shadow_ms,
+                      "closest_sorted_mrays_s": m / closest_sorted_ms / 1e3,
+                      "shadow_sorted_mrays_s": m / shadow_sorted_ms / 1e3,
+                      "sorted_form": "rays sorted by the Morton code of their origin first (sort timed); "
+                                     "the same answers as the given order",
+                      "sorted_vs_given_order_mismatches": sorted_mismatches,
                       "closest_hit_frac": hit_frac,
                       "reference_order_nodes_per_ray": nodes_per_ray, "reference_order_tris_per_ray": tris_per_ray,
                       "reference_order_gather_gbs": fetch_bytes / (refo_ms * 1e-3) / 1e9,

@@ -96,6 +96,9 @@ def lib() -> C.CDLL:
             "clr_trace_closest": [C.POINTER(ClrBvh), vp, u32, vp, vp, vp],
             "clr_trace_closest_ordered": [C.POINTER(ClrBvh), vp, u32, vp, vp, vp],
             "clr_trace_shadow": [C.POINTER(ClrBvh), vp, u32, vp, vp],
+            "clr_trace_sort_workspace_bytes": [u32, C.POINTER(C.c_uint64)],
+            "clr_trace_closest_sorted": [C.POINTER(ClrBvh), vp, u32, vp, vp, vp, C.c_uint64, vp],
+            "clr_trace_shadow_sorted": [C.POINTER(ClrBvh), vp, u32, vp, vp, C.c_uint64, vp],
             "clr_device_status": [C.POINTER(u32), i32],
             "clr_trace_replays": [C.POINTER(C.c_uint64), i32],
             "clr_debug_set_wait_limits": [u32, u32],

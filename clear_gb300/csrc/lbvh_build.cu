@@ -1570,6 +1570,155 @@ extern "C" int clr_lbvh_build_batched(clr_lbvh* h, const float* vx, const float*
     return CLR_OK;
 }
 
+// ---------------------------------------------------------------- ray order
+//
+// Rays sorted by the Morton code of their origin before the searches: the
+// rays a warp searches together then start in the same region of the scene
+// and share the tree's nodes in L1 / L2.  The order changes no ray's answer
+// (each is written to its own index).  Keys: the origin quantised to 8 bits
+// per axis in the tree's root box (clamped outside it), 24 bits, sorted by
+// three one-sweep passes of the build's radix sort.
+constexpr int kRayKeyBits = 8;
+constexpr int kRayPasses = 3;
+
+__global__ void __launch_bounds__(256) k_ray_keys(const float4* __restrict__ rays, uint32_t n,
+                                                  const float* __restrict__ root_box, uint32_t* __restrict__ keys,
+                                                  unsigned int* __restrict__ hist) {
+    __shared__ unsigned int sh[kRayPasses * kRadix];
+    for (int i = threadIdx.x; i < kRayPasses * kRadix; i += blockDim.x) sh[i] = 0;
+    float mn[3], sc[3];
+    for (int k = 0; k < 3; ++k) {
+        mn[k] = __ldg(root_box + k);
+        const float ext = __ldg(root_box + 4 + k) - mn[k];
+        sc[k] = ext > 0.f ? (float)(1 << kRayKeyBits) / ext : 0.f;
+    }
+    __syncthreads();
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const float4 o = __ldg(rays + 2ull * i);
+        const float c[3] = {o.x, o.y, o.z};
+        uint32_t q[3];
+        for (int k = 0; k < 3; ++k) {
+            const float f = (c[k] - mn[k]) * sc[k];  // NaN and out-of-box origins clamp below
+            q[k] = f > 0.f ? (uint32_t)fminf(f, (float)((1 << kRayKeyBits) - 1)) : 0u;
+        }
+        const uint32_t key = spread3_10(q[0]) | (spread3_10(q[1]) << 1) | (spread3_10(q[2]) << 2);
+        keys[i] = key;
+        for (int p = 0; p < kRayPasses; ++p) atomicAdd(&sh[p * kRadix + ((key >> (8 * p)) & 0xFFu)], 1u);
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < kRayPasses * kRadix; i += blockDim.x)
+        if (sh[i]) atomicAdd(hist + i, sh[i]);
+}
+
+namespace {
+struct RaySortLayout {
+    uint32_t* keys[2];
+    uint32_t* vals[2];
+    unsigned int* hist;     // [pass][256]
+    unsigned int* tiles;    // [pass] tile counters
+    unsigned int* status;   // [pass][tile][256]
+    size_t status_stride;
+    char* zero;             // hist, tile counters, status: cleared per call
+    size_t zero_bytes;
+};
+}  // namespace
+
+static size_t ray_sort_layout(uint32_t n, char* base, RaySortLayout* L) {
+    constexpr unsigned int kTile = kSortThreads * SortCfg<uint32_t>::kItems;
+    const size_t tiles = div_up(n ? n : 1, kTile);
+    size_t off = 0;
+    auto take = [&](size_t bytes) {
+        const size_t o = off;
+        off = align_up(off + bytes, 256);
+        return o;
+    };
+    const size_t o_k0 = take(4ull * n), o_k1 = take(4ull * n), o_v0 = take(4ull * n), o_v1 = take(4ull * n);
+    const size_t o_zero = off;
+    const size_t o_hist = take(4ull * kRayPasses * kRadix), o_tiles = take(4ull * kRayPasses),
+                 o_status = take(4ull * kRayPasses * tiles * kRadix);
+    if (base && L) {
+        L->keys[0] = reinterpret_cast<uint32_t*>(base + o_k0);
+        L->keys[1] = reinterpret_cast<uint32_t*>(base + o_k1);
+        L->vals[0] = reinterpret_cast<uint32_t*>(base + o_v0);
+        L->vals[1] = reinterpret_cast<uint32_t*>(base + o_v1);
+        L->hist = reinterpret_cast<unsigned int*>(base + o_hist);
+        L->tiles = reinterpret_cast<unsigned int*>(base + o_tiles);
+        L->status = reinterpret_cast<unsigned int*>(base + o_status);
+        L->status_stride = tiles * kRadix;
+        L->zero = base + o_zero;
+        L->zero_bytes = off - o_zero;
+    }
+    return off;
+}
+
+// Sorts the ray indices by origin key; returns the order (in the workspace).
+static int ray_order(const clr_bvh* bvh, const float* rays, uint32_t n, void* workspace, uint64_t workspace_bytes,
+                     cudaStream_t st, const uint32_t** order) {
+    if (!bvh || !rays) return clr_set_error(CLR_EINVAL, "trace (sorted): NULL bvh or rays");
+    if (!bvh->root_box) return clr_set_error(CLR_EINVAL, "trace (sorted): bvh has no root box");
+    if (!workspace || workspace_bytes < ray_sort_layout(n, nullptr, nullptr))
+        return clr_set_error(CLR_ECAPACITY, "trace (sorted): workspace of %llu bytes is smaller than %zu",
+                             (unsigned long long)workspace_bytes, ray_sort_layout(n, nullptr, nullptr));
+    if (reinterpret_cast<uintptr_t>(workspace) & 255u)
+        return clr_set_error(CLR_EINVAL, "trace (sorted): workspace must be 256-byte aligned");
+    if (reinterpret_cast<uintptr_t>(rays) & 15u) return clr_set_error(CLR_EINVAL, "trace: rays must be 16-byte aligned");
+    RaySortLayout L;
+    ray_sort_layout(n, static_cast<char*>(workspace), &L);
+    CLR_CUDA_TRY(cudaMemsetAsync(L.zero, 0, L.zero_bytes, st));
+    const unsigned int grid = std::min(div_up(n, 256u), (unsigned int)clr_sm_count() * 8u);
+    k_ray_keys<<<grid, 256, 0, st>>>(reinterpret_cast<const float4*>(rays), n, bvh->root_box, L.keys[0], L.hist);
+    CLR_LAUNCH_CHECK("k_ray_keys");
+    constexpr int kTile = kSortThreads * SortCfg<uint32_t>::kItems;
+    const unsigned int tiles = div_up(n, kTile);
+    for (int p = 0; p < kRayPasses; ++p) {
+        const int src = p & 1, dst = src ^ 1;
+        if (p == 0)
+            k_onesweep<uint32_t, true><<<tiles, kSortThreads, 0, st>>>(
+                L.keys[src], nullptr, L.keys[dst], L.vals[dst], n, 8 * p, L.hist + p * kRadix,
+                L.status + p * L.status_stride, L.tiles + p, g_sort_spin_limit);
+        else
+            k_onesweep<uint32_t, false><<<tiles, kSortThreads, 0, st>>>(
+                L.keys[src], L.vals[src], L.keys[dst], L.vals[dst], n, 8 * p, L.hist + p * kRadix,
+                L.status + p * L.status_stride, L.tiles + p, g_sort_spin_limit);
+        CLR_LAUNCH_CHECK("k_onesweep (rays)");
+    }
+    *order = L.vals[kRayPasses & 1];
+    return CLR_OK;
+}
+
+int clr_trace_closest_in_order(const clr_bvh* bvh, const float* rays, uint32_t num_rays, const uint32_t* order,
+                               uint32_t* hit_id, float* hit_t, void* stream);
+int clr_trace_shadow_in_order(const clr_bvh* bvh, const float* rays, uint32_t num_rays, const uint32_t* order,
+                              uint8_t* occluded, void* stream);
+
+extern "C" int clr_trace_sort_workspace_bytes(uint32_t num_rays, uint64_t* bytes) {
+    if (!bytes) return clr_set_error(CLR_EINVAL, "clr_trace_sort_workspace_bytes: bytes is NULL");
+    *bytes = ray_sort_layout(num_rays, nullptr, nullptr);
+    return CLR_OK;
+}
+
+extern "C" int clr_trace_closest_sorted(const clr_bvh* bvh, const float* rays, uint32_t num_rays, uint32_t* hit_id,
+                                        float* hit_t, void* workspace, uint64_t workspace_bytes, void* stream) {
+    if (num_rays == 0) return clr_trace_closest_in_order(bvh, rays, 0, nullptr, hit_id, hit_t, stream);
+    if (!bvh || bvh->num_tris == 0) return clr_trace_closest_in_order(bvh, rays, num_rays, nullptr, hit_id, hit_t, stream);
+    const uint32_t* order = nullptr;
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    int rc = ray_order(bvh, rays, num_rays, workspace, workspace_bytes, st, &order);
+    if (rc != CLR_OK) return rc;
+    return clr_trace_closest_in_order(bvh, rays, num_rays, order, hit_id, hit_t, stream);
+}
+
+extern "C" int clr_trace_shadow_sorted(const clr_bvh* bvh, const float* rays, uint32_t num_rays, uint8_t* occluded,
+                                       void* workspace, uint64_t workspace_bytes, void* stream) {
+    if (num_rays == 0) return clr_trace_shadow_in_order(bvh, rays, 0, nullptr, occluded, stream);
+    if (!bvh || bvh->num_tris == 0) return clr_trace_shadow_in_order(bvh, rays, num_rays, nullptr, occluded, stream);
+    const uint32_t* order = nullptr;
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    int rc = ray_order(bvh, rays, num_rays, workspace, workspace_bytes, st, &order);
+    if (rc != CLR_OK) return rc;
+    return clr_trace_shadow_in_order(bvh, rays, num_rays, order, occluded, stream);
+}
+
 extern "C" int clr_lbvh_export_reference(clr_lbvh* h, const clr_bvh* bvh, void* inodes, void* lnodes,
                                          uint32_t* parents, uint32_t* sorted_idx, uint64_t* keys, void* stream) {
     if (!h || !bvh) return clr_set_error(CLR_EINVAL, "clr_lbvh_export_reference: NULL argument");

@@ -123,12 +123,15 @@ __device__ __forceinline__ void closest_step(ClosestState& s, const float4* __re
 static __device__ unsigned long long g_replays = 0;
 
 // kFast: the nearer-first search with replay; otherwise the reference's order.
-// Both give the reference's ids and distances.
+// Both give the reference's ids and distances.  With `order`, the r-th ray
+// searched is rays[order[r]] (results go to its own index): rays sorted by
+// origin share the tree's nodes within a warp.
 template <bool kFast>
 __global__ void __launch_bounds__(kTraceThreads) k_trace_closest(const float4* __restrict__ nodes,
                                                                  const float4* __restrict__ tris,
                                                                  const float* __restrict__ root_box, uint32_t n,
                                                                  const float4* __restrict__ rays, uint32_t nr,
+                                                                 const uint32_t* __restrict__ order,
                                                                  uint32_t* __restrict__ hit_id,
                                                                  float* __restrict__ hit_t) {
     const uint32_t P = gridDim.x * blockDim.x;
@@ -137,7 +140,8 @@ __global__ void __launch_bounds__(kTraceThreads) k_trace_closest(const float4* _
     const float S = replay_scale(root_box);
     uint2 stack[kStackSize];
     ClosestState s;
-    closest_begin(s, rays, r, root_box, n, tris, stack, !kFast);
+    uint32_t q = order ? __ldg(order + r) : r;
+    closest_begin(s, rays, q, root_box, n, tris, stack, !kFast);
     unsigned int replays = 0;
     // a valid tree pops each internal node at most once per ray and search
     uint32_t guard = 0;
@@ -150,15 +154,16 @@ __global__ void __launch_bounds__(kTraceThreads) k_trace_closest(const float4* _
         if (kFast && !s.exact && needs_replay(s.t, s.gbest, s.t2, S)) {
             ++replays;
             guard = 0;
-            closest_begin(s, rays, r, root_box, n, tris, stack, true);
+            closest_begin(s, rays, q, root_box, n, tris, stack, true);
             continue;
         }
-        hit_id[r] = s.best;
-        hit_t[r] = s.t;
+        hit_id[q] = s.best;
+        hit_t[q] = s.t;
         r += P;
         if (r >= nr) break;
         guard = 0;
-        closest_begin(s, rays, r, root_box, n, tris, stack, !kFast);
+        q = order ? __ldg(order + r) : r;
+        closest_begin(s, rays, q, root_box, n, tris, stack, !kFast);
     }
     if (kFast && replays) atomicAdd(&g_replays, (unsigned long long)replays);
 }
@@ -169,10 +174,12 @@ __global__ void __launch_bounds__(kTraceThreads) k_trace_shadow(const float4* __
                                                                 const float4* __restrict__ tris,
                                                                 const float* __restrict__ root_box, uint32_t n,
                                                                 const float4* __restrict__ rays, uint32_t nr,
+                                                                const uint32_t* __restrict__ order,
                                                                 uint8_t* __restrict__ occluded) {
     const uint32_t P = gridDim.x * blockDim.x;
     uint32_t stack[kStackSize];
-    for (uint32_t r = blockIdx.x * blockDim.x + threadIdx.x; r < nr; r += P) {
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < nr; i += P) {
+        const uint32_t r = order ? __ldg(order + i) : i;
         const Ray ray = load_ray(rays, r);
         const float ix = 1.0f / ray.dx, iy = 1.0f / ray.dy, iz = 1.0f / ray.dz;
         const float tmax = ray.tmax;
@@ -245,27 +252,51 @@ static int check_trace_args(const clr_bvh* bvh, const float* rays, uint32_t num_
 }
 
 template <bool kFast>
-static int trace_closest(const clr_bvh* bvh, const float* rays, uint32_t num_rays, uint32_t* hit_id, float* hit_t,
-                         void* stream) {
+static int trace_closest(const clr_bvh* bvh, const float* rays, uint32_t num_rays, const uint32_t* order,
+                         uint32_t* hit_id, float* hit_t, void* stream) {
     int rc = check_trace_args(bvh, rays, num_rays, hit_id);
     if (rc != CLR_OK || num_rays == 0) return rc;
     if (!hit_t) return clr_set_error(CLR_EINVAL, "clr_trace_closest: hit_t is NULL");
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     k_trace_closest<kFast><<<persistent_grid(k_trace_closest<kFast>, num_rays), kTraceThreads, 0, st>>>(
         static_cast<const float4*>(bvh->nodes), static_cast<const float4*>(bvh->tris), bvh->root_box, bvh->num_tris,
-        reinterpret_cast<const float4*>(rays), num_rays, hit_id, hit_t);
+        reinterpret_cast<const float4*>(rays), num_rays, order, hit_id, hit_t);
     CLR_LAUNCH_CHECK("k_trace_closest");
     return CLR_OK;
 }
 
+static int trace_shadow(const clr_bvh* bvh, const float* rays, uint32_t num_rays, const uint32_t* order,
+                        uint8_t* occluded, void* stream) {
+    int rc = check_trace_args(bvh, rays, num_rays, occluded);
+    if (rc != CLR_OK || num_rays == 0) return rc;
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    // shadow segments are short (most end at the first accepted triangle):
+    // one ray per thread with hardware block scheduling balances them best
+    k_trace_shadow<<<div_up(num_rays, kTraceThreads), kTraceThreads, 0, st>>>(
+        static_cast<const float4*>(bvh->nodes), static_cast<const float4*>(bvh->tris), bvh->root_box, bvh->num_tris,
+        reinterpret_cast<const float4*>(rays), num_rays, order, occluded);
+    CLR_LAUNCH_CHECK("k_trace_shadow");
+    return CLR_OK;
+}
+
+// The searches over a ray order (lbvh_build.cu sorts the rays).
+int clr_trace_closest_in_order(const clr_bvh* bvh, const float* rays, uint32_t num_rays, const uint32_t* order,
+                               uint32_t* hit_id, float* hit_t, void* stream) {
+    return trace_closest<true>(bvh, rays, num_rays, order, hit_id, hit_t, stream);
+}
+int clr_trace_shadow_in_order(const clr_bvh* bvh, const float* rays, uint32_t num_rays, const uint32_t* order,
+                              uint8_t* occluded, void* stream) {
+    return trace_shadow(bvh, rays, num_rays, order, occluded, stream);
+}
+
 extern "C" int clr_trace_closest(const clr_bvh* bvh, const float* rays, uint32_t num_rays, uint32_t* hit_id,
                                  float* hit_t, void* stream) {
-    return trace_closest<false>(bvh, rays, num_rays, hit_id, hit_t, stream);
+    return trace_closest<false>(bvh, rays, num_rays, nullptr, hit_id, hit_t, stream);
 }
 
 extern "C" int clr_trace_closest_ordered(const clr_bvh* bvh, const float* rays, uint32_t num_rays, uint32_t* hit_id,
                                          float* hit_t, void* stream) {
-    return trace_closest<true>(bvh, rays, num_rays, hit_id, hit_t, stream);
+    return trace_closest<true>(bvh, rays, num_rays, nullptr, hit_id, hit_t, stream);
 }
 
 extern "C" int clr_trace_replays(uint64_t* count, int clear) {
@@ -282,14 +313,5 @@ extern "C" int clr_trace_replays(uint64_t* count, int clear) {
 
 extern "C" int clr_trace_shadow(const clr_bvh* bvh, const float* rays, uint32_t num_rays, uint8_t* occluded,
                                 void* stream) {
-    int rc = check_trace_args(bvh, rays, num_rays, occluded);
-    if (rc != CLR_OK || num_rays == 0) return rc;
-    cudaStream_t st = static_cast<cudaStream_t>(stream);
-    // shadow segments are short (most end at the first accepted triangle):
-    // one ray per thread with hardware block scheduling balances them best
-    k_trace_shadow<<<div_up(num_rays, kTraceThreads), kTraceThreads, 0, st>>>(
-        static_cast<const float4*>(bvh->nodes), static_cast<const float4*>(bvh->tris), bvh->root_box, bvh->num_tris,
-        reinterpret_cast<const float4*>(rays), num_rays, occluded);
-    CLR_LAUNCH_CHECK("k_trace_shadow");
-    return CLR_OK;
+    return trace_shadow(bvh, rays, num_rays, nullptr, occluded, stream);
 }

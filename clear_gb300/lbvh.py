@@ -216,13 +216,24 @@ def _rays(rays: torch.Tensor, device) -> torch.Tensor:
     return r
 
 
+def _sort_workspace(m: int, device) -> tuple[torch.Tensor, int]:
+    """A 256-byte aligned scratch buffer for the sorted-order searches (torch's
+    caching allocator keeps it between calls)."""
+    n = C.c_uint64(0)
+    call("clr_trace_sort_workspace_bytes", C.c_uint32(m), C.byref(n))
+    ws = torch.empty(int(n.value) + 256, dtype=torch.uint8, device=device)
+    off = (-ws.data_ptr()) % 256
+    return ws, off
+
+
 def trace_closest(bvh: BVH, rays: torch.Tensor, hit_id: torch.Tensor | None = None,
-                  hit_t: torch.Tensor | None = None, ordered: bool = True):
+                  hit_t: torch.Tensor | None = None, ordered: bool = True, sort: bool = False):
     """Closest hit for rays packed {ox,oy,oz,tmax,dx,dy,dz,0}.  Returns
-    (hit_id int32 [-1 = miss], hit_t float32), the reference's answer in both
-    forms: ordered=True (default) visits the nearer child first and replays in
+    (hit_id int32 [-1 = miss], hit_t float32), the reference's answer in every
+    form: ordered=True (default) visits the nearer child first and replays in
     the reference's order the rays whose answer could depend on the order;
-    ordered=False searches every ray in the reference's order."""
+    ordered=False searches every ray in the reference's order; sort=True (with
+    ordered) first sorts the rays by origin (clr_trace_closest_sorted)."""
     r = _rays(rays, bvh.device)
     m = r.shape[0]
     if hit_id is None:
@@ -230,8 +241,15 @@ def trace_closest(bvh: BVH, rays: torch.Tensor, hit_id: torch.Tensor | None = No
     if hit_t is None:
         hit_t = torch.empty(m, dtype=torch.float32, device=bvh.device)
     with torch.cuda.device(bvh.device):
-        call("clr_trace_closest_ordered" if ordered else "clr_trace_closest", C.byref(bvh.c), _ptr(r),
-             C.c_uint32(m), _ptr(hit_id), _ptr(hit_t), _stream(bvh.device))
+        if sort:
+            if not ordered:
+                raise ValueError("sort=True searches nearer-first (ordered=True)")
+            ws, off = _sort_workspace(m, bvh.device)
+            call("clr_trace_closest_sorted", C.byref(bvh.c), _ptr(r), C.c_uint32(m), _ptr(hit_id), _ptr(hit_t),
+                 C.c_void_p(ws.data_ptr() + off), C.c_uint64(ws.numel() - off), _stream(bvh.device))
+        else:
+            call("clr_trace_closest_ordered" if ordered else "clr_trace_closest", C.byref(bvh.c), _ptr(r),
+                 C.c_uint32(m), _ptr(hit_id), _ptr(hit_t), _stream(bvh.device))
     return hit_id, hit_t
 
 
@@ -243,14 +261,20 @@ def trace_replays(clear: bool = True) -> int:
     return int(v.value)
 
 
-def trace_shadow(bvh: BVH, rays: torch.Tensor, occluded: torch.Tensor | None = None):
-    """Any-hit query: 1 where a triangle is hit at 0 <= t <= tmax."""
+def trace_shadow(bvh: BVH, rays: torch.Tensor, occluded: torch.Tensor | None = None, sort: bool = False):
+    """Any-hit query: 1 where a triangle is hit at 0 <= t <= tmax; sort=True
+    searches the rays in origin order (clr_trace_shadow_sorted)."""
     r = _rays(rays, bvh.device)
     m = r.shape[0]
     if occluded is None:
         occluded = torch.empty(m, dtype=torch.uint8, device=bvh.device)
     with torch.cuda.device(bvh.device):
-        call("clr_trace_shadow", C.byref(bvh.c), _ptr(r), C.c_uint32(m), _ptr(occluded), _stream(bvh.device))
+        if sort:
+            ws, off = _sort_workspace(m, bvh.device)
+            call("clr_trace_shadow_sorted", C.byref(bvh.c), _ptr(r), C.c_uint32(m), _ptr(occluded),
+                 C.c_void_p(ws.data_ptr() + off), C.c_uint64(ws.numel() - off), _stream(bvh.device))
+        else:
+            call("clr_trace_shadow", C.byref(bvh.c), _ptr(r), C.c_uint32(m), _ptr(occluded), _stream(bvh.device))
     return occluded
 
 

@@ -220,6 +220,21 @@ CLR_API int clr_trace_replays(uint64_t* count, int clear);
  * 0 <= t <= tmax. */
 CLR_API int clr_trace_shadow(const clr_bvh* bvh, const float* rays, uint32_t num_rays, uint8_t* occluded, void* stream);
 
+/* clr_trace_closest_ordered and clr_trace_shadow with the rays searched in
+ * the order of the Morton code of their origins (8 bits per axis in the
+ * tree's root box): the rays a warp searches together start in the same
+ * region and share the tree's nodes in the caches.  The same answers, each
+ * written at its ray's own index; for rays given in no spatial order (random
+ * directions and origins) about 1.8x the throughput, for rays already
+ * ordered (a camera's) a cost of about a millisecond per 16 M rays.  The
+ * 256-byte aligned device workspace holds clr_trace_sort_workspace_bytes(n)
+ * bytes (16 per ray and the sort's tile words); its contents are scratch. */
+CLR_API int clr_trace_sort_workspace_bytes(uint32_t num_rays, uint64_t* bytes);
+CLR_API int clr_trace_closest_sorted(const clr_bvh* bvh, const float* rays, uint32_t num_rays, uint32_t* hit_id,
+                                     float* hit_t, void* workspace, uint64_t workspace_bytes, void* stream);
+CLR_API int clr_trace_shadow_sorted(const clr_bvh* bvh, const float* rays, uint32_t num_rays, uint8_t* occluded,
+                                    void* workspace, uint64_t workspace_bytes, void* stream);
+
 /* ----------------------------------------------------------- path tracer */
 
 /*

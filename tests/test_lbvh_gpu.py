@@ -123,13 +123,38 @@ def test_trace_parity(cuda, n):
     rays = W.closest_rays(20000, seed=n)
     rays[::7, 3] = 0.05  # some finite tmax
     oids, ots = oracle.trace_closest(vx, vy, vz, None, ob, rays)
-    for ordered in (False, True):
-        ids, ts = lbvh.trace_closest(bvh, torch.from_numpy(rays).to(cuda), ordered=ordered)
+    for ordered, sort in ((False, False), (True, False), (True, True)):
+        ids, ts = lbvh.trace_closest(bvh, torch.from_numpy(rays).to(cuda), ordered=ordered, sort=sort)
         np.testing.assert_array_equal(ids.cpu().numpy().view(np.uint32), oids)
         np.testing.assert_array_equal(ts.cpu().numpy(), ots)
     srays = W.shadow_rays(20000, seed=n + 1)
-    occ = lbvh.trace_shadow(bvh, torch.from_numpy(srays).to(cuda)).cpu().numpy()
-    np.testing.assert_array_equal(occ, oracle.trace_shadow(vx, vy, vz, None, ob, srays))
+    oocc = oracle.trace_shadow(vx, vy, vz, None, ob, srays)
+    for sort in (False, True):
+        occ = lbvh.trace_shadow(bvh, torch.from_numpy(srays).to(cuda), sort=sort).cpu().numpy()
+        np.testing.assert_array_equal(occ, oocc)
+    no_device_errors()
+
+
+def test_trace_sorted_order_edge_cases(cuda):
+    """Searches in origin order: the same answers as the given order for ray
+    counts around the sort's tile size, origins far outside the scene and
+    non-finite ones, a scene whose box is flat on one axis, and no rays."""
+    n = 5000
+    vx, vy, vz = W.triangle_soup(n, seed=31)
+    vy = np.full_like(vy, 0.5)  # flat: the root box has no extent in y
+    b, bvh, _ = gpu_build(cuda, vx, vy, vz, None, n, 10)
+    for m in (1, 4095, 4096, 4097, 70001):
+        rays = W.closest_rays(m, seed=m)
+        rays[: m // 3, :3] *= 1e6
+        if m > 10:
+            rays[5, 0] = np.nan
+            rays[6, 1] = np.inf
+        r = torch.from_numpy(rays).to(cuda)
+        ids, ts = lbvh.trace_closest(bvh, r)
+        ids_s, ts_s = lbvh.trace_closest(bvh, r, sort=True)
+        assert torch.equal(ids, ids_s) and torch.equal(ts.view(torch.int32), ts_s.view(torch.int32)), m
+        assert torch.equal(lbvh.trace_shadow(bvh, r), lbvh.trace_shadow(bvh, r, sort=True)), m
+    lbvh.trace_closest(bvh, torch.empty((0, 8), device=cuda), sort=True)
     no_device_errors()
 
 
