@@ -726,6 +726,20 @@ static inline DScene make_dscene(const clr_scene* scene) {
     return sc;
 }
 
+// Blocks for a ray kernel: no more than fit on the GPU at once.  Its loop
+// hands each thread a fixed run of rays; blocks beyond the resident ones would
+// start only as the first finish, and the last of them would end the launch.
+template <typename K>
+static inline unsigned int resident_grid(K kernel, int block, size_t smem, unsigned int work_blocks) {
+    int per_sm = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, block, smem) != cudaSuccess || per_sm <= 0) {
+        cudaGetLastError();
+        per_sm = 1;
+    }
+    const unsigned int full = (unsigned int)(clr_sm_count() * per_sm);
+    return std::max(1u, std::min(work_blocks, full));
+}
+
 static inline bool same_scene(const DScene& a, const DScene& b) {
     return a.vertices == b.vertices && a.normals == b.normals && a.tangents == b.tangents && a.uvs == b.uvs &&
            a.faces == b.faces && a.lights == b.lights && a.materials == b.materials && a.textures == b.textures &&
