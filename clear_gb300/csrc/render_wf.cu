@@ -346,9 +346,8 @@ struct WfArgs {
     uint32_t* rand_states;
     float4* px;
     bool ordered;
-    unsigned int grid;        // partition
+    unsigned int grid;        // shade kernels
     unsigned int grid_trace;  // extend and shadow: the resident blocks
-    unsigned int grid_shade[2];  // escaped and hit shading: the resident blocks
 };
 
 static void wf_block(const WfArgs& a, cudaStream_t st) {
@@ -358,9 +357,9 @@ static void wf_block(const WfArgs& a, cudaStream_t st) {
         else k_wf_extend<false><<<a.grid_trace, kWfThreads, 0, st>>>(a.sc, a.S, cur);
         k_wf_reset<<<1, 1, 0, st>>>(a.S, cur ^ 1);
         k_wf_partition<<<a.grid, kWfThreads, 0, st>>>(a.S, a.S.q[cur], cur);
-        k_wf_shade<false><<<a.grid_shade[0], kWfThreads, 0, st>>>(a.sc, a.S, cur, a.width, a.row0, a.rand_states, a.px, a.spp,
+        k_wf_shade<false><<<a.grid, kWfThreads, 0, st>>>(a.sc, a.S, cur, a.width, a.row0, a.rand_states, a.px, a.spp,
                                                          a.max_depth);
-        k_wf_shade<true><<<a.grid_shade[1], kWfThreads, 0, st>>>(a.sc, a.S, cur, a.width, a.row0, a.rand_states, a.px, a.spp,
+        k_wf_shade<true><<<a.grid, kWfThreads, 0, st>>>(a.sc, a.S, cur, a.width, a.row0, a.rand_states, a.px, a.spp,
                                                         a.max_depth);
         if (a.ordered) k_wf_shadow<true><<<a.grid_trace, kWfThreads, 0, st>>>(a.sc, a.S, a.px);
         else k_wf_shadow<false><<<a.grid_trace, kWfThreads, 0, st>>>(a.sc, a.S, a.px);
@@ -371,7 +370,7 @@ static bool same_args(const WfArgs& x, const WfArgs& y) {
     return same_scene(x.sc, y.sc) && x.S.org == y.S.org && x.S.count == y.S.count && x.S.qs == y.S.qs &&
            x.width == y.width && x.row0 == y.row0 && x.spp == y.spp && x.max_depth == y.max_depth &&
            x.rand_states == y.rand_states && x.px == y.px && x.ordered == y.ordered && x.grid == y.grid &&
-           x.grid_trace == y.grid_trace && x.grid_shade[0] == y.grid_shade[0] && x.grid_shade[1] == y.grid_shade[1];
+           x.grid_trace == y.grid_trace;
 }
 
 thread_local BlockGraphCache<WfArgs> t_wf_graphs;
@@ -418,19 +417,7 @@ extern "C" int clr_render_wavefront_rows(const clr_scene* scene, uint32_t width,
                            resident_grid(k_wf_shadow<true>, kWfThreads, 0, work))
                 : std::min(resident_grid(k_wf_extend<false>, kWfThreads, 0, work),
                            resident_grid(k_wf_shadow<false>, kWfThreads, 0, work));
-    const WfArgs a{sc,
-                   S,
-                   width,
-                   row0,
-                   spp,
-                   max_depth,
-                   rand_states,
-                   px,
-                   ordered,
-                   grid,
-                   grid_trace,
-                   {resident_grid(k_wf_shade<false>, kWfThreads, 0, work),
-                    resident_grid(k_wf_shade<true>, kWfThreads, 0, work)}};
+    const WfArgs a{sc, S, width, row0, spp, max_depth, rand_states, px, ordered, grid, grid_trace};
     cudaGraphExec_t exec = t_wf_graphs.get(a, wf_block, same_args);
     cudaGetLastError();  // a failed capture leaves no error behind: the kernels are launched directly
     // every iteration advances each unfinished pixel by one path vertex; a
