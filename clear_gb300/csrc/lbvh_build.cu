@@ -28,6 +28,9 @@
 #include <mutex>
 #include <new>
 
+#include <cuda.h>
+#include <cudaTypedefs.h>
+
 #include "common.cuh"
 #include "lbvh_internal.cuh"
 
@@ -466,12 +469,10 @@ __device__ __forceinline__ TriVerts load_tri_staged(const float* vx, const float
 }
 
 
-// Writes leaf `leaf`'s triangle record and returns its box (calcAABBs).
-// `tid` indexes the (global) vertex arrays, `rec_id` is the id recorded.
-__device__ __forceinline__ void emit_leaf(const float* vx, const float* vy, const float* vz, const uint32_t* tri,
-                                          const float4* stage, uint32_t tid, uint32_t rec_id, uint32_t leaf,
-                                          float4* __restrict__ tris, float box[6]) {
-    const TriVerts tv = load_tri_staged(vx, vy, vz, tri, stage, tid);
+// Writes leaf `leaf`'s triangle record from its vertices and returns its box
+// (calcAABBs).
+__device__ __forceinline__ void emit_leaf_verts(const TriVerts& tv, uint32_t rec_id, uint32_t leaf,
+                                                float4* __restrict__ tris, float box[6]) {
     for (int k = 0; k < 3; ++k) {
         box[k] = fminf(tv.p[0][k], fminf(tv.p[1][k], tv.p[2][k]));
         box[3 + k] = fmaxf(tv.p[0][k], fmaxf(tv.p[1][k], tv.p[2][k]));
@@ -480,6 +481,69 @@ __device__ __forceinline__ void emit_leaf(const float* vx, const float* vy, cons
     r[0] = make_float4(tv.p[0][0], tv.p[0][1], tv.p[0][2], __uint_as_float(rec_id));
     r[1] = make_float4(fsub(tv.p[1][0], tv.p[0][0]), fsub(tv.p[1][1], tv.p[0][1]), fsub(tv.p[1][2], tv.p[0][2]), 0.f);
     r[2] = make_float4(fsub(tv.p[2][0], tv.p[0][0]), fsub(tv.p[2][1], tv.p[0][1]), fsub(tv.p[2][2], tv.p[0][2]), 0.f);
+}
+
+// The same from triangle `tid` of the (global) vertex arrays or its staging
+// record; `rec_id` is the id recorded.
+__device__ __forceinline__ void emit_leaf(const float* vx, const float* vy, const float* vz, const uint32_t* tri,
+                                          const float4* stage, uint32_t tid, uint32_t rec_id, uint32_t leaf,
+                                          float4* __restrict__ tris, float box[6]) {
+    emit_leaf_verts(load_tri_staged(vx, vy, vz, tri, stage, tid), rec_id, leaf, tris, box);
+}
+
+// ---------------------------------------------------- staging-record gather
+//
+// The tree pass reads its leaves' staging records in key order: scattered
+// 48-byte rows of the staging array.  With the array described as a 2-D
+// tensor (n rows of 12 floats), one TMA tile::gather4 copy brings four such
+// rows into shared memory; eight lanes of a warp issue the warp's 32 rows,
+// and the warp waits on its own mbarrier (bounded) -- instead of 96 scattered
+// 16-byte loads through L1 per warp.
+constexpr int kStageFloats = 12;
+// one gather4 copy (4 rows, 192 bytes) per 256-byte slot: tensor copies into
+// shared memory start on 128-byte boundaries
+constexpr int kGatherSlotFloats = 64;
+constexpr unsigned int kGatherWaitLimit = 1u << 22;
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+// Stages the staging records of leaves B + 32 w .. + 31 (w = this warp) into
+// `rows`: lane l's record at rows[(l / 4) * kGatherSlotFloats + (l % 4) * 12]
+// (triangle ids tj per lane, id 0 for lanes past the array: a valid row whose
+// copy is not used).  Returns false if the wait gave up.
+__device__ __forceinline__ bool gather_warp_records(const CUtensorMap* tmap, uint64_t* bar, float* rows, uint32_t tj) {
+    const int lane = threadIdx.x & 31;
+    const uint32_t b = smem_u32(bar);
+    if (lane == 0) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(b) : "memory");
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(b),
+                     "r"(32u * kStageFloats * 4u)
+                     : "memory");
+    }
+    const uint32_t r0 = __shfl_sync(0xFFFFFFFFu, tj, (4 * lane) & 31);
+    const uint32_t r1 = __shfl_sync(0xFFFFFFFFu, tj, (4 * lane + 1) & 31);
+    const uint32_t r2 = __shfl_sync(0xFFFFFFFFu, tj, (4 * lane + 2) & 31);
+    const uint32_t r3 = __shfl_sync(0xFFFFFFFFu, tj, (4 * lane + 3) & 31);
+    if (lane < 8)
+        asm volatile(
+            "cp.async.bulk.tensor.2d.shared::cta.global.tile::gather4.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, "
+            "%4, %5, %6}], [%7];" ::"r"(smem_u32(rows + lane * kGatherSlotFloats)),
+            "l"(tmap), "r"(0), "r"(r0), "r"(r1), "r"(r2), "r"(r3), "r"(b)
+            : "memory");
+    uint32_t done = 0;
+    for (unsigned int spins = 0; !done; ++spins) {
+        asm volatile(
+            "{ .reg .pred p; mbarrier.try_wait.parity.shared::cta.b64 p, [%1], 0; selp.u32 %0, 1, 0, p; }"
+            : "=r"(done)
+            : "r"(b)
+            : "memory");
+        if (!done && spins > kGatherWaitLimit) {
+            clr_raise(CLR_DEVERR_QUEUE);
+            return false;
+        }
+    }
+    return true;
 }
 
 // Adjacent common prefix delta(i, i+1), i in [0, n-2].
@@ -700,8 +764,9 @@ __device__ __forceinline__ unsigned int atomic_add_acq_rel_cta(unsigned int* p, 
     return old;
 }
 
-template <typename KeyT, bool kWide>
-__global__ void __launch_bounds__(kTreeBlock, 16) k_build_tree(const KeyT* __restrict__ keys,
+template <typename KeyT, bool kWide, bool kTma>
+__global__ void __launch_bounds__(kTreeBlock, 16) k_build_tree(const __grid_constant__ CUtensorMap stage_map,
+                                                           const KeyT* __restrict__ keys,
                                                            const uint32_t* __restrict__ sidx, uint32_t n, int kbits,
                                                            const float* __restrict__ vx, const float* __restrict__ vy,
                                                            const float* __restrict__ vz, const uint32_t* __restrict__ tri,
@@ -718,6 +783,9 @@ __global__ void __launch_bounds__(kTreeBlock, 16) k_build_tree(const KeyT* __res
     // child slots of the block's nodes: {box min xyz, box max x}, {box max yz, ref, far end}
     __shared__ __align__(16) float4 s_slot[kTreeBlock][2][2];
     __shared__ unsigned int s_cnt[kTreeBlock];
+    // staging records gathered by TMA (kTma) and each warp's mbarrier
+    __shared__ __align__(128) float s_rec[kTma ? (kTreeBlock / 4) * kGatherSlotFloats : 1];
+    __shared__ __align__(8) uint64_t s_bar[kTreeBlock / 32];
     const uint32_t B = blockIdx.x * kTreeBlock;
     const uint32_t E = min(B + kTreeBlock - 1, n - 1);
     const int nd = (int)(E - B) + 2;  // entries of s_d (<= kTreeBlock + 1)
@@ -775,7 +843,19 @@ __global__ void __launch_bounds__(kTreeBlock, 16) k_build_tree(const KeyT* __res
     // merges two adjacent leaves whose parent is their own node (no block
     // barrier after this: a warp climbs while the block's other warps gather)
     float box[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
-    if (j < n) {
+    if (kTma) {
+        if (B + 32u * warp < n) {  // the warp has leaves
+            const uint32_t tj = j < n ? __ldg(sidx + j) : 0u;
+            float* rows = s_rec + 8 * warp * kGatherSlotFloats;
+            if (gather_warp_records(&stage_map, &s_bar[warp], rows, tj) && j < n) {
+                const float* r = rows + (lane >> 2) * kGatherSlotFloats + (lane & 3) * kStageFloats;
+                TriVerts tv;
+#pragma unroll
+                for (int k = 0; k < 9; ++k) tv.p[k / 3][k % 3] = r[k];
+                emit_leaf_verts(tv, tj, j, tris, box);
+            }
+        }
+    } else if (j < n) {
         const uint32_t tj = __ldg(sidx + j);
         emit_leaf(vx, vy, vz, tri, stage, tj, tj, j, tris, box);
     }
@@ -1279,6 +1359,42 @@ static cudaError_t clear_for_build(clr_lbvh* h, uint32_t n, int items, int npass
     return cudaMemsetAsync(h->zero_region, 0, h->zero_prefix_bytes + 4ull * npasses * h->status_stride, st);
 }
 
+// cuTensorMapEncodeTiled through the runtime's driver entry point (null when
+// the driver does not offer it: the tree pass then gathers with plain loads).
+static PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
+    static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        void* f = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &f, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(f);
+        cudaGetLastError();
+    });
+    return fn;
+}
+
+// The staging array (n rows of 12 floats, 48-byte rows) as a tensor map whose
+// box is one row: the tile::gather4 form.
+static bool stage_map_for(clr_lbvh* h, uint32_t n) {
+    if (h->map_base == h->stage && h->map_rows == n) return h->map_ok;
+    h->map_base = h->stage;
+    h->map_rows = n;
+    h->map_ok = false;
+    PFN_cuTensorMapEncodeTiled_v12000 enc = tensor_map_encoder();
+    if (!enc || (reinterpret_cast<uintptr_t>(h->stage) & 15u)) return false;
+    const cuuint64_t dims[2] = {(cuuint64_t)kStageFloats, (cuuint64_t)n};
+    const cuuint64_t strides[1] = {(cuuint64_t)kStageFloats * sizeof(float)};
+    const cuuint32_t box[2] = {(cuuint32_t)kStageFloats, 1u};
+    const cuuint32_t estride[2] = {1u, 1u};
+    h->map_ok = enc(&h->stage_map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, const_cast<float4*>(h->stage), dims, strides,
+                    box, estride, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                    CU_TENSOR_MAP_L2_PROMOTION_NONE, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+    return h->map_ok;
+}
+
 template <typename KeyT>
 static int run_build(clr_lbvh* h, const float* vx, const float* vy, const float* vz, const uint32_t* tri,
                      uint32_t n, uint32_t bits, clr_bvh* out, cudaStream_t st) {
@@ -1322,14 +1438,17 @@ static int run_build(clr_lbvh* h, const float* vx, const float* vy, const float*
         uint32_t* worklist = h->vals[fin ^ 1];
         unsigned int* wl_count = h->tile_ctr + kMaxPasses;
         const bool wide = (reinterpret_cast<uintptr_t>(out->nodes) & 31u) == 0u;  // 32-byte node stores
-        if (wide)
-            k_build_tree<KeyT, true><<<div_up(n, kTreeBlock), kTreeBlock, 0, st>>>(
-                keys[fin], h->vals[fin], n, kbits, vx, vy, vz, tri, h->stage, reinterpret_cast<float*>(out->nodes),
-                tris, h->counters, h->karras_idx, out->root_box, worklist, wl_count);
-        else
-            k_build_tree<KeyT, false><<<div_up(n, kTreeBlock), kTreeBlock, 0, st>>>(
-                keys[fin], h->vals[fin], n, kbits, vx, vy, vz, tri, h->stage, reinterpret_cast<float*>(out->nodes),
-                tris, h->counters, h->karras_idx, out->root_box, worklist, wl_count);
+        const bool tma = h->stage != nullptr && stage_map_for(h, n);               // TMA record gathers
+        const unsigned int grid = div_up(n, kTreeBlock);
+        float* nodes = reinterpret_cast<float*>(out->nodes);
+#define CLR_TREE_ARGS                                                                                               \
+    keys[fin], h->vals[fin], n, kbits, vx, vy, vz, tri, h->stage, nodes, tris, h->counters, h->karras_idx, out->root_box, \
+        worklist, wl_count
+        if (wide && tma) k_build_tree<KeyT, true, true><<<grid, kTreeBlock, 0, st>>>(h->stage_map, CLR_TREE_ARGS);
+        else if (wide) k_build_tree<KeyT, true, false><<<grid, kTreeBlock, 0, st>>>(h->stage_map, CLR_TREE_ARGS);
+        else if (tma) k_build_tree<KeyT, false, true><<<grid, kTreeBlock, 0, st>>>(h->stage_map, CLR_TREE_ARGS);
+        else k_build_tree<KeyT, false, false><<<grid, kTreeBlock, 0, st>>>(h->stage_map, CLR_TREE_ARGS);
+#undef CLR_TREE_ARGS
         CLR_LAUNCH_CHECK("k_build_tree");
         k_build_tree_top<KeyT><<<clr_sm_count() * 4, 256, 0, st>>>(keys[fin], n, kbits, reinterpret_cast<float*>(out->nodes),
                                                              h->counters, h->karras_idx, out->root_box, worklist,

@@ -4,6 +4,7 @@
 #include <stddef.h>
 #include <stdint.h>
 
+#include <cuda.h>
 #include <cuda_runtime.h>
 
 namespace clr {
@@ -25,6 +26,12 @@ constexpr int kMaxDepth = 96;
 
 // Builder handle: the scratch pool and what the last build left in it.
 struct clr_lbvh {
+    // the staging array as a tensor of n rows x 12 floats, for the tree pass's
+    // TMA gathers (encoded for map_base / map_rows; map_ok false = unavailable)
+    CUtensorMap stage_map{};
+    const void* map_base = nullptr;
+    uint32_t map_rows = 0;
+    bool map_ok = false;
     uint32_t capacity = 0;
     void* pool = nullptr;
     size_t pool_bytes = 0;
