@@ -102,6 +102,7 @@ def lib() -> C.CDLL:
             "clr_device_status": [C.POINTER(u32), i32],
             "clr_trace_replays": [C.POINTER(C.c_uint64), i32],
             "clr_debug_set_wait_limits": [u32, u32],
+            "clr_debug_set_tma_gather": [i32],
             "clr_debug_lookback_stall": [vp, vp, u32, vp],
             "clr_lbvh_set_profiling": [vp, i32],
             "clr_render": [vp, u32, u32, vp, vp, u32, u32, u32, vp],

@@ -1376,9 +1376,13 @@ static PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
     return fn;
 }
 
+// Cleared only by clr_debug_set_tma_gather.
+static bool g_tma_gather = true;
+
 // The staging array (n rows of 12 floats, 48-byte rows) as a tensor map whose
 // box is one row: the tile::gather4 form.
 static bool stage_map_for(clr_lbvh* h, uint32_t n) {
+    if (!g_tma_gather) return false;
     if (h->map_base == h->stage && h->map_rows == n) return h->map_ok;
     h->map_base = h->stage;
     h->map_rows = n;
@@ -2006,6 +2010,11 @@ int clr_batch_set_iteration_cap(uint32_t cap);  // render_batch.cu
 extern "C" int clr_debug_set_wait_limits(uint32_t sort_spin_limit, uint32_t batch_iteration_cap) {
     g_sort_spin_limit = sort_spin_limit ? sort_spin_limit : kSpinLimit;
     return clr_batch_set_iteration_cap(batch_iteration_cap);
+}
+
+extern "C" int clr_debug_set_tma_gather(int enable) {
+    g_tma_gather = enable != 0;
+    return CLR_OK;
 }
 
 extern "C" int clr_debug_lookback_stall(uint32_t* keys, uint32_t* scratch, uint32_t tile_keys, void* stream) {

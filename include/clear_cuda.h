@@ -555,6 +555,11 @@ CLR_API int clr_debug_set_wait_limits(uint32_t sort_spin_limit, uint32_t batch_i
  * returns.  scratch holds 4 * (4 * tile_keys + 769) bytes. */
 CLR_API int clr_debug_lookback_stall(uint32_t* keys, uint32_t* scratch, uint32_t tile_keys, void* stream);
 
+/* Whether the LBVH tree pass gathers its staging records with TMA copies
+ * (1, the default where the driver offers the tensor-map encoder) or with
+ * plain loads (0); both give the same tree.  Process-wide; for tests. */
+CLR_API int clr_debug_set_tma_gather(int enable);
+
 #ifdef __cplusplus
 }
 #endif

@@ -63,6 +63,26 @@ def test_build_parity(cuda, n, bits):
     no_device_errors()
 
 
+@pytest.mark.parametrize("n, bits", [(4097, 10), (300001, 10), (65537, 20)])
+def test_tma_and_plain_record_gathers_agree(cuda, n, bits):
+    """The tree pass gathers its leaves' staging records with TMA copies or,
+    where the driver lacks the tensor-map encoder, with plain loads: the same
+    tree, byte for byte, and the oracle's."""
+    vx, vy, vz = W.triangle_soup(n, seed=77 + n)
+    refs = []
+    try:
+        for tma in (1, 0):
+            _lib.call("clr_debug_set_tma_gather", tma)
+            _, _, ref = gpu_build(cuda, vx, vy, vz, None, n, bits)
+            refs.append(ref)
+    finally:
+        _lib.call("clr_debug_set_tma_gather", 1)
+    for k in refs[0]:
+        assert np.array_equal(refs[0][k], refs[1][k]), k
+    assert_build_equal(refs[0], oracle.lbvh_build(vx, vy, vz, None, n, bits), n)
+    no_device_errors()
+
+
 def test_build_parity_indexed_and_planar(cuda):
     # indexed input with shared vertices, duplicate centroids and a flat z axis
     rng = np.random.default_rng(5)
