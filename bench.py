@@ -655,7 +655,9 @@ def run_ours(args):
             per.setdefault(key, []).append(ms)
     builder.set_profiling(False)
     kern_ms = {k: statistics.mean(v) for k, v in per.items()}
-    launches_per_build = sum(len(v) for v in per.values()) // args.steps
+    # kernels per build: one per timed pass, two for the tree pass (k_build_tree
+    # and k_build_tree_top)
+    launches_per_build = sum(len(v) * (2 if k == "build_tree" else 1) for k, v in per.items()) // args.steps
 
     # ---- e2e through the C ABI from pinned host memory: every step uploads
     # its vertices (clr_lbvh_build_host) and reads the root record back; a
