@@ -754,6 +754,8 @@ __device__ __forceinline__ void tree_climb(const KeyT* __restrict__ keys, const 
 // reached by threads of two blocks and uses the device-scope protocol of
 // tree_climb; so are all its ancestors.
 constexpr int kTreeBlock = 128;
+// largest tree whose block-crossing climbs run inside the tree pass
+constexpr uint32_t kClimbHereMaxTris = 2u << 20;
 
 __device__ __forceinline__ unsigned int atomic_add_acq_rel_cta(unsigned int* p, unsigned int v) {
     unsigned int old;
@@ -776,7 +778,8 @@ __global__ void __launch_bounds__(kTreeBlock, 16) k_build_tree(const __grid_cons
                                                            uint32_t* __restrict__ karras_idx,
                                                            float* __restrict__ root_box,
                                                            uint32_t* __restrict__ worklist,
-                                                           unsigned int* __restrict__ wl_count) {
+                                                           unsigned int* __restrict__ wl_count,
+                                                           int climb_here) {
     __shared__ int s_d[kTreeBlock + 1];           // delta(k, k+1), k = B-1 .. E
     __shared__ int s_wmin[3][kTreeBlock / 32];     // per warp: prefix min, suffix min from lanes 0 and 1
     __shared__ unsigned char s_local[kTreeBlock];  // node split at B + i lies inside the block
@@ -932,6 +935,13 @@ __global__ void __launch_bounds__(kTreeBlock, 16) k_build_tree(const __grid_cons
             box[4] = fmaxf(a1.x, c1.x);
             box[5] = fmaxf(a1.y, c1.y);
         } else {
+            if (climb_here) {
+                // small trees: continue with the device-scope climb right here
+                // (its waits are for first arrivals, which are running)
+                climb_global<KeyT>(keys, n, kbits, nodes, counters, karras_idx, root_box, lo, hi, d_lo, d_hi, ref,
+                                   box);
+                return;
+            }
             // first node across a block edge: deliver this child; the second
             // arrival hands the finished node to k_build_tree_top, so that this
             // block retires instead of waiting on device-scope climbs.  Both
@@ -1443,21 +1453,28 @@ static int run_build(clr_lbvh* h, const float* vx, const float* vy, const float*
         unsigned int* wl_count = h->tile_ctr + kMaxPasses;
         const bool wide = (reinterpret_cast<uintptr_t>(out->nodes) & 31u) == 0u;  // 32-byte node stores
         const bool tma = h->stage != nullptr && stage_map_for(h, n);               // TMA record gathers
+        // block-crossing climbs: inside the tree pass for small trees (no
+        // second launch, the climbs overlap the other blocks), handed to
+        // k_build_tree_top for large ones (blocks held by long climbs would
+        // delay the rest of the pass)
+        const bool climb_here = n <= kClimbHereMaxTris;
         const unsigned int grid = div_up(n, kTreeBlock);
         float* nodes = reinterpret_cast<float*>(out->nodes);
 #define CLR_TREE_ARGS                                                                                               \
     keys[fin], h->vals[fin], n, kbits, vx, vy, vz, tri, h->stage, nodes, tris, h->counters, h->karras_idx, out->root_box, \
-        worklist, wl_count
+        worklist, wl_count, climb_here ? 1 : 0
         if (wide && tma) k_build_tree<KeyT, true, true><<<grid, kTreeBlock, 0, st>>>(h->stage_map, CLR_TREE_ARGS);
         else if (wide) k_build_tree<KeyT, true, false><<<grid, kTreeBlock, 0, st>>>(h->stage_map, CLR_TREE_ARGS);
         else if (tma) k_build_tree<KeyT, false, true><<<grid, kTreeBlock, 0, st>>>(h->stage_map, CLR_TREE_ARGS);
         else k_build_tree<KeyT, false, false><<<grid, kTreeBlock, 0, st>>>(h->stage_map, CLR_TREE_ARGS);
 #undef CLR_TREE_ARGS
         CLR_LAUNCH_CHECK("k_build_tree");
-        k_build_tree_top<KeyT><<<clr_sm_count() * 4, 256, 0, st>>>(keys[fin], n, kbits, reinterpret_cast<float*>(out->nodes),
-                                                             h->counters, h->karras_idx, out->root_box, worklist,
-                                                             wl_count);
-        CLR_LAUNCH_CHECK("k_build_tree_top");
+        if (!climb_here) {
+            k_build_tree_top<KeyT><<<clr_sm_count() * 4, 256, 0, st>>>(
+                keys[fin], n, kbits, reinterpret_cast<float*>(out->nodes), h->counters, h->karras_idx, out->root_box,
+                worklist, wl_count);
+            CLR_LAUNCH_CHECK("k_build_tree_top");
+        }
         timer.done("build_tree");
     }
     return CLR_OK;

@@ -63,6 +63,16 @@ def test_build_parity(cuda, n, bits):
     no_device_errors()
 
 
+@pytest.mark.parametrize("n", [(2 << 20), (2 << 20) + 1])
+def test_build_parity_either_side_of_the_climb_threshold(cuda, n):
+    """Trees up to 2 Mi triangles finish their block-crossing climbs inside the
+    tree pass, larger ones in k_build_tree_top: both exact."""
+    vx, vy, vz = W.triangle_soup(n, seed=5 + n)
+    _, _, ref = gpu_build(cuda, vx, vy, vz, None, n, 10)
+    assert_build_equal(ref, oracle.lbvh_build(vx, vy, vz, None, n, 10), n)
+    no_device_errors()
+
+
 @pytest.mark.parametrize("n, bits", [(4097, 10), (300001, 10), (65537, 20)])
 def test_tma_and_plain_record_gathers_agree(cuda, n, bits):
     """The tree pass gathers its leaves' staging records with TMA copies or,
