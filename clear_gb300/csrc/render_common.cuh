@@ -752,7 +752,9 @@ static inline bool same_scene(const DScene& a, const DScene& b) {
 // argument set (`same` compares two sets): the loops launch several kernels
 // per iteration, and their launch gaps cost more than the kernels of a small
 // image.  Returns null when capture is not possible; the caller then launches
-// the kernels itself.  `drop` forgets the graph after a failed launch.
+// the kernels itself.  `drop` forgets the graph after a failed launch.  A
+// thread's graphs and capture streams are not destroyed when it exits (the
+// runtime may be shut down by then): one graph per device per thread remains.
 template <typename Args>
 struct BlockGraphCache {
     static constexpr int kDevices = 64;
