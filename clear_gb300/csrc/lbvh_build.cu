@@ -531,19 +531,18 @@ __device__ __forceinline__ bool gather_warp_records(const CUtensorMap* tmap, uin
             "%4, %5, %6}], [%7];" ::"r"(smem_u32(rows + lane * kGatherSlotFloats)),
             "l"(tmap), "r"(0), "r"(r0), "r"(r1), "r"(r2), "r"(r3), "r"(b)
             : "memory");
+    // wait for the copies; if they take implausibly long, report it and keep
+    // waiting (again bounded) so that no copy lands after the block is gone
     uint32_t done = 0;
-    for (unsigned int spins = 0; !done; ++spins) {
+    for (unsigned int spins = 0; !done && spins <= 2 * kGatherWaitLimit; ++spins) {
         asm volatile(
             "{ .reg .pred p; mbarrier.try_wait.parity.shared::cta.b64 p, [%1], 0; selp.u32 %0, 1, 0, p; }"
             : "=r"(done)
             : "r"(b)
             : "memory");
-        if (!done && spins > kGatherWaitLimit) {
-            clr_raise(CLR_DEVERR_QUEUE);
-            return false;
-        }
+        if (!done && spins == kGatherWaitLimit) clr_raise(CLR_DEVERR_QUEUE);
     }
-    return true;
+    return done != 0;
 }
 
 // Adjacent common prefix delta(i, i+1), i in [0, n-2].
