@@ -507,6 +507,20 @@ constexpr unsigned int kGatherWaitLimit = 1u << 22;
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
 
+// The copies have not completed within the limit: report it, then keep
+// waiting (again bounded) so that no copy lands after the block is gone.
+static __device__ __noinline__ bool gather_wait_overdue(uint32_t bar) {
+    clr_raise(CLR_DEVERR_QUEUE);
+    uint32_t done = 0;
+    for (unsigned int spins = 0; !done && spins < kGatherWaitLimit; ++spins)
+        asm volatile(
+            "{ .reg .pred p; mbarrier.try_wait.parity.shared::cta.b64 p, [%1], 0; selp.u32 %0, 1, 0, p; }"
+            : "=r"(done)
+            : "r"(bar)
+            : "memory");
+    return false;
+}
+
 // Stages the staging records of leaves B + 32 w .. + 31 (w = this warp) into
 // `rows`: lane l's record at rows[(l / 4) * kGatherSlotFloats + (l % 4) * 12]
 // (triangle ids tj per lane, id 0 for lanes past the array: a valid row whose
@@ -531,18 +545,16 @@ __device__ __forceinline__ bool gather_warp_records(const CUtensorMap* tmap, uin
             "%4, %5, %6}], [%7];" ::"r"(smem_u32(rows + lane * kGatherSlotFloats)),
             "l"(tmap), "r"(0), "r"(r0), "r"(r1), "r"(r2), "r"(r3), "r"(b)
             : "memory");
-    // wait for the copies; if they take implausibly long, report it and keep
-    // waiting (again bounded) so that no copy lands after the block is gone
     uint32_t done = 0;
-    for (unsigned int spins = 0; !done && spins <= 2 * kGatherWaitLimit; ++spins) {
+    for (unsigned int spins = 0; !done; ++spins) {
         asm volatile(
             "{ .reg .pred p; mbarrier.try_wait.parity.shared::cta.b64 p, [%1], 0; selp.u32 %0, 1, 0, p; }"
             : "=r"(done)
             : "r"(b)
             : "memory");
-        if (!done && spins == kGatherWaitLimit) clr_raise(CLR_DEVERR_QUEUE);
+        if (!done && spins > kGatherWaitLimit) return gather_wait_overdue(b);
     }
-    return done != 0;
+    return true;
 }
 
 // Adjacent common prefix delta(i, i+1), i in [0, n-2].
