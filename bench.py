@@ -468,9 +468,21 @@ def bench_adjoint(dev, spp=32, res=512) -> dict:
     torch.cuda.synchronize()
     fwd = ev[0].elapsed_time(ev[1]) / reps
     adj = ev[2].elapsed_time(ev[3]) / reps
+    # The same adjoint with every replayed ray traced again (no hit records
+    # carried from the primal pass).
+    g2, ge2 = torch.zeros_like(grad), torch.zeros_like(genv)
+    ev[0].record(stream)
+    for _ in range(reps):
+        ds.render_adjoint(seeds.clone(), dloss, spp, 5, tex, kind, g2, info["env_tex"], ge2, retrace=True)
+    ev[1].record(stream)
+    torch.cuda.synchronize()
+    adj_rt = ev[0].elapsed_time(ev[1]) / reps
     return {"workload": f"adjoint cornell 8 materials + 64x32 env, {w}x{h}, {spp} spp, depth 5",
             "params": 16 * 3 + genv.shape[0] * 3, "forward_ms": fwd, "adjoint_ms": adj,
-            "adjoint_over_forward": adj / fwd, "forward_msamples_s": w * h * spp / fwd / 1e3,
+            "adjoint_over_forward": adj / fwd, "adjoint_retrace_ms": adj_rt,
+            "adjoint_retrace_over_forward": adj_rt / fwd,
+            "retrace_grad_rel_diff": float((torch.linalg.norm(g2 - grad) / torch.linalg.norm(grad)).item()),
+            "forward_msamples_s": w * h * spp / fwd / 1e3,
             "adjoint_msamples_s": w * h * spp / adj / 1e3,
             "grad_norm": float(torch.linalg.norm(grad).item()), "env_grad_norm": float(torch.linalg.norm(genv).item())}
 

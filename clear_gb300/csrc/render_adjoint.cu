@@ -307,14 +307,14 @@ __global__ void __launch_bounds__(kAdThreads) k_ad_init(DScene sc, AdState S, ui
 
 // Closest hit of every queued path of both passes.
 template <bool kOrdered>
-__global__ void __launch_bounds__(kAdThreads, 8) k_ad_extend(DScene sc, AdState S, int cur) {
+__global__ void __launch_bounds__(kAdThreads, 8) k_ad_extend(DScene sc, AdState S, int cur, int cached) {
     const uint32_t n0 = S.count[2 * cur], n = n0 + S.count[2 * cur + 1];
     const uint32_t* q0 = queue(S, cur, 0);
     const uint32_t* q1 = queue(S, cur, 1);
     uint2 stack[kStackSize];
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         const uint32_t p = i < n0 ? q0[i] : q1[i - n0];
-        if (i >= n0) {  // replay pass: the primal found this vertex's hit already
+        if (cached && i >= n0) {  // replay pass: the primal found this vertex's hit already
             const uint32_t depth = S.misc[p].x;
             if (depth < kAdCache) {
                 S.hit[p] = S.hitc[(size_t)kAdCache * p + depth];
@@ -455,7 +455,8 @@ __device__ __forceinline__ void next_event(const DScene& sc, const BSDF& bsdf, c
 // the replay would end in, so the pixel goes on with its next sample.
 __global__ void __launch_bounds__(kAdThreads, 4) k_ad_primal(DScene sc, AdState S, int cur, uint32_t width,
                                                           uint32_t* __restrict__ rand_states, uint32_t max_depth,
-                                                          const float4* __restrict__ dloss, uint32_t spp) {
+                                                          const float4* __restrict__ dloss, uint32_t spp,
+                                                          int cached) {
     const uint32_t n = S.count[2 * cur];
     const uint32_t* qin = queue(S, cur, 0);
     const Camera cam = load_camera(sc);
@@ -476,7 +477,7 @@ __global__ void __launch_bounds__(kAdThreads, 4) k_ad_primal(DScene sc, AdState 
             const float initY = a4.w;
             uint32_t depth = m.x, sampledType = m.y;
             bool ended = false;
-            if (depth < kAdCache) S.hitc[(size_t)kAdCache * p + depth] = h4;  // for the replay pass
+            if (cached && depth < kAdCache) S.hitc[(size_t)kAdCache * p + depth] = h4;  // for the replay pass
             const uint32_t hid = __float_as_uint(h4.x);
             uint32_t light_face = __float_as_uint(o4.w);
             SurfPt sp;
@@ -789,7 +790,7 @@ __global__ void __launch_bounds__(kAdThreads, 4) k_ad_replay(DScene sc, AdState 
 }
 
 template <bool kOrdered>
-__global__ void __launch_bounds__(kAdThreads, 8) k_ad_shadow(DScene sc, AdState S, AdParams P) {
+__global__ void __launch_bounds__(kAdThreads, 8) k_ad_shadow(DScene sc, AdState S, AdParams P, int cached) {
     const uint32_t n = S.count[4];
     if (blockIdx.x * blockDim.x >= n) return;
     const GradSink sink = sink_begin(P);
@@ -801,12 +802,12 @@ __global__ void __launch_bounds__(kAdThreads, 8) k_ad_shadow(DScene sc, AdState 
         const uint32_t p = pw & kShPixMask, depth = pw >> kShDepthShift;
         const bool replay = (flags & 2u) != 0;
         bool visible;
-        if (replay && depth < kAdCache) {
+        if (cached && replay && depth < kAdCache) {
             visible = (S.visc[p] >> depth) & 1u;  // the primal traced this ray
         } else {
             visible = shadow_visible<kOrdered>(sc, mk(a.x, a.y, a.z), mk(b.x, b.y, b.z), __float_as_uint(a.w), stack);
             // one entry per path per launch: this is the bit's only writer
-            if (!replay && depth < kAdCache)
+            if (cached && !replay && depth < kAdCache)
                 S.visc[p] = (S.visc[p] & ~(1u << depth)) | ((visible ? 1u : 0u) << depth);
         }
         if (!visible) continue;
@@ -927,7 +928,7 @@ struct AdArgs {
     AdParams P;
     uint32_t width, spp, max_depth;
     uint32_t* rand_states;
-    bool ordered, tape;
+    bool ordered, tape, cached;
     unsigned int grid;
     size_t smem;
 };
@@ -935,19 +936,19 @@ struct AdArgs {
 static void ad_block(const AdArgs& a, cudaStream_t st) {
     for (int k = 0; k < kAdBlockIters; ++k) {
         const int cur = k & 1;
-        if (a.ordered) k_ad_extend<true><<<a.grid, kAdThreads, 0, st>>>(a.sc, a.S, cur);
-        else k_ad_extend<false><<<a.grid, kAdThreads, 0, st>>>(a.sc, a.S, cur);
+        if (a.ordered) k_ad_extend<true><<<a.grid, kAdThreads, 0, st>>>(a.sc, a.S, cur, a.cached);
+        else k_ad_extend<false><<<a.grid, kAdThreads, 0, st>>>(a.sc, a.S, cur, a.cached);
         k_ad_reset<<<1, 1, 0, st>>>(a.S, cur ^ 1);
         k_ad_primal<<<a.grid, kAdThreads, 0, st>>>(a.sc, a.S, cur, a.width, a.rand_states, a.max_depth, a.P.dloss,
-                                                    a.spp);
+                                                    a.spp, a.cached);
         if (a.tape)
             k_ad_replay<true><<<a.grid, kAdThreads, a.smem, st>>>(a.sc, a.S, a.P, cur, a.width, a.rand_states, a.spp,
                                                                   a.max_depth);
         else
             k_ad_replay<false><<<a.grid, kAdThreads, a.smem, st>>>(a.sc, a.S, a.P, cur, a.width, a.rand_states, a.spp,
                                                                    a.max_depth);
-        if (a.ordered) k_ad_shadow<true><<<a.grid, kAdThreads, a.smem, st>>>(a.sc, a.S, a.P);
-        else k_ad_shadow<false><<<a.grid, kAdThreads, a.smem, st>>>(a.sc, a.S, a.P);
+        if (a.ordered) k_ad_shadow<true><<<a.grid, kAdThreads, a.smem, st>>>(a.sc, a.S, a.P, a.cached);
+        else k_ad_shadow<false><<<a.grid, kAdThreads, a.smem, st>>>(a.sc, a.S, a.P, a.cached);
     }
 }
 
@@ -958,7 +959,7 @@ static bool same_ad_args(const AdArgs& x, const AdArgs& y) {
            p.env_tex == q.env_tex && p.grad_env == q.grad_env && p.dloss == q.dloss && p.tape.rec == q.tape.rec &&
            p.tape.cap == q.tape.cap && p.tape.count == q.tape.count && x.width == y.width && x.spp == y.spp &&
            x.max_depth == y.max_depth && x.rand_states == y.rand_states && x.ordered == y.ordered &&
-           x.tape == y.tape && x.grid == y.grid && x.smem == y.smem;
+           x.tape == y.tape && x.cached == y.cached && x.grid == y.grid && x.smem == y.smem;
 }
 
 thread_local BlockGraphCache<AdArgs> t_ad_graphs;
@@ -1033,6 +1034,7 @@ extern "C" int clr_render_adjoint(const clr_scene* scene, uint32_t width, uint32
     a.rand_states = rand_states;
     a.ordered = ordered;
     a.tape = A.tape != nullptr;
+    a.cached = (flags & CLR_ADJOINT_RETRACE) == 0;
     a.grid = grid;
     a.smem = smem;
     cudaGraphExec_t exec = t_ad_graphs.get(a, ad_block, same_ad_args);

@@ -14,6 +14,7 @@ from .scene import FACE_DTYPE, NONE32, Scene, zenith_weights
 from .scenes import pixel_seeds
 
 RENDER_ORDERED = 0x1
+ADJOINT_RETRACE = 0x4
 RENDER_WAVEFRONT = 0x2  # clr_render: the wavefront form on the library's own workspace
 NO_TEX = 0xFFFFFFFF
 TAPE_WORDS = 32
@@ -118,13 +119,15 @@ class DeviceScene:
                        param_tex: torch.Tensor, param_kind: torch.Tensor, grad: torch.Tensor,
                        env_tex: int | None = None, grad_env: torch.Tensor | None = None,
                        tape: torch.Tensor | None = None, tape_count: torch.Tensor | None = None,
-                       ordered: bool = True) -> None:
+                       ordered: bool = True, retrace: bool = False) -> None:
         """Adds sum_p dloss[p] . dAccum[p]/dtheta to `grad` (K x 4 float32) and
         `grad_env` (texels x 4) for the samples clr_render_wavefront would
         take from the same `rng` (advanced in place).  param_tex (int32) /
         param_kind (uint8) list the differentiated constant textures by their
         textures-blob offsets.  `tape` (records x 32 int32) with `tape_count`
-        (1 int32, zeroed by the caller) records the replayed paths."""
+        (1 int32, zeroed by the caller) records the replayed paths.
+        retrace=True traces every replayed ray again (CLR_ADJOINT_RETRACE)
+        instead of taking the primal pass's hits for the first 8 vertices."""
         K = int(param_tex.numel())
         p = _lib.ClrAdjointParams(
             param_tex.data_ptr() if K else None, param_kind.data_ptr() if K else None, K,
@@ -137,7 +140,8 @@ class DeviceScene:
         with torch.cuda.device(self.device), self._workspace_turn(cur, self.adjoint_workspace(K)) as ws:
             _lib.call("clr_render_adjoint", C.byref(self.c), C.c_uint32(self.width), C.c_uint32(self.height),
                       C.c_void_p(rng.data_ptr()), C.c_void_p(dloss.data_ptr()), C.c_uint32(spp),
-                      C.c_uint32(max_depth), C.c_uint32(RENDER_ORDERED if ordered else 0), C.byref(p),
+                      C.c_uint32(max_depth),
+                      C.c_uint32((RENDER_ORDERED if ordered else 0) | (ADJOINT_RETRACE if retrace else 0)), C.byref(p),
                       C.c_void_p(ws.data_ptr()), C.c_uint64(ws.numel()), stream)
 
     def adjoint_workspace(self, num_params: int) -> torch.Tensor:

@@ -478,6 +478,11 @@ typedef struct clr_adjoint_params {
  * replay pass).  width * height must stay below 2^27 (CLR_EINVAL). */
 CLR_API int clr_render_adjoint_workspace_bytes(uint32_t width, uint32_t height, uint32_t num_params,
                                                uint64_t* bytes);
+/* clr_render_adjoint flag: the replay pass traces every ray again instead of
+ * taking the primal pass's hit records and next-event visibilities for the
+ * first 8 vertices: the same paths and gradients, with the replay's
+ * intersections all recomputed from the RNG seeds (more traversal work). */
+#define CLR_ADJOINT_RETRACE 0x4u
 CLR_API int clr_render_adjoint(const clr_scene* scene, uint32_t width, uint32_t height, uint32_t* rand_states,
                                const float* dloss_daccum, uint32_t spp, uint32_t max_depth, uint32_t flags,
                                const clr_adjoint_params* params, void* workspace, uint64_t workspace_bytes,

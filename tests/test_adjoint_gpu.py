@@ -280,3 +280,31 @@ def test_adjoint_rejects_bad_arguments(cuda):
     torch.cuda.synchronize()
     assert int(count.item()) > 8
     assert _lib.device_status() == 0
+
+
+@pytest.mark.gpu
+def test_adjoint_cached_and_retraced_replay_agree(cuda):
+    """The replay pass takes the primal pass's hit records and next-event
+    visibilities for a path's first 8 vertices, or traces those rays again
+    (CLR_ADJOINT_RETRACE): the same paths, so the same gradients (up to the
+    order of their atomic sums) and the same random-number states."""
+    sc, info, ds, tex, kind = _setup(cuda)
+    target = _target(cuda, info)
+    rng, pix = ds.new_frame()
+    seeds = rng.clone()
+    ds.render(rng, pix, SPP, 12, wavefront=True)
+    dloss = _dloss(pix, target)
+    T = info["env"].shape[0] * info["env"].shape[1]
+    out = []
+    for retrace in (False, True):
+        grad = torch.zeros((16, 4), dtype=torch.float32, device=cuda)
+        genv = torch.zeros((T, 4), dtype=torch.float32, device=cuda)
+        r = seeds.clone()
+        ds.render_adjoint(r, dloss, SPP, 12, tex, kind, grad, info["env_tex"], genv, retrace=retrace)
+        torch.cuda.synchronize()
+        out.append((grad.double(), genv.double(), r))
+    assert torch.equal(out[0][2], out[1][2]) and torch.equal(out[0][2], rng)
+    for k in (0, 1):
+        a, b = out[0][k], out[1][k]
+        assert torch.allclose(a, b, rtol=1e-5, atol=1e-6 * float(a.abs().max())), k
+    assert _lib.device_status() == 0
