@@ -181,7 +181,7 @@ def ncu_traffic(kernel: str):
     with open(p) as fh:
         d = json.load(fh)
     v = d.get(kernel)
-    return None if v is None else float(v["bytes_per_launch_scaled"])
+    return None if v is None else float(v["bytes_per_launch"])
 
 
 def host_threads() -> int:
