@@ -63,6 +63,19 @@ def test_build_parity(cuda, n, bits):
     no_device_errors()
 
 
+@pytest.mark.parametrize("bits", [1, 3, 7, 21])
+@pytest.mark.parametrize("n", [2, 4097, 65543])
+def test_build_parity_other_key_widths(cuda, n, bits):
+    """Key widths either side of the common 10 and 20 bits per axis: 1 bit
+    (eight distinct Morton keys, so most of the tree splits on the sorted
+    positions), 3 and 7 bits (one and three sort passes) and 21 bits (63-bit
+    keys, eight passes)."""
+    vx, vy, vz = W.triangle_soup(n, seed=7 + n)
+    _, _, ref = gpu_build(cuda, vx, vy, vz, None, n, bits)
+    assert_build_equal(ref, oracle.lbvh_build(vx, vy, vz, None, n, bits), n)
+    no_device_errors()
+
+
 @pytest.mark.parametrize("n", [(2 << 20), (2 << 20) + 1])
 def test_build_parity_either_side_of_the_climb_threshold(cuda, n):
     """Trees up to 2 Mi triangles finish their block-crossing climbs inside the
