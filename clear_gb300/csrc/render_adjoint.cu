@@ -22,7 +22,9 @@
 //                 derivatives.
 // Between its passes a path keeps its RNG state and, for its first kAdCache
 // vertices, the primal's hit records and next-event visibilities, so that the
-// replay traces only what lies deeper (the same rays give the same answers).
+// replay traces only what lies deeper (the same rays give the same answers);
+// with CLR_ADJOINT_RETRACE (`cached` = 0 in the kernels) it keeps only the
+// RNG state and the replay traces every ray again.
 //
 // Gradients of the material parameters are summed per block in shared memory
 // and kept per block in the workspace; one reduction adds them to the caller's
