@@ -111,6 +111,26 @@ inline void traceShadow(void* stream, const clr_bvh& bvh, const float* rays, uin
     check(clr_trace_shadow(&bvh, rays, numRays, occluded, stream));
 }
 
+// Workspace bytes of the sorted queries below for numRays rays.
+inline uint64_t traceSortWorkspaceBytes(uint32_t numRays) {
+    uint64_t b = 0;
+    check(clr_trace_sort_workspace_bytes(numRays, &b));
+    return b;
+}
+
+// traceClosest(ordered = true) and traceShadow with the rays searched in the
+// order of their origins' Morton codes (for incoherent ray lists): the same
+// answers, in the callers' ray order.  `workspace` (256-byte aligned) holds
+// traceSortWorkspaceBytes(numRays) bytes.
+inline void traceClosestSorted(void* stream, const clr_bvh& bvh, const float* rays, uint32_t numRays,
+                               uint32_t* hitId, float* hitT, void* workspace, uint64_t workspaceBytes) {
+    check(clr_trace_closest_sorted(&bvh, rays, numRays, hitId, hitT, workspace, workspaceBytes, stream));
+}
+inline void traceShadowSorted(void* stream, const clr_bvh& bvh, const float* rays, uint32_t numRays,
+                              uint8_t* occluded, void* workspace, uint64_t workspaceBytes) {
+    check(clr_trace_shadow_sorted(&bvh, rays, numRays, occluded, workspace, workspaceBytes, stream));
+}
+
 // The pathtracing launches: spp samples added to every pixel of `pixels`
 // (float4 per pixel) from the per-pixel random states.
 inline void render(void* stream, const clr_scene& scene, uint32_t width, uint32_t height, uint32_t* randStates,
@@ -131,6 +151,25 @@ inline void renderWavefront(void* stream, const clr_scene& scene, uint32_t width
                             uint64_t workspaceBytes, uint32_t maxDepth = 100, uint32_t flags = CLR_RENDER_ORDERED) {
     check(clr_render_wavefront(&scene, width, height, randStates, pixels, spp, maxDepth, flags, workspace,
                                workspaceBytes, stream));
+}
+
+inline uint64_t renderAdjointWorkspaceBytes(uint32_t width, uint32_t height, uint32_t numParams) {
+    uint64_t b = 0;
+    check(clr_render_adjoint_workspace_bytes(width, height, numParams, &b));
+    return b;
+}
+
+// Gradients of an image loss (dlossDaccum: float4 per pixel) for the samples
+// renderWavefront would take from the same randStates (advanced as it would
+// advance them); `workspace` (256-byte aligned) holds
+// renderAdjointWorkspaceBytes(width, height, params.num_params) bytes.
+// flags: CLR_RENDER_ORDERED, CLR_ADJOINT_RETRACE.
+inline void renderAdjoint(void* stream, const clr_scene& scene, uint32_t width, uint32_t height,
+                          uint32_t* randStates, const float* dlossDaccum, uint32_t spp,
+                          const clr_adjoint_params& params, void* workspace, uint64_t workspaceBytes,
+                          uint32_t maxDepth = 100, uint32_t flags = CLR_RENDER_ORDERED) {
+    check(clr_render_adjoint(&scene, width, height, randStates, dlossDaccum, spp, maxDepth, flags, &params,
+                             workspace, workspaceBytes, stream));
 }
 
 }  // namespace clr

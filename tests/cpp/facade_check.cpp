@@ -45,6 +45,21 @@ int main() {
     cudaMemcpy(&ht, t, 4, cudaMemcpyDeviceToHost);
     std::printf("gpu: hit %u at t %g, %zu timed passes\n", hid, ht, passes.size());
     bool ok = hid == 0 && ht == 1.0f && !passes.empty();
+    // the same query with the rays sorted by origin first
+    {
+        const uint64_t wsb = clr::traceSortWorkspaceBytes(1);
+        void* ws = nullptr;
+        cudaMalloc(&ws, wsb);
+        cudaMemset(id, 0xFF, 4);
+        clr::traceClosestSorted(nullptr, bvh, rays, 1, id, t, ws, wsb);
+        uint32_t sid = 1;
+        float st = 0;
+        cudaMemcpy(&sid, id, 4, cudaMemcpyDeviceToHost);
+        cudaMemcpy(&st, t, 4, cudaMemcpyDeviceToHost);
+        std::printf("gpu: sorted query hit %u at t %g\n", sid, st);
+        ok = ok && sid == hid && st == ht;
+        cudaFree(ws);
+    }
     // the same soup uploaded from host arrays: same tree, root record read back
     {
         clr_bvh hb{};
