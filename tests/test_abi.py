@@ -35,3 +35,27 @@ def test_sort_workspace_size_without_gpu():
         sizes.append(b.value)
     assert sizes == sorted(sizes)
     assert L.clr_trace_sort_workspace_bytes(C.c_uint32(10), None) != 0
+
+
+def test_python_constants_match_the_header():
+    """Every flag and size the Python mirror passes across the C ABI has the
+    value the header defines."""
+    import os
+    import re
+
+    from clear_gb300 import batch, render
+
+    hdr = open(os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "include",
+                            "clear_cuda.h")).read()
+    defs = {m.group(1): int(m.group(2), 0) for m in re.finditer(r"^#define (CLR_\w+)\s+(0x[0-9a-fA-F]+|\d+)u?\b", hdr,
+                                                                 re.M)}
+    pairs = {"CLR_DEVERR_SORT_TIMEOUT": _lib.DEVERR_SORT_TIMEOUT, "CLR_DEVERR_STACK": _lib.DEVERR_STACK,
+             "CLR_DEVERR_REFIT": _lib.DEVERR_REFIT, "CLR_DEVERR_QUEUE": _lib.DEVERR_QUEUE,
+             "CLR_DEVERR_INPUT": _lib.DEVERR_INPUT, "CLR_NODE_BYTES": _lib.NODE_BYTES,
+             "CLR_TRI_BYTES": _lib.TRI_BYTES, "CLR_REF_NODE_BYTES": _lib.REF_NODE_BYTES,
+             "CLR_SCENE_ALPHA": render.SCENE_ALPHA, "CLR_RENDER_ORDERED": render.RENDER_ORDERED,
+             "CLR_RENDER_WAVEFRONT": render.RENDER_WAVEFRONT, "CLR_ADJOINT_RETRACE": render.ADJOINT_RETRACE,
+             "CLR_TAPE_WORDS": render.TAPE_WORDS, "CLR_TAPE_VISIBLE": render.TAPE_VISIBLE,
+             "CLR_BATCH_GRAPH": batch.BATCH_GRAPH}
+    for name, value in pairs.items():
+        assert defs.get(name) == value, (name, defs.get(name), value)
