@@ -104,9 +104,11 @@ class LBVHBuilder:
 
     def perform(self, vertices, faces, num_faces: int, num_bits_per_dim: int = 10,
                 out: BVH | None = None) -> BVH:
-        """Build the LBVH.  vertices = (vx, vy, vz) float32 tensors; faces =
-        (num_faces, 3) integer tensor of vertex indices, or None for an
-        unindexed soup (vertex k of triangle t at 3t+k)."""
+        """Build the LBVH on the current stream.  vertices = (vx, vy, vz)
+        float32 tensors; faces = (num_faces, 3) integer tensor of vertex
+        indices, or None for an unindexed soup (vertex k of triangle t at
+        3t+k).  A builder's builds share its scratch pool: builds on other
+        streams must wait for this one (separate builders do not)."""
         vx, vy, vz = (_f32(v, self.device) for v in vertices)
         tri = None
         if faces is not None:

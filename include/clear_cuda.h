@@ -95,7 +95,10 @@ CLR_API int clr_lbvh_destroy(clr_lbvh* h);
  * main.cpp:365; 10 gives 30-bit keys).  Fills out->nodes/tris/root_box and
  * sets out->num_tris and out->bits_per_dim.  No host synchronisation:
  * the scene box stays on the device (the reference reads it back,
- * LBVHBuilder.cpp:229). */
+ * LBVHBuilder.cpp:229).  The builds of one handle share its scratch pool, as
+ * the reference's builder shares its buffers: issue them on one stream, or
+ * make a second stream wait for the first's build; separate handles build
+ * concurrently. */
 CLR_API int clr_lbvh_build(clr_lbvh* h, const float* vx, const float* vy, const float* vz, const uint32_t* tri,
                    uint32_t num_tris, uint32_t bits_per_dim, clr_bvh* out, void* stream);
 
